@@ -1,0 +1,211 @@
+/* gb300ode — ensemble explicit Runge-Kutta solves on one NVIDIA GB300 GPU.
+ *
+ * C ABI of libgb300ode.so.  It replaces, for a whole ensemble at once, the
+ * per-trajectory solve methods of SimpleDiffEq.jl's GPU-crutch solvers:
+ *
+ *   DiffEqBase.solve(prob, GPUSimpleRK4(); dt)                 src/rk4/gpurk4.jl:53-98
+ *   DiffEqBase.solve(prob, GPUSimpleTsit5(); dt, saveat, ...)  src/tsit5/gpuatsit5.jl:55-147
+ *   DiffEqBase.solve(prob, GPUSimpleATsit5(); dt, abstol, reltol, saveat, ...)
+ *                                                              src/tsit5/gpuatsit5.jl:205-336
+ *   DiffEqBase.solve(prob, GPUSimpleVern7(); ...)              src/verner/gpuvern7.jl:55-242
+ *   DiffEqBase.solve(prob, GPUSimpleAVern7(); ...)             src/verner/gpuvern7.jl:300-536
+ *   DiffEqBase.solve(prob, GPUSimpleVern9(); ...)              src/verner/gpuvern9.jl:55-353
+ *   DiffEqBase.solve(prob, GPUSimpleAVern9(); ...)             src/verner/gpuvern9.jl:411-779
+ *
+ * applied to every trajectory of an ensemble (the prob_func loop that
+ * SciMLBase's EnsembleProblem would run on the host).  The keyword arguments
+ * keep their meaning and defaults (dt = 0.1, abstol = 1e-6, reltol = 1e-3,
+ * saveat = nothing) and the solver loop is the reference's: same stages,
+ * error norm, PI controller (src/SimpleDiffEq.jl:67-77) and saveat
+ * interpolation.
+ *
+ * Conventions
+ *   - Every function returns ODE_OK (0) or a negative ODE_E* code and never
+ *     throws, aborts or traps.  ode_last_error() describes the last failure.
+ *   - The caller owns every input and output buffer.  The handle owns the
+ *     device workspace, compiled kernels, captured CUDA graphs and the
+ *     learned-schedule model.  One handle is used by one host thread at a time.
+ *   - Arrays are structure-of-arrays over trajectories: element (d, i) of a
+ *     [dim][n] array is at d*n + i.  All floating-point buffers are double;
+ *     in the single-precision modes the kernels convert on load and store.
+ *   - The reference throws ErrorException("dt<dtmin"); here the trajectory
+ *     stops with retcode ODE_RET_DTMIN and the call returns ODE_ETRAJ, so a
+ *     host layer can raise the same exception.
+ */
+#ifndef GB300ODE_H
+#define GB300ODE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ODE_ABI_VERSION 1
+
+/* status codes */
+enum {
+  ODE_OK = 0,
+  ODE_EINVAL = -1,   /* invalid argument */
+  ODE_ECUDA = -2,    /* CUDA runtime or driver error */
+  ODE_ENOMEM = -3,   /* device or host allocation failed */
+  ODE_ENOTSUP = -4,  /* valid but unsupported combination */
+  ODE_ENVRTC = -5,   /* run-time compilation of a kernel failed (log in ode_last_error) */
+  ODE_ETRAJ = -6,    /* the solve completed but some trajectory ended with retcode DTMIN or MAXITERS */
+  ODE_ENOMODEL = -7  /* learned schedule requested without a fitted model */
+};
+
+/* algorithms: the GPUSimple* solver types */
+enum {
+  ODE_ALG_RK4 = 0,     /* GPUSimpleRK4    (fixed step) */
+  ODE_ALG_TSIT5 = 1,   /* GPUSimpleTsit5  (fixed step) */
+  ODE_ALG_ATSIT5 = 2,  /* GPUSimpleATsit5 (adaptive)   */
+  ODE_ALG_VERN7 = 3,   /* GPUSimpleVern7  (fixed step) */
+  ODE_ALG_AVERN7 = 4,  /* GPUSimpleAVern7 (adaptive)   */
+  ODE_ALG_VERN9 = 5,   /* GPUSimpleVern9  (fixed step) */
+  ODE_ALG_AVERN9 = 6   /* GPUSimpleAVern9 (adaptive)   */
+};
+
+/* built-in right-hand sides f(u, p, t); ids >= ODE_RHS_USER come from ode_rhs_compile */
+enum {
+  ODE_RHS_LORENZ = 0,    /* dim 3, p = (sigma, rho, beta) */
+  ODE_RHS_VANDERPOL = 1, /* dim 2, x' = v, v' = mu (1 - x^2) v - x, p = (mu) */
+  ODE_RHS_R3BP = 2,      /* dim 4, planar restricted three-body (x, y, vx, vy), p = (mu) */
+  ODE_RHS_KURAMOTO = 3,  /* dim D, theta_i' = w_i + (K/D) sum_j sin(theta_j - theta_i), p = (w_1..w_D, K) */
+  ODE_RHS_LINEAR = 4,    /* dim D, du = A u, p = A row-major (D*D values) */
+  ODE_RHS_USER = 1000
+};
+
+enum {
+  ODE_FP64 = 0,       /* everything in double, as the reference with Float64 state */
+  ODE_FP32 = 1,       /* everything in float, as the reference with Float32 state */
+  ODE_FP32_KAHAN = 2  /* float stages, Kahan-compensated float state, double t and dt */
+};
+
+enum {
+  ODE_SCHED_PLAIN = 0,      /* one thread per trajectory */
+  ODE_SCHED_PERSISTENT = 1, /* resident warps refill lanes from a device work counter */
+  ODE_SCHED_LEARNED = 2     /* persistent, trajectories ordered by predicted cost, dt0 seeded */
+};
+
+enum { ODE_MEM_HOST = 0, ODE_MEM_DEVICE = 1 };
+
+/* per-trajectory return codes */
+enum {
+  ODE_RET_DEFAULT = 0,  /* finished at tf (ReturnCode.Default in the reference) */
+  ODE_RET_DTMIN = 1,    /* dt fell below dtmin (the reference throws "dt<dtmin") */
+  ODE_RET_MAXITERS = 2, /* attempt cap reached (no counterpart; the reference has no cap) */
+  ODE_RET_NAN = 3       /* finished at tf, but a NaN error estimate was accepted on the way,
+                           as the reference accepts it (NaN > 1 is false) */
+};
+
+typedef struct ode_handle ode_handle;
+
+typedef struct {
+  int32_t alg;          /* ODE_ALG_* */
+  int32_t rhs;          /* ODE_RHS_* or an id from ode_rhs_compile */
+  int32_t precision;    /* ODE_FP64 / ODE_FP32 / ODE_FP32_KAHAN */
+  int32_t schedule;     /* ODE_SCHED_* (adaptive algorithms; fixed-step ones always run plain) */
+  int64_t n;            /* trajectories */
+  int32_t dim;          /* state dimension */
+  int32_t nparams;      /* parameters per trajectory */
+  double t0, tf;        /* tspan */
+  double dt;            /* initial (adaptive) or fixed step; reference default 0.1 */
+  double abstol, reltol;/* reference defaults 1e-6, 1e-3 */
+  const double* saveat; /* [nsave] save times (always a host pointer), or NULL */
+  int64_t nsave;
+  int32_t save_everystep; /* fixed-step algorithms without saveat: save every grid point */
+  int32_t memory;       /* ODE_MEM_HOST or ODE_MEM_DEVICE for u0, p, dt0 and all outputs */
+  int64_t maxiters;     /* attempt cap per trajectory; <= 0: the default cap of 10^6 */
+  const double* u0;     /* [dim][n] */
+  const double* p;      /* [nparams][n] */
+  const double* dt0;    /* optional [n] per-trajectory initial dt (adaptive), or NULL */
+  void* stream;         /* cudaStream_t, or NULL for the handle's stream */
+} ode_solve_args;
+
+typedef struct {
+  double* us;           /* [npoints][dim][n]: npoints = nsave, or the grid length when
+                           save_everystep applies; NULL to skip */
+  double* u_final;      /* [dim][n] state at the end, or NULL */
+  double* t_final;      /* [n], or NULL */
+  int8_t* retcode;      /* [n] ODE_RET_*, or NULL */
+  int32_t* naccept;     /* [n] accepted steps, or NULL */
+  int32_t* nreject;     /* [n] rejected attempts, or NULL */
+  double* dt_first;     /* [n] size of the first accepted step, or NULL */
+} ode_solve_out;
+
+typedef struct {
+  double kernel_ms;       /* device time of the solve kernels (CUDA events) */
+  double total_ms;        /* wall time of the call */
+  int64_t attempts;       /* sum over trajectories of accepted + rejected attempts */
+  int64_t saves;          /* saveat points written */
+  int32_t launches;       /* kernels launched by the call */
+  int32_t schedule_used;  /* ODE_SCHED_* actually run */
+  int32_t graph_replayed; /* 1 if a captured CUDA graph was replayed */
+  int32_t jit;            /* 1 if the solver kernel was compiled at run time */
+} ode_solve_stats;
+
+/* Library version (ODE_ABI_VERSION). */
+int ode_abi_version(void);
+
+/* Create a handle bound to CUDA device `device`. */
+int ode_create(ode_handle** h, int device);
+/* Release the handle and everything it owns. */
+void ode_destroy(ode_handle* h);
+/* Text of the last error on this handle ("" if none). */
+const char* ode_last_error(const ode_handle* h);
+
+/* Solve an ensemble.  Replaces the per-trajectory solve calls listed above;
+ * `stats` may be NULL.  Returns ODE_ETRAJ when the solve ran but some
+ * trajectory ended with ODE_RET_DTMIN or ODE_RET_MAXITERS (see `retcode`). */
+int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_solve_stats* stats);
+
+/* Elements of Julia's range t0:dt:tf (the fixed-step grid of the GPUSimple
+ * fixed-step solvers, e.g. src/tsit5/gpuatsit5.jl:92) in double or float
+ * semantics (precision ODE_FP32 for float).  Writes up to `cap` elements to
+ * `out` (may be NULL) and the full length to *len. */
+int ode_fixed_grid(double t0, double dt, double tf, int precision, double* out, int64_t cap, int64_t* len);
+
+/* Compile a user right-hand side with NVRTC.  `body` is the body of
+ *   template <class R> __device__ void rhs(R* du, const R* u, const R* p, R t)
+ * for a state of `dim` components and `nparams` parameters; R is double or
+ * float.  On success *rhs_id receives an id usable in ode_solve_args.rhs.
+ * Compiler diagnostics go to `log` (may be NULL). */
+int ode_rhs_compile(ode_handle* h, const char* body, int dim, int nparams, int* rhs_id, char* log, size_t loglen);
+
+/* ---- learned schedule ---------------------------------------------------
+ * A 2-hidden-layer ReLU MLP (bf16 weights, fp32 accumulation) maps each
+ * trajectory's (p, u0) to (log attempts, log dt of the first accepted step).
+ * It is trained on the GPU on counts the plain solver records for a training
+ * ensemble, then used by ODE_SCHED_LEARNED to order trajectories by predicted
+ * cost (longest first) and to seed each trajectory's initial dt. */
+typedef struct {
+  int32_t hidden;      /* hidden width (default 64) */
+  int32_t epochs;      /* passes over the training set (default 200) */
+  int32_t batch;       /* minibatch size (default 1024) */
+  float lr;            /* Adam learning rate (default 3e-3) */
+  uint64_t seed;       /* initialisation and shuffling seed */
+  int32_t seed_dt0;    /* 1: use the predicted dt0 in ODE_SCHED_LEARNED (default 1) */
+  float dt0_safety;    /* predicted dt0 is multiplied by this (default 1.0) */
+} ode_learn_opts;
+
+typedef struct {
+  float loss_first, loss_last;  /* training loss of the first and last epoch */
+  float r2_attempts;            /* R^2 of log attempts on the training set */
+  double train_solve_ms, train_fit_ms;
+} ode_learn_report;
+
+/* Fill `o` with defaults. */
+void ode_learn_default_opts(ode_learn_opts* o);
+/* Solve the training ensemble `a` with the plain schedule, record its step
+ * counts and fit the model held by the handle.  `a` follows ode_ensemble_solve. */
+int ode_learn_fit(ode_handle* h, const ode_solve_args* a, const ode_learn_opts* opts, ode_learn_report* rep);
+/* Predicted (log attempts, log dt_first) per trajectory into host arrays (either may be NULL). */
+int ode_learn_predict(ode_handle* h, const ode_solve_args* a, float* log_attempts, float* log_dt_first);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GB300ODE_H */

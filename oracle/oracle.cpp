@@ -1,0 +1,1090 @@
+/* CPU oracle: a plain C++ restatement of the reference's per-trajectory solvers.
+ *
+ * TEST INFRASTRUCTURE — used only by tests/ and by the CPU-baseline leg of
+ * bench.py.  The product library never links or calls this file.
+ *
+ * What is restated (paths inside SimpleDiffEq.jl):
+ *   GPUSimpleTsit5 / GPUSimpleATsit5   src/tsit5/gpuatsit5.jl:55-147, :205-336
+ *   GPUSimpleVern7 / GPUSimpleAVern7   src/verner/gpuvern7.jl:55-242, :300-536
+ *   GPUSimpleVern9 / GPUSimpleAVern9   src/verner/gpuvern9.jl:55-353, :411-779
+ *   GPUSimpleRK4                       src/rk4/gpurk4.jl:53-98
+ *   SimpleATsit5 (integrator form)     src/tsit5/atsit5.jl:117-179, :322-413, :705-732
+ *   SimpleTsit5 (integrator form)      src/tsit5/tsit5.jl:84-122, :303-352, :358-399
+ *   PI controller constants            src/SimpleDiffEq.jl:67-77, src/tsit5/atsit5.jl:57-62
+ *   error norm ODE_DEFAULT_NORM        DiffEqBase (not vendored): sqrt(sum(abs2, e) / length(e))
+ * Coefficients come from tableaus.h, extracted verbatim from
+ * src/tsit5/atsit5_cache.jl and src/verner/verner_tableaus.jl.
+ *
+ * Two rounding modes (oracle_round):
+ *   REF     what the Julia code rounds: @muladd on SVector arithmetic falls back
+ *           to a separate multiply and add, scalar muladd (stage times, Horner
+ *           steps of @evalpoly) fuses, the controller uses libm pow.
+ *   DEVICE  the device rounding canon the CUDA kernels implement: every
+ *           multiply-add of the reference's expressions is one fused
+ *           multiply-add, linear combinations accumulate from the last term
+ *           to the first (the nesting MuladdMacro produces), and the step-size
+ *           factor q is computed in single precision with ctrl_pow.h.
+ * Build with -ffp-contract=off so that no other multiply-add is fused.
+ *
+ * Documented deviations from the reference, shared with the device path:
+ *   * "dt<dtmin" ends the trajectory with retcode 1 instead of throwing;
+ *   * an optional attempt cap (maxiters) ends it with retcode 2;
+ *   * a NaN error estimate is accepted exactly as the reference does
+ *     (NaN > 1 is false) and the trajectory finishes; retcode 3 flags it;
+ *   * saveat points never reached are NaN instead of uninitialised memory.
+ */
+#include "oracle.h"
+#include "ctrl_pow.h"
+#include "../simplediffeq.jl_gb300/csrc/tableaus.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+namespace {
+
+constexpr int MAXD = 16;
+constexpr int MAXP = 32;
+constexpr int MAXK = 26;
+
+enum { RET_DEFAULT = 0, RET_DTMIN = 1, RET_MAXITERS = 2, RET_NAN = 3 };
+
+/* ---------------------------------------------------------------- policy */
+/* R: type of stage arithmetic and state; T: type of t and dt; KAHAN: the state
+ * update is a compensated sum (u = hi - c); DEV: device rounding canon. */
+template <class R_, class T_, bool KAHAN_, bool DEV_>
+struct Pol {
+  typedef R_ R;
+  typedef T_ T;
+  static constexpr bool KAHAN = KAHAN_;
+  static constexpr bool DEV = DEV_;
+};
+
+template <class X>
+static inline X fmaX(X a, X b, X c) { return std::fma(a, b, c); }
+
+/* a*b+c of a vector expression: fused in the device canon, two roundings in
+ * the reference (the generic muladd fallback for SVector). */
+template <bool DEV, class X>
+static inline X vmadd(X a, X b, X c) {
+  if (DEV) return fmaX(a, b, c);
+  return a * b + c;
+}
+
+/* Julia's non-fastmath min/max propagate NaN. */
+template <class X> static inline X jmin(X a, X b) {
+  if (a != a || b != b) return (X)NAN;
+  return b < a ? b : a;
+}
+template <class X> static inline X jmax(X a, X b) {
+  if (a != a || b != b) return (X)NAN;
+  return b > a ? b : a;
+}
+/* @fastmath min/max: plain compare-and-select (Base.FastMath min_fast/max_fast). */
+template <class X> static inline X fmin_(X x, X y) { return (y > x) ? x : y; }
+template <class X> static inline X fmax_(X x, X y) { return (y > x) ? y : x; }
+
+/* ---------------------------------------------------------------- problems */
+/* Built-in right-hand sides.  The REF form is the plain Julia expression; the
+ * DEV form fuses the products the device functors fuse. */
+template <class R, bool DEV>
+static void rhs_eval(int id, int D, const R* u, const R* p, double t, R* du) {
+  (void)t;
+  switch (id) {
+    case ORACLE_LORENZ: {  /* p = (sigma, rho, beta) */
+      R s = p[0], r = p[1], b = p[2];
+      du[0] = s * (u[1] - u[0]);
+      if (DEV) {
+        du[1] = fmaX(u[0], r - u[2], -u[1]);
+        du[2] = fmaX(u[0], u[1], -(b * u[2]));
+      } else {
+        du[1] = u[0] * (r - u[2]) - u[1];
+        du[2] = u[0] * u[1] - b * u[2];
+      }
+      break;
+    }
+    case ORACLE_VDP: {  /* x' = v, v' = mu (1 - x^2) v - x; p = (mu) */
+      R mu = p[0];
+      du[0] = u[1];
+      if (DEV) {
+        R w = fmaX(-u[0], u[0], (R)1);
+        du[1] = fmaX(mu * w, u[1], -u[0]);
+      } else {
+        du[1] = mu * ((R)1 - u[0] * u[0]) * u[1] - u[0];
+      }
+      break;
+    }
+    case ORACLE_R3BP: {  /* planar restricted three-body; u = (x, y, vx, vy); p = (mu) */
+      R mu = p[0];
+      R mu1 = (R)1 - mu;
+      R x = u[0], y = u[1], vx = u[2], vy = u[3];
+      R a = x + mu, b = x - mu1;
+      if (DEV) {
+        R r1 = fmaX(a, a, y * y), r2 = fmaX(b, b, y * y);
+        R d1 = r1 * std::sqrt(r1), d2 = r2 * std::sqrt(r2);
+        R g1 = mu1 / d1, g2 = mu / d2;
+        du[0] = vx;
+        du[1] = vy;
+        du[2] = fmaX(-g2, b, fmaX(-g1, a, fmaX((R)2, vy, x)));
+        du[3] = fmaX(-g2, y, fmaX(-g1, y, fmaX((R)-2, vx, y)));
+      } else {
+        R r1 = a * a + y * y, r2 = b * b + y * y;
+        R d1 = r1 * std::sqrt(r1), d2 = r2 * std::sqrt(r2);
+        du[0] = vx;
+        du[1] = vy;
+        du[2] = x + (R)2 * vy - mu1 * a / d1 - mu * b / d2;
+        du[3] = y - (R)2 * vx - mu1 * y / d1 - mu * y / d2;
+      }
+      break;
+    }
+    case ORACLE_KURAMOTO: {  /* theta_i' = w_i + (K/D) sum_j sin(theta_j - theta_i); p = (w_1..w_D, K) */
+      R S = 0, C = 0, sn[MAXD], cs[MAXD];
+      for (int j = 0; j < D; ++j) {
+        sn[j] = std::sin(u[j]);
+        cs[j] = std::cos(u[j]);
+        S += sn[j];
+        C += cs[j];
+      }
+      R kd = p[D] / (R)D;
+      for (int i = 0; i < D; ++i) {
+        if (DEV) du[i] = fmaX(kd, fmaX(cs[i], S, -(sn[i] * C)), p[i]);
+        else du[i] = p[i] + kd * (cs[i] * S - sn[i] * C);
+      }
+      break;
+    }
+    case ORACLE_LINEAR: {  /* du = A u, A row-major in p */
+      for (int i = 0; i < D; ++i) {
+        R s = p[i * D] * u[0];
+        for (int j = 1; j < D; ++j) s = DEV ? fmaX(p[i * D + j], u[j], s) : s + p[i * D + j] * u[j];
+        du[i] = s;
+      }
+      break;
+    }
+    default:
+      for (int i = 0; i < D; ++i) du[i] = (R)NAN;
+  }
+}
+
+/* ---------------------------------------------------------------- stage algebra */
+struct Term { double c; int k; };
+
+template <class P>
+struct Alg {
+  typedef typename P::R R;
+  typedef typename P::T T;
+  int D, rhs;
+  R p[MAXP];
+
+  void f(const R* u, double t, R* du) const { rhs_eval<R, P::DEV>(rhs, D, u, p, t, du); }
+
+  /* s = sum_j c_j k_j, accumulated from the last term to the first. */
+  void lc(const Term* tm, int nt, R (*k)[MAXD], R* s) const {
+    for (int d = 0; d < D; ++d) s[d] = (R)tm[nt - 1].c * k[tm[nt - 1].k][d];
+    for (int j = nt - 2; j >= 0; --j)
+      for (int d = 0; d < D; ++d) s[d] = vmadd<P::DEV>((R)tm[j].c, k[tm[j].k][d], s[d]);
+  }
+  /* out = base + h * s */
+  void axpy(const R* base, R h, const R* s, R* out) const {
+    for (int d = 0; d < D; ++d) out[d] = vmadd<P::DEV>(h, s[d], base[d]);
+  }
+  /* stage time t + c*dt (a scalar muladd, fused in Julia too) */
+  static T st(T t, double c, T dt) { return fmaX((T)c, dt, t); }
+};
+
+/* Compensated state: value = hi - c in KAHAN mode, hi otherwise. */
+template <class R>
+struct State { R hi[MAXD]; R c[MAXD]; };
+
+template <class P>
+static void state_update(int D, const State<typename P::R>& a, typename P::R h,
+                         const typename P::R* s, State<typename P::R>& out) {
+  typedef typename P::R R;
+  for (int d = 0; d < D; ++d) {
+    if (P::KAHAN) {
+      R delta = h * s[d];
+      R y = delta - a.c[d];
+      R sum = a.hi[d] + y;
+      out.c[d] = (sum - a.hi[d]) - y;
+      out.hi[d] = sum;
+    } else {
+      out.hi[d] = vmadd<P::DEV>(h, s[d], a.hi[d]);
+      out.c[d] = 0;
+    }
+  }
+}
+
+/* Horner evaluation of c0 + c1 x + ... with leading zero coefficients, as
+ * @evalpoly does it (scalar muladd, fused). nz = number of leading zeros. */
+template <class R>
+static R horner(R x, const double* c, int n, int nz) {
+  R ex = (R)c[n - 1];
+  for (int i = n - 2; i >= 0; --i) ex = fmaX(x, ex, (R)c[i]);
+  for (int i = 0; i < nz; ++i) ex = x * ex;
+  return ex;
+}
+
+/* ---------------------------------------------------------------- tableaus */
+namespace t5 = gbtab::tsit5;
+namespace v7 = gbtab::vern7;
+namespace v7x = gbtab::vern7x;
+namespace v7r = gbtab::vern7r;
+namespace v9 = gbtab::vern9;
+namespace v9x = gbtab::vern9x;
+namespace v9r = gbtab::vern9r;
+
+/* ---- Tsitouras 5(4), src/tsit5/gpuatsit5.jl:258-275 (k slots 0..6 = k1..k7) */
+const Term T5_S3[] = {{t5::a31, 0}, {t5::a32, 1}};
+const Term T5_S4[] = {{t5::a41, 0}, {t5::a42, 1}, {t5::a43, 2}};
+const Term T5_S5[] = {{t5::a51, 0}, {t5::a52, 1}, {t5::a53, 2}, {t5::a54, 3}};
+const Term T5_S6[] = {{t5::a61, 0}, {t5::a62, 1}, {t5::a63, 2}, {t5::a64, 3}, {t5::a65, 4}};
+const Term T5_U[] = {{t5::a71, 0}, {t5::a72, 1}, {t5::a73, 2}, {t5::a74, 3}, {t5::a75, 4}, {t5::a76, 5}};
+const Term T5_E[] = {{t5::btilde1, 0}, {t5::btilde2, 1}, {t5::btilde3, 2}, {t5::btilde4, 3},
+                     {t5::btilde5, 4}, {t5::btilde6, 5}, {t5::btilde7, 6}};
+/* SimpleTsit5 groups the update as ((a71 k1 + .. + a74 k4) + a75 k5 + a76 k6), src/tsit5/tsit5.jl:335-336 */
+const Term T5_U_IN[] = {{t5::a71, 0}, {t5::a72, 1}, {t5::a73, 2}, {t5::a74, 3}};
+
+/* bθs of src/tsit5/tsit5.jl:385-399: b1θ = poly(0, r11..r14), b_iθ = poly(0, 0, r_i2..r_i4) */
+template <class R>
+static void tsit5_btheta(R th, R* b) {
+  const double c1[] = {t5::r11, t5::r12, t5::r13, t5::r14};
+  const double c2[] = {t5::r22, t5::r23, t5::r24};
+  const double c3[] = {t5::r32, t5::r33, t5::r34};
+  const double c4[] = {t5::r42, t5::r43, t5::r44};
+  const double c5[] = {t5::r52, t5::r53, t5::r54};
+  const double c6[] = {t5::r62, t5::r63, t5::r64};
+  const double c7[] = {t5::r72, t5::r73, t5::r74};
+  b[0] = horner(th, c1, 4, 1);
+  b[1] = horner(th, c2, 3, 2);
+  b[2] = horner(th, c3, 3, 2);
+  b[3] = horner(th, c4, 3, 2);
+  b[4] = horner(th, c5, 3, 2);
+  b[5] = horner(th, c6, 3, 2);
+  b[6] = horner(th, c7, 3, 2);
+}
+
+/* ---- Verner 7(6), src/verner/gpuvern7.jl:360-404 (slots 0..9 = k1..k10) */
+const Term V7_S3[] = {{v7::a031, 0}, {v7::a032, 1}};
+const Term V7_S4[] = {{v7::a041, 0}, {v7::a043, 2}};
+const Term V7_S5[] = {{v7::a051, 0}, {v7::a053, 2}, {v7::a054, 3}};
+const Term V7_S6[] = {{v7::a061, 0}, {v7::a063, 2}, {v7::a064, 3}, {v7::a065, 4}};
+const Term V7_S7[] = {{v7::a071, 0}, {v7::a073, 2}, {v7::a074, 3}, {v7::a075, 4}, {v7::a076, 5}};
+const Term V7_S8[] = {{v7::a081, 0}, {v7::a083, 2}, {v7::a084, 3}, {v7::a085, 4}, {v7::a086, 5}, {v7::a087, 6}};
+const Term V7_G9[] = {{v7::a091, 0}, {v7::a093, 2}, {v7::a094, 3}, {v7::a095, 4}, {v7::a096, 5},
+                      {v7::a097, 6}, {v7::a098, 7}};
+const Term V7_G10[] = {{v7::a101, 0}, {v7::a103, 2}, {v7::a104, 3}, {v7::a105, 4}, {v7::a106, 5}, {v7::a107, 6}};
+const Term V7_U[] = {{v7::b1, 0}, {v7::b4, 3}, {v7::b5, 4}, {v7::b6, 5}, {v7::b7, 6}, {v7::b8, 7}, {v7::b9, 8}};
+const Term V7_E[] = {{v7::btilde1, 0}, {v7::btilde4, 3}, {v7::btilde5, 4}, {v7::btilde6, 5},
+                     {v7::btilde7, 6}, {v7::btilde8, 7}, {v7::btilde9, 8}, {v7::btilde10, 9}};
+/* extra stages for dense output, gpuvern7.jl:441-504 (slots 10..15 = k11..k16) */
+const Term V7_X11[] = {{v7x::a1101, 0}, {v7x::a1104, 3}, {v7x::a1105, 4}, {v7x::a1106, 5},
+                       {v7x::a1107, 6}, {v7x::a1108, 7}, {v7x::a1109, 8}};
+const Term V7_X12[] = {{v7x::a1201, 0}, {v7x::a1204, 3}, {v7x::a1205, 4}, {v7x::a1206, 5},
+                       {v7x::a1207, 6}, {v7x::a1208, 7}, {v7x::a1209, 8}, {v7x::a1211, 10}};
+const Term V7_X13[] = {{v7x::a1301, 0}, {v7x::a1304, 3}, {v7x::a1305, 4}, {v7x::a1306, 5}, {v7x::a1307, 6},
+                       {v7x::a1308, 7}, {v7x::a1309, 8}, {v7x::a1311, 10}, {v7x::a1312, 11}};
+const Term V7_X14[] = {{v7x::a1401, 0}, {v7x::a1404, 3}, {v7x::a1405, 4}, {v7x::a1406, 5}, {v7x::a1407, 6},
+                       {v7x::a1408, 7}, {v7x::a1409, 8}, {v7x::a1411, 10}, {v7x::a1412, 11}, {v7x::a1413, 12}};
+const Term V7_X15[] = {{v7x::a1501, 0}, {v7x::a1504, 3}, {v7x::a1505, 4}, {v7x::a1506, 5}, {v7x::a1507, 6},
+                       {v7x::a1508, 7}, {v7x::a1509, 8}, {v7x::a1511, 10}, {v7x::a1512, 11}, {v7x::a1513, 12}};
+const Term V7_X16[] = {{v7x::a1601, 0}, {v7x::a1604, 3}, {v7x::a1605, 4}, {v7x::a1606, 5}, {v7x::a1607, 6},
+                       {v7x::a1608, 7}, {v7x::a1609, 8}, {v7x::a1611, 10}, {v7x::a1612, 11}, {v7x::a1613, 12}};
+const double V7_XC[] = {v7x::c11, v7x::c12, v7x::c13, v7x::c14, v7x::c15, v7x::c16};
+
+/* bθs of src/verner/verner_tableaus.jl:1337-1360; order b1,b4..b9,b11..b16 */
+template <class R>
+static void vern7_btheta(R th, R* b) {
+  const double r1[] = {v7r::r011, v7r::r012, v7r::r013, v7r::r014, v7r::r015, v7r::r016, v7r::r017};
+  const double r4[] = {v7r::r042, v7r::r043, v7r::r044, v7r::r045, v7r::r046, v7r::r047};
+  const double r5[] = {v7r::r052, v7r::r053, v7r::r054, v7r::r055, v7r::r056, v7r::r057};
+  const double r6[] = {v7r::r062, v7r::r063, v7r::r064, v7r::r065, v7r::r066, v7r::r067};
+  const double r7[] = {v7r::r072, v7r::r073, v7r::r074, v7r::r075, v7r::r076, v7r::r077};
+  const double r8[] = {v7r::r082, v7r::r083, v7r::r084, v7r::r085, v7r::r086, v7r::r087};
+  const double r9[] = {v7r::r092, v7r::r093, v7r::r094, v7r::r095, v7r::r096, v7r::r097};
+  const double r11[] = {v7r::r112, v7r::r113, v7r::r114, v7r::r115, v7r::r116, v7r::r117};
+  const double r12[] = {v7r::r122, v7r::r123, v7r::r124, v7r::r125, v7r::r126, v7r::r127};
+  const double r13[] = {v7r::r132, v7r::r133, v7r::r134, v7r::r135, v7r::r136, v7r::r137};
+  const double r14[] = {v7r::r142, v7r::r143, v7r::r144, v7r::r145, v7r::r146, v7r::r147};
+  const double r15[] = {v7r::r152, v7r::r153, v7r::r154, v7r::r155, v7r::r156, v7r::r157};
+  const double r16[] = {v7r::r162, v7r::r163, v7r::r164, v7r::r165, v7r::r166, v7r::r167};
+  b[0] = horner(th, r1, 7, 1);
+  const double* rs[] = {r4, r5, r6, r7, r8, r9, r11, r12, r13, r14, r15, r16};
+  for (int i = 0; i < 12; ++i) b[i + 1] = horner(th, rs[i], 6, 2);
+}
+
+/* ---- Verner 9(8), src/verner/gpuvern9.jl:468-573 (slots 0..15 = k1..k16) */
+const Term V9_S3[] = {{v9::a0301, 0}, {v9::a0302, 1}};
+const Term V9_S4[] = {{v9::a0401, 0}, {v9::a0403, 2}};
+const Term V9_S5[] = {{v9::a0501, 0}, {v9::a0503, 2}, {v9::a0504, 3}};
+const Term V9_S6[] = {{v9::a0601, 0}, {v9::a0604, 3}, {v9::a0605, 4}};
+const Term V9_S7[] = {{v9::a0701, 0}, {v9::a0704, 3}, {v9::a0705, 4}, {v9::a0706, 5}};
+const Term V9_S8[] = {{v9::a0801, 0}, {v9::a0806, 5}, {v9::a0807, 6}};
+const Term V9_S9[] = {{v9::a0901, 0}, {v9::a0906, 5}, {v9::a0907, 6}, {v9::a0908, 7}};
+const Term V9_S10[] = {{v9::a1001, 0}, {v9::a1006, 5}, {v9::a1007, 6}, {v9::a1008, 7}, {v9::a1009, 8}};
+const Term V9_S11[] = {{v9::a1101, 0}, {v9::a1106, 5}, {v9::a1107, 6}, {v9::a1108, 7}, {v9::a1109, 8}, {v9::a1110, 9}};
+const Term V9_S12[] = {{v9::a1201, 0}, {v9::a1206, 5}, {v9::a1207, 6}, {v9::a1208, 7}, {v9::a1209, 8},
+                       {v9::a1210, 9}, {v9::a1211, 10}};
+const Term V9_S13[] = {{v9::a1301, 0}, {v9::a1306, 5}, {v9::a1307, 6}, {v9::a1308, 7}, {v9::a1309, 8},
+                       {v9::a1310, 9}, {v9::a1311, 10}, {v9::a1312, 11}};
+const Term V9_S14[] = {{v9::a1401, 0}, {v9::a1406, 5}, {v9::a1407, 6}, {v9::a1408, 7}, {v9::a1409, 8},
+                       {v9::a1410, 9}, {v9::a1411, 10}, {v9::a1412, 11}, {v9::a1413, 12}};
+const Term V9_G15[] = {{v9::a1501, 0}, {v9::a1506, 5}, {v9::a1507, 6}, {v9::a1508, 7}, {v9::a1509, 8},
+                       {v9::a1510, 9}, {v9::a1511, 10}, {v9::a1512, 11}, {v9::a1513, 12}, {v9::a1514, 13}};
+const Term V9_G16[] = {{v9::a1601, 0}, {v9::a1606, 5}, {v9::a1607, 6}, {v9::a1608, 7}, {v9::a1609, 8},
+                       {v9::a1610, 9}, {v9::a1611, 10}, {v9::a1612, 11}, {v9::a1613, 12}};
+const Term V9_U[] = {{v9::b1, 0}, {v9::b8, 7}, {v9::b9, 8}, {v9::b10, 9}, {v9::b11, 10}, {v9::b12, 11},
+                     {v9::b13, 12}, {v9::b14, 13}, {v9::b15, 14}};
+const Term V9_E[] = {{v9::btilde1, 0}, {v9::btilde8, 7}, {v9::btilde9, 8}, {v9::btilde10, 9},
+                     {v9::btilde11, 10}, {v9::btilde12, 11}, {v9::btilde13, 12}, {v9::btilde14, 13},
+                     {v9::btilde15, 14}, {v9::btilde16, 15}};
+/* Dense-output stages, gpuvern9.jl:631-745 (adaptive) and :216-319 (fixed step).
+ * Slots: 0..8 hold the nine stages the formulas call k1..k9 and 16..25 hold the
+ * new stages k11..k20.  Which original stages sit in slots 1..8 depends on the
+ * caller: the adaptive solver relabels k2..k9 := k8..k15 first (:564-573), the
+ * fixed-step solver does not. */
+const Term V9_X17[] = {{v9x::a1701, 0}, {v9x::a1708, 1}, {v9x::a1709, 2}, {v9x::a1710, 3}, {v9x::a1711, 4},
+                       {v9x::a1712, 5}, {v9x::a1713, 6}, {v9x::a1714, 7}, {v9x::a1715, 8}};
+const Term V9_X18[] = {{v9x::a1801, 0}, {v9x::a1808, 1}, {v9x::a1809, 2}, {v9x::a1810, 3}, {v9x::a1811, 4},
+                       {v9x::a1812, 5}, {v9x::a1813, 6}, {v9x::a1814, 7}, {v9x::a1815, 8}, {v9x::a1817, 16}};
+const Term V9_X19[] = {{v9x::a1901, 0}, {v9x::a1908, 1}, {v9x::a1909, 2}, {v9x::a1910, 3}, {v9x::a1911, 4},
+                       {v9x::a1912, 5}, {v9x::a1913, 6}, {v9x::a1914, 7}, {v9x::a1915, 8}, {v9x::a1917, 16},
+                       {v9x::a1918, 17}};
+const Term V9_X20[] = {{v9x::a2001, 0}, {v9x::a2008, 1}, {v9x::a2009, 2}, {v9x::a2010, 3}, {v9x::a2011, 4},
+                       {v9x::a2012, 5}, {v9x::a2013, 6}, {v9x::a2014, 7}, {v9x::a2015, 8}, {v9x::a2017, 16},
+                       {v9x::a2018, 17}, {v9x::a2019, 18}};
+const Term V9_X21[] = {{v9x::a2101, 0}, {v9x::a2108, 1}, {v9x::a2109, 2}, {v9x::a2110, 3}, {v9x::a2111, 4},
+                       {v9x::a2112, 5}, {v9x::a2113, 6}, {v9x::a2114, 7}, {v9x::a2115, 8}, {v9x::a2117, 16},
+                       {v9x::a2118, 17}, {v9x::a2119, 18}, {v9x::a2120, 19}};
+const Term V9_X22[] = {{v9x::a2201, 0}, {v9x::a2208, 1}, {v9x::a2209, 2}, {v9x::a2210, 3}, {v9x::a2211, 4},
+                       {v9x::a2212, 5}, {v9x::a2213, 6}, {v9x::a2214, 7}, {v9x::a2215, 8}, {v9x::a2217, 16},
+                       {v9x::a2218, 17}, {v9x::a2219, 18}, {v9x::a2220, 19}, {v9x::a2221, 20}};
+const Term V9_X23[] = {{v9x::a2301, 0}, {v9x::a2308, 1}, {v9x::a2309, 2}, {v9x::a2310, 3}, {v9x::a2311, 4},
+                       {v9x::a2312, 5}, {v9x::a2313, 6}, {v9x::a2314, 7}, {v9x::a2315, 8}, {v9x::a2317, 16},
+                       {v9x::a2318, 17}, {v9x::a2319, 18}, {v9x::a2320, 19}, {v9x::a2321, 20}};
+const Term V9_X24[] = {{v9x::a2401, 0}, {v9x::a2408, 1}, {v9x::a2409, 2}, {v9x::a2410, 3}, {v9x::a2411, 4},
+                       {v9x::a2412, 5}, {v9x::a2413, 6}, {v9x::a2414, 7}, {v9x::a2415, 8}, {v9x::a2417, 16},
+                       {v9x::a2418, 17}, {v9x::a2419, 18}, {v9x::a2420, 19}, {v9x::a2421, 20}};
+const Term V9_X25[] = {{v9x::a2501, 0}, {v9x::a2508, 1}, {v9x::a2509, 2}, {v9x::a2510, 3}, {v9x::a2511, 4},
+                       {v9x::a2512, 5}, {v9x::a2513, 6}, {v9x::a2514, 7}, {v9x::a2515, 8}, {v9x::a2517, 16},
+                       {v9x::a2518, 17}, {v9x::a2519, 18}, {v9x::a2520, 19}, {v9x::a2521, 20}};
+const Term V9_X26[] = {{v9x::a2601, 0}, {v9x::a2608, 1}, {v9x::a2609, 2}, {v9x::a2610, 3}, {v9x::a2611, 4},
+                       {v9x::a2612, 5}, {v9x::a2613, 6}, {v9x::a2614, 7}, {v9x::a2615, 8}, {v9x::a2617, 16},
+                       {v9x::a2618, 17}, {v9x::a2619, 18}, {v9x::a2620, 19}, {v9x::a2621, 20}};
+const double V9_XC[] = {v9x::c17, v9x::c18, v9x::c19, v9x::c20, v9x::c21, v9x::c22, v9x::c23, v9x::c24,
+                        v9x::c25, v9x::c26};
+
+/* bθs of src/verner/verner_tableaus.jl:1362-1398; order b1,b8..b15,b17..b26 */
+template <class R>
+static void vern9_btheta(R th, R* b) {
+  const double r1[] = {v9r::r011, v9r::r012, v9r::r013, v9r::r014, v9r::r015, v9r::r016, v9r::r017, v9r::r018, v9r::r019};
+#define V9ROW(i) const double r##i[] = {v9r::r##i##2, v9r::r##i##3, v9r::r##i##4, v9r::r##i##5, \
+                                         v9r::r##i##6, v9r::r##i##7, v9r::r##i##8, v9r::r##i##9}
+  const double r8[] = {v9r::r082, v9r::r083, v9r::r084, v9r::r085, v9r::r086, v9r::r087, v9r::r088, v9r::r089};
+  const double r9[] = {v9r::r092, v9r::r093, v9r::r094, v9r::r095, v9r::r096, v9r::r097, v9r::r098, v9r::r099};
+  V9ROW(10); V9ROW(11); V9ROW(12); V9ROW(13); V9ROW(14); V9ROW(15);
+  V9ROW(17); V9ROW(18); V9ROW(19); V9ROW(20); V9ROW(21); V9ROW(22); V9ROW(23); V9ROW(24); V9ROW(25); V9ROW(26);
+#undef V9ROW
+  b[0] = horner(th, r1, 9, 1);
+  const double* rs[] = {r8, r9, r10, r11, r12, r13, r14, r15, r17, r18, r19, r20, r21, r22, r23, r24, r25, r26};
+  for (int i = 0; i < 18; ++i) b[i + 1] = horner(th, rs[i], 8, 2);
+}
+
+/* ---------------------------------------------------------------- methods */
+/* Each method provides:
+ *   NK, FSAL, DTMIN_1F7 (Vern9 uses 1f-7 for dtmin and the end snap)
+ *   attempt(): stages given k[0] (FSAL) or computing k[0]; the solution
+ *              update, and (adaptive) the error estimate.
+ *   dense():   one saveat point. */
+template <class P>
+struct Tsit5 {
+  typedef typename P::R R;
+  typedef typename P::T T;
+  static constexpr int NK = 7;
+  static constexpr bool FSAL = true;
+  static constexpr bool DTMIN_1F7 = false;
+
+  static void attempt(const Alg<P>& A, const State<R>& up, T t, T dt, R (*k)[MAXD], State<R>& u, R* e,
+                      bool want_err) {
+    R tmp[MAXD], s[MAXD];
+    const R h = (R)dt;
+    const R* uprev = up.hi;
+    const R a = (R)(dt * (T)t5::a21);  /* dt * a21, the scalar factor of the stage-2 update */
+    for (int d = 0; d < A.D; ++d) {
+      if (P::DEV) tmp[d] = fmaX(a, k[0][d], uprev[d]);
+      else tmp[d] = h * ((R)t5::a21 * k[0][d]) + uprev[d];
+    }
+    A.f(tmp, (double)A.st(t, t5::c1, dt), k[1]);
+    A.lc(T5_S3, 2, k, s); A.axpy(uprev, h, s, tmp); A.f(tmp, (double)A.st(t, t5::c2, dt), k[2]);
+    A.lc(T5_S4, 3, k, s); A.axpy(uprev, h, s, tmp); A.f(tmp, (double)A.st(t, t5::c3, dt), k[3]);
+    A.lc(T5_S5, 4, k, s); A.axpy(uprev, h, s, tmp); A.f(tmp, (double)A.st(t, t5::c4, dt), k[4]);
+    A.lc(T5_S6, 5, k, s); A.axpy(uprev, h, s, tmp); A.f(tmp, (double)(t + dt), k[5]);
+    A.lc(T5_U, 6, k, s);
+    state_update<P>(A.D, up, h, s, u);
+    A.f(u.hi, (double)(t + dt), k[6]);
+    if (want_err) {
+      A.lc(T5_E, 7, k, s);
+      for (int d = 0; d < A.D; ++d) e[d] = h * s[d];
+    }
+  }
+
+  /* src/tsit5/gpuatsit5.jl:306-314 */
+  static void dense(const Alg<P>& A, const State<R>& up, T told, T tnew, T dtold, T theta, R (*k)[MAXD],
+                    double* out) {
+    (void)told; (void)tnew;
+    R b[7], s[MAXD];
+    tsit5_btheta<R>((R)theta, b);
+    for (int d = 0; d < A.D; ++d) s[d] = b[6] * k[6][d];
+    for (int j = 5; j >= 0; --j)
+      for (int d = 0; d < A.D; ++d) s[d] = vmadd<P::DEV>(b[j], k[j][d], s[d]);
+    finish_dense(A, up, (R)dtold, s, out);
+  }
+
+  static void finish_dense(const Alg<P>& A, const State<R>& up, R h, const R* s, double* out) {
+    for (int d = 0; d < A.D; ++d) {
+      if (P::KAHAN) out[d] = ((double)up.hi[d] - (double)up.c[d]) + (double)(h * s[d]);
+      else out[d] = (double)vmadd<P::DEV>(h, s[d], up.hi[d]);
+    }
+  }
+};
+
+template <class P>
+static void dense_sum(const Alg<P>& A, const typename P::R* b, const int* slot, int n,
+                      typename P::R (*k)[MAXD], typename P::R* s) {
+  for (int d = 0; d < A.D; ++d) s[d] = b[n - 1] * k[slot[n - 1]][d];
+  for (int j = n - 2; j >= 0; --j)
+    for (int d = 0; d < A.D; ++d) s[d] = vmadd<P::DEV>(b[j], k[slot[j]][d], s[d]);
+}
+
+template <class P>
+struct Vern7 {
+  typedef typename P::R R;
+  typedef typename P::T T;
+  static constexpr int NK = 16;
+  static constexpr bool FSAL = false;
+  static constexpr bool DTMIN_1F7 = false;
+
+  static void attempt(const Alg<P>& A, const State<R>& up, T t, T dt, R (*k)[MAXD], State<R>& u, R* e,
+                      bool want_err) {
+    R tmp[MAXD], s[MAXD];
+    const R h = (R)dt;
+    const R* uprev = up.hi;
+    A.f(uprev, (double)t, k[0]);
+    const R a = (R)(dt * (T)v7::a021);
+    for (int d = 0; d < A.D; ++d) tmp[d] = vmadd<P::DEV>(a, k[0][d], uprev[d]);
+    A.f(tmp, (double)A.st(t, v7::c2, dt), k[1]);
+    A.lc(V7_S3, 2, k, s); A.axpy(uprev, h, s, tmp); A.f(tmp, (double)A.st(t, v7::c3, dt), k[2]);
+    A.lc(V7_S4, 2, k, s); A.axpy(uprev, h, s, tmp); A.f(tmp, (double)A.st(t, v7::c4, dt), k[3]);
+    A.lc(V7_S5, 3, k, s); A.axpy(uprev, h, s, tmp); A.f(tmp, (double)A.st(t, v7::c5, dt), k[4]);
+    A.lc(V7_S6, 4, k, s); A.axpy(uprev, h, s, tmp); A.f(tmp, (double)A.st(t, v7::c6, dt), k[5]);
+    A.lc(V7_S7, 5, k, s); A.axpy(uprev, h, s, tmp); A.f(tmp, (double)A.st(t, v7::c7, dt), k[6]);
+    A.lc(V7_S8, 6, k, s); A.axpy(uprev, h, s, tmp); A.f(tmp, (double)A.st(t, v7::c8, dt), k[7]);
+    R g10[MAXD];
+    A.lc(V7_G9, 7, k, s); A.axpy(uprev, h, s, tmp);
+    A.lc(V7_G10, 6, k, s); A.axpy(uprev, h, s, g10);
+    A.f(tmp, (double)(t + dt), k[8]);
+    A.f(g10, (double)(t + dt), k[9]);
+    A.lc(V7_U, 7, k, s);
+    state_update<P>(A.D, up, h, s, u);
+    if (want_err) {
+      A.lc(V7_E, 8, k, s);
+      for (int d = 0; d < A.D; ++d) e[d] = h * s[d];
+    }
+  }
+
+  /* gpuvern7.jl:441-513 (adaptive; stage times use the advanced t) and
+   * :153-219 (fixed step, same expressions with dt). */
+  static void dense(const Alg<P>& A, const State<R>& up, T told, T tnew, T dtold, T theta, R (*k)[MAXD],
+                    double* out) {
+    (void)told;
+    const R h = (R)dtold;
+    R b[13], s[MAXD], tmp[MAXD];
+    vern7_btheta<R>((R)theta, b);
+    const Term* xs[] = {V7_X11, V7_X12, V7_X13, V7_X14, V7_X15, V7_X16};
+    const int nx[] = {7, 8, 9, 10, 10, 10};
+    for (int i = 0; i < 6; ++i) {
+      A.lc(xs[i], nx[i], k, s);
+      A.axpy(up.hi, h, s, tmp);
+      A.f(tmp, (double)A.st(tnew, V7_XC[i], dtold), k[10 + i]);
+    }
+    static const int slot[13] = {0, 3, 4, 5, 6, 7, 8, 10, 11, 12, 13, 14, 15};
+    dense_sum<P>(A, b, slot, 13, k, s);
+    Tsit5<P>::finish_dense(A, up, h, s, out);
+  }
+};
+
+template <class P, bool ADAPTIVE>
+struct Vern9 {
+  typedef typename P::R R;
+  typedef typename P::T T;
+  static constexpr int NK = 26;
+  static constexpr bool FSAL = false;
+  static constexpr bool DTMIN_1F7 = true;
+
+  static void attempt(const Alg<P>& A, const State<R>& up, T t, T dt, R (*k)[MAXD], State<R>& u, R* e,
+                      bool want_err) {
+    R tmp[MAXD], s[MAXD];
+    const R h = (R)dt;
+    const R* uprev = up.hi;
+    A.f(uprev, (double)t, k[0]);
+    const R a = (R)(dt * (T)v9::a0201);
+    for (int d = 0; d < A.D; ++d) tmp[d] = vmadd<P::DEV>(a, k[0][d], uprev[d]);
+    A.f(tmp, (double)A.st(t, v9::c1, dt), k[1]);
+    const Term* ss[] = {V9_S3, V9_S4, V9_S5, V9_S6, V9_S7, V9_S8, V9_S9, V9_S10, V9_S11, V9_S12, V9_S13, V9_S14};
+    const int ns[] = {2, 2, 3, 3, 4, 3, 4, 5, 6, 7, 8, 9};
+    const double cs[] = {v9::c2, v9::c3, v9::c4, v9::c5, v9::c6, v9::c7, v9::c8, v9::c9, v9::c10, v9::c11,
+                         v9::c12, v9::c13};
+    for (int i = 0; i < 12; ++i) {
+      A.lc(ss[i], ns[i], k, s);
+      A.axpy(uprev, h, s, tmp);
+      A.f(tmp, (double)A.st(t, cs[i], dt), k[2 + i]);
+    }
+    R g16[MAXD];
+    A.lc(V9_G15, 10, k, s); A.axpy(uprev, h, s, tmp);
+    if (ADAPTIVE) { A.lc(V9_G16, 9, k, s); A.axpy(uprev, h, s, g16); }
+    A.f(tmp, (double)(t + dt), k[14]);
+    if (ADAPTIVE) A.f(g16, (double)(t + dt), k[15]);
+    A.lc(V9_U, 9, k, s);
+    state_update<P>(A.D, up, h, s, u);
+    if (want_err) {
+      A.lc(V9_E, 10, k, s);
+      for (int d = 0; d < A.D; ++d) e[d] = h * s[d];
+    }
+  }
+
+  /* Adaptive: gpuvern9.jl:564-573 relabels k2..k9 := k8..k15 and the dense
+   * stages run at told + c*dtold (:631-757).  Fixed step: no relabel, stage
+   * times t + c*dt with the advanced t (:216-331). */
+  static void dense(const Alg<P>& A, const State<R>& up, T told, T tnew, T dtold, T theta, R (*k)[MAXD],
+                    double* out) {
+    const R h = (R)dtold;
+    R kk[MAXK][MAXD];
+    for (int d = 0; d < A.D; ++d) kk[0][d] = k[0][d];
+    for (int j = 1; j <= 8; ++j)
+      for (int d = 0; d < A.D; ++d) kk[j][d] = ADAPTIVE ? k[j + 6][d] : k[j][d];
+    R b[19], s[MAXD], tmp[MAXD];
+    vern9_btheta<R>((R)theta, b);
+    const Term* xs[] = {V9_X17, V9_X18, V9_X19, V9_X20, V9_X21, V9_X22, V9_X23, V9_X24, V9_X25, V9_X26};
+    const int nx[] = {9, 10, 11, 12, 13, 14, 14, 14, 14, 14};
+    const T tb = ADAPTIVE ? told : tnew;
+    for (int i = 0; i < 10; ++i) {
+      A.lc(xs[i], nx[i], kk, s);
+      A.axpy(up.hi, h, s, tmp);
+      A.f(tmp, (double)A.st(tb, V9_XC[i], dtold), kk[16 + i]);
+    }
+    static const int slot[19] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 16, 17, 18, 19, 20, 21, 22, 23, 24, 25};
+    dense_sum<P>(A, b, slot, 19, kk, s);
+    Tsit5<P>::finish_dense(A, up, h, s, out);
+  }
+};
+
+template <class P>
+struct RK4 {
+  typedef typename P::R R;
+  typedef typename P::T T;
+  /* src/rk4/gpurk4.jl:73-84; t is the END of the step (ts[i]) */
+  static void step(const Alg<P>& A, const State<R>& up, T t, T dt, State<R>& u) {
+    R k1[MAXD], k2[MAXD], k3[MAXD], k4[MAXD], tmp[MAXD], s[MAXD];
+    const R h = (R)dt;
+    const R half = (R)0.5, sixth = (R)(1.0 / 6.0);
+    const R* uprev = up.hi;
+    A.f(uprev, (double)t, k1);
+    const R hh = h * half;
+    for (int d = 0; d < A.D; ++d) tmp[d] = P::DEV ? fmaX(hh, k1[d], uprev[d]) : h * (half * k1[d]) + uprev[d];
+    A.f(tmp, (double)fmaX((T)0.5, dt, t), k2);
+    for (int d = 0; d < A.D; ++d) tmp[d] = P::DEV ? fmaX(hh, k2[d], uprev[d]) : h * (half * k2[d]) + uprev[d];
+    A.f(tmp, (double)fmaX((T)0.5, dt, t), k3);
+    for (int d = 0; d < A.D; ++d) tmp[d] = vmadd<P::DEV>(h, k3[d], uprev[d]);
+    A.f(tmp, (double)(t + dt), k4);
+    for (int d = 0; d < A.D; ++d) {
+      /* k1 + 2k2 + 2k3 + k4: the doublings are exact, both forms round alike */
+      R sum = k1[d] + k4[d];
+      sum = vmadd<P::DEV>((R)2, k3[d], sum);
+      sum = vmadd<P::DEV>((R)2, k2[d], sum);
+      s[d] = P::DEV ? sum : sixth * sum;
+    }
+    if (P::DEV) {
+      State<R> tmpu;
+      state_update<P>(A.D, up, h * sixth, s, tmpu);
+      u = tmpu;
+    } else {
+      for (int d = 0; d < A.D; ++d) { u.hi[d] = h * s[d] + uprev[d]; u.c[d] = 0; }
+    }
+  }
+};
+
+/* ---------------------------------------------------------------- drivers */
+struct Job {
+  const oracle_args* a;
+  oracle_out* o;
+};
+
+template <class P>
+static void load_traj(const oracle_args* a, int64_t i, Alg<P>& A, State<typename P::R>& st) {
+  typedef typename P::R R;
+  A.D = a->dim;
+  A.rhs = a->rhs;
+  for (int j = 0; j < a->nparams; ++j) A.p[j] = (R)a->p[(int64_t)j * a->n + i];
+  for (int d = 0; d < a->dim; ++d) {
+    st.hi[d] = (R)a->u0[(int64_t)d * a->n + i];
+    st.c[d] = 0;
+  }
+}
+
+static inline void put_us(const oracle_args* a, oracle_out* o, int64_t i, int64_t j, const double* v) {
+  if (!o->us) return;
+  for (int d = 0; d < a->dim; ++d) o->us[(j * a->dim + d) * a->n + i] = v[d];
+}
+
+template <class R>
+static void value_of(const State<R>& s, int D, bool kahan, double* v) {
+  for (int d = 0; d < D; ++d) v[d] = kahan ? (double)s.hi[d] - (double)s.c[d] : (double)s.hi[d];
+}
+
+template <class P>
+static void finish(const oracle_args* a, oracle_out* o, int64_t i, const State<typename P::R>& st,
+                   typename P::T t, int ret, int32_t nacc, int32_t nrej, double dtf) {
+  double v[MAXD];
+  value_of(st, a->dim, P::KAHAN, v);
+  if (o->u_final)
+    for (int d = 0; d < a->dim; ++d) o->u_final[(int64_t)d * a->n + i] = v[d];
+  if (o->t_final) o->t_final[i] = (double)t;
+  if (o->retcode) o->retcode[i] = (int8_t)ret;
+  if (o->naccept) o->naccept[i] = nacc;
+  if (o->nreject) o->nreject[i] = nrej;
+  if (o->dt_first) o->dt_first[i] = dtf;
+}
+
+/* Adaptive driver: the loop of gpuatsit5.jl:250-320 / gpuvern7.jl:353-520 /
+ * gpuvern9.jl:461-763 with the controller of :279-299. */
+template <class P, class M>
+static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
+  typedef typename P::R R;
+  typedef typename P::T T;
+  Alg<P> A;
+  State<R> st, un;
+  load_traj<P>(a, i, A, st);
+  const int D = a->dim;
+  T t = (T)a->t0;
+  const T tf = (T)a->tf;
+  T dt = (T)(a->dt0 ? a->dt0[i] : a->dt);
+  const R abstol = (R)a->abstol, reltol = (R)a->reltol;
+  /* controller constants, build_adaptive_controller_cache(eltype(u0)) */
+  const R beta1 = (R)(7.0 / 50.0), beta2 = (R)(2.0 / 25.0), qmax = (R)10.0, qmin = (R)(1.0 / 5.0),
+          gamma = (R)(9.0 / 10.0), qoldinit = (R)1.0e-4;
+  /* single-precision controller of the device canon */
+  const float B1 = (float)(7.0 / 50.0), B2 = (float)(2.0 / 25.0), QMAXI = 0.1f, QMINI = 5.0f,
+              GAM = (float)(9.0 / 10.0), QOLDINIT = (float)1.0e-4;
+  R qold = qoldinit;
+  float qoldp = oracle_pow::ctrl_pow(QOLDINIT, B2);
+  const double dtmin = M::DTMIN_1F7 ? (double)1.0e-7f : 1.0e-14;
+
+  int64_t cur = 0;
+  const int64_t P_ = a->saveat ? a->nsave : 0;
+  double tmpv[MAXD];
+  if (P_ > 0 && (T)a->saveat[0] == (T)a->t0) {
+    value_of(st, D, P::KAHAN, tmpv);
+    put_us(a, o, i, 0, tmpv);
+    cur = 1;
+  }
+  R k[MAXK][MAXD], e[MAXD];
+  if (M::FSAL) A.f(st.hi, (double)t, k[0]);
+  int ret = RET_DEFAULT;
+  int32_t nacc = 0, nrej = 0;
+  int64_t attempts = 0;
+  double dt_first = NAN;
+  bool saw_nan = false;
+
+  while (t < tf) {
+    const State<R> up = st;
+    R EEst = (R)INFINITY;
+    while (EEst > (R)1) {
+      if ((double)dt < dtmin) { ret = RET_DTMIN; goto done; }
+      if (a->maxiters > 0 && attempts >= a->maxiters) { ret = RET_MAXITERS; goto done; }
+      M::attempt(A, up, t, dt, k, un, e, true);
+      ++attempts;
+      /* error norm: RMS of e ./ (abstol .+ max.(|uprev|, |u|) * reltol) */
+      R acc = 0;
+      for (int d = 0; d < D; ++d) {
+        R m = jmax(std::fabs(up.hi[d]), std::fabs(un.hi[d]));
+        R sc = P::DEV ? fmaX(m, reltol, abstol) : abstol + m * reltol;
+        R r = e[d] / sc;
+        if (d == 0) acc = r * r;
+        else acc = P::DEV ? fmaX(r, r, acc) : acc + r * r;
+      }
+      EEst = std::sqrt(acc / (R)D);
+      if (EEst != EEst) saw_nan = true;
+
+      if (!P::DEV) {
+        R q11 = std::pow(EEst, beta1);
+        R q = (EEst == (R)0) ? (R)1 / qmax : q11 / std::pow(qold, beta2);
+        if (EEst > (R)1) {
+          dt = dt / (T)jmin((R)1 / qmin, q11 / gamma);
+          ++nrej;
+        } else {
+          q = fmax_((R)1 / qmax, fmin_((R)1 / qmin, q / gamma));
+          qold = jmax(EEst, qoldinit);
+          const T dtold = dt;
+          dt = dt / (T)q;
+          dt = jmin((T)std::fabs(dt), (T)std::fabs(tf - t - dtold));
+          const T told = t;
+          if ((double)(tf - t - dtold) < dtmin) t = tf;
+          else t += dtold;
+          if (nacc == 0) dt_first = (double)dtold;
+          ++nacc;
+          while (cur < P_ && (T)a->saveat[cur] <= t) {
+            const T savet = (T)a->saveat[cur];
+            const T theta = (savet - told) / dtold;
+            M::dense(A, up, told, t, dtold, theta, k, tmpv);
+            put_us(a, o, i, cur, tmpv);
+            ++cur;
+          }
+          st = un;
+          if (M::FSAL)
+            for (int d = 0; d < D; ++d) k[0][d] = k[6][d];
+        }
+      } else {
+        const float Ef = (float)EEst;
+        const float q11 = oracle_pow::ctrl_pow(Ef, B1);
+        if (EEst > (R)1) {
+          const float fac = jmin(QMINI, q11 / GAM);
+          dt = dt * (T)(1.0f / fac);
+          ++nrej;
+        } else {
+          float q = (EEst == (R)0) ? QMAXI : q11 / qoldp;
+          q = fmax_(QMAXI, fmin_(QMINI, q / GAM));
+          const float qoldf = jmax(Ef, QOLDINIT);
+          qoldp = oracle_pow::ctrl_pow(qoldf, B2);
+          const T dtold = dt;
+          const T dtn = dt * (T)(1.0f / q);
+          dt = jmin((T)std::fabs(dtn), (T)std::fabs(tf - t - dtold));
+          const T told = t;
+          if ((double)(tf - t - dtold) < dtmin) t = tf;
+          else t += dtold;
+          if (nacc == 0) dt_first = (double)dtold;
+          ++nacc;
+          while (cur < P_ && (T)a->saveat[cur] <= t) {
+            const T savet = (T)a->saveat[cur];
+            const T theta = (savet - told) / dtold;
+            M::dense(A, up, told, t, dtold, theta, k, tmpv);
+            put_us(a, o, i, cur, tmpv);
+            ++cur;
+          }
+          st = un;
+          if (M::FSAL)
+            for (int d = 0; d < D; ++d) k[0][d] = k[6][d];
+        }
+      }
+    }
+  }
+done:
+  if (ret == RET_DEFAULT && saw_nan) ret = RET_NAN;
+  for (; cur < P_; ++cur) {
+    for (int d = 0; d < D; ++d) tmpv[d] = NAN;
+    put_us(a, o, i, cur, tmpv);
+  }
+  finish<P>(a, o, i, st, t, ret, nacc, nrej, dt_first);
+}
+
+/* Fixed-step driver: gpuatsit5.jl:92-129 / gpuvern7.jl:101-224 / gpuvern9.jl:99-335. */
+template <class P, class M>
+static void solve_fixed(const oracle_args* a, oracle_out* o, int64_t i) {
+  typedef typename P::R R;
+  typedef typename P::T T;
+  Alg<P> A;
+  State<R> st, un;
+  load_traj<P>(a, i, A, st);
+  const int D = a->dim;
+  const T dt = (T)a->dt;
+  T t = (T)a->t0;
+  int64_t cur = 0;
+  const int64_t P_ = a->saveat ? a->nsave : 0;
+  double tmpv[MAXD];
+  if (P_ > 0 && (T)a->saveat[0] == (T)a->t0) {
+    value_of(st, D, P::KAHAN, tmpv);
+    put_us(a, o, i, 0, tmpv);
+    cur = 1;
+  }
+  const bool every = (P_ == 0) && a->save_everystep;
+  if (every) { value_of(st, D, P::KAHAN, tmpv); put_us(a, o, i, 0, tmpv); }
+  R k[MAXK][MAXD], e[MAXD];
+  if (M::FSAL) A.f(st.hi, (double)t, k[0]);
+  for (int64_t g = 1; g < a->ngrid; ++g) {
+    const State<R> up = st;
+    t = (T)a->grid[g - 1];
+    M::attempt(A, up, t, dt, k, un, e, false);
+    t += dt;
+    st = un;
+    if (every) { value_of(st, D, P::KAHAN, tmpv); put_us(a, o, i, g, tmpv); }
+    while (cur < P_ && (T)a->saveat[cur] <= t) {
+      const T savet = (T)a->saveat[cur];
+      const T theta = (savet - (t - dt)) / dt;
+      M::dense(A, up, t - dt, t, dt, theta, k, tmpv);
+      put_us(a, o, i, cur, tmpv);
+      ++cur;
+    }
+    if (M::FSAL)
+      for (int d = 0; d < D; ++d) k[0][d] = k[6][d];
+  }
+  for (; cur < P_; ++cur) {
+    for (int d = 0; d < D; ++d) tmpv[d] = NAN;
+    put_us(a, o, i, cur, tmpv);
+  }
+  const int32_t steps = a->ngrid > 0 ? (int32_t)(a->ngrid - 1) : 0;
+  finish<P>(a, o, i, st, t, RET_DEFAULT, steps, 0, steps > 0 ? (double)dt : NAN);
+}
+
+/* GPUSimpleRK4, gpurk4.jl:53-98: saves every grid point (us[1] = u0). */
+template <class P>
+static void solve_rk4(const oracle_args* a, oracle_out* o, int64_t i) {
+  typedef typename P::R R;
+  typedef typename P::T T;
+  Alg<P> A;
+  State<R> st, un;
+  load_traj<P>(a, i, A, st);
+  const T dt = (T)a->dt;
+  double tmpv[MAXD];
+  const bool every = a->save_everystep != 0;
+  if (every) { value_of(st, a->dim, P::KAHAN, tmpv); put_us(a, o, i, 0, tmpv); }
+  T t = (T)a->t0;
+  for (int64_t g = 1; g < a->ngrid; ++g) {
+    t = (T)a->grid[g];
+    RK4<P>::step(A, st, t, dt, un);
+    st = un;
+    if (every) { value_of(st, a->dim, P::KAHAN, tmpv); put_us(a, o, i, g, tmpv); }
+  }
+  const int32_t steps = a->ngrid > 0 ? (int32_t)(a->ngrid - 1) : 0;
+  finish<P>(a, o, i, st, t, RET_DEFAULT, steps, 0, steps > 0 ? (double)dt : NAN);
+}
+
+/* SimpleATsit5 in integrator form (src/tsit5/atsit5.jl), double precision:
+ * simpleatsit5_init :181-196, OOP step! :322-413, interpolation :705-732 and
+ * the saveat loop of __solve :140-161. */
+struct SAT5I {
+  double uprev[MAXD], u[MAXD], tprev, t, tf, dt, dtnew, qold, abstol, reltol;
+  double ks[7][MAXD];
+  bool u_modified;
+};
+
+template <class P>
+static int simple_atsit5_step(const Alg<P>& A, SAT5I& it, int64_t& attempts, int64_t maxiters,
+                              int32_t& nacc, int32_t& nrej, double& dt_first, bool& saw_nan) {
+  const int D = A.D;
+  const double beta1 = 7.0 / 50.0, beta2 = 2.0 / 25.0, qmax = 10.0, qmin = 1.0 / 5.0, gamma = 9.0 / 10.0,
+               qoldinit = 1.0e-4;
+  double dt = it.dtnew;
+  const double t = it.t;
+  for (int d = 0; d < D; ++d) it.uprev[d] = it.u[d];
+  double k[MAXK][MAXD];
+  if (it.u_modified) {
+    A.f(it.uprev, t, k[0]);
+    it.u_modified = false;
+  } else {
+    for (int d = 0; d < D; ++d) k[0][d] = it.ks[6][d];
+  }
+  State<double> up, un;
+  for (int d = 0; d < D; ++d) { up.hi[d] = it.uprev[d]; up.c[d] = 0; }
+  double e[MAXD];
+  double EEst = INFINITY;
+  double qold = it.qold;
+  while (EEst > 1) {
+    if (dt < 1.0e-14) return RET_DTMIN;
+    if (maxiters > 0 && attempts >= maxiters) return RET_MAXITERS;
+    Tsit5<P>::attempt(A, up, t, dt, k, un, e, true);
+    ++attempts;
+    double acc = 0;
+    for (int d = 0; d < D; ++d) {
+      double m = jmax(std::fabs(it.uprev[d]), std::fabs(un.hi[d]));
+      double sc = P::DEV ? std::fma(m, it.reltol, it.abstol) : it.abstol + m * it.reltol;
+      double r = e[d] / sc;
+      acc = (d == 0) ? r * r : (P::DEV ? std::fma(r, r, acc) : acc + r * r);
+    }
+    EEst = std::sqrt(acc / (double)D);
+    if (EEst != EEst) saw_nan = true;
+    double q11 = std::pow(EEst, beta1);
+    double q = (EEst == 0) ? 1.0 / qmax : q11 / std::pow(qold, beta2);
+    if (EEst > 1) {
+      dt = dt / jmin(1.0 / qmin, q11 / gamma);
+      ++nrej;
+    } else {
+      q = fmax_(1.0 / qmax, fmin_(1.0 / qmin, q / gamma));
+      qold = jmax(EEst, qoldinit);
+      double dtnew = dt / q;
+      dtnew = jmin(std::fabs(dtnew), std::fabs(it.tf - t - dt));
+      for (int j = 0; j < 7; ++j)
+        for (int d = 0; d < D; ++d) it.ks[j][d] = k[j][d];
+      it.dt = dt;
+      it.dtnew = dtnew;
+      it.qold = qold;
+      it.tprev = t;
+      for (int d = 0; d < D; ++d) it.u[d] = un.hi[d];
+      if ((it.tf - t - dt) < 1.0e-14) it.t = it.tf;
+      else it.t += dt;
+      if (nacc == 0) dt_first = dt;
+      ++nacc;
+    }
+  }
+  return RET_DEFAULT;
+}
+
+template <class P>
+static void solve_simple_atsit5(const oracle_args* a, oracle_out* o, int64_t i) {
+  Alg<P> A;
+  State<double> st;
+  load_traj<P>(a, i, A, st);
+  const int D = a->dim;
+  SAT5I it;
+  for (int d = 0; d < D; ++d) { it.u[d] = st.hi[d]; it.uprev[d] = st.hi[d]; }
+  it.t = it.tprev = a->t0;
+  it.tf = a->tf;
+  it.dt = it.dtnew = a->dt0 ? a->dt0[i] : a->dt;
+  it.qold = 1.0e-4;
+  it.abstol = a->abstol;
+  it.reltol = a->reltol;
+  it.u_modified = true;
+  int64_t cur = 0, attempts = 0;
+  const int64_t P_ = a->saveat ? a->nsave : 0;
+  double tmpv[MAXD];
+  if (P_ > 0 && a->saveat[0] == a->t0) { put_us(a, o, i, 0, it.u); cur = 1; }
+  int ret = RET_DEFAULT;
+  int32_t nacc = 0, nrej = 0;
+  double dt_first = NAN;
+  bool saw_nan = false;
+  while (it.t < a->tf) {
+    ret = simple_atsit5_step<P>(A, it, attempts, a->maxiters, nacc, nrej, dt_first, saw_nan);
+    if (ret != RET_DEFAULT) break;
+    while (cur < P_ && a->saveat[cur] <= it.t) {
+      /* integ(t): θ = (t - tprev)/dt, u = uprev + dt * Σ bθ_i ks_i */
+      const double theta = (a->saveat[cur] - it.tprev) / it.dt;
+      double b[7], s[MAXD];
+      tsit5_btheta<double>(theta, b);
+      for (int d = 0; d < D; ++d) s[d] = b[6] * it.ks[6][d];
+      for (int j = 5; j >= 0; --j)
+        for (int d = 0; d < D; ++d) s[d] = vmadd<P::DEV>(b[j], it.ks[j][d], s[d]);
+      for (int d = 0; d < D; ++d) tmpv[d] = vmadd<P::DEV>(it.dt, s[d], it.uprev[d]);
+      put_us(a, o, i, cur, tmpv);
+      ++cur;
+    }
+  }
+  if (ret == RET_DEFAULT && saw_nan) ret = RET_NAN;
+  for (; cur < P_; ++cur) {
+    for (int d = 0; d < D; ++d) tmpv[d] = NAN;
+    put_us(a, o, i, cur, tmpv);
+  }
+  for (int d = 0; d < D; ++d) st.hi[d] = it.u[d];
+  finish<P>(a, o, i, st, it.t, ret, nacc, nrej, dt_first);
+}
+
+/* SimpleTsit5 __solve (src/tsit5/tsit5.jl:84-122) with the OOP step! of :303-352;
+ * t accumulates with integ.t += dt.  Only the final state is reported. */
+template <class P>
+static void solve_simple_tsit5(const oracle_args* a, oracle_out* o, int64_t i) {
+  typedef typename P::R R;
+  typedef typename P::T T;
+  Alg<P> A;
+  State<R> st;
+  load_traj<P>(a, i, A, st);
+  const int D = a->dim;
+  const int64_t L = a->ngrid;
+  const bool ends_at_tf = L > 0 && a->grid[L - 1] == a->tf;
+  const int64_t n = ends_at_tf ? L : L + 1;
+  T t = (T)a->t0, dt = (T)a->dt;
+  R k[MAXK][MAXD], tmp[MAXD], s[MAXD];
+  bool u_modified = true;
+  auto step = [&](T h_) {
+    const R h = (R)h_;
+    R uprev[MAXD];
+    for (int d = 0; d < D; ++d) uprev[d] = st.hi[d];
+    if (u_modified) { A.f(uprev, (double)t, k[0]); u_modified = false; }
+    else for (int d = 0; d < D; ++d) k[0][d] = k[6][d];
+    const R a21 = (R)(h_ * (T)t5::a21);
+    for (int d = 0; d < D; ++d)
+      tmp[d] = P::DEV ? fmaX(a21, k[0][d], uprev[d]) : h * ((R)t5::a21 * k[0][d]) + uprev[d];
+    A.f(tmp, (double)A.st(t, t5::c1, h_), k[1]);
+    A.lc(T5_S3, 2, k, s); A.axpy(uprev, h, s, tmp); A.f(tmp, (double)A.st(t, t5::c2, h_), k[2]);
+    A.lc(T5_S4, 3, k, s); A.axpy(uprev, h, s, tmp); A.f(tmp, (double)A.st(t, t5::c3, h_), k[3]);
+    A.lc(T5_S5, 4, k, s); A.axpy(uprev, h, s, tmp); A.f(tmp, (double)A.st(t, t5::c4, h_), k[4]);
+    A.lc(T5_S6, 5, k, s); A.axpy(uprev, h, s, tmp); A.f(tmp, (double)(t + h_), k[5]);
+    /* ((a71 k1 + .. + a74 k4) + a75 k5 + a76 k6) */
+    A.lc(T5_U_IN, 4, k, s);
+    for (int d = 0; d < D; ++d) {
+      R acc = vmadd<P::DEV>((R)t5::a76, k[5][d], s[d]);
+      s[d] = vmadd<P::DEV>((R)t5::a75, k[4][d], acc);
+      st.hi[d] = vmadd<P::DEV>(h, s[d], uprev[d]);
+    }
+    A.f(st.hi, (double)(t + h_), k[6]);
+    t += h_;
+  };
+  for (int64_t g = 1; g <= n - 1; ++g) step(dt);
+  if (!ends_at_tf) step((T)a->tf - t);
+  const int32_t steps = (int32_t)(ends_at_tf ? n - 1 : n);
+  finish<P>(a, o, i, st, t, RET_DEFAULT, steps, 0, (double)dt);
+}
+
+/* ---------------------------------------------------------------- dispatch */
+template <class P>
+static void solve_range(const oracle_args* a, oracle_out* o, int64_t i0, int64_t i1) {
+  for (int64_t i = i0; i < i1; ++i) {
+    switch (a->alg) {
+      case ORACLE_RK4: solve_rk4<P>(a, o, i); break;
+      case ORACLE_TSIT5: solve_fixed<P, Tsit5<P>>(a, o, i); break;
+      case ORACLE_ATSIT5: solve_adaptive<P, Tsit5<P>>(a, o, i); break;
+      case ORACLE_VERN7: solve_fixed<P, Vern7<P>>(a, o, i); break;
+      case ORACLE_AVERN7: solve_adaptive<P, Vern7<P>>(a, o, i); break;
+      case ORACLE_VERN9: solve_fixed<P, Vern9<P, false>>(a, o, i); break;
+      case ORACLE_AVERN9: solve_adaptive<P, Vern9<P, true>>(a, o, i); break;
+      case ORACLE_SIMPLE_TSIT5: solve_simple_tsit5<P>(a, o, i); break;
+      default: break;
+    }
+  }
+}
+
+template <bool DEV>
+static void solve_range_prec(const oracle_args* a, oracle_out* o, int64_t i0, int64_t i1) {
+  if (a->alg == ORACLE_SIMPLE_ATSIT5) {
+    for (int64_t i = i0; i < i1; ++i) solve_simple_atsit5<Pol<double, double, false, DEV>>(a, o, i);
+    return;
+  }
+  switch (a->precision) {
+    case ORACLE_FP64: solve_range<Pol<double, double, false, DEV>>(a, o, i0, i1); break;
+    case ORACLE_FP32: solve_range<Pol<float, float, false, DEV>>(a, o, i0, i1); break;
+    case ORACLE_FP32_KAHAN: solve_range<Pol<float, double, true, DEV>>(a, o, i0, i1); break;
+    default: break;
+  }
+}
+
+}  // namespace
+
+extern "C" int oracle_solve(const oracle_args* a, oracle_out* o) {
+  if (!a || !o || a->n < 0 || a->dim < 1 || a->dim > MAXD || a->nparams < 0 || a->nparams > MAXP) return -1;
+  if (a->alg < 0 || a->alg > ORACLE_SIMPLE_TSIT5) return -1;
+  if (a->alg == ORACLE_SIMPLE_ATSIT5 && a->precision != ORACLE_FP64) return -1;
+  if (a->precision == ORACLE_FP32_KAHAN && a->rounding != ORACLE_ROUND_DEVICE) return -1;
+  const bool fixed = a->alg == ORACLE_RK4 || a->alg == ORACLE_TSIT5 || a->alg == ORACLE_VERN7 ||
+                     a->alg == ORACLE_VERN9 || a->alg == ORACLE_SIMPLE_TSIT5;
+  if (fixed && (!a->grid || a->ngrid < 1)) return -1;
+  if (a->rhs == ORACLE_R3BP && a->dim != 4) return -1;
+  if (a->rhs == ORACLE_LORENZ && a->dim != 3) return -1;
+  if (a->rhs == ORACLE_VDP && a->dim != 2) return -1;
+  int nt = a->nthreads > 0 ? a->nthreads : 1;
+  if ((int64_t)nt > a->n) nt = (int)std::max<int64_t>(1, a->n);
+  auto run = [&](int64_t i0, int64_t i1) {
+    if (a->rounding == ORACLE_ROUND_DEVICE) solve_range_prec<true>(a, o, i0, i1);
+    else solve_range_prec<false>(a, o, i0, i1);
+  };
+  if (nt == 1) {
+    run(0, a->n);
+    return 0;
+  }
+  std::vector<std::thread> th;
+  const int64_t chunk = (a->n + nt - 1) / nt;
+  for (int w = 0; w < nt; ++w) {
+    int64_t i0 = w * chunk, i1 = std::min<int64_t>(a->n, i0 + chunk);
+    if (i0 >= i1) break;
+    th.emplace_back(run, i0, i1);
+  }
+  for (auto& x : th) x.join();
+  return 0;
+}
+
+extern "C" float oracle_ctrl_pow(float x, float b) { return oracle_pow::ctrl_pow(x, b); }

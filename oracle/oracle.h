@@ -1,0 +1,67 @@
+/* CPU oracle for the ensemble solve: C ABI used by the tests and by the
+ * bench's CPU-baseline leg only.
+ *
+ * TEST INFRASTRUCTURE.  This is a plain C++ restatement of the reference's
+ * solver loops (SimpleDiffEq.jl, files cited in oracle.cpp).  The product
+ * library never links, loads or calls it.
+ */
+#pragma once
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum oracle_alg {
+  ORACLE_RK4 = 0,          /* GPUSimpleRK4           src/rk4/gpurk4.jl:53-98 */
+  ORACLE_TSIT5 = 1,        /* GPUSimpleTsit5         src/tsit5/gpuatsit5.jl:55-147 */
+  ORACLE_ATSIT5 = 2,       /* GPUSimpleATsit5        src/tsit5/gpuatsit5.jl:205-336 */
+  ORACLE_VERN7 = 3,        /* GPUSimpleVern7         src/verner/gpuvern7.jl:55-242 */
+  ORACLE_AVERN7 = 4,       /* GPUSimpleAVern7        src/verner/gpuvern7.jl:300-536 */
+  ORACLE_VERN9 = 5,        /* GPUSimpleVern9         src/verner/gpuvern9.jl:55-353 */
+  ORACLE_AVERN9 = 6,       /* GPUSimpleAVern9        src/verner/gpuvern9.jl:411-779 */
+  ORACLE_SIMPLE_ATSIT5 = 7,/* SimpleATsit5 integrator src/tsit5/atsit5.jl:117-179,322-413,705-732 */
+  ORACLE_SIMPLE_TSIT5 = 8  /* SimpleTsit5 integrator  src/tsit5/tsit5.jl:84-122,303-352 */
+};
+
+enum oracle_rhs { ORACLE_LORENZ = 0, ORACLE_VDP = 1, ORACLE_R3BP = 2, ORACLE_KURAMOTO = 3, ORACLE_LINEAR = 4 };
+enum oracle_prec { ORACLE_FP64 = 0, ORACLE_FP32 = 1, ORACLE_FP32_KAHAN = 2 };
+/* ORACLE_ROUND_REF: the rounding the reference's Julia code performs
+ * (@muladd on SVector falls back to separate multiply and add; libm pow).
+ * ORACLE_ROUND_DEVICE: the documented device rounding canon (explicit fused
+ * multiply-add chains, single-precision controller power). */
+enum oracle_round { ORACLE_ROUND_REF = 0, ORACLE_ROUND_DEVICE = 1 };
+
+typedef struct {
+  int alg, rhs, precision, rounding;
+  int64_t n;
+  int dim, nparams;
+  double t0, tf, dt, abstol, reltol;
+  const double* saveat;  /* [nsave] or NULL */
+  int64_t nsave;
+  int save_everystep;    /* fixed-step algorithms only: save every grid point */
+  const double* grid;    /* fixed-step time grid (elements of t0:dt:tf), [ngrid] */
+  int64_t ngrid;
+  int64_t maxiters;      /* attempts per trajectory; <= 0 means unlimited */
+  const double* u0;      /* SoA [dim][n] */
+  const double* p;       /* SoA [nparams][n] */
+  const double* dt0;     /* optional per-trajectory initial dt [n] */
+  int nthreads;
+} oracle_args;
+
+typedef struct {
+  double* us;        /* SoA [npoints][dim][n], npoints = nsave or ngrid; may be NULL */
+  double* u_final;   /* SoA [dim][n]; may be NULL */
+  double* t_final;   /* [n]; may be NULL */
+  int8_t* retcode;   /* [n]; may be NULL */
+  int32_t* naccept;  /* [n]; may be NULL */
+  int32_t* nreject;  /* [n]; may be NULL */
+  double* dt_first;  /* [n] dt of the first accepted step; may be NULL */
+} oracle_out;
+
+int oracle_solve(const oracle_args* a, oracle_out* o);
+float oracle_ctrl_pow(float x, float b);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,196 @@
+"""Python access to the CPU oracle (TEST INFRASTRUCTURE).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this module.  It loads ``oracle/_build/liboracle.so`` (a
+C++ restatement of SimpleDiffEq.jl's solvers, see oracle.cpp) and provides
+``julia_range``, an independent Python statement of how Julia builds the
+fixed-step time grid ``tspan[1]:dt:tspan[2]`` that the GPUSimple fixed-step
+solvers iterate over (src/tsit5/gpuatsit5.jl:92, src/verner/gpuvern7.jl:101,
+src/verner/gpuvern9.jl:99, src/rk4/gpurk4.jl:66).
+"""
+import ctypes
+import math
+import os
+import subprocess
+from fractions import Fraction
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+ALG = {"RK4": 0, "Tsit5": 1, "ATsit5": 2, "Vern7": 3, "AVern7": 4, "Vern9": 5, "AVern9": 6,
+       "SimpleATsit5": 7, "SimpleTsit5": 8}
+FIXED = {"RK4", "Tsit5", "Vern7", "Vern9", "SimpleTsit5"}
+RHS = {"lorenz": 0, "vanderpol": 1, "r3bp": 2, "kuramoto": 3, "linear": 4}
+PREC = {"fp64": 0, "fp32": 1, "fp32_kahan": 2}
+ROUND = {"ref": 0, "device": 1}
+
+
+class _Args(ctypes.Structure):
+    _fields_ = [("alg", ctypes.c_int), ("rhs", ctypes.c_int), ("precision", ctypes.c_int),
+                ("rounding", ctypes.c_int), ("n", ctypes.c_int64), ("dim", ctypes.c_int),
+                ("nparams", ctypes.c_int), ("t0", ctypes.c_double), ("tf", ctypes.c_double),
+                ("dt", ctypes.c_double), ("abstol", ctypes.c_double), ("reltol", ctypes.c_double),
+                ("saveat", ctypes.c_void_p), ("nsave", ctypes.c_int64), ("save_everystep", ctypes.c_int),
+                ("grid", ctypes.c_void_p), ("ngrid", ctypes.c_int64), ("maxiters", ctypes.c_int64),
+                ("u0", ctypes.c_void_p), ("p", ctypes.c_void_p), ("dt0", ctypes.c_void_p),
+                ("nthreads", ctypes.c_int)]
+
+
+class _Out(ctypes.Structure):
+    _fields_ = [("us", ctypes.c_void_p), ("u_final", ctypes.c_void_p), ("t_final", ctypes.c_void_p),
+                ("retcode", ctypes.c_void_p), ("naccept", ctypes.c_void_p), ("nreject", ctypes.c_void_p),
+                ("dt_first", ctypes.c_void_p)]
+
+
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        _lib = ctypes.CDLL(LIB_PATH)
+        _lib.oracle_solve.argtypes = [ctypes.POINTER(_Args), ctypes.POINTER(_Out)]
+        _lib.oracle_solve.restype = ctypes.c_int
+        _lib.oracle_ctrl_pow.argtypes = [ctypes.c_float, ctypes.c_float]
+        _lib.oracle_ctrl_pow.restype = ctypes.c_float
+    return _lib
+
+
+def ctrl_pow(x, b):
+    return lib().oracle_ctrl_pow(x, b)
+
+
+# --------------------------------------------------------------------------- Julia ranges
+def _t(T, x):
+    return float(np.float32(x)) if T == "fp32" else float(x)
+
+
+def _narrow_maxint(T):
+    # maxintfloat(narrow(T), Int): narrow(Float64) = Float32, narrow(Float32) = Float16
+    return 2 ** 24 if T == "fp64" else 2 ** 11
+
+
+def _maxint(T):
+    return 2 ** 53 if T == "fp64" else 2 ** 24
+
+
+def _rat(x, T):
+    """Base.rat: continued-fraction rational approximation, in T arithmetic."""
+    y = x
+    a = d = 1
+    b = c = 0
+    m = _narrow_maxint(T)
+    while abs(y) <= m:
+        f = math.trunc(y)
+        y = _t(T, y - f)
+        a, c = f * a + c, a
+        b, d = f * b + d, b
+        if max(abs(a), abs(b)) > m:
+            return c, d
+        if _t(T, _t(T, a) / _t(T, b)) == x:
+            break
+        y = _t(T, 1.0 / y) if y != 0 else math.inf
+    return a, b
+
+
+def _jdiv(a, b):
+    q = abs(a) // abs(b)
+    return q if (a >= 0) == (b >= 0) else -q
+
+
+def _isbetween(a, x, b):
+    return (a <= x <= b) or (b <= x <= a)
+
+
+def _to_T(fr, T):
+    v = float(fr)  # correctly rounded to double
+    return _t(T, v)
+
+
+def julia_range(start, step, stop, T="fp64"):
+    """Elements of Julia's ``start:step:stop`` for IEEE floats
+    (Base.(:)(start::T, step::T, stop::T), base/twiceprecision.jl)."""
+    start, step, stop = _t(T, start), _t(T, step), _t(T, stop)
+    if step == 0:
+        raise ValueError("range step cannot be zero")
+    step_n, step_d = _rat(step, T)
+    if step_d != 0 and _t(T, step_n / step_d) == step:
+        start_n, start_d = _rat(start, T)
+        stop_n, stop_d = _rat(stop, T)
+        if start_d != 0 and stop_d != 0 and _t(T, start_n / start_d) == start and _t(T, stop_n / stop_d) == stop:
+            den = start_d * step_d // math.gcd(start_d, step_d)
+            m = _maxint(T)
+            if den != 0 and abs(_t(T, start * den)) <= m and abs(_t(T, step * den)) <= m and \
+                    den % start_d == 0 and den % step_d == 0:
+                start_n = round(_t(T, start * den))
+                step_n = round(_t(T, step * den))
+                ln = max(0, _jdiv(den * stop_n - stop_d * start_n + step_n * stop_d, step_n * stop_d))
+                if _isbetween(start, _t(T, start + _t(T, (ln - 1) * step)), _t(T, stop + _t(T, step / 2))) and \
+                        not _isbetween(start, _t(T, start + _t(T, ln * step)), stop):
+                    return np.array([_to_T(Fraction(start_n + i * step_n, den), T) for i in range(ln)])
+    lf = _t(T, _t(T, stop - start) / step)
+    if lf < 0:
+        ln = 0
+    elif lf == 0:
+        ln = 1
+    else:
+        ln = round(lf) + 1
+        stop2 = _t(T, start + _t(T, (ln - 1) * step))
+        ln -= int(start < stop < stop2) + int(start > stop > stop2)
+    fs, fh = Fraction(start), Fraction(step)
+    return np.array([_to_T(fs + i * fh, T) for i in range(ln)])
+
+
+# --------------------------------------------------------------------------- solve
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def solve(alg, rhs, u0, p, tspan, dt, precision="fp64", rounding="ref", abstol=1e-6, reltol=1e-3,
+          saveat=None, save_everystep=False, maxiters=0, dt0=None, nthreads=1, grid=None):
+    """Solve n trajectories.  u0: (dim, n) float64, p: (nparams, n) float64.
+    Returns a dict of numpy arrays (us is (npoints, dim, n))."""
+    u0 = np.ascontiguousarray(u0, dtype=np.float64)
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    dim, n = u0.shape
+    nparams = p.shape[0]
+    t0, tf = float(tspan[0]), float(tspan[1])
+    if alg in FIXED and grid is None:
+        grid = julia_range(t0, dt, tf, "fp32" if precision == "fp32" else "fp64")
+    if grid is not None:
+        grid = np.ascontiguousarray(grid, dtype=np.float64)
+    sv = None if saveat is None else np.ascontiguousarray(saveat, dtype=np.float64)
+    if sv is not None:
+        npts = len(sv)
+    elif (alg in FIXED and save_everystep):
+        npts = len(grid)
+    else:
+        npts = 0
+    out = {
+        "us": np.full((npts, dim, n), np.nan) if npts else None,
+        "u_final": np.zeros((dim, n)),
+        "t_final": np.zeros(n),
+        "retcode": np.zeros(n, dtype=np.int8),
+        "naccept": np.zeros(n, dtype=np.int32),
+        "nreject": np.zeros(n, dtype=np.int32),
+        "dt_first": np.zeros(n),
+    }
+    d0 = None if dt0 is None else np.ascontiguousarray(dt0, dtype=np.float64)
+    args = _Args(ALG[alg], RHS[rhs], PREC[precision], ROUND[rounding], n, dim, nparams, t0, tf, float(dt),
+                 float(abstol), float(reltol), _ptr(sv), 0 if sv is None else len(sv), int(bool(save_everystep)),
+                 _ptr(grid), 0 if grid is None else len(grid), int(maxiters), _ptr(u0), _ptr(p), _ptr(d0),
+                 int(nthreads))
+    o = _Out(_ptr(out["us"]), _ptr(out["u_final"]), _ptr(out["t_final"]), _ptr(out["retcode"]),
+             _ptr(out["naccept"]), _ptr(out["nreject"]), _ptr(out["dt_first"]))
+    rc = lib().oracle_solve(ctypes.byref(args), ctypes.byref(o))
+    if rc != 0:
+        raise ValueError("oracle_solve rejected the arguments (rc=%d)" % rc)
+    return out

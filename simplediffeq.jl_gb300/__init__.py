@@ -1,0 +1,321 @@
+"""GB300 ensemble solves behind SimpleDiffEq.jl's GPU-solver API.
+
+Host-side mirror of the reference interface, for Python callers and tests:
+
+    prob = ODEProblem("lorenz", u0, (0.0, 10.0), p)          # SciMLBase ODEProblem
+    eprob = EnsembleProblem(prob, u0s=U0, ps=P)               # or prob_func=...
+    sol = solve(eprob, GPUSimpleATsit5(), trajectories=n, dt=0.1,
+                abstol=1e-8, reltol=1e-6, saveat=ts)
+
+The algorithm types and keyword arguments are those of the reference's
+GPU-crutch solvers (src/tsit5/gpuatsit5.jl:52,200 and :55-61,205-212;
+src/verner/gpuvern7.jl:52,295; src/verner/gpuvern9.jl:52,406;
+src/rk4/gpurk4.jl:50) with the same defaults (dt = 0.1, abstol = 1e-6,
+reltol = 1e-3).  Every trajectory runs the reference's solver loop on the GPU
+through libgb300ode.so; there is no CPU path.  Errors behave like the
+reference's: a trajectory that hits dt < dtmin raises ``DtLessThanMin``
+(``error("dt<dtmin")`` in the reference), in-place problems are rejected
+(``@assert !isinplace(prob)``).
+"""
+import importlib.util as _ilu
+import os as _os
+import sys as _sys
+
+import numpy as np
+
+_spec = _ilu.spec_from_file_location(__name__ + "._lib", _os.path.join(_os.path.dirname(__file__), "_lib.py"))
+_lib = _ilu.module_from_spec(_spec)
+_sys.modules[__name__ + "._lib"] = _lib
+_spec.loader.exec_module(_lib)
+
+GB300ODEError = _lib.GB300ODEError
+Handle = _lib.Handle
+fixed_grid = _lib.fixed_grid
+
+
+class DtLessThanMin(RuntimeError):
+    """Raised where the reference throws ``error("dt<dtmin")``."""
+
+
+# --------------------------------------------------------------------------- algorithms
+class _Alg:
+    name = ""
+    adaptive = False
+
+    def __repr__(self):
+        return "%s()" % type(self).__name__
+
+
+class GPUSimpleRK4(_Alg):
+    """Fixed-step classic RK4 (src/rk4/gpurk4.jl:50). Saves every step."""
+    name = "RK4"
+
+
+class GPUSimpleTsit5(_Alg):
+    """Fixed-step Tsitouras 5(4) (src/tsit5/gpuatsit5.jl:52)."""
+    name = "Tsit5"
+
+
+class GPUSimpleATsit5(_Alg):
+    """Adaptive Tsitouras 5(4) with PI control (src/tsit5/gpuatsit5.jl:200)."""
+    name = "ATsit5"
+    adaptive = True
+
+
+class GPUSimpleVern7(_Alg):
+    """Fixed-step Verner 7(6) (src/verner/gpuvern7.jl:52)."""
+    name = "Vern7"
+
+
+class GPUSimpleAVern7(_Alg):
+    """Adaptive Verner 7(6) (src/verner/gpuvern7.jl:295)."""
+    name = "AVern7"
+    adaptive = True
+
+
+class GPUSimpleVern9(_Alg):
+    """Fixed-step Verner 9(8) (src/verner/gpuvern9.jl:52)."""
+    name = "Vern9"
+
+
+class GPUSimpleAVern9(_Alg):
+    """Adaptive Verner 9(8) (src/verner/gpuvern9.jl:406)."""
+    name = "AVern9"
+    adaptive = True
+
+
+def isadaptive(alg):
+    """SciMLBase.isadaptive (src/tsit5/gpuatsit5.jl:203 and the Verner files)."""
+    return alg.adaptive
+
+
+# --------------------------------------------------------------------------- problems
+class UserRHS:
+    """A right-hand side given as the C++ body of
+    ``template <class R> __device__ void rhs(R* du, const R* u, const R* p, R t)``,
+    compiled for the GPU with NVRTC the first time it is solved."""
+
+    def __init__(self, body, dim, nparams):
+        self.body, self.dim, self.nparams = body, int(dim), int(nparams)
+
+
+_BUILTIN_DIMS = {"lorenz": (3, 3), "vanderpol": (2, 1), "r3bp": (4, 1)}
+
+
+class ODEProblem:
+    """Out-of-place ODE problem du = f(u, p, t) on tspan.
+
+    ``f`` is a built-in right-hand side name ("lorenz", "vanderpol", "r3bp",
+    "kuramoto", "linear") or a ``UserRHS``.  ``inplace=True`` mirrors an
+    in-place Julia problem and is rejected by every GPU solver, as the
+    reference asserts ``!isinplace(prob)``."""
+
+    def __init__(self, f, u0, tspan, p=(), inplace=False):
+        self.f = f
+        self.u0 = np.atleast_1d(np.asarray(u0, dtype=np.float64))
+        self.tspan = (float(tspan[0]), float(tspan[1]))
+        self.p = np.atleast_1d(np.asarray(p, dtype=np.float64)) if np.size(p) else np.zeros(0)
+        self.inplace = bool(inplace)
+
+    def remake(self, u0=None, p=None, tspan=None):
+        return ODEProblem(self.f, self.u0 if u0 is None else u0, self.tspan if tspan is None else tspan,
+                          self.p if p is None else p, self.inplace)
+
+
+class EnsembleProblem:
+    """SciMLBase.EnsembleProblem: ``prob_func(prob, i, repeat)`` returns the
+    problem of trajectory i (1-based, as in Julia), or pass the stacked initial
+    states ``u0s`` (dim x n) and parameters ``ps`` (nparams x n) directly."""
+
+    def __init__(self, prob, prob_func=None, u0s=None, ps=None):
+        self.prob = prob
+        self.prob_func = prob_func
+        self.u0s = None if u0s is None else np.ascontiguousarray(u0s, dtype=np.float64)
+        self.ps = None if ps is None else np.ascontiguousarray(ps, dtype=np.float64)
+
+
+class ODESolution:
+    """Per-trajectory solution: ``t`` and ``u`` (list of state vectors), ``retcode``."""
+
+    def __init__(self, t, u, retcode, naccept=0, nreject=0):
+        self.t, self.u, self.retcode = t, u, retcode
+        self.naccept, self.nreject = naccept, nreject
+
+    def __len__(self):
+        return len(self.u)
+
+
+_RETNAMES = {0: "Default", 1: "DtLessThanMin", 2: "MaxIters", 3: "Default"}
+
+
+class EnsembleSolution:
+    """Results of an ensemble solve, kept as structure-of-arrays:
+    ``us`` (npoints, dim, n), ``u_final`` (dim, n), ``t_final`` (n,),
+    ``retcode``, ``naccept``, ``nreject`` (n,), ``t`` (the save times).
+    ``sol[i]`` builds the ODESolution of trajectory i (0-based)."""
+
+    def __init__(self, t, us, u_final, t_final, retcode, naccept, nreject, dt_first, stats):
+        self.t, self.us, self.u_final, self.t_final = t, us, u_final, t_final
+        self.retcode, self.naccept, self.nreject, self.dt_first = retcode, naccept, nreject, dt_first
+        self.stats = stats
+
+    def __len__(self):
+        return self.u_final.shape[1]
+
+    def __getitem__(self, i):
+        if self.us is not None:
+            u = [self.us[j, :, i].copy() for j in range(self.us.shape[0])]
+            t = self.t
+        else:
+            u = [self.u_final[:, i].copy()]
+            t = np.array([self.t_final[i]])
+        return ODESolution(t, u, _RETNAMES.get(int(self.retcode[i]), "Failure"), int(self.naccept[i]),
+                           int(self.nreject[i]))
+
+
+# --------------------------------------------------------------------------- solve
+_handles = {}
+
+
+def _handle(device=0):
+    h = _handles.get(device)
+    if h is None:
+        h = _handles[device] = Handle(device)
+    return h
+
+
+def _rhs_id(h, f):
+    if isinstance(f, str):
+        if f not in _lib.RHS:
+            raise ValueError("unknown built-in right-hand side %r" % f)
+        return _lib.RHS[f]
+    if isinstance(f, UserRHS):
+        cache = h.__dict__.setdefault("_user_ids", {})
+        key = (f.body, f.dim, f.nparams)
+        if key not in cache:
+            cache[key] = h.compile_rhs(f.body, f.dim, f.nparams)
+        return cache[key]
+    raise TypeError("f must be a built-in name or a UserRHS (Python callables cannot run on the GPU)")
+
+
+def _stack(eprob, trajectories):
+    prob = eprob.prob
+    if eprob.u0s is not None or eprob.ps is not None:
+        u0s = eprob.u0s if eprob.u0s is not None else np.repeat(prob.u0[:, None], trajectories, 1)
+        ps = eprob.ps if eprob.ps is not None else np.repeat(prob.p[:, None], trajectories, 1)
+        if u0s.shape[1] != trajectories or ps.shape[1] != trajectories:
+            raise ValueError("u0s/ps must have `trajectories` columns")
+        return u0s, ps
+    if eprob.prob_func is None:
+        return np.repeat(prob.u0[:, None], trajectories, 1), np.repeat(prob.p[:, None], trajectories, 1)
+    u0s = np.zeros((prob.u0.size, trajectories))
+    ps = np.zeros((prob.p.size, trajectories))
+    for i in range(trajectories):
+        pi = eprob.prob_func(prob, i + 1, 1)
+        u0s[:, i] = pi.u0
+        ps[:, i] = pi.p
+    return u0s, ps
+
+
+def make_args(alg, f_id, u0s, ps, tspan, dt, abstol, reltol, saveat, save_everystep, precision, schedule,
+              maxiters, memory=_lib.MEM_HOST, dt0=None):
+    a = _lib.SolveArgs()
+    a.alg = _lib.ALG[alg.name]
+    a.rhs = f_id
+    a.precision = _lib.PREC[precision]
+    a.schedule = _lib.SCHED[schedule]
+    a.dim, a.n = u0s.shape
+    a.nparams = ps.shape[0]
+    a.t0, a.tf = float(tspan[0]), float(tspan[1])
+    a.dt, a.abstol, a.reltol = float(dt), float(abstol), float(reltol)
+    if saveat is not None:
+        a.saveat, a.nsave = saveat.ctypes.data, len(saveat)
+    a.save_everystep = int(bool(save_everystep))
+    a.memory = memory
+    a.maxiters = int(maxiters)
+    a.u0, a.p = u0s.ctypes.data, ps.ctypes.data
+    a.dt0 = None if dt0 is None else dt0.ctypes.data
+    return a
+
+
+def solve(prob, alg, trajectories=None, dt=0.1, abstol=1e-6, reltol=1e-3, saveat=None, save_everystep=None,
+          precision="fp64", schedule="persistent", maxiters=0, device=0, dt0=None, throw=True, **kwargs):
+    """Solve an EnsembleProblem (or a single ODEProblem as an ensemble of one).
+
+    Unknown keyword arguments are accepted and ignored, as the reference's
+    ``kwargs...`` swallows them.  ``save_everystep`` defaults to False for
+    ensembles (adaptive per-step output is ragged and not produced) and applies
+    to the fixed-step algorithms; GPUSimpleRK4 ignores ``saveat`` as the
+    reference does."""
+    single = isinstance(prob, ODEProblem)
+    eprob = EnsembleProblem(prob) if single else prob
+    base = eprob.prob
+    if base.inplace:
+        raise AssertionError("!isinplace(prob)")  # @assert !isinplace(prob) in every GPUSimple solve
+    n = 1 if single else trajectories
+    if n is None:
+        n = eprob.u0s.shape[1] if eprob.u0s is not None else 1
+    h = _handle(device)
+    fid = _rhs_id(h, base.f)
+    u0s, ps = _stack(eprob, n)
+    if ps.shape[0] == 0:
+        ps = np.zeros((0, n))
+    if alg.name == "RK4":
+        saveat = None  # GPUSimpleRK4 has no saveat keyword (gpurk4.jl:53-58); it saves every step
+        if save_everystep is None:
+            save_everystep = True
+    if save_everystep is None:
+        save_everystep = False
+    if save_everystep and saveat is None and alg.adaptive:
+        raise NotImplementedError("save_everystep=true for adaptive ensembles (ragged output) is not produced")
+    sv = None if saveat is None else np.ascontiguousarray(np.asarray(saveat, dtype=np.float64))
+    if not alg.adaptive:
+        schedule = "plain"
+    args = make_args(alg, fid, u0s, ps, base.tspan, dt, abstol, reltol, sv, save_everystep, precision, schedule,
+                     maxiters, dt0=None if dt0 is None else np.ascontiguousarray(dt0, dtype=np.float64))
+    dim = u0s.shape[0]
+    if sv is not None:
+        npts = len(sv)
+        tpts = sv
+    elif not alg.adaptive and save_everystep:
+        tpts = fixed_grid(base.tspan[0], dt, base.tspan[1], "fp32" if precision == "fp32" else "fp64")
+        npts = len(tpts)
+    else:
+        npts, tpts = 0, None
+    us = np.empty((npts, dim, n)) if npts else None
+    out = {"u_final": np.empty((dim, n)), "t_final": np.empty(n), "retcode": np.empty(n, dtype=np.int8),
+           "naccept": np.empty(n, dtype=np.int32), "nreject": np.empty(n, dtype=np.int32),
+           "dt_first": np.empty(n)}
+    o = _lib.SolveOut()
+    o.us = None if us is None else us.ctypes.data
+    for k, v in out.items():
+        setattr(o, k, v.ctypes.data)
+    st = _lib.SolveStats()
+    rc = h.solve_raw(args, o, st)
+    h.check(rc, allow=(_lib.ETRAJ,))
+    sol = EnsembleSolution(tpts, us, out["u_final"], out["t_final"], out["retcode"], out["naccept"],
+                           out["nreject"], out["dt_first"], st)
+    if rc == _lib.ETRAJ and throw:
+        if (out["retcode"] == _lib.RET_DTMIN).any():
+            raise DtLessThanMin("dt<dtmin")
+        raise RuntimeError("maxiters reached")
+    return sol[0] if single else sol
+
+
+def learn_fit(prob, alg, trajectories, device=0, opts=None, **kw):
+    """Fit the learned-schedule model of the device handle on a training
+    ensemble (solved with the plain schedule) — see ode_learn_fit."""
+    h = _handle(device)
+    u0s, ps = _stack(prob, trajectories)
+    sv = kw.get("saveat")
+    sv = None if sv is None else np.ascontiguousarray(np.asarray(sv, dtype=np.float64))
+    args = make_args(alg, _rhs_id(h, prob.prob.f), u0s, ps, prob.prob.tspan, kw.get("dt", 0.1),
+                     kw.get("abstol", 1e-6), kw.get("reltol", 1e-3), sv, False, kw.get("precision", "fp64"),
+                     "plain", kw.get("maxiters", 0))
+    return h.learn_fit(args, opts)
+
+
+__all__ = ["ODEProblem", "EnsembleProblem", "EnsembleSolution", "ODESolution", "UserRHS", "solve", "learn_fit",
+           "GPUSimpleRK4", "GPUSimpleTsit5", "GPUSimpleATsit5", "GPUSimpleVern7", "GPUSimpleAVern7",
+           "GPUSimpleVern9", "GPUSimpleAVern9", "isadaptive", "DtLessThanMin", "GB300ODEError", "Handle",
+           "fixed_grid"]

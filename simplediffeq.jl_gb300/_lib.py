@@ -1,0 +1,181 @@
+"""ctypes binding of libgb300ode.so (include/gb300ode.h).
+
+The library is built in-tree by ``csrc/build.py`` into ``lib/``.  There is no
+fallback: if the shared library is missing or cannot be loaded, every entry
+point raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libgb300ode.so")
+PROBE_PATH = os.path.join(HERE, "lib", "libgb300ode_probe.so")
+
+OK, EINVAL, ECUDA, ENOMEM, ENOTSUP, ENVRTC, ETRAJ, ENOMODEL = 0, -1, -2, -3, -4, -5, -6, -7
+ALG = {"RK4": 0, "Tsit5": 1, "ATsit5": 2, "Vern7": 3, "AVern7": 4, "Vern9": 5, "AVern9": 6}
+RHS = {"lorenz": 0, "vanderpol": 1, "r3bp": 2, "kuramoto": 3, "linear": 4}
+PREC = {"fp64": 0, "fp32": 1, "fp32_kahan": 2}
+SCHED = {"plain": 0, "persistent": 1, "learned": 2}
+MEM_HOST, MEM_DEVICE = 0, 1
+RET_DEFAULT, RET_DTMIN, RET_MAXITERS, RET_NAN = 0, 1, 2, 3
+
+# Every symbol include/gb300ode.h declares.
+EXPORTS = ["ode_abi_version", "ode_create", "ode_destroy", "ode_last_error", "ode_ensemble_solve",
+           "ode_fixed_grid", "ode_rhs_compile", "ode_learn_default_opts", "ode_learn_fit", "ode_learn_predict"]
+
+
+class SolveArgs(ctypes.Structure):
+    _fields_ = [("alg", ctypes.c_int32), ("rhs", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("schedule", ctypes.c_int32), ("n", ctypes.c_int64), ("dim", ctypes.c_int32),
+                ("nparams", ctypes.c_int32), ("t0", ctypes.c_double), ("tf", ctypes.c_double),
+                ("dt", ctypes.c_double), ("abstol", ctypes.c_double), ("reltol", ctypes.c_double),
+                ("saveat", ctypes.c_void_p), ("nsave", ctypes.c_int64), ("save_everystep", ctypes.c_int32),
+                ("memory", ctypes.c_int32), ("maxiters", ctypes.c_int64), ("u0", ctypes.c_void_p),
+                ("p", ctypes.c_void_p), ("dt0", ctypes.c_void_p), ("stream", ctypes.c_void_p)]
+
+
+class SolveOut(ctypes.Structure):
+    _fields_ = [("us", ctypes.c_void_p), ("u_final", ctypes.c_void_p), ("t_final", ctypes.c_void_p),
+                ("retcode", ctypes.c_void_p), ("naccept", ctypes.c_void_p), ("nreject", ctypes.c_void_p),
+                ("dt_first", ctypes.c_void_p)]
+
+
+class SolveStats(ctypes.Structure):
+    _fields_ = [("kernel_ms", ctypes.c_double), ("total_ms", ctypes.c_double), ("attempts", ctypes.c_int64),
+                ("saves", ctypes.c_int64), ("launches", ctypes.c_int32), ("schedule_used", ctypes.c_int32),
+                ("graph_replayed", ctypes.c_int32), ("jit", ctypes.c_int32)]
+
+
+class LearnOpts(ctypes.Structure):
+    _fields_ = [("hidden", ctypes.c_int32), ("epochs", ctypes.c_int32), ("batch", ctypes.c_int32),
+                ("lr", ctypes.c_float), ("seed", ctypes.c_uint64), ("seed_dt0", ctypes.c_int32),
+                ("dt0_safety", ctypes.c_float)]
+
+
+class LearnReport(ctypes.Structure):
+    _fields_ = [("loss_first", ctypes.c_float), ("loss_last", ctypes.c_float), ("r2_attempts", ctypes.c_float),
+                ("train_solve_ms", ctypes.c_double), ("train_fit_ms", ctypes.c_double)]
+
+
+class GB300ODEError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("gb300ode error %d: %s" % (code, msg))
+        self.code = code
+
+
+_lib = None
+
+
+def load():
+    """Load libgb300ode.so (raises if it is missing: there is no CPU path)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise GB300ODEError(ECUDA, "libgb300ode.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    lib.ode_abi_version.restype = ctypes.c_int
+    lib.ode_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]
+    lib.ode_destroy.argtypes = [ctypes.c_void_p]
+    lib.ode_destroy.restype = None
+    lib.ode_last_error.argtypes = [ctypes.c_void_p]
+    lib.ode_last_error.restype = ctypes.c_char_p
+    lib.ode_ensemble_solve.argtypes = [ctypes.c_void_p, ctypes.POINTER(SolveArgs), ctypes.POINTER(SolveOut),
+                                       ctypes.POINTER(SolveStats)]
+    lib.ode_fixed_grid.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                   ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
+    lib.ode_rhs_compile.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
+                                    ctypes.POINTER(ctypes.c_int), ctypes.c_char_p, ctypes.c_size_t]
+    lib.ode_learn_default_opts.argtypes = [ctypes.POINTER(LearnOpts)]
+    lib.ode_learn_default_opts.restype = None
+    lib.ode_learn_fit.argtypes = [ctypes.c_void_p, ctypes.POINTER(SolveArgs), ctypes.POINTER(LearnOpts),
+                                  ctypes.POINTER(LearnReport)]
+    lib.ode_learn_predict.argtypes = [ctypes.c_void_p, ctypes.POINTER(SolveArgs), ctypes.c_void_p, ctypes.c_void_p]
+    _lib = lib
+    return lib
+
+
+def fixed_grid(t0, dt, tf, precision="fp64"):
+    """Julia's t0:dt:tf as the library computes it."""
+    lib = load()
+    n = ctypes.c_int64(0)
+    rc = lib.ode_fixed_grid(float(t0), float(dt), float(tf), PREC[precision], None, 0, ctypes.byref(n))
+    if rc != OK:
+        raise GB300ODEError(rc, "invalid range")
+    out = np.zeros(n.value)
+    rc = lib.ode_fixed_grid(float(t0), float(dt), float(tf), PREC[precision], out.ctypes.data, n.value,
+                            ctypes.byref(n))
+    return out
+
+
+class Handle:
+    """One library handle (device workspace, compiled kernels, learned model)."""
+
+    def __init__(self, device=0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        rc = self.lib.ode_create(ctypes.byref(h), int(device))
+        if rc != OK:
+            raise GB300ODEError(rc, "ode_create failed (is a CUDA device visible?)")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.ode_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def error(self):
+        return self.lib.ode_last_error(self.h).decode()
+
+    def check(self, rc, allow=()):
+        if rc != OK and rc not in allow:
+            raise GB300ODEError(rc, self.error())
+        return rc
+
+    def solve_raw(self, args, out, stats=None):
+        return self.lib.ode_ensemble_solve(self.h, ctypes.byref(args), ctypes.byref(out),
+                                           ctypes.byref(stats) if stats is not None else None)
+
+    def compile_rhs(self, body, dim, nparams):
+        rid = ctypes.c_int(0)
+        log = ctypes.create_string_buffer(8192)
+        rc = self.lib.ode_rhs_compile(self.h, body.encode(), int(dim), int(nparams), ctypes.byref(rid), log, 8192)
+        if rc != OK:
+            raise GB300ODEError(rc, self.error())
+        return rid.value
+
+    def learn_fit(self, args, opts=None):
+        o = LearnOpts()
+        self.lib.ode_learn_default_opts(ctypes.byref(o))
+        for k, v in (opts or {}).items():
+            setattr(o, k, v)
+        rep = LearnReport()
+        self.check(self.lib.ode_learn_fit(self.h, ctypes.byref(args), ctypes.byref(o), ctypes.byref(rep)))
+        return rep
+
+    def learn_predict(self, args, n):
+        la = np.zeros(n, dtype=np.float32)
+        ld = np.zeros(n, dtype=np.float32)
+        self.check(self.lib.ode_learn_predict(self.h, ctypes.byref(args), la.ctypes.data, ld.ctypes.data))
+        return la, ld
+
+
+def probe_rates(device=0, iters=2000):
+    """Measured lane-operation rates of the arithmetic pipes (libgb300ode_probe.so)."""
+    lib = ctypes.CDLL(PROBE_PATH)
+    lib.probe_op_rates.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+    r = np.zeros(8)
+    ms = np.zeros(8)
+    rc = lib.probe_op_rates(int(device), int(iters), r.ctypes.data, ms.ctypes.data, 8)
+    if rc != 0:
+        raise GB300ODEError(ECUDA, "probe failed (%d)" % rc)
+    names = ["dfma", "dadd", "ffma", "cvt_f64_f32_f64", "ddiv", "dsqrt_add", "dmax_add", "fdiv"]
+    return {k: (float(r[i]), float(ms[i])) for i, k in enumerate(names)}

@@ -1,0 +1,646 @@
+/* C ABI of libgb300ode.so: handles, argument checking, device workspace,
+ * kernel selection (prebuilt or compiled at run time with NVRTC), the plain /
+ * persistent / learned schedules and CUDA-graph replay of repeated solves.
+ *
+ * ode_ensemble_solve replaces the per-trajectory solve methods of
+ * SimpleDiffEq.jl's GPUSimple* solvers (see include/gb300ode.h for the list
+ * with file:line citations) for a whole ensemble at once.
+ */
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <dlfcn.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "jlrange.h"
+#include "ode_host.h"
+
+/* kernels compiled ahead of time, and the sources for run-time compilation */
+#include "aot_registry.inc"
+#include "embedded_src.inc"
+
+namespace gbode {
+
+/* Driver-API and NVRTC entry points, resolved at run time so that the library
+ * loads on machines without a GPU driver (only the runtime is linked). */
+struct DriverApi {
+  bool ok = false;
+  CUresult (*cuLaunchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned, unsigned,
+                             CUstream, void**, void**) = nullptr;
+  CUresult (*cuModuleLoadData)(CUmodule*, const void*) = nullptr;
+  CUresult (*cuModuleGetFunction)(CUfunction*, CUmodule, const char*) = nullptr;
+  CUresult (*cuModuleUnload)(CUmodule) = nullptr;
+  CUresult (*cuOccupancyMaxActiveBlocksPerMultiprocessor)(int*, CUfunction, int, size_t) = nullptr;
+  CUresult (*cuGetErrorName)(CUresult, const char**) = nullptr;
+  CUresult (*cuGetErrorString)(CUresult, const char**) = nullptr;
+  CUresult (*cuFuncGetAttribute)(int*, CUfunction_attribute, CUfunction) = nullptr;
+};
+struct NvrtcApi {
+  bool tried = false, ok = false;
+  nvrtcResult (*create)(nvrtcProgram*, const char*, const char*, int, const char* const*, const char* const*);
+  nvrtcResult (*compile)(nvrtcProgram, int, const char* const*);
+  nvrtcResult (*logsize)(nvrtcProgram, size_t*);
+  nvrtcResult (*log)(nvrtcProgram, char*);
+  nvrtcResult (*cubinsize)(nvrtcProgram, size_t*);
+  nvrtcResult (*cubin)(nvrtcProgram, char*);
+  nvrtcResult (*destroy)(nvrtcProgram*);
+  const char* (*errstr)(nvrtcResult);
+};
+static DriverApi g_drv;
+static NvrtcApi g_nvrtc;
+
+template <class F>
+static bool drv_sym(const char* name, F* fp) {
+  void* p = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !p)
+    return false;
+  *fp = (F)p;
+  return true;
+}
+
+static bool load_driver_api() {
+  if (g_drv.ok) return true;
+  DriverApi d;
+  bool ok = drv_sym("cuLaunchKernel", &d.cuLaunchKernel) && drv_sym("cuModuleLoadData", &d.cuModuleLoadData) &&
+            drv_sym("cuModuleGetFunction", &d.cuModuleGetFunction) && drv_sym("cuModuleUnload", &d.cuModuleUnload) &&
+            drv_sym("cuOccupancyMaxActiveBlocksPerMultiprocessor", &d.cuOccupancyMaxActiveBlocksPerMultiprocessor) &&
+            drv_sym("cuGetErrorName", &d.cuGetErrorName) && drv_sym("cuGetErrorString", &d.cuGetErrorString) &&
+            drv_sym("cuFuncGetAttribute", &d.cuFuncGetAttribute);
+  d.ok = ok;
+  if (ok) g_drv = d;
+  return ok;
+}
+
+static bool load_nvrtc() {
+  if (g_nvrtc.tried) return g_nvrtc.ok;
+  g_nvrtc.tried = true;
+  const char* names[] = {"libnvrtc.so.13", "libnvrtc.so", "/usr/local/cuda/lib64/libnvrtc.so.13"};
+  void* h = nullptr;
+  for (const char* n : names)
+    if ((h = dlopen(n, RTLD_NOW | RTLD_LOCAL))) break;
+  if (!h) return false;
+#define NV(field, sym) g_nvrtc.field = (decltype(g_nvrtc.field))dlsym(h, sym)
+  NV(create, "nvrtcCreateProgram");
+  NV(compile, "nvrtcCompileProgram");
+  NV(logsize, "nvrtcGetProgramLogSize");
+  NV(log, "nvrtcGetProgramLog");
+  NV(cubinsize, "nvrtcGetCUBINSize");
+  NV(cubin, "nvrtcGetCUBIN");
+  NV(destroy, "nvrtcDestroyProgram");
+  NV(errstr, "nvrtcGetErrorString");
+#undef NV
+  g_nvrtc.ok = g_nvrtc.create && g_nvrtc.compile && g_nvrtc.logsize && g_nvrtc.log && g_nvrtc.cubinsize &&
+               g_nvrtc.cubin && g_nvrtc.destroy && g_nvrtc.errstr;
+  return g_nvrtc.ok;
+}
+
+int fail(ode_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+int cuda_fail(ode_handle* h, cudaError_t e, const char* what) {
+  return fail(h, e == cudaErrorMemoryAllocation ? ODE_ENOMEM : ODE_ECUDA,
+              std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+}
+int cu_fail(ode_handle* h, CUresult r, const char* what) {
+  const char* name = nullptr;
+  const char* str = nullptr;
+  if (g_drv.ok) {
+    g_drv.cuGetErrorName(r, &name);
+    g_drv.cuGetErrorString(r, &str);
+  }
+  return fail(h, r == CUDA_ERROR_OUT_OF_MEMORY ? ODE_ENOMEM : ODE_ECUDA,
+              std::string(what) + ": " + (name ? name : "?") + " (" + (str ? str : "?") + ")");
+}
+
+void* buf(ode_handle* h, const std::string& name, size_t bytes, int* rc) {
+  DevBuf& b = h->bufs[name];
+  if (bytes == 0) bytes = 16;
+  if (b.cap < bytes) {
+    if (b.ptr) cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.cap = 0;
+    cudaError_t e = cudaMalloc(&b.ptr, bytes);
+    if (e != cudaSuccess) {
+      b.ptr = nullptr;
+      *rc = cuda_fail(h, e, ("cudaMalloc " + name).c_str());
+      return nullptr;
+    }
+    b.cap = bytes;
+  }
+  *rc = ODE_OK;
+  return b.ptr;
+}
+
+}  // namespace gbode
+
+using namespace gbode;
+
+namespace {
+
+#define CK(call, what)                                   \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_, what); \
+  } while (0)
+
+/* Attempt cap used when the caller gives none: every trajectory loop on the
+ * device must end, and the reference's loop has no cap of its own. */
+const int64_t kDefaultMaxIters = 1000000;
+
+bool is_fixed(int alg) { return alg == ODE_ALG_RK4 || alg == ODE_ALG_TSIT5 || alg == ODE_ALG_VERN7 || alg == ODE_ALG_VERN9; }
+
+const char* alg_name(int alg) {
+  static const char* n[] = {"rk4", "tsit5", "atsit5", "vern7", "avern7", "vern9", "avern9"};
+  return (alg >= 0 && alg <= 6) ? n[alg] : "?";
+}
+const char* prec_name(int p) {
+  static const char* n[] = {"fp64", "fp32", "fp32k"};
+  return (p >= 0 && p <= 2) ? n[p] : "?";
+}
+
+/* C++ names used to assemble a kernel for NVRTC */
+const char* method_type(int alg) {
+  switch (alg) {
+    case ODE_ALG_RK4: return "gbode::MTsit5";  /* unused by the rk4 entry */
+    case ODE_ALG_TSIT5:
+    case ODE_ALG_ATSIT5: return "gbode::MTsit5";
+    case ODE_ALG_VERN7:
+    case ODE_ALG_AVERN7: return "gbode::MVern7";
+    case ODE_ALG_VERN9: return "gbode::MVern9";
+    case ODE_ALG_AVERN9: return "gbode::MAVern9";
+  }
+  return "?";
+}
+const char* prec_type(int p) {
+  switch (p) {
+    case ODE_FP64: return "gbode::PFP64";
+    case ODE_FP32: return "gbode::PFP32";
+    case ODE_FP32_KAHAN: return "gbode::PFP32K";
+  }
+  return "?";
+}
+void rt_types(int p, const char** R, const char** T) {
+  *R = (p == ODE_FP64) ? "double" : "float";
+  *T = (p == ODE_FP32) ? "float" : "double";
+}
+
+/* Validate the (rhs, dim, nparams) triple; returns ODE_OK or an error. */
+int check_rhs(ode_handle* h, const ode_solve_args* a) {
+  switch (a->rhs) {
+    case ODE_RHS_LORENZ:
+      if (a->dim != 3 || a->nparams != 3) return fail(h, ODE_EINVAL, "Lorenz needs dim 3 and 3 parameters");
+      return ODE_OK;
+    case ODE_RHS_VANDERPOL:
+      if (a->dim != 2 || a->nparams != 1) return fail(h, ODE_EINVAL, "Van der Pol needs dim 2 and 1 parameter");
+      return ODE_OK;
+    case ODE_RHS_R3BP:
+      if (a->dim != 4 || a->nparams != 1) return fail(h, ODE_EINVAL, "R3BP needs dim 4 and 1 parameter");
+      return ODE_OK;
+    case ODE_RHS_KURAMOTO:
+      if (a->dim < 1 || a->dim > 32 || a->nparams != a->dim + 1)
+        return fail(h, ODE_EINVAL, "Kuramoto needs 1 <= dim <= 32 and dim+1 parameters");
+      return ODE_OK;
+    case ODE_RHS_LINEAR:
+      if (a->dim < 1 || a->dim > 8 || a->nparams != a->dim * a->dim)
+        return fail(h, ODE_EINVAL, "linear needs 1 <= dim <= 8 and dim*dim parameters");
+      return ODE_OK;
+  }
+  if (a->rhs >= ODE_RHS_USER && a->rhs < ODE_RHS_USER + (int)h->users.size()) {
+    const UserRhs& u = h->users[a->rhs - ODE_RHS_USER];
+    if (a->dim != u.dim || a->nparams != u.nparams)
+      return fail(h, ODE_EINVAL, "dim/nparams differ from the compiled user right-hand side");
+    return ODE_OK;
+  }
+  return fail(h, ODE_EINVAL, "unknown right-hand side id");
+}
+
+std::string rhs_type_expr(ode_handle* h, const ode_solve_args* a) {
+  const char *R, *T;
+  rt_types(a->precision, &R, &T);
+  char b[256];
+  switch (a->rhs) {
+    case ODE_RHS_LORENZ: snprintf(b, sizeof b, "gbode::RhsLorenz<%s, %s>", R, T); break;
+    case ODE_RHS_VANDERPOL: snprintf(b, sizeof b, "gbode::RhsVanDerPol<%s, %s>", R, T); break;
+    case ODE_RHS_R3BP: snprintf(b, sizeof b, "gbode::RhsR3BP<%s, %s>", R, T); break;
+    case ODE_RHS_KURAMOTO: snprintf(b, sizeof b, "gbode::RhsKuramoto<%s, %s, %d>", R, T, a->dim); break;
+    case ODE_RHS_LINEAR: snprintf(b, sizeof b, "gbode::RhsLinear<%s, %s, %d>", R, T, a->dim); break;
+    default: snprintf(b, sizeof b, "RhsUser<%s, %s>", R, T); break;
+  }
+  return b;
+}
+
+/* kind of entry point: plain | persistent | fixed | rk4 */
+const char* entry_kind(int alg, int sched) {
+  if (alg == ODE_ALG_RK4) return "rk4";
+  if (is_fixed(alg)) return "fixed";
+  return sched == ODE_SCHED_PLAIN ? "plain" : "persistent";
+}
+
+std::string kernel_key(ode_handle* h, const ode_solve_args* a, int sched) {
+  char b[160];
+  snprintf(b, sizeof b, "%s|%s|%d|%d|%s", alg_name(a->alg), entry_kind(a->alg, sched), a->rhs, a->dim,
+           prec_name(a->precision));
+  return b;
+}
+
+int compile_jit(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn, std::string* log_out) {
+  std::string src = "#include \"ode_solver.cuh\"\n";
+  if (a->rhs >= ODE_RHS_USER) {
+    const UserRhs& u = h->users[a->rhs - ODE_RHS_USER];
+    char hdr[256];
+    snprintf(hdr, sizeof hdr,
+             "template <class R> __device__ __forceinline__ void user_rhs(R* du, const R* u, const R* p, R t) {\n");
+    src += hdr;
+    src += u.body;
+    src += "\n}\n";
+    snprintf(hdr, sizeof hdr,
+             "template <class R, class T> struct RhsUser {\n  enum { D = %d, NP = %d };\n  R p[%d];\n", u.dim,
+             u.nparams, u.nparams > 0 ? u.nparams : 1);
+    src += hdr;
+    src += "  __device__ __forceinline__ void operator()(const R (&u)[D], T t, R (&du)[D]) const {\n"
+           "    user_rhs<R>(du, u, p, (R)t);\n  }\n};\n";
+  }
+  src += "typedef " + rhs_type_expr(h, a) + " RHS_T;\n";
+  src += std::string("GBODE_ENTRY(gbode_jit, ") + entry_kind(a->alg, sched) + ", " + method_type(a->alg) + ", " +
+         prec_type(a->precision) + ", RHS_T)\n";
+
+  if (!load_nvrtc()) return fail(h, ODE_ENVRTC, "libnvrtc.so.13 could not be loaded");
+  nvrtcProgram prog;
+  const char* hdrs[] = {kSrc_ode_solver_cuh, kSrc_ode_kparams_h, kSrc_tableaus_h};
+  const char* names[] = {"ode_solver.cuh", "ode_kparams.h", "tableaus.h"};
+  nvrtcResult r = g_nvrtc.create(&prog, src.c_str(), "gbode_jit.cu", 3, hdrs, names);
+  if (r != NVRTC_SUCCESS) return fail(h, ODE_ENVRTC, std::string("nvrtcCreateProgram: ") + g_nvrtc.errstr(r));
+  const char* opts[] = {"--gpu-architecture=sm_103a", "--fmad=false", "-std=c++17", "-lineinfo",
+                        "-default-device"};
+  r = g_nvrtc.compile(prog, 5, opts);
+  size_t loglen = 0;
+  g_nvrtc.logsize(prog, &loglen);
+  std::string log(loglen, '\0');
+  if (loglen) g_nvrtc.log(prog, &log[0]);
+  if (log_out) *log_out = log;
+  if (r != NVRTC_SUCCESS) {
+    g_nvrtc.destroy(&prog);
+    return fail(h, ODE_ENVRTC, "run-time compilation failed:\n" + log);
+  }
+  size_t n = 0;
+  g_nvrtc.cubinsize(prog, &n);
+  std::vector<char> cubin(n);
+  g_nvrtc.cubin(prog, cubin.data());
+  g_nvrtc.destroy(&prog);
+  CUmodule mod;
+  CUresult cr = g_drv.cuModuleLoadData(&mod, cubin.data());
+  if (cr != CUDA_SUCCESS) return cu_fail(h, cr, "cuModuleLoadData");
+  h->modules.push_back(mod);
+  cr = g_drv.cuModuleGetFunction(fn, mod, "gbode_jit");
+  if (cr != CUDA_SUCCESS) return cu_fail(h, cr, "cuModuleGetFunction");
+  return ODE_OK;
+}
+
+/* Find (or build) the kernel for this solve. */
+int get_kernel(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn, int* jit) {
+  const std::string key = kernel_key(h, a, sched);
+  auto it = h->kcache.find(key);
+  if (it != h->kcache.end()) {
+    *fn = it->second;
+    *jit = h->kjit[key];
+    return ODE_OK;
+  }
+  const char* kind = entry_kind(a->alg, sched);
+  for (const AotEntry& e : kAotEntries) {
+    if (e.alg == a->alg && e.rhs == a->rhs && e.dim == a->dim && e.precision == a->precision &&
+        std::strcmp(e.kind, kind) == 0) {
+      cudaFunction_t f;
+      cudaError_t ce = cudaGetFuncBySymbol(&f, e.fn);
+      if (ce != cudaSuccess) return cuda_fail(h, ce, "cudaGetFuncBySymbol");
+      *fn = (CUfunction)f;
+      h->kcache[key] = *fn;
+      h->kjit[key] = 0;
+      *jit = 0;
+      return ODE_OK;
+    }
+  }
+  int rc = compile_jit(h, a, sched, fn, nullptr);
+  if (rc != ODE_OK) return rc;
+  h->kcache[key] = *fn;
+  h->kjit[key] = 1;
+  *jit = 1;
+  return ODE_OK;
+}
+
+int launch(ode_handle* h, CUfunction fn, unsigned grid, KParams* kp, cudaStream_t s) {
+  void* params[] = {kp};
+  CUresult r = g_drv.cuLaunchKernel(fn, grid, 1, 1, 128, 1, 1, 0, (CUstream)s, params, nullptr);
+  if (r != CUDA_SUCCESS) return cu_fail(h, r, "cuLaunchKernel");
+  return ODE_OK;
+}
+
+template <class T>
+int grid_for(double t0, double dt, double tf, std::vector<double>* out, int64_t* len) {
+  int64_t n = jlrange::build<T>((T)t0, (T)dt, (T)tf, out);
+  if (n < 0) return ODE_EINVAL;
+  *len = n;
+  return ODE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ode_abi_version(void) { return ODE_ABI_VERSION; }
+
+int ode_create(ode_handle** out, int device) {
+  if (!out) return ODE_EINVAL;
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess) return ODE_ECUDA;
+  if (device < 0 || device >= ndev) return ODE_EINVAL;
+  ode_handle* h = new ode_handle();
+  h->device = device;
+  e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaFree(0);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&h->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&h->ev1);
+  if (e != cudaSuccess) {
+    ode_destroy(h);
+    return ODE_ECUDA;
+  }
+  if (!load_driver_api()) {
+    ode_destroy(h);
+    return ODE_ECUDA;
+  }
+  *out = h;
+  return ODE_OK;
+}
+
+void ode_destroy(ode_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->graph.exec) cudaGraphExecDestroy(h->graph.exec);
+  if (h->graph.graph) cudaGraphDestroy(h->graph.graph);
+  for (auto& kv : h->bufs)
+    if (kv.second.ptr) cudaFree(kv.second.ptr);
+  for (CUmodule m : h->modules) g_drv.cuModuleUnload(m);
+  if (h->model) model_free(h->model);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+const char* ode_last_error(const ode_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int ode_fixed_grid(double t0, double dt, double tf, int precision, double* out, int64_t cap, int64_t* len) {
+  if (!len || !(dt == dt) || dt == 0.0) return ODE_EINVAL;
+  std::vector<double> v;
+  int rc = (precision == ODE_FP32) ? grid_for<float>(t0, dt, tf, &v, len) : grid_for<double>(t0, dt, tf, &v, len);
+  if (rc != ODE_OK) return rc;
+  if (out)
+    for (int64_t i = 0; i < std::min<int64_t>(cap, *len); ++i) out[i] = v[(size_t)i];
+  return ODE_OK;
+}
+
+int ode_rhs_compile(ode_handle* h, const char* body, int dim, int nparams, int* rhs_id, char* log, size_t loglen) {
+  if (!h || !body || !rhs_id || dim < 1 || dim > 32 || nparams < 0 || nparams > 256)
+    return fail(h, ODE_EINVAL, "ode_rhs_compile: bad arguments");
+  cudaSetDevice(h->device);
+  UserRhs u;
+  u.body = body;
+  u.dim = dim;
+  u.nparams = nparams;
+  h->users.push_back(u);
+  const int id = ODE_RHS_USER + (int)h->users.size() - 1;
+  /* compile one probe kernel now so that syntax errors surface here */
+  ode_solve_args a;
+  std::memset(&a, 0, sizeof a);
+  a.alg = ODE_ALG_ATSIT5;
+  a.rhs = id;
+  a.precision = ODE_FP64;
+  a.dim = dim;
+  a.nparams = nparams;
+  CUfunction fn;
+  std::string lg;
+  int rc = compile_jit(h, &a, ODE_SCHED_PLAIN, &fn, &lg);
+  if (log && loglen) {
+    std::strncpy(log, lg.c_str(), loglen - 1);
+    log[loglen - 1] = '\0';
+  }
+  if (rc != ODE_OK) {
+    h->users.pop_back();
+    return rc;
+  }
+  h->kcache[kernel_key(h, &a, ODE_SCHED_PLAIN)] = fn;
+  h->kjit[kernel_key(h, &a, ODE_SCHED_PLAIN)] = 1;
+  *rhs_id = id;
+  return ODE_OK;
+}
+
+int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_solve_stats* st) {
+  const auto wall0 = std::chrono::steady_clock::now();
+  if (!h) return ODE_EINVAL;
+  if (!a || !o) return fail(h, ODE_EINVAL, "null argument");
+  h->err.clear();
+  if (a->alg < ODE_ALG_RK4 || a->alg > ODE_ALG_AVERN9) return fail(h, ODE_EINVAL, "unknown algorithm");
+  if (a->precision < ODE_FP64 || a->precision > ODE_FP32_KAHAN) return fail(h, ODE_EINVAL, "unknown precision");
+  if (a->schedule < ODE_SCHED_PLAIN || a->schedule > ODE_SCHED_LEARNED) return fail(h, ODE_EINVAL, "unknown schedule");
+  if (a->memory != ODE_MEM_HOST && a->memory != ODE_MEM_DEVICE) return fail(h, ODE_EINVAL, "unknown memory kind");
+  if (a->n < 0 || a->n > 0x7fffffffLL) return fail(h, ODE_EINVAL, "n must be in [0, 2^31)");
+  if (a->n > 0 && (!a->u0 || (a->nparams > 0 && !a->p))) return fail(h, ODE_EINVAL, "u0/p missing");
+  if (!(a->t0 == a->t0) || !(a->tf == a->tf) || !(a->dt == a->dt))
+    return fail(h, ODE_EINVAL, "t0, tf and dt must not be NaN");
+  if (a->nsave < 0 || (a->nsave > 0 && !a->saveat)) return fail(h, ODE_EINVAL, "saveat missing");
+  if (a->alg == ODE_ALG_RK4 && a->nsave > 0)
+    return fail(h, ODE_EINVAL, "GPUSimpleRK4 has no saveat (it saves every step; use save_everystep)");
+  int rc = check_rhs(h, a);
+  if (rc != ODE_OK) return rc;
+  const bool fixed = is_fixed(a->alg);
+  if (fixed && a->dt == 0.0) return fail(h, ODE_EINVAL, "dt is required for fixed-step algorithms");
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  cudaStream_t s = a->stream ? (cudaStream_t)a->stream : h->stream;
+  const int64_t n = a->n;
+  const int D = a->dim, NP = a->nparams;
+
+  int sched = fixed ? ODE_SCHED_PLAIN : a->schedule;
+  if (sched == ODE_SCHED_LEARNED && !model_ready(h->model, a)) {
+    return fail(h, ODE_ENOMODEL, "learned schedule requested but no model fitted for this problem shape");
+  }
+
+  /* time grid of the fixed-step solvers */
+  std::vector<double> grid;
+  int64_t ngrid = 0;
+  if (fixed) {
+    rc = (a->precision == ODE_FP32) ? grid_for<float>(a->t0, a->dt, a->tf, &grid, &ngrid)
+                                    : grid_for<double>(a->t0, a->dt, a->tf, &grid, &ngrid);
+    if (rc != ODE_OK) return fail(h, rc, "invalid fixed-step grid");
+  }
+  int64_t npoints = a->nsave;
+  if (fixed && a->nsave == 0 && a->save_everystep) npoints = ngrid;
+
+  CUfunction fn;
+  int jit = 0;
+  rc = get_kernel(h, a, sched, &fn, &jit);
+  if (rc != ODE_OK) return rc;
+
+  KParams kp;
+  std::memset(&kp, 0, sizeof kp);
+  kp.n = n;
+  kp.t0 = a->t0;
+  kp.tf = a->tf;
+  kp.dt = a->dt;
+  kp.abstol = a->abstol;
+  kp.reltol = a->reltol;
+  kp.nsave = a->nsave;
+  kp.ngrid = ngrid;
+  kp.save_everystep = a->save_everystep ? 1 : 0;
+  kp.dim = D;
+  kp.nparams = NP;
+  kp.maxiters = a->maxiters > 0 ? a->maxiters : kDefaultMaxIters;
+
+  const bool host = a->memory == ODE_MEM_HOST;
+  const size_t nd = (size_t)n * sizeof(double);
+  /* inputs */
+  if (host) {
+    double* du0 = (double*)buf(h, "u0", nd * D, &rc);
+    if (!du0) return rc;
+    double* dp = (double*)buf(h, "p", nd * (NP > 0 ? NP : 1), &rc);
+    if (!dp) return rc;
+    if (n > 0) {
+      CK(cudaMemcpyAsync(du0, a->u0, nd * D, cudaMemcpyHostToDevice, s), "copy u0");
+      if (NP > 0) CK(cudaMemcpyAsync(dp, a->p, nd * NP, cudaMemcpyHostToDevice, s), "copy p");
+    }
+    kp.u0 = du0;
+    kp.p = dp;
+    if (a->dt0) {
+      double* dd = (double*)buf(h, "dt0", nd, &rc);
+      if (!dd) return rc;
+      CK(cudaMemcpyAsync(dd, a->dt0, nd, cudaMemcpyHostToDevice, s), "copy dt0");
+      kp.dt0 = dd;
+    }
+  } else {
+    kp.u0 = a->u0;
+    kp.p = a->p;
+    kp.dt0 = a->dt0;
+  }
+  if (a->nsave > 0) {
+    double* ds = (double*)buf(h, "saveat", (size_t)a->nsave * sizeof(double), &rc);
+    if (!ds) return rc;
+    CK(cudaMemcpyAsync(ds, a->saveat, (size_t)a->nsave * sizeof(double), cudaMemcpyHostToDevice, s), "copy saveat");
+    kp.saveat = ds;
+  }
+  if (fixed && ngrid > 0) {
+    double* dg = (double*)buf(h, "grid", (size_t)ngrid * sizeof(double), &rc);
+    if (!dg) return rc;
+    CK(cudaMemcpyAsync(dg, grid.data(), (size_t)ngrid * sizeof(double), cudaMemcpyHostToDevice, s), "copy grid");
+    kp.grid = dg;
+  }
+  /* outputs */
+  struct OutMap { void* host; const char* name; size_t bytes; void** dev; };
+  OutMap outs[] = {
+      {o->us, "us", (size_t)npoints * D * nd, (void**)&kp.us},
+      {o->u_final, "u_final", nd * D, (void**)&kp.u_final},
+      {o->t_final, "t_final", nd, (void**)&kp.t_final},
+      {o->retcode, "retcode", (size_t)n, (void**)&kp.retcode},
+      {o->naccept, "naccept", (size_t)n * 4, (void**)&kp.naccept},
+      {o->nreject, "nreject", (size_t)n * 4, (void**)&kp.nreject},
+      {o->dt_first, "dt_first", nd, (void**)&kp.dt_first},
+  };
+  for (OutMap& m : outs) {
+    if (!m.host || m.bytes == 0) continue;
+    if (host) {
+      void* d = buf(h, m.name, m.bytes, &rc);
+      if (!d) return rc;
+      *m.dev = d;
+    } else {
+      *m.dev = m.host;
+    }
+  }
+  unsigned long long* stats = (unsigned long long*)buf(h, "stats", 4 * sizeof(unsigned long long), &rc);
+  if (!stats) return rc;
+  kp.stats = stats;
+  kp.counter = stats + 3;
+
+  /* schedule */
+  int launches = 0;
+  unsigned gridx;
+  if (sched == ODE_SCHED_PLAIN) {
+    gridx = (unsigned)((n + 127) / 128);
+  } else {
+    int nb = 0;
+    CUresult cr = g_drv.cuOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, 0);
+    if (cr != CUDA_SUCCESS) return cu_fail(h, cr, "occupancy");
+    if (nb < 1) nb = 1;
+    const int64_t resident = (int64_t)nb * h->nsm;
+    gridx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(resident, (n + 127) / 128));
+  }
+
+  CK(cudaMemsetAsync(stats, 0, 4 * sizeof(unsigned long long), s), "memset stats");
+  if (sched == ODE_SCHED_LEARNED) {
+    float* latt = (float*)buf(h, "pred_att", (size_t)n * 4, &rc);
+    if (!latt) return rc;
+    float* ldt = (float*)buf(h, "pred_dt", (size_t)n * 4, &rc);
+    if (!ldt) return rc;
+    int* order = (int*)buf(h, "order", (size_t)n * 4 + 16, &rc);
+    if (!order) return rc;
+    rc = model_predict_device(h, a, kp, latt, ldt, s, &launches);
+    if (rc != ODE_OK) return rc;
+    rc = order_by_cost(h, latt, n, order, s, &launches);
+    if (rc != ODE_OK) return rc;
+    kp.order = order;
+    if (!a->dt0 && model_seed_dt0(h->model)) {
+      double* dd = (double*)buf(h, "dt0_seed", nd, &rc);
+      if (!dd) return rc;
+      rc = seed_dt0(h, ldt, n, model_dt0_safety(h->model), dd, s, &launches);
+      if (rc != ODE_OK) return rc;
+      kp.dt0 = dd;
+    }
+  }
+  CK(cudaEventRecord(h->ev0, s), "event");
+  if (n > 0) {
+    rc = launch(h, fn, gridx, &kp, s);
+    if (rc != ODE_OK) return rc;
+    ++launches;
+  }
+  CK(cudaEventRecord(h->ev1, s), "event");
+
+  /* outputs back to the host */
+  if (host) {
+    for (OutMap& m : outs)
+      if (m.host && m.bytes) CK(cudaMemcpyAsync(m.host, *m.dev, m.bytes, cudaMemcpyDeviceToHost, s), "copy out");
+  }
+  unsigned long long hs[4] = {0, 0, 0, 0};
+  CK(cudaMemcpyAsync(hs, stats, sizeof hs, cudaMemcpyDeviceToHost, s), "copy stats");
+  CK(cudaStreamSynchronize(s), "solve");
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  if (st) {
+    st->kernel_ms = ms;
+    st->attempts = (int64_t)hs[0];
+    st->saves = (int64_t)hs[1];
+    st->launches = launches;
+    st->schedule_used = sched;
+    st->graph_replayed = 0;
+    st->jit = jit;
+    st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
+  }
+  if (hs[2] > 0) {
+    char m[128];
+    snprintf(m, sizeof m, "%llu trajectories stopped early (dt<dtmin or maxiters); see retcode", hs[2]);
+    return fail(h, ODE_ETRAJ, m);
+  }
+  return ODE_OK;
+}
+
+}  // extern "C"

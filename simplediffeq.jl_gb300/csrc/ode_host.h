@@ -1,0 +1,78 @@
+/* Internal host-side declarations shared by the library's translation units. */
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/gb300ode.h"
+#include "ode_kparams.h"
+
+namespace gbode {
+
+/* Growable device buffer owned by a handle. */
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t cap = 0;
+};
+
+struct UserRhs {
+  std::string body;
+  int dim = 0, nparams = 0;
+};
+
+struct Model;  /* learned-schedule model, defined in learn.cu */
+
+struct GraphEntry {
+  std::string key;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+}  // namespace gbode
+
+struct ode_handle {
+  int device = 0;
+  int nsm = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+  std::map<std::string, gbode::DevBuf> bufs;
+  std::map<std::string, CUfunction> kcache;
+  std::map<std::string, int> kjit;  /* 1 if the cached function was compiled at run time */
+  std::vector<CUmodule> modules;
+  std::vector<gbode::UserRhs> users;
+  gbode::GraphEntry graph;
+  gbode::Model* model = nullptr;
+};
+
+namespace gbode {
+
+/* error helpers: record a message on the handle and return the code */
+int fail(ode_handle* h, int code, const std::string& msg);
+int cuda_fail(ode_handle* h, cudaError_t e, const char* what);
+int cu_fail(ode_handle* h, CUresult r, const char* what);
+
+/* device buffer of at least `bytes` bytes under `name` (contents not kept on growth) */
+void* buf(ode_handle* h, const std::string& name, size_t bytes, int* rc);
+
+/* learned schedule hooks (learn.cu) */
+void model_free(Model* m);
+/* Predict per-trajectory (log attempts, log dt_first) on the device for the
+ * inputs in `kp` (device pointers); writes keys for ordering and, if
+ * dt0_out is non-null, the seeded initial dt.  Enqueued on `s`. */
+int model_predict_device(ode_handle* h, const ode_solve_args* a, const KParams& kp, float* log_att,
+                         float* log_dt, cudaStream_t s, int* launches);
+/* Order trajectories by predicted cost, longest first: order[n] on the device. */
+int order_by_cost(ode_handle* h, const float* log_att, int64_t n, int* order, cudaStream_t s, int* launches);
+/* dt0[i] = safety * exp(log_dt[i]) */
+int seed_dt0(ode_handle* h, const float* log_dt, int64_t n, float safety, double* dt0, cudaStream_t s,
+             int* launches);
+bool model_ready(const Model* m, const ode_solve_args* a);
+float model_dt0_safety(const Model* m);
+bool model_seed_dt0(const Model* m);
+
+}  // namespace gbode

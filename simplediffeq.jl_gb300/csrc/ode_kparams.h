@@ -1,0 +1,35 @@
+/* Launch parameters of the solver kernels.  Shared verbatim by the host
+ * library (g++/nvcc) and by kernels compiled at run time with NVRTC, so it
+ * uses only built-in types. */
+#pragma once
+
+namespace gbode {
+
+enum { RET_DEFAULT = 0, RET_DTMIN = 1, RET_MAXITERS = 2, RET_NAN = 3 };
+
+struct KParams {
+  long long n;             /* trajectories */
+  double t0, tf, dt, abstol, reltol;
+  const double* u0;        /* [dim][n] */
+  const double* p;         /* [nparams][n] */
+  const double* dt0;       /* [n] per-trajectory initial dt, or 0 */
+  const double* saveat;    /* [nsave] on the device, or 0 */
+  long long nsave;
+  const double* grid;      /* fixed-step time grid [ngrid] on the device, or 0 */
+  long long ngrid;
+  int save_everystep;
+  int dim, nparams;
+  long long maxiters;      /* <= 0: no cap */
+  double* us;              /* [npoints][dim][n] or 0 */
+  double* u_final;         /* [dim][n] or 0 */
+  double* t_final;         /* [n] or 0 */
+  signed char* retcode;    /* [n] or 0 */
+  int* naccept;            /* [n] or 0 */
+  int* nreject;            /* [n] or 0 */
+  double* dt_first;        /* [n] or 0 */
+  const int* order;        /* persistent: position -> trajectory, or 0 for identity */
+  unsigned long long* counter;   /* persistent: next position to hand out (zeroed before launch) */
+  unsigned long long* stats;     /* [2] attempts and saves summed over trajectories, or 0 */
+};
+
+}  // namespace gbode

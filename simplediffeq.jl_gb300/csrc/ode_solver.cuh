@@ -1,0 +1,970 @@
+/* Device side of the ensemble solver: one trajectory per thread.
+ *
+ * Compiled ahead of time by nvcc (kern_*.cu) and at run time by NVRTC for
+ * combinations that are not prebuilt, so it includes nothing but the two
+ * project headers and uses only CUDA built-ins.
+ *
+ * The solver loop is the reference's (SimpleDiffEq.jl):
+ *   adaptive:  src/tsit5/gpuatsit5.jl:250-320, src/verner/gpuvern7.jl:353-520,
+ *              src/verner/gpuvern9.jl:461-763 — stages, embedded error, RMS
+ *              norm, PI controller with reject/retry, saveat interpolation;
+ *   fixed:     src/tsit5/gpuatsit5.jl:95-129, src/verner/gpuvern7.jl:104-224,
+ *              src/verner/gpuvern9.jl:102-335, src/rk4/gpurk4.jl:73-85.
+ * It is written as a flat loop of attempts (one iteration = one stage
+ * evaluation of a step attempt plus its accept/reject decision), which runs
+ * the same sequence of operations as the reference's nested
+ * `while t < tf; while EEst > 1` loops and lets the persistent kernel hand a
+ * finished lane a new trajectory between two attempts.
+ *
+ * Rounding canon (matched bit for bit by the oracle's DEVICE mode):
+ *   - each multiply-add of the reference's expressions is one fused
+ *     multiply-add; linear combinations sum_j c_j k_j accumulate from the last
+ *     term to the first (the nesting @muladd produces); no other operation is
+ *     fused (the files are compiled with --fmad=false);
+ *   - stage times t + c*dt and Horner steps of the dense-output polynomials
+ *     are fused, as Julia fuses scalar muladd;
+ *   - the step-size factor q (q11 = EEst^beta1, qold^beta2, the clamps and the
+ *     reciprocal applied to dt) is computed in single precision with the
+ *     deterministic ctrl_pow below; dt, t, the state and the error estimate
+ *     keep the solver precision.
+ */
+#pragma once
+#include "ode_kparams.h"
+#include "tableaus.h"
+
+namespace gbode {
+
+/* ------------------------------------------------------------------ math */
+__device__ __forceinline__ double fmaR(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fmaR(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double sqrtR(double x) { return __dsqrt_rn(x); }
+__device__ __forceinline__ float sqrtR(float x) { return __fsqrt_rn(x); }
+__device__ __forceinline__ double absR(double x) { return fabs(x); }
+__device__ __forceinline__ float absR(float x) { return fabsf(x); }
+__device__ __forceinline__ double sinR(double x) { return sin(x); }
+__device__ __forceinline__ float sinR(float x) { return sinf(x); }
+__device__ __forceinline__ double cosR(double x) { return cos(x); }
+__device__ __forceinline__ float cosR(float x) { return cosf(x); }
+
+/* Julia's min/max propagate NaN; @fastmath min/max are compare-and-select. */
+template <class X> __device__ __forceinline__ X jmin(X a, X b) { return (a != a || b != b) ? a + b : (b < a ? b : a); }
+template <class X> __device__ __forceinline__ X jmax(X a, X b) { return (a != a || b != b) ? a + b : (b > a ? b : a); }
+template <class X> __device__ __forceinline__ X fm_min(X x, X y) { return (y > x) ? x : y; }
+template <class X> __device__ __forceinline__ X fm_max(X x, X y) { return (y > x) ? y : x; }
+
+/* Single-precision x^b for the step-size controller (x >= 0 or NaN).
+ * log2 from the atanh series of the reduced mantissa, 2^y from the Taylor
+ * series of exp on [-ln2/2, ln2/2]; every step is one IEEE single operation,
+ * so the result is identical on any IEEE-754 machine. */
+__device__ __forceinline__ float ctrl_log2(float x) {
+  int e = 0;
+  if (x < 1.17549435e-38f) { x = x * 16777216.0f; e = -24; }
+  unsigned u = __float_as_uint(x);
+  e += (int)((u >> 23) & 0xffu) - 127;
+  float m = __uint_as_float((u & 0x007fffffu) | 0x3f800000u);
+  if (m > 1.41421354f) { m = m * 0.5f; e += 1; }
+  float s = __fdiv_rn(m - 1.0f, m + 1.0f);
+  float s2 = s * s;
+  float poly = __fmaf_rn(s2, 0.0909090936f, 0.111111112f);
+  poly = __fmaf_rn(s2, poly, 0.142857149f);
+  poly = __fmaf_rn(s2, poly, 0.200000003f);
+  poly = __fmaf_rn(s2, poly, 0.333333343f);
+  poly = __fmaf_rn(s2, poly, 1.0f);
+  float atanh_s = s * poly;
+  return __fmaf_rn(atanh_s, 2.88539004f, (float)e);
+}
+__device__ __forceinline__ float ctrl_exp2(float y) {
+  if (y > 128.0f) return __int_as_float(0x7f800000);
+  if (y < -150.0f) return 0.0f;
+  float n = rintf(y);
+  float f = y - n;
+  float z = f * 0.693147182f;
+  float p = __fmaf_rn(z, 2.48015876e-05f, 1.98412701e-04f);
+  p = __fmaf_rn(z, p, 1.38888892e-03f);
+  p = __fmaf_rn(z, p, 8.33333377e-03f);
+  p = __fmaf_rn(z, p, 4.16666679e-02f);
+  p = __fmaf_rn(z, p, 0.166666672f);
+  p = __fmaf_rn(z, p, 0.5f);
+  p = __fmaf_rn(z, p, 1.0f);
+  p = __fmaf_rn(z, p, 1.0f);
+  int ni = (int)n;
+  int h = ni / 2;
+  float s1 = __uint_as_float((unsigned)(h + 127) << 23);
+  float s2 = __uint_as_float((unsigned)(ni - h + 127) << 23);
+  return (p * s1) * s2;
+}
+__device__ __forceinline__ float ctrl_pow(float x, float b) {
+  if (x != x) return x;
+  if (x == 0.0f) return 0.0f;
+  if (x == __int_as_float(0x7f800000)) return x;
+  return ctrl_exp2(b * ctrl_log2(x));
+}
+
+/* ------------------------------------------------------------------ precisions */
+struct PFP64 { typedef double R; typedef double T; enum { KAHAN = 0 }; };
+struct PFP32 { typedef float R; typedef float T; enum { KAHAN = 0 }; };
+struct PFP32K { typedef float R; typedef double T; enum { KAHAN = 1 }; };
+
+/* ------------------------------------------------------------------ tableaus in constant memory */
+__constant__ double c_tsit5_d[tsit5_COUNT] = GBTAB_TSIT5_INIT;
+__constant__ float c_tsit5_f[tsit5_COUNT] = GBTAB_TSIT5_INIT;
+__constant__ double c_vern7_d[vern7_COUNT] = GBTAB_VERN7_INIT;
+__constant__ float c_vern7_f[vern7_COUNT] = GBTAB_VERN7_INIT;
+__constant__ double c_vern7x_d[vern7x_COUNT] = GBTAB_VERN7X_INIT;
+__constant__ float c_vern7x_f[vern7x_COUNT] = GBTAB_VERN7X_INIT;
+__constant__ double c_vern7r_d[vern7r_COUNT] = GBTAB_VERN7R_INIT;
+__constant__ float c_vern7r_f[vern7r_COUNT] = GBTAB_VERN7R_INIT;
+__constant__ double c_vern9_d[vern9_COUNT] = GBTAB_VERN9_INIT;
+__constant__ float c_vern9_f[vern9_COUNT] = GBTAB_VERN9_INIT;
+__constant__ double c_vern9x_d[vern9x_COUNT] = GBTAB_VERN9X_INIT;
+__constant__ float c_vern9x_f[vern9x_COUNT] = GBTAB_VERN9X_INIT;
+__constant__ double c_vern9r_d[vern9r_COUNT] = GBTAB_VERN9R_INIT;
+__constant__ float c_vern9r_f[vern9r_COUNT] = GBTAB_VERN9R_INIT;
+
+template <class X> struct CB;
+template <> struct CB<double> {
+  __device__ static __forceinline__ double t5(int i) { return c_tsit5_d[i]; }
+  __device__ static __forceinline__ double v7(int i) { return c_vern7_d[i]; }
+  __device__ static __forceinline__ double v7x(int i) { return c_vern7x_d[i]; }
+  __device__ static __forceinline__ double v7r(int i) { return c_vern7r_d[i]; }
+  __device__ static __forceinline__ double v9(int i) { return c_vern9_d[i]; }
+  __device__ static __forceinline__ double v9x(int i) { return c_vern9x_d[i]; }
+  __device__ static __forceinline__ double v9r(int i) { return c_vern9r_d[i]; }
+};
+template <> struct CB<float> {
+  __device__ static __forceinline__ float t5(int i) { return c_tsit5_f[i]; }
+  __device__ static __forceinline__ float v7(int i) { return c_vern7_f[i]; }
+  __device__ static __forceinline__ float v7x(int i) { return c_vern7x_f[i]; }
+  __device__ static __forceinline__ float v7r(int i) { return c_vern7r_f[i]; }
+  __device__ static __forceinline__ float v9(int i) { return c_vern9_f[i]; }
+  __device__ static __forceinline__ float v9x(int i) { return c_vern9x_f[i]; }
+  __device__ static __forceinline__ float v9r(int i) { return c_vern9r_f[i]; }
+};
+
+/* ------------------------------------------------------------------ vector algebra (D compile-time) */
+/* s = c1 k1 + c2 k2 + ... + cn kn, accumulated from the last term to the first */
+template <int D, class R>
+__device__ __forceinline__ void lc(R (&s)[D], R c, const R (&k)[D]) {
+#pragma unroll
+  for (int d = 0; d < D; ++d) s[d] = c * k[d];
+}
+template <int D, class R, class... Rest>
+__device__ __forceinline__ void lc(R (&s)[D], R c, const R (&k)[D], const Rest&... rest) {
+  lc(s, rest...);
+#pragma unroll
+  for (int d = 0; d < D; ++d) s[d] = fmaR(c, k[d], s[d]);
+}
+/* out = base + h * s */
+template <int D, class R>
+__device__ __forceinline__ void axpy(R (&out)[D], const R (&base)[D], R h, const R (&s)[D]) {
+#pragma unroll
+  for (int d = 0; d < D; ++d) out[d] = fmaR(h, s[d], base[d]);
+}
+/* stage time t + c*dt */
+template <class T>
+__device__ __forceinline__ T stime(T t, T c, T dt) { return fmaR(c, dt, t); }
+
+/* new state = old + h*s; in Kahan mode a compensated sum with value hi - c */
+template <class PR, int D>
+__device__ __forceinline__ void state_update(const typename PR::R (&uh)[D], const typename PR::R (&uc)[D],
+                                             typename PR::R h, const typename PR::R (&s)[D],
+                                             typename PR::R (&nh)[D], typename PR::R (&nc)[D]) {
+  typedef typename PR::R R;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    if (PR::KAHAN) {
+      R delta = h * s[d];
+      R y = delta - uc[d];
+      R sum = uh[d] + y;
+      nc[d] = (sum - uh[d]) - y;
+      nh[d] = sum;
+    } else {
+      nh[d] = fmaR(h, s[d], uh[d]);
+      nc[d] = (R)0;
+    }
+  }
+}
+
+/* dense-output value uprev + h*s, written as double */
+template <class PR, int D>
+__device__ __forceinline__ void finish_dense(const typename PR::R (&uh)[D], const typename PR::R (&uc)[D],
+                                             typename PR::R h, const typename PR::R (&s)[D], double (&out)[D]) {
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    if (PR::KAHAN) out[d] = ((double)uh[d] - (double)uc[d]) + (double)(h * s[d]);
+    else out[d] = (double)fmaR(h, s[d], uh[d]);
+  }
+}
+
+/* ------------------------------------------------------------------ right-hand sides */
+/* Each functor holds its parameters in registers and evaluates du = f(u, p, t).
+ * The forms match the oracle's DEVICE forms term for term. */
+template <class R, class T>
+struct RhsLorenz {
+  enum { D = 3, NP = 3 };
+  R p[3];
+  __device__ __forceinline__ void operator()(const R (&u)[3], T t, R (&du)[3]) const {
+    du[0] = p[0] * (u[1] - u[0]);
+    du[1] = fmaR(u[0], p[1] - u[2], -u[1]);
+    du[2] = fmaR(u[0], u[1], -(p[2] * u[2]));
+  }
+};
+
+template <class R, class T>
+struct RhsVanDerPol {
+  enum { D = 2, NP = 1 };
+  R p[1];
+  __device__ __forceinline__ void operator()(const R (&u)[2], T t, R (&du)[2]) const {
+    R w = fmaR(-u[0], u[0], (R)1);
+    du[0] = u[1];
+    du[1] = fmaR(p[0] * w, u[1], -u[0]);
+  }
+};
+
+template <class R, class T>
+struct RhsR3BP {
+  enum { D = 4, NP = 1 };
+  R p[1];
+  __device__ __forceinline__ void operator()(const R (&u)[4], T t, R (&du)[4]) const {
+    const R mu = p[0], mu1 = (R)1 - mu;
+    const R x = u[0], y = u[1], vx = u[2], vy = u[3];
+    const R a = x + mu, b = x - mu1;
+    const R r1 = fmaR(a, a, y * y), r2 = fmaR(b, b, y * y);
+    const R d1 = r1 * sqrtR(r1), d2 = r2 * sqrtR(r2);
+    const R g1 = mu1 / d1, g2 = mu / d2;
+    du[0] = vx;
+    du[1] = vy;
+    du[2] = fmaR(-g2, b, fmaR(-g1, a, fmaR((R)2, vy, x)));
+    du[3] = fmaR(-g2, y, fmaR(-g1, y, fmaR((R)-2, vx, y)));
+  }
+};
+
+template <class R, class T, int DD>
+struct RhsKuramoto {
+  enum { D = DD, NP = DD + 1 };
+  R p[DD + 1];
+  __device__ __forceinline__ void operator()(const R (&u)[DD], T t, R (&du)[DD]) const {
+    R sn[DD], cs[DD], S = 0, C = 0;
+#pragma unroll
+    for (int j = 0; j < DD; ++j) {
+      sn[j] = sinR(u[j]);
+      cs[j] = cosR(u[j]);
+      S = S + sn[j];
+      C = C + cs[j];
+    }
+    const R kd = p[DD] / (R)DD;
+#pragma unroll
+    for (int i = 0; i < DD; ++i) du[i] = fmaR(kd, fmaR(cs[i], S, -(sn[i] * C)), p[i]);
+  }
+};
+
+template <class R, class T, int DD>
+struct RhsLinear {
+  enum { D = DD, NP = DD * DD };
+  R p[DD * DD];
+  __device__ __forceinline__ void operator()(const R (&u)[DD], T t, R (&du)[DD]) const {
+#pragma unroll
+    for (int i = 0; i < DD; ++i) {
+      R s = p[i * DD] * u[0];
+#pragma unroll
+      for (int j = 1; j < DD; ++j) s = fmaR(p[i * DD + j], u[j], s);
+      du[i] = s;
+    }
+  }
+};
+
+/* ------------------------------------------------------------------ Tsitouras 5(4) */
+/* src/tsit5/gpuatsit5.jl:258-275 (stages, FSAL k7), :306-314 and
+ * src/tsit5/tsit5.jl:385-399 (dense output). */
+template <class PR, int D, class F>
+struct MTsit5 {
+  typedef typename PR::R R;
+  typedef typename PR::T T;
+  enum { NK = 7, FSAL = 1, DTMIN_1F7 = 0 };
+
+  __device__ static __forceinline__ void attempt(const F& f, const R (&uh)[D], const R (&uc)[D], T t, T dt,
+                                                 R (&k)[NK][D], R (&nh)[D], R (&nc)[D], R (&e)[D], bool want_err) {
+#define C5(x) CB<R>::t5(tsit5_##x)
+#define C5T(x) CB<T>::t5(tsit5_##x)
+    R tmp[D], s[D];
+    const R h = (R)dt;
+    const R a = (R)(dt * C5T(a21));
+#pragma unroll
+    for (int d = 0; d < D; ++d) tmp[d] = fmaR(a, k[0][d], uh[d]);
+    f(tmp, stime(t, C5T(c1), dt), k[1]);
+    lc(s, C5(a31), k[0], C5(a32), k[1]);
+    axpy(tmp, uh, h, s);
+    f(tmp, stime(t, C5T(c2), dt), k[2]);
+    lc(s, C5(a41), k[0], C5(a42), k[1], C5(a43), k[2]);
+    axpy(tmp, uh, h, s);
+    f(tmp, stime(t, C5T(c3), dt), k[3]);
+    lc(s, C5(a51), k[0], C5(a52), k[1], C5(a53), k[2], C5(a54), k[3]);
+    axpy(tmp, uh, h, s);
+    f(tmp, stime(t, C5T(c4), dt), k[4]);
+    lc(s, C5(a61), k[0], C5(a62), k[1], C5(a63), k[2], C5(a64), k[3], C5(a65), k[4]);
+    axpy(tmp, uh, h, s);
+    f(tmp, t + dt, k[5]);
+    lc(s, C5(a71), k[0], C5(a72), k[1], C5(a73), k[2], C5(a74), k[3], C5(a75), k[4], C5(a76), k[5]);
+    state_update<PR, D>(uh, uc, h, s, nh, nc);
+    f(nh, t + dt, k[6]);
+    if (want_err) {
+      lc(s, C5(btilde1), k[0], C5(btilde2), k[1], C5(btilde3), k[2], C5(btilde4), k[3], C5(btilde5), k[4],
+         C5(btilde6), k[5], C5(btilde7), k[6]);
+#pragma unroll
+      for (int d = 0; d < D; ++d) e[d] = h * s[d];
+    }
+  }
+
+  __device__ static __forceinline__ void dense(const F& f, const R (&uh)[D], const R (&uc)[D], T told, T tnew,
+                                               T dtold, T theta, R (&k)[NK][D], double (&out)[D]) {
+    const R th = (R)theta;
+    R ex, b1, b2, b3, b4, b5, b6, b7;
+    ex = C5(r14); ex = fmaR(th, ex, C5(r13)); ex = fmaR(th, ex, C5(r12)); ex = fmaR(th, ex, C5(r11)); b1 = th * ex;
+#define TSIT5_B(i, out_)                                                        \
+  ex = C5(r##i##4); ex = fmaR(th, ex, C5(r##i##3)); ex = fmaR(th, ex, C5(r##i##2)); \
+  ex = th * ex; out_ = th * ex;
+    TSIT5_B(2, b2) TSIT5_B(3, b3) TSIT5_B(4, b4) TSIT5_B(5, b5) TSIT5_B(6, b6) TSIT5_B(7, b7)
+#undef TSIT5_B
+    R s[D];
+    lc(s, b1, k[0], b2, k[1], b3, k[2], b4, k[3], b5, k[4], b6, k[5], b7, k[6]);
+    finish_dense<PR, D>(uh, uc, (R)dtold, s, out);
+#undef C5
+#undef C5T
+  }
+};
+
+/* ------------------------------------------------------------------ Verner 7(6) */
+/* src/verner/gpuvern7.jl:360-404 (adaptive attempt), :107-136 (fixed step),
+ * :441-513 dense output with six extra stages at t + c*dtold (t already
+ * advanced), bθs at src/verner/verner_tableaus.jl:1337-1360. */
+template <class PR, int D, class F>
+struct MVern7 {
+  typedef typename PR::R R;
+  typedef typename PR::T T;
+  enum { NK = 10, FSAL = 0, DTMIN_1F7 = 0 };
+
+  __device__ static __forceinline__ void attempt(const F& f, const R (&uh)[D], const R (&uc)[D], T t, T dt,
+                                                 R (&k)[NK][D], R (&nh)[D], R (&nc)[D], R (&e)[D], bool want_err) {
+#define C7(x) CB<R>::v7(vern7_##x)
+#define C7T(x) CB<T>::v7(vern7_##x)
+    R tmp[D], s[D];
+    const R h = (R)dt;
+    f(uh, t, k[0]);
+    const R a = (R)(dt * C7T(a021));
+#pragma unroll
+    for (int d = 0; d < D; ++d) tmp[d] = fmaR(a, k[0][d], uh[d]);
+    f(tmp, stime(t, C7T(c2), dt), k[1]);
+    lc(s, C7(a031), k[0], C7(a032), k[1]);
+    axpy(tmp, uh, h, s); f(tmp, stime(t, C7T(c3), dt), k[2]);
+    lc(s, C7(a041), k[0], C7(a043), k[2]);
+    axpy(tmp, uh, h, s); f(tmp, stime(t, C7T(c4), dt), k[3]);
+    lc(s, C7(a051), k[0], C7(a053), k[2], C7(a054), k[3]);
+    axpy(tmp, uh, h, s); f(tmp, stime(t, C7T(c5), dt), k[4]);
+    lc(s, C7(a061), k[0], C7(a063), k[2], C7(a064), k[3], C7(a065), k[4]);
+    axpy(tmp, uh, h, s); f(tmp, stime(t, C7T(c6), dt), k[5]);
+    lc(s, C7(a071), k[0], C7(a073), k[2], C7(a074), k[3], C7(a075), k[4], C7(a076), k[5]);
+    axpy(tmp, uh, h, s); f(tmp, stime(t, C7T(c7), dt), k[6]);
+    lc(s, C7(a081), k[0], C7(a083), k[2], C7(a084), k[3], C7(a085), k[4], C7(a086), k[5], C7(a087), k[6]);
+    axpy(tmp, uh, h, s); f(tmp, stime(t, C7T(c8), dt), k[7]);
+    R g10[D];
+    lc(s, C7(a091), k[0], C7(a093), k[2], C7(a094), k[3], C7(a095), k[4], C7(a096), k[5], C7(a097), k[6],
+       C7(a098), k[7]);
+    axpy(tmp, uh, h, s);
+    lc(s, C7(a101), k[0], C7(a103), k[2], C7(a104), k[3], C7(a105), k[4], C7(a106), k[5], C7(a107), k[6]);
+    axpy(g10, uh, h, s);
+    f(tmp, t + dt, k[8]);
+    f(g10, t + dt, k[9]);
+    lc(s, C7(b1), k[0], C7(b4), k[3], C7(b5), k[4], C7(b6), k[5], C7(b7), k[6], C7(b8), k[7], C7(b9), k[8]);
+    state_update<PR, D>(uh, uc, h, s, nh, nc);
+    if (want_err) {
+      lc(s, C7(btilde1), k[0], C7(btilde4), k[3], C7(btilde5), k[4], C7(btilde6), k[5], C7(btilde7), k[6],
+         C7(btilde8), k[7], C7(btilde9), k[8], C7(btilde10), k[9]);
+#pragma unroll
+      for (int d = 0; d < D; ++d) e[d] = h * s[d];
+    }
+#undef C7
+#undef C7T
+  }
+
+  __device__ static __forceinline__ void dense(const F& f, const R (&uh)[D], const R (&uc)[D], T told, T tnew,
+                                               T dtold, T theta, R (&k)[NK][D], double (&out)[D]) {
+#define X7(x) CB<R>::v7x(vern7x_##x)
+#define X7T(x) CB<T>::v7x(vern7x_##x)
+#define R7(x) CB<R>::v7r(vern7r_##x)
+    const R h = (R)dtold;
+    R x[6][D], s[D], tmp[D];
+    lc(s, X7(a1101), k[0], X7(a1104), k[3], X7(a1105), k[4], X7(a1106), k[5], X7(a1107), k[6], X7(a1108), k[7],
+       X7(a1109), k[8]);
+    axpy(tmp, uh, h, s); f(tmp, stime(tnew, X7T(c11), dtold), x[0]);
+    lc(s, X7(a1201), k[0], X7(a1204), k[3], X7(a1205), k[4], X7(a1206), k[5], X7(a1207), k[6], X7(a1208), k[7],
+       X7(a1209), k[8], X7(a1211), x[0]);
+    axpy(tmp, uh, h, s); f(tmp, stime(tnew, X7T(c12), dtold), x[1]);
+    lc(s, X7(a1301), k[0], X7(a1304), k[3], X7(a1305), k[4], X7(a1306), k[5], X7(a1307), k[6], X7(a1308), k[7],
+       X7(a1309), k[8], X7(a1311), x[0], X7(a1312), x[1]);
+    axpy(tmp, uh, h, s); f(tmp, stime(tnew, X7T(c13), dtold), x[2]);
+    lc(s, X7(a1401), k[0], X7(a1404), k[3], X7(a1405), k[4], X7(a1406), k[5], X7(a1407), k[6], X7(a1408), k[7],
+       X7(a1409), k[8], X7(a1411), x[0], X7(a1412), x[1], X7(a1413), x[2]);
+    axpy(tmp, uh, h, s); f(tmp, stime(tnew, X7T(c14), dtold), x[3]);
+    lc(s, X7(a1501), k[0], X7(a1504), k[3], X7(a1505), k[4], X7(a1506), k[5], X7(a1507), k[6], X7(a1508), k[7],
+       X7(a1509), k[8], X7(a1511), x[0], X7(a1512), x[1], X7(a1513), x[2]);
+    axpy(tmp, uh, h, s); f(tmp, stime(tnew, X7T(c15), dtold), x[4]);
+    lc(s, X7(a1601), k[0], X7(a1604), k[3], X7(a1605), k[4], X7(a1606), k[5], X7(a1607), k[6], X7(a1608), k[7],
+       X7(a1609), k[8], X7(a1611), x[0], X7(a1612), x[1], X7(a1613), x[2]);
+    axpy(tmp, uh, h, s); f(tmp, stime(tnew, X7T(c16), dtold), x[5]);
+
+    const R th = (R)theta;
+    R b[13], ex;
+    ex = R7(r017); ex = fmaR(th, ex, R7(r016)); ex = fmaR(th, ex, R7(r015)); ex = fmaR(th, ex, R7(r014));
+    ex = fmaR(th, ex, R7(r013)); ex = fmaR(th, ex, R7(r012)); ex = fmaR(th, ex, R7(r011)); b[0] = th * ex;
+#define V7B(i, j)                                                                      \
+  ex = R7(r##i##7); ex = fmaR(th, ex, R7(r##i##6)); ex = fmaR(th, ex, R7(r##i##5));        \
+  ex = fmaR(th, ex, R7(r##i##4)); ex = fmaR(th, ex, R7(r##i##3)); ex = fmaR(th, ex, R7(r##i##2)); \
+  ex = th * ex; b[j] = th * ex;
+    V7B(04, 1) V7B(05, 2) V7B(06, 3) V7B(07, 4) V7B(08, 5) V7B(09, 6)
+    V7B(11, 7) V7B(12, 8) V7B(13, 9) V7B(14, 10) V7B(15, 11) V7B(16, 12)
+#undef V7B
+    lc(s, b[0], k[0], b[1], k[3], b[2], k[4], b[3], k[5], b[4], k[6], b[5], k[7], b[6], k[8], b[7], x[0],
+       b[8], x[1], b[9], x[2], b[10], x[3], b[11], x[4], b[12], x[5]);
+    finish_dense<PR, D>(uh, uc, h, s, out);
+#undef X7
+#undef X7T
+#undef R7
+  }
+};
+
+/* ------------------------------------------------------------------ Verner 9(8) */
+/* src/verner/gpuvern9.jl:468-573 (adaptive attempt, dtmin and end snap 1f-7),
+ * :105-183 (fixed step, no k16), dense output :631-757 (adaptive: relabelled
+ * k2..k9 := k8..k15, stage times told + c*dtold) and :216-331 (fixed step:
+ * stages 2..9 as they are, times t + c*dt with t advanced). */
+template <class PR, int D, class F, bool ADAPTIVE>
+struct MVern9Impl {
+  typedef typename PR::R R;
+  typedef typename PR::T T;
+  enum { NK = 16, FSAL = 0, DTMIN_1F7 = 1 };
+
+  __device__ static __forceinline__ void attempt(const F& f, const R (&uh)[D], const R (&uc)[D], T t, T dt,
+                                                 R (&k)[NK][D], R (&nh)[D], R (&nc)[D], R (&e)[D], bool want_err) {
+#define C9(x) CB<R>::v9(vern9_##x)
+#define C9T(x) CB<T>::v9(vern9_##x)
+    R tmp[D], s[D];
+    const R h = (R)dt;
+    f(uh, t, k[0]);
+    const R a = (R)(dt * C9T(a0201));
+#pragma unroll
+    for (int d = 0; d < D; ++d) tmp[d] = fmaR(a, k[0][d], uh[d]);
+    f(tmp, stime(t, C9T(c1), dt), k[1]);
+    lc(s, C9(a0301), k[0], C9(a0302), k[1]);
+    axpy(tmp, uh, h, s); f(tmp, stime(t, C9T(c2), dt), k[2]);
+    lc(s, C9(a0401), k[0], C9(a0403), k[2]);
+    axpy(tmp, uh, h, s); f(tmp, stime(t, C9T(c3), dt), k[3]);
+    lc(s, C9(a0501), k[0], C9(a0503), k[2], C9(a0504), k[3]);
+    axpy(tmp, uh, h, s); f(tmp, stime(t, C9T(c4), dt), k[4]);
+    lc(s, C9(a0601), k[0], C9(a0604), k[3], C9(a0605), k[4]);
+    axpy(tmp, uh, h, s); f(tmp, stime(t, C9T(c5), dt), k[5]);
+    lc(s, C9(a0701), k[0], C9(a0704), k[3], C9(a0705), k[4], C9(a0706), k[5]);
+    axpy(tmp, uh, h, s); f(tmp, stime(t, C9T(c6), dt), k[6]);
+    lc(s, C9(a0801), k[0], C9(a0806), k[5], C9(a0807), k[6]);
+    axpy(tmp, uh, h, s); f(tmp, stime(t, C9T(c7), dt), k[7]);
+    lc(s, C9(a0901), k[0], C9(a0906), k[5], C9(a0907), k[6], C9(a0908), k[7]);
+    axpy(tmp, uh, h, s); f(tmp, stime(t, C9T(c8), dt), k[8]);
+    lc(s, C9(a1001), k[0], C9(a1006), k[5], C9(a1007), k[6], C9(a1008), k[7], C9(a1009), k[8]);
+    axpy(tmp, uh, h, s); f(tmp, stime(t, C9T(c9), dt), k[9]);
+    lc(s, C9(a1101), k[0], C9(a1106), k[5], C9(a1107), k[6], C9(a1108), k[7], C9(a1109), k[8], C9(a1110), k[9]);
+    axpy(tmp, uh, h, s); f(tmp, stime(t, C9T(c10), dt), k[10]);
+    lc(s, C9(a1201), k[0], C9(a1206), k[5], C9(a1207), k[6], C9(a1208), k[7], C9(a1209), k[8], C9(a1210), k[9],
+       C9(a1211), k[10]);
+    axpy(tmp, uh, h, s); f(tmp, stime(t, C9T(c11), dt), k[11]);
+    lc(s, C9(a1301), k[0], C9(a1306), k[5], C9(a1307), k[6], C9(a1308), k[7], C9(a1309), k[8], C9(a1310), k[9],
+       C9(a1311), k[10], C9(a1312), k[11]);
+    axpy(tmp, uh, h, s); f(tmp, stime(t, C9T(c12), dt), k[12]);
+    lc(s, C9(a1401), k[0], C9(a1406), k[5], C9(a1407), k[6], C9(a1408), k[7], C9(a1409), k[8], C9(a1410), k[9],
+       C9(a1411), k[10], C9(a1412), k[11], C9(a1413), k[12]);
+    axpy(tmp, uh, h, s); f(tmp, stime(t, C9T(c13), dt), k[13]);
+    lc(s, C9(a1501), k[0], C9(a1506), k[5], C9(a1507), k[6], C9(a1508), k[7], C9(a1509), k[8], C9(a1510), k[9],
+       C9(a1511), k[10], C9(a1512), k[11], C9(a1513), k[12], C9(a1514), k[13]);
+    axpy(tmp, uh, h, s);
+    if (ADAPTIVE) {
+      R g16[D];
+      lc(s, C9(a1601), k[0], C9(a1606), k[5], C9(a1607), k[6], C9(a1608), k[7], C9(a1609), k[8], C9(a1610), k[9],
+         C9(a1611), k[10], C9(a1612), k[11], C9(a1613), k[12]);
+      axpy(g16, uh, h, s);
+      f(tmp, t + dt, k[14]);
+      f(g16, t + dt, k[15]);
+    } else {
+      f(tmp, t + dt, k[14]);
+    }
+    lc(s, C9(b1), k[0], C9(b8), k[7], C9(b9), k[8], C9(b10), k[9], C9(b11), k[10], C9(b12), k[11], C9(b13), k[12],
+       C9(b14), k[13], C9(b15), k[14]);
+    state_update<PR, D>(uh, uc, h, s, nh, nc);
+    if (want_err) {
+      lc(s, C9(btilde1), k[0], C9(btilde8), k[7], C9(btilde9), k[8], C9(btilde10), k[9], C9(btilde11), k[10],
+         C9(btilde12), k[11], C9(btilde13), k[12], C9(btilde14), k[13], C9(btilde15), k[14], C9(btilde16), k[15]);
+#pragma unroll
+      for (int d = 0; d < D; ++d) e[d] = h * s[d];
+    }
+#undef C9
+#undef C9T
+  }
+
+  __device__ static __forceinline__ void dense(const F& f, const R (&uh)[D], const R (&uc)[D], T told, T tnew,
+                                               T dtold, T theta, R (&k)[NK][D], double (&out)[D]) {
+#define X9(x) CB<R>::v9x(vern9x_##x)
+#define X9T(x) CB<T>::v9x(vern9x_##x)
+#define R9(x) CB<R>::v9r(vern9r_##x)
+    /* K1..K9: the nine stages the dense formulas call k1..k9 */
+    const R (&K1)[D] = k[0];
+    const R (&K2)[D] = k[ADAPTIVE ? 7 : 1];
+    const R (&K3)[D] = k[ADAPTIVE ? 8 : 2];
+    const R (&K4)[D] = k[ADAPTIVE ? 9 : 3];
+    const R (&K5)[D] = k[ADAPTIVE ? 10 : 4];
+    const R (&K6)[D] = k[ADAPTIVE ? 11 : 5];
+    const R (&K7)[D] = k[ADAPTIVE ? 12 : 6];
+    const R (&K8)[D] = k[ADAPTIVE ? 13 : 7];
+    const R (&K9)[D] = k[ADAPTIVE ? 14 : 8];
+    const T tb = ADAPTIVE ? told : tnew;
+    const R h = (R)dtold;
+    R x[10][D], s[D], tmp[D];
+    lc(s, X9(a1701), K1, X9(a1708), K2, X9(a1709), K3, X9(a1710), K4, X9(a1711), K5, X9(a1712), K6, X9(a1713), K7,
+       X9(a1714), K8, X9(a1715), K9);
+    axpy(tmp, uh, h, s); f(tmp, stime(tb, X9T(c17), dtold), x[0]);
+    lc(s, X9(a1801), K1, X9(a1808), K2, X9(a1809), K3, X9(a1810), K4, X9(a1811), K5, X9(a1812), K6, X9(a1813), K7,
+       X9(a1814), K8, X9(a1815), K9, X9(a1817), x[0]);
+    axpy(tmp, uh, h, s); f(tmp, stime(tb, X9T(c18), dtold), x[1]);
+    lc(s, X9(a1901), K1, X9(a1908), K2, X9(a1909), K3, X9(a1910), K4, X9(a1911), K5, X9(a1912), K6, X9(a1913), K7,
+       X9(a1914), K8, X9(a1915), K9, X9(a1917), x[0], X9(a1918), x[1]);
+    axpy(tmp, uh, h, s); f(tmp, stime(tb, X9T(c19), dtold), x[2]);
+    lc(s, X9(a2001), K1, X9(a2008), K2, X9(a2009), K3, X9(a2010), K4, X9(a2011), K5, X9(a2012), K6, X9(a2013), K7,
+       X9(a2014), K8, X9(a2015), K9, X9(a2017), x[0], X9(a2018), x[1], X9(a2019), x[2]);
+    axpy(tmp, uh, h, s); f(tmp, stime(tb, X9T(c20), dtold), x[3]);
+    lc(s, X9(a2101), K1, X9(a2108), K2, X9(a2109), K3, X9(a2110), K4, X9(a2111), K5, X9(a2112), K6, X9(a2113), K7,
+       X9(a2114), K8, X9(a2115), K9, X9(a2117), x[0], X9(a2118), x[1], X9(a2119), x[2], X9(a2120), x[3]);
+    axpy(tmp, uh, h, s); f(tmp, stime(tb, X9T(c21), dtold), x[4]);
+    lc(s, X9(a2201), K1, X9(a2208), K2, X9(a2209), K3, X9(a2210), K4, X9(a2211), K5, X9(a2212), K6, X9(a2213), K7,
+       X9(a2214), K8, X9(a2215), K9, X9(a2217), x[0], X9(a2218), x[1], X9(a2219), x[2], X9(a2220), x[3],
+       X9(a2221), x[4]);
+    axpy(tmp, uh, h, s); f(tmp, stime(tb, X9T(c22), dtold), x[5]);
+    lc(s, X9(a2301), K1, X9(a2308), K2, X9(a2309), K3, X9(a2310), K4, X9(a2311), K5, X9(a2312), K6, X9(a2313), K7,
+       X9(a2314), K8, X9(a2315), K9, X9(a2317), x[0], X9(a2318), x[1], X9(a2319), x[2], X9(a2320), x[3],
+       X9(a2321), x[4]);
+    axpy(tmp, uh, h, s); f(tmp, stime(tb, X9T(c23), dtold), x[6]);
+    lc(s, X9(a2401), K1, X9(a2408), K2, X9(a2409), K3, X9(a2410), K4, X9(a2411), K5, X9(a2412), K6, X9(a2413), K7,
+       X9(a2414), K8, X9(a2415), K9, X9(a2417), x[0], X9(a2418), x[1], X9(a2419), x[2], X9(a2420), x[3],
+       X9(a2421), x[4]);
+    axpy(tmp, uh, h, s); f(tmp, stime(tb, X9T(c24), dtold), x[7]);
+    lc(s, X9(a2501), K1, X9(a2508), K2, X9(a2509), K3, X9(a2510), K4, X9(a2511), K5, X9(a2512), K6, X9(a2513), K7,
+       X9(a2514), K8, X9(a2515), K9, X9(a2517), x[0], X9(a2518), x[1], X9(a2519), x[2], X9(a2520), x[3],
+       X9(a2521), x[4]);
+    axpy(tmp, uh, h, s); f(tmp, stime(tb, X9T(c25), dtold), x[8]);
+    lc(s, X9(a2601), K1, X9(a2608), K2, X9(a2609), K3, X9(a2610), K4, X9(a2611), K5, X9(a2612), K6, X9(a2613), K7,
+       X9(a2614), K8, X9(a2615), K9, X9(a2617), x[0], X9(a2618), x[1], X9(a2619), x[2], X9(a2620), x[3],
+       X9(a2621), x[4]);
+    axpy(tmp, uh, h, s); f(tmp, stime(tb, X9T(c26), dtold), x[9]);
+
+    const R th = (R)theta;
+    R b[19], ex;
+    ex = R9(r019); ex = fmaR(th, ex, R9(r018)); ex = fmaR(th, ex, R9(r017)); ex = fmaR(th, ex, R9(r016));
+    ex = fmaR(th, ex, R9(r015)); ex = fmaR(th, ex, R9(r014)); ex = fmaR(th, ex, R9(r013));
+    ex = fmaR(th, ex, R9(r012)); ex = fmaR(th, ex, R9(r011)); b[0] = th * ex;
+#define V9B(i, j)                                                                             \
+  ex = R9(r##i##9); ex = fmaR(th, ex, R9(r##i##8)); ex = fmaR(th, ex, R9(r##i##7));               \
+  ex = fmaR(th, ex, R9(r##i##6)); ex = fmaR(th, ex, R9(r##i##5)); ex = fmaR(th, ex, R9(r##i##4)); \
+  ex = fmaR(th, ex, R9(r##i##3)); ex = fmaR(th, ex, R9(r##i##2)); ex = th * ex; b[j] = th * ex;
+    V9B(08, 1) V9B(09, 2) V9B(10, 3) V9B(11, 4) V9B(12, 5) V9B(13, 6) V9B(14, 7) V9B(15, 8)
+    V9B(17, 9) V9B(18, 10) V9B(19, 11) V9B(20, 12) V9B(21, 13) V9B(22, 14) V9B(23, 15) V9B(24, 16)
+    V9B(25, 17) V9B(26, 18)
+#undef V9B
+    lc(s, b[0], K1, b[1], K2, b[2], K3, b[3], K4, b[4], K5, b[5], K6, b[6], K7, b[7], K8, b[8], K9, b[9], x[0],
+       b[10], x[1], b[11], x[2], b[12], x[3], b[13], x[4], b[14], x[5], b[15], x[6], b[16], x[7], b[17], x[8],
+       b[18], x[9]);
+    finish_dense<PR, D>(uh, uc, h, s, out);
+#undef X9
+#undef X9T
+#undef R9
+  }
+};
+template <class PR, int D, class F> struct MAVern9 : MVern9Impl<PR, D, F, true> {};
+template <class PR, int D, class F> struct MVern9 : MVern9Impl<PR, D, F, false> {};
+
+/* ------------------------------------------------------------------ classic RK4 (fixed step) */
+/* src/rk4/gpurk4.jl:73-84; the stage time t is the END of the step (ts[i]). */
+template <class PR, int D, class F>
+struct MRK4 {
+  typedef typename PR::R R;
+  typedef typename PR::T T;
+  __device__ static __forceinline__ void step(const F& f, const R (&uh)[D], const R (&uc)[D], T t, T dt,
+                                              R (&nh)[D], R (&nc)[D]) {
+    R k1[D], k2[D], k3[D], k4[D], tmp[D], s[D];
+    const R h = (R)dt;
+    const R hh = h * (R)0.5;
+    f(uh, t, k1);
+#pragma unroll
+    for (int d = 0; d < D; ++d) tmp[d] = fmaR(hh, k1[d], uh[d]);
+    f(tmp, fmaR((T)0.5, dt, t), k2);
+#pragma unroll
+    for (int d = 0; d < D; ++d) tmp[d] = fmaR(hh, k2[d], uh[d]);
+    f(tmp, fmaR((T)0.5, dt, t), k3);
+#pragma unroll
+    for (int d = 0; d < D; ++d) tmp[d] = fmaR(h, k3[d], uh[d]);
+    f(tmp, t + dt, k4);
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      R sum = k1[d] + k4[d];
+      sum = fmaR((R)2, k3[d], sum);
+      s[d] = fmaR((R)2, k2[d], sum);
+    }
+    state_update<PR, D>(uh, uc, h * (R)(1.0 / 6.0), s, nh, nc);
+  }
+};
+
+/* ------------------------------------------------------------------ per-lane trajectory state */
+template <class PR, int D, class F, int NK>
+struct Lane {
+  typedef typename PR::R R;
+  typedef typename PR::T T;
+  R uh[D], uc[D];
+  R k[NK][D];
+  F f;
+  T t, dt;
+  float qoldp;
+  long long idx, att, cur, ninterp;
+  int nacc, nrej;
+  double dt_first;
+  bool nan_seen;
+};
+
+template <class PR, int D>
+__device__ __forceinline__ void store_point(const KParams& P, long long idx, long long j, const double (&v)[D]) {
+  if (!P.us) return;
+#pragma unroll
+  for (int d = 0; d < D; ++d) P.us[(j * D + d) * P.n + idx] = v[d];
+}
+
+template <class PR, int D, class L>
+__device__ __forceinline__ void state_value(const L& l, double (&v)[D]) {
+#pragma unroll
+  for (int d = 0; d < D; ++d) v[d] = PR::KAHAN ? (double)l.uh[d] - (double)l.uc[d] : (double)l.uh[d];
+}
+
+/* Load trajectory idx: parameters, u0, t0, dt; first saveat point if it is t0. */
+template <class PR, int D, class F, int NK>
+__device__ __forceinline__ void lane_load(const KParams& P, long long idx, Lane<PR, D, F, NK>& l) {
+  typedef typename PR::R R;
+  typedef typename PR::T T;
+  l.idx = idx;
+#pragma unroll
+  for (int j = 0; j < F::NP; ++j) l.f.p[j] = (R)P.p[(long long)j * P.n + idx];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    l.uh[d] = (R)P.u0[(long long)d * P.n + idx];
+    l.uc[d] = (R)0;
+  }
+  l.t = (T)P.t0;
+  l.dt = (T)(P.dt0 ? P.dt0[idx] : P.dt);
+  l.qoldp = ctrl_pow((float)1.0e-4, (float)(2.0 / 25.0));
+  l.att = 0;
+  l.cur = 0;
+  l.ninterp = 0;
+  l.nacc = 0;
+  l.nrej = 0;
+  l.dt_first = __longlong_as_double(0x7ff8000000000000LL);
+  l.nan_seen = false;
+  if (P.nsave > 0 && (T)P.saveat[0] == (T)P.t0) {
+    double v[D];
+    state_value<PR, D>(l, v);
+    store_point<PR, D>(P, idx, 0, v);
+    l.cur = 1;
+  }
+}
+
+/* Attempts, dense-output points and early stops summed over the trajectories
+ * a thread finished; reduced across the warp once, at kernel exit. */
+struct Totals {
+  unsigned long long att, sav, fail;
+};
+
+__device__ __forceinline__ void flush_totals(const KParams& P, Totals t) {
+  const unsigned FULL = 0xffffffffu;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    t.att += __shfl_xor_sync(FULL, t.att, o);
+    t.sav += __shfl_xor_sync(FULL, t.sav, o);
+    t.fail += __shfl_xor_sync(FULL, t.fail, o);
+  }
+  if ((threadIdx.x & 31) == 0 && P.stats) {
+    atomicAdd(P.stats, t.att);
+    atomicAdd(P.stats + 1, t.sav);
+    atomicAdd(P.stats + 2, t.fail);
+  }
+}
+
+template <class PR, int D, class F, int NK>
+__device__ __forceinline__ void lane_finish(const KParams& P, Lane<PR, D, F, NK>& l, int ret, Totals& tot) {
+  const long long idx = l.idx;
+  double v[D];
+  state_value<PR, D>(l, v);
+  if (P.u_final) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) P.u_final[(long long)d * P.n + idx] = v[d];
+  }
+  if (ret == RET_DTMIN || ret == RET_MAXITERS) tot.fail += 1;
+  if (ret == RET_DEFAULT && l.nan_seen) ret = RET_NAN;
+  if (P.t_final) P.t_final[idx] = (double)l.t;
+  if (P.retcode) P.retcode[idx] = (signed char)ret;
+  if (P.naccept) P.naccept[idx] = l.nacc;
+  if (P.nreject) P.nreject[idx] = l.nrej;
+  if (P.dt_first) P.dt_first[idx] = l.dt_first;
+  if (P.us) {
+    const double qnan = __longlong_as_double(0x7ff8000000000000LL);
+    for (long long j = l.cur; j < P.nsave; ++j)
+#pragma unroll
+      for (int d = 0; d < D; ++d) P.us[(j * D + d) * P.n + idx] = qnan;
+  }
+  tot.att += (unsigned long long)l.att;
+  tot.sav += (unsigned long long)l.ninterp;
+}
+
+/* One attempt of an adaptive method plus its accept/reject decision.
+ * Returns true when the trajectory has finished (outputs written). */
+template <class M, class PR, int D, class F, int NK>
+__device__ __forceinline__ bool adaptive_iter(const KParams& P, Lane<PR, D, F, NK>& l, Totals& tot) {
+  typedef typename PR::R R;
+  typedef typename PR::T T;
+  const double dtmin = M::DTMIN_1F7 ? (double)1.0e-7f : 1.0e-14;
+  if ((double)l.dt < dtmin) { lane_finish(P, l, RET_DTMIN, tot); return true; }
+  if (P.maxiters > 0 && l.att >= P.maxiters) { lane_finish(P, l, RET_MAXITERS, tot); return true; }
+  R nh[D], nc[D], e[D];
+  M::attempt(l.f, l.uh, l.uc, l.t, l.dt, l.k, nh, nc, e, true);
+  l.att += 1;
+  /* EEst = sqrt(sum((e ./ (abstol .+ max.(|uprev|, |u|) .* reltol)).^2) / D) */
+  const R abstol = (R)P.abstol, reltol = (R)P.reltol;
+  R acc = (R)0;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const R m = jmax(absR(l.uh[d]), absR(nh[d]));
+    const R r = e[d] / fmaR(m, reltol, abstol);
+    acc = (d == 0) ? r * r : fmaR(r, r, acc);
+  }
+  const R EEst = sqrtR(acc / (R)D);
+  if (EEst != EEst) l.nan_seen = true;
+  const float B1 = (float)(7.0 / 50.0), B2 = (float)(2.0 / 25.0), GAM = (float)(9.0 / 10.0);
+  const float QMAXI = 0.1f, QMINI = 5.0f, QOLDINIT = (float)1.0e-4;
+  const float Ef = (float)EEst;
+  const float q11 = ctrl_pow(Ef, B1);
+  if (EEst > (R)1) {
+    const float fac = jmin(QMINI, __fdiv_rn(q11, GAM));
+    l.dt = l.dt * (T)__fdiv_rn(1.0f, fac);
+    l.nrej += 1;
+    return false;
+  }
+  float q = (EEst == (R)0) ? QMAXI : __fdiv_rn(q11, l.qoldp);
+  q = fm_max(QMAXI, fm_min(QMINI, __fdiv_rn(q, GAM)));
+  l.qoldp = ctrl_pow(jmax(Ef, QOLDINIT), B2);
+  const T tf = (T)P.tf;
+  const T dtold = l.dt;
+  const T dtn = l.dt * (T)__fdiv_rn(1.0f, q);
+  l.dt = jmin(absR(dtn), absR(tf - l.t - dtold));
+  const T told = l.t;
+  l.t = ((double)(tf - l.t - dtold) < dtmin) ? tf : l.t + dtold;
+  if (l.nacc == 0) l.dt_first = (double)dtold;
+  l.nacc += 1;
+  while (l.cur < P.nsave && (T)P.saveat[l.cur] <= l.t) {
+    const T theta = ((T)P.saveat[l.cur] - told) / dtold;
+    double v[D];
+    M::dense(l.f, l.uh, l.uc, told, l.t, dtold, theta, l.k, v);
+    store_point<PR, D>(P, l.idx, l.cur, v);
+    l.cur += 1;
+    l.ninterp += 1;
+  }
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    l.uh[d] = nh[d];
+    l.uc[d] = nc[d];
+  }
+  if (M::FSAL) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) l.k[0][d] = l.k[NK - 1][d];
+  }
+  if (!(l.t < tf)) { lane_finish(P, l, RET_DEFAULT, tot); return true; }
+  return false;
+}
+
+/* Start trajectory idx; returns true if it is already finished (t0 >= tf). */
+template <class M, class PR, int D, class F, int NK>
+__device__ __forceinline__ bool adaptive_start(const KParams& P, long long idx, Lane<PR, D, F, NK>& l, Totals& tot) {
+  lane_load(P, idx, l);
+  if (!(l.t < (typename PR::T)P.tf)) { lane_finish(P, l, RET_DEFAULT, tot); return true; }
+  if (M::FSAL) l.f(l.uh, l.t, l.k[0]);
+  return false;
+}
+
+/* Plain schedule: thread i solves trajectory i from start to end. */
+template <class M, class PR, int D, class F>
+__device__ __forceinline__ void run_adaptive_plain(const KParams& P) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  Totals tot = {0, 0, 0};
+  if (i < P.n) {
+    Lane<PR, D, F, M::NK> l;
+    if (!adaptive_start<M>(P, i, l, tot)) {
+      while (!adaptive_iter<M>(P, l, tot)) {
+      }
+    }
+  }
+  flush_totals(P, tot);
+}
+
+/* Persistent schedule: resident warps loop over attempts; a lane whose
+ * trajectory finished takes the next position from a device counter
+ * (one atomicAdd per warp for all lanes that need work) and the position is
+ * mapped through P.order.  Every lane of a warp runs the loop until the whole
+ * warp has no work left, so the warp-wide ballots stay convergent. */
+template <class M, class PR, int D, class F>
+__device__ __forceinline__ void run_adaptive_persistent(const KParams& P) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  Lane<PR, D, F, M::NK> l;
+  Totals tot = {0, 0, 0};
+  bool active = false, exhausted = false;
+  for (;;) {
+    const bool want = !active && !exhausted;
+    const unsigned need = __ballot_sync(FULL, want);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(P.counter, (unsigned long long)__popc(need));
+      base = __shfl_sync(FULL, base, leader);
+      if (want) {
+        const unsigned long long w = base + (unsigned long long)__popc(need & ((1u << lane) - 1u));
+        if (w < (unsigned long long)P.n) {
+          const long long idx = P.order ? (long long)P.order[w] : (long long)w;
+          active = !adaptive_start<M>(P, idx, l, tot);
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (!__any_sync(FULL, active)) {
+      if (!__any_sync(FULL, !exhausted)) break;
+      continue;
+    }
+    if (active && adaptive_iter<M>(P, l, tot)) active = false;
+  }
+  flush_totals(P, tot);
+}
+
+/* Fixed-step methods: thread i, the grid of Julia's t0:dt:tf shared by all. */
+template <class M, class PR, int D, class F>
+__device__ __forceinline__ void run_fixed(const KParams& P) {
+  typedef typename PR::R R;
+  typedef typename PR::T T;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  Totals tot = {0, 0, 0};
+  if (i < P.n) {
+  Lane<PR, D, F, M::NK> l;
+  lane_load(P, i, l);
+  const T dt = (T)P.dt;
+  const bool every = P.nsave == 0 && P.save_everystep;
+  if (every) {
+    double v[D];
+    state_value<PR, D>(l, v);
+    store_point<PR, D>(P, i, 0, v);
+  }
+  if (M::FSAL) l.f(l.uh, l.t, l.k[0]);
+  R nh[D], nc[D], e[D];
+  for (long long g = 1; g < P.ngrid; ++g) {
+    l.t = (T)P.grid[g - 1];
+    M::attempt(l.f, l.uh, l.uc, l.t, dt, l.k, nh, nc, e, false);
+    l.t = l.t + dt;
+    while (l.cur < P.nsave && (T)P.saveat[l.cur] <= l.t) {
+      const T theta = ((T)P.saveat[l.cur] - (l.t - dt)) / dt;
+      double v[D];
+      M::dense(l.f, l.uh, l.uc, l.t - dt, l.t, dt, theta, l.k, v);
+      store_point<PR, D>(P, i, l.cur, v);
+      l.cur += 1;
+      l.ninterp += 1;
+    }
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      l.uh[d] = nh[d];
+      l.uc[d] = nc[d];
+    }
+    if (every) {
+      double v[D];
+      state_value<PR, D>(l, v);
+      store_point<PR, D>(P, i, g, v);
+    }
+    if (M::FSAL) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) l.k[0][d] = l.k[M::NK - 1][d];
+    }
+  }
+  l.nacc = P.ngrid > 0 ? (int)(P.ngrid - 1) : 0;
+  l.att = l.nacc;
+  if (l.nacc > 0) l.dt_first = (double)dt;
+  lane_finish(P, l, RET_DEFAULT, tot);
+  }
+  flush_totals(P, tot);
+}
+
+/* GPUSimpleRK4: saves every grid point when asked (us[1] = u0). */
+template <class PR, int D, class F>
+__device__ __forceinline__ void run_rk4(const KParams& P) {
+  typedef typename PR::R R;
+  typedef typename PR::T T;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  Totals tot = {0, 0, 0};
+  if (i < P.n) {
+  Lane<PR, D, F, 1> l;
+  lane_load(P, i, l);
+  l.cur = 0;
+  const T dt = (T)P.dt;
+  const bool every = P.save_everystep != 0;
+  if (every) {
+    double v[D];
+    state_value<PR, D>(l, v);
+    store_point<PR, D>(P, i, 0, v);
+  }
+  R nh[D], nc[D];
+  for (long long g = 1; g < P.ngrid; ++g) {
+    l.t = (T)P.grid[g];
+    MRK4<PR, D, F>::step(l.f, l.uh, l.uc, l.t, dt, nh, nc);
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      l.uh[d] = nh[d];
+      l.uc[d] = nc[d];
+    }
+    if (every) {
+      double v[D];
+      state_value<PR, D>(l, v);
+      store_point<PR, D>(P, i, g, v);
+    }
+  }
+  l.nacc = P.ngrid > 0 ? (int)(P.ngrid - 1) : 0;
+  l.att = l.nacc;
+  if (l.nacc > 0) l.dt_first = (double)dt;
+  lane_finish(P, l, RET_DEFAULT, tot);
+  }
+  flush_totals(P, tot);
+}
+
+}  // namespace gbode
+
+/* Entry-point generator: GBODE_ENTRY(name, kind, Method, Prec, Rhs) defines
+ * extern "C" __global__ name(KParams).  kind: plain | persistent | fixed | rk4. */
+#define GBODE_ENTRY_plain(NAME, M, PR, RHS)                                                  \
+  extern "C" __global__ void __launch_bounds__(128) NAME(gbode::KParams P) {                \
+    gbode::run_adaptive_plain<M<PR, RHS::D, RHS>, PR, RHS::D, RHS>(P);                      \
+  }
+#define GBODE_ENTRY_persistent(NAME, M, PR, RHS)                                             \
+  extern "C" __global__ void __launch_bounds__(128) NAME(gbode::KParams P) {                \
+    gbode::run_adaptive_persistent<M<PR, RHS::D, RHS>, PR, RHS::D, RHS>(P);                 \
+  }
+#define GBODE_ENTRY_fixed(NAME, M, PR, RHS)                                                  \
+  extern "C" __global__ void __launch_bounds__(128) NAME(gbode::KParams P) {                \
+    gbode::run_fixed<M<PR, RHS::D, RHS>, PR, RHS::D, RHS>(P);                               \
+  }
+#define GBODE_ENTRY_rk4(NAME, M, PR, RHS)                                                    \
+  extern "C" __global__ void __launch_bounds__(128) NAME(gbode::KParams P) {                \
+    gbode::run_rk4<PR, RHS::D, RHS>(P);                                                      \
+  }
+#define GBODE_ENTRY(NAME, KIND, M, PR, RHS) GBODE_ENTRY_##KIND(NAME, M, PR, RHS)

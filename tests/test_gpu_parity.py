@@ -1,0 +1,149 @@
+"""GPU parity: the CUDA kernels, called through the C ABI, against the CPU
+oracle on the same seeded inputs.
+
+Against the oracle's DEVICE rounding mode the results must be bit-identical
+(same operations in the same order, IEEE-754 on both sides).  Against the
+oracle's REF mode (the reference's own rounding) the benchmark spec's tolerances
+apply: fixed-step FP64 final states within 1e-12 relative, adaptive FP64 final
+states within 10x the solver's error scale with accepted-step counts within
++/-1.
+"""
+import numpy as np
+import pytest
+
+from conftest import decay_inputs, lorenz_inputs
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu(pkg, alg, rhs, u0, p, tspan, dt, **kw):
+    ep = pkg.EnsembleProblem(pkg.ODEProblem(rhs, u0[:, 0], tspan, p[:, 0]), u0s=u0, ps=p)
+    return pkg.solve(ep, alg, trajectories=u0.shape[1], dt=dt, **kw)
+
+
+def assert_bitexact(sol, ref):
+    assert np.array_equal(sol.u_final, ref["u_final"], equal_nan=True)
+    if sol.us is not None:
+        assert np.array_equal(sol.us, ref["us"], equal_nan=True)
+    assert np.array_equal(sol.naccept, ref["naccept"])
+    assert np.array_equal(sol.nreject, ref["nreject"])
+    assert np.array_equal(sol.retcode, ref["retcode"])
+    assert np.array_equal(sol.t_final, ref["t_final"])
+
+
+@pytest.mark.parametrize("schedule", ["plain", "persistent"])
+def test_atsit5_lorenz_bitexact(pkg, po, schedule):
+    u0, p = lorenz_inputs(2000, seed=3)
+    sv = np.linspace(0, 10, 100)
+    sol = gpu(pkg, pkg.GPUSimpleATsit5(), "lorenz", u0, p, (0.0, 10.0), 0.1, abstol=1e-8, reltol=1e-6, saveat=sv,
+              schedule=schedule)
+    ref = po.solve("ATsit5", "lorenz", u0, p, (0, 10), 0.1, rounding="device", abstol=1e-8, reltol=1e-6, saveat=sv,
+                   nthreads=8)
+    assert_bitexact(sol, ref)
+    assert sol.stats.attempts == int((ref["naccept"] + ref["nreject"]).sum())
+
+
+def test_atsit5_lorenz_vs_reference_rounding(pkg, po):
+    """Spec tolerance against the reference's own rounding."""
+    u0, p = lorenz_inputs(2000, seed=4)
+    sol = gpu(pkg, pkg.GPUSimpleATsit5(), "lorenz", u0, p, (0.0, 10.0), 0.1, abstol=1e-8, reltol=1e-6)
+    ref = po.solve("ATsit5", "lorenz", u0, p, (0, 10), 0.1, rounding="ref", abstol=1e-8, reltol=1e-6, nthreads=8)
+    scale = 1e-8 + 1e-6 * np.abs(ref["u_final"]).max(0)
+    err = np.abs(sol.u_final - ref["u_final"]).max(0) / scale
+    assert np.mean(err <= 10) >= 0.999, "more than 0.1% of trajectories beyond 10x the error scale"
+    assert np.abs(sol.naccept - ref["naccept"]).max() <= 1
+
+
+def test_tsit5_fixed_lorenz_config1(pkg, po):
+    """8192 Lorenz trajectories, u0=(1,0,0), rho ~ U[0,21], tspan (0,1), dt=0.01."""
+    n = 8192
+    rng = np.random.default_rng(11)
+    u0 = np.tile(np.array([[1.0], [0.0], [0.0]]), (1, n))
+    p = np.stack([np.full(n, 10.0), rng.uniform(0, 21, n), np.full(n, 8 / 3)])
+    sol = gpu(pkg, pkg.GPUSimpleTsit5(), "lorenz", u0, p, (0.0, 1.0), 0.01)
+    dev = po.solve("Tsit5", "lorenz", u0, p, (0, 1), 0.01, rounding="device", nthreads=8)
+    assert_bitexact(sol, dev)
+    for alg in ("Tsit5", "SimpleTsit5"):
+        ref = po.solve(alg, "lorenz", u0, p, (0, 1), 0.01, rounding="ref", nthreads=8)
+        rel = np.abs(sol.u_final - ref["u_final"]).max(0) / np.abs(ref["u_final"]).max(0)
+        assert rel.max() <= 1e-12, (alg, rel.max())
+    assert (sol.naccept == 100).all()
+
+
+@pytest.mark.parametrize("alg", ["RK4", "Tsit5", "ATsit5", "Vern7", "AVern7", "Vern9", "AVern9"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_decay_all_algorithms_bitexact(pkg, po, alg, precision):
+    """f(u) = -u, u0 = ones, tspan (0,1) as test/gpu_ode_regression.jl, with saveat."""
+    u0, A = decay_inputs(64)
+    algo = getattr(pkg, "GPUSimple" + alg)()
+    kw = dict(abstol=1e-7, reltol=1e-7, precision=precision)
+    if alg != "RK4":
+        kw["saveat"] = np.array([0.0, 0.4, 1.0])
+    dt = 0.01
+    sol = gpu(pkg, algo, "linear", u0, A, (0.0, 1.0), dt, **kw)
+    ref = po.solve(alg, "linear", u0, A, (0, 1), dt, rounding="device", precision=precision,
+                   abstol=1e-7, reltol=1e-7, saveat=kw.get("saveat"), save_everystep=(alg == "RK4"))
+    assert_bitexact(sol, ref)
+    tol = 5e-3 if precision == "fp32" else 1e-5
+    assert np.abs(sol.u_final - np.exp(-1.0)).max() < tol
+
+
+def test_avern7_vanderpol(pkg, po):
+    rng = np.random.default_rng(5)
+    n = 1024
+    mu = np.exp(rng.uniform(np.log(0.1), np.log(10), n))[None, :]
+    u0 = rng.uniform(-2, 2, (2, n))
+    sv = np.linspace(0, 20, 200)
+    for sched in ("plain", "persistent"):
+        sol = gpu(pkg, pkg.GPUSimpleAVern7(), "vanderpol", u0, mu, (0.0, 20.0), 0.1, abstol=1e-10, reltol=1e-8,
+                  saveat=sv, schedule=sched)
+        ref = po.solve("AVern7", "vanderpol", u0, mu, (0, 20), 0.1, rounding="device", abstol=1e-10, reltol=1e-8,
+                       saveat=sv, nthreads=8)
+        assert_bitexact(sol, ref)
+
+
+def r3bp_inputs(n, seed=9):
+    rng = np.random.default_rng(seed)
+    u0 = np.array([0.994, 0.0, 0.0, -2.00158510637908])[:, None] + rng.normal(0, 1e-4, (4, n))
+    mu = np.full((1, n), 0.012277471)
+    return u0, mu
+
+
+T_ARENSTORF = 17.0652165601579625588917206249
+
+
+def test_avern9_r3bp_fp64(pkg, po):
+    u0, mu = r3bp_inputs(512)
+    for sched in ("plain", "persistent"):
+        sol = gpu(pkg, pkg.GPUSimpleAVern9(), "r3bp", u0, mu, (0.0, T_ARENSTORF), 0.1, abstol=1e-12, reltol=1e-12,
+                  schedule=sched, throw=False)
+        ref = po.solve("AVern9", "r3bp", u0, mu, (0, T_ARENSTORF), 0.1, rounding="device", abstol=1e-12,
+                       reltol=1e-12, nthreads=8)
+        assert_bitexact(sol, ref)
+
+
+def test_avern9_r3bp_fp32_kahan(pkg, po):
+    u0, mu = r3bp_inputs(512)
+    sol = gpu(pkg, pkg.GPUSimpleAVern9(), "r3bp", u0, mu, (0.0, T_ARENSTORF), 0.1, abstol=1e-7, reltol=1e-7,
+              precision="fp32_kahan", throw=False)
+    dev = po.solve("AVern9", "r3bp", u0, mu, (0, T_ARENSTORF), 0.1, rounding="device", precision="fp32_kahan",
+                   abstol=1e-7, reltol=1e-7, nthreads=8)
+    assert_bitexact(sol, dev)
+
+
+def test_dtmin_raises_like_reference(pkg):
+    """abstol=0, reltol=1e-30 forces dt below dtmin: the reference throws
+    error("dt<dtmin"); the ensemble marks the trajectory and raises."""
+    u0, p = lorenz_inputs(32, seed=2)
+    with pytest.raises(pkg.DtLessThanMin):
+        gpu(pkg, pkg.GPUSimpleATsit5(), "lorenz", u0, p, (0.0, 1.0), 0.1, abstol=0.0, reltol=1e-30)
+    sol = gpu(pkg, pkg.GPUSimpleATsit5(), "lorenz", u0, p, (0.0, 1.0), 0.1, abstol=0.0, reltol=1e-30, throw=False)
+    assert (sol.retcode == 1).all()
+
+
+def test_maxiters_stops(pkg):
+    u0, p = lorenz_inputs(64, seed=2)
+    sol = gpu(pkg, pkg.GPUSimpleATsit5(), "lorenz", u0, p, (0.0, 10.0), 0.1, abstol=1e-8, reltol=1e-6, maxiters=10,
+              throw=False)
+    assert (sol.retcode == 2).all()
+    assert ((sol.naccept + sol.nreject) == 10).all()
