@@ -11,7 +11,8 @@
  * 2^y = 2^n * exp(f ln 2), n = round(y), |f| <= 1/2, from the Taylor series of
  * exp to degree 8 (truncation < 3e-10).  Every step is an IEEE single
  * operation or an explicit fmaf, so any IEEE-754 machine gives the same bits.
- * Accuracy is about 2 ulp, far more than a step-size factor needs.
+ * Relative error below 2e-6 over the whole float range, far more accuracy
+ * than a step-size factor needs.
  */
 #pragma once
 #include <cmath>

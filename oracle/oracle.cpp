@@ -21,9 +21,9 @@
  *           steps of @evalpoly) fuses, the controller uses libm pow.
  *   DEVICE  the device rounding canon the CUDA kernels implement: every
  *           multiply-add of the reference's expressions is one fused
- *           multiply-add, linear combinations accumulate from the last term
- *           to the first (the nesting MuladdMacro produces), and the step-size
- *           factor q is computed in single precision with ctrl_pow.h.
+ *           multiply-add (linear combinations accumulate left to right in
+ *           both modes, see Alg::lc), and the step-size factor q is computed
+ *           in single precision with ctrl_pow.h.
  * Build with -ffp-contract=off so that no other multiply-add is fused.
  *
  * Documented deviations from the reference, shared with the device path:
@@ -179,10 +179,16 @@ struct Alg {
 
   void f(const R* u, double t, R* du) const { rhs_eval<R, P::DEV>(rhs, D, u, p, t, du); }
 
-  /* s = sum_j c_j k_j, accumulated from the last term to the first. */
+  /* s = sum_j c_j k_j accumulated left to right, the nesting @muladd gives a
+   * sum of products (s = c_1 k_1, then s = muladd(c_j, k_j, s)).  This order is
+   * pinned by the reference's own test/gpusimpleatsit5_tests.jl:59-60, which
+   * requires SimpleTsit5 and GPUSimpleTsit5 to agree over a chaotic Lorenz
+   * run although they group the update differently (src/tsit5/tsit5.jl:335
+   * vs src/tsit5/gpuatsit5.jl:109): only left-to-right accumulation makes
+   * both groupings round identically. */
   void lc(const Term* tm, int nt, R (*k)[MAXD], R* s) const {
-    for (int d = 0; d < D; ++d) s[d] = (R)tm[nt - 1].c * k[tm[nt - 1].k][d];
-    for (int j = nt - 2; j >= 0; --j)
+    for (int d = 0; d < D; ++d) s[d] = (R)tm[0].c * k[tm[0].k][d];
+    for (int j = 1; j < nt; ++j)
       for (int d = 0; d < D; ++d) s[d] = vmadd<P::DEV>((R)tm[j].c, k[tm[j].k][d], s[d]);
   }
   /* out = base + h * s */
@@ -434,8 +440,8 @@ struct Tsit5 {
     (void)told; (void)tnew;
     R b[7], s[MAXD];
     tsit5_btheta<R>((R)theta, b);
-    for (int d = 0; d < A.D; ++d) s[d] = b[6] * k[6][d];
-    for (int j = 5; j >= 0; --j)
+    for (int d = 0; d < A.D; ++d) s[d] = b[0] * k[0][d];
+    for (int j = 1; j < 7; ++j)
       for (int d = 0; d < A.D; ++d) s[d] = vmadd<P::DEV>(b[j], k[j][d], s[d]);
     finish_dense(A, up, (R)dtold, s, out);
   }
@@ -451,8 +457,8 @@ struct Tsit5 {
 template <class P>
 static void dense_sum(const Alg<P>& A, const typename P::R* b, const int* slot, int n,
                       typename P::R (*k)[MAXD], typename P::R* s) {
-  for (int d = 0; d < A.D; ++d) s[d] = b[n - 1] * k[slot[n - 1]][d];
-  for (int j = n - 2; j >= 0; --j)
+  for (int d = 0; d < A.D; ++d) s[d] = b[0] * k[slot[0]][d];
+  for (int j = 1; j < n; ++j)
     for (int d = 0; d < A.D; ++d) s[d] = vmadd<P::DEV>(b[j], k[slot[j]][d], s[d]);
 }
 
@@ -597,10 +603,11 @@ struct RK4 {
     for (int d = 0; d < A.D; ++d) tmp[d] = vmadd<P::DEV>(h, k3[d], uprev[d]);
     A.f(tmp, (double)(t + dt), k4);
     for (int d = 0; d < A.D; ++d) {
-      /* k1 + 2k2 + 2k3 + k4: the doublings are exact, both forms round alike */
+      /* k1 + 2k2 + 2k3 + k4 = muladd(2, k3, muladd(2, k2, k1 + k4)); the
+       * doublings are exact, so fused and unfused forms round alike */
       R sum = k1[d] + k4[d];
-      sum = vmadd<P::DEV>((R)2, k3[d], sum);
       sum = vmadd<P::DEV>((R)2, k2[d], sum);
+      sum = vmadd<P::DEV>((R)2, k3[d], sum);
       s[d] = P::DEV ? sum : sixth * sum;
     }
     if (P::DEV) {
@@ -958,8 +965,8 @@ static void solve_simple_atsit5(const oracle_args* a, oracle_out* o, int64_t i) 
       const double theta = (a->saveat[cur] - it.tprev) / it.dt;
       double b[7], s[MAXD];
       tsit5_btheta<double>(theta, b);
-      for (int d = 0; d < D; ++d) s[d] = b[6] * it.ks[6][d];
-      for (int j = 5; j >= 0; --j)
+      for (int d = 0; d < D; ++d) s[d] = b[0] * it.ks[0][d];
+      for (int j = 1; j < 7; ++j)
         for (int d = 0; d < D; ++d) s[d] = vmadd<P::DEV>(b[j], it.ks[j][d], s[d]);
       for (int d = 0; d < D; ++d) tmpv[d] = vmadd<P::DEV>(it.dt, s[d], it.uprev[d]);
       put_us(a, o, i, cur, tmpv);
@@ -1008,15 +1015,18 @@ static void solve_simple_tsit5(const oracle_args* a, oracle_out* o, int64_t i) {
     /* ((a71 k1 + .. + a74 k4) + a75 k5 + a76 k6) */
     A.lc(T5_U_IN, 4, k, s);
     for (int d = 0; d < D; ++d) {
-      R acc = vmadd<P::DEV>((R)t5::a76, k[5][d], s[d]);
-      s[d] = vmadd<P::DEV>((R)t5::a75, k[4][d], acc);
+      R acc = vmadd<P::DEV>((R)t5::a75, k[4][d], s[d]);
+      s[d] = vmadd<P::DEV>((R)t5::a76, k[5][d], acc);
       st.hi[d] = vmadd<P::DEV>(h, s[d], uprev[d]);
     }
     A.f(st.hi, (double)(t + h_), k[6]);
     t += h_;
   };
   for (int64_t g = 1; g <= n - 1; ++g) step(dt);
-  if (!ends_at_tf) step((T)a->tf - t);
+  if (!ends_at_tf) {
+    step((T)a->tf - t);
+    t = (T)a->tf;  /* push!(ts, tspan[2]) */
+  }
   const int32_t steps = (int32_t)(ends_at_tf ? n - 1 : n);
   finish<P>(a, o, i, st, t, RET_DEFAULT, steps, 0, (double)dt);
 }

@@ -18,9 +18,9 @@
  *
  * Rounding canon (matched bit for bit by the oracle's DEVICE mode):
  *   - each multiply-add of the reference's expressions is one fused
- *     multiply-add; linear combinations sum_j c_j k_j accumulate from the last
- *     term to the first (the nesting @muladd produces); no other operation is
- *     fused (the files are compiled with --fmad=false);
+ *     multiply-add; linear combinations sum_j c_j k_j accumulate left to right
+ *     (the nesting @muladd produces); no other operation is fused (the files
+ *     are compiled with --fmad=false);
  *   - stage times t + c*dt and Horner steps of the dense-output polynomials
  *     are fused, as Julia fuses scalar muladd;
  *   - the step-size factor q (q11 = EEst^beta1, qold^beta2, the clamps and the
@@ -142,17 +142,22 @@ template <> struct CB<float> {
 };
 
 /* ------------------------------------------------------------------ vector algebra (D compile-time) */
-/* s = c1 k1 + c2 k2 + ... + cn kn, accumulated from the last term to the first */
+/* s = c1 k1 + c2 k2 + ... + cn kn, accumulated left to right:
+ * s = c1 k1, then s = fma(ci, ki, s) for i = 2..n (the order @muladd nests
+ * a sum of products in) */
 template <int D, class R>
-__device__ __forceinline__ void lc(R (&s)[D], R c, const R (&k)[D]) {
+__device__ __forceinline__ void lc_acc(R (&s)[D]) {}
+template <int D, class R, class... Rest>
+__device__ __forceinline__ void lc_acc(R (&s)[D], R c, const R (&k)[D], const Rest&... rest) {
 #pragma unroll
-  for (int d = 0; d < D; ++d) s[d] = c * k[d];
+  for (int d = 0; d < D; ++d) s[d] = fmaR(c, k[d], s[d]);
+  lc_acc(s, rest...);
 }
 template <int D, class R, class... Rest>
 __device__ __forceinline__ void lc(R (&s)[D], R c, const R (&k)[D], const Rest&... rest) {
-  lc(s, rest...);
 #pragma unroll
-  for (int d = 0; d < D; ++d) s[d] = fmaR(c, k[d], s[d]);
+  for (int d = 0; d < D; ++d) s[d] = c * k[d];
+  lc_acc(s, rest...);
 }
 /* out = base + h * s */
 template <int D, class R>
@@ -610,8 +615,8 @@ struct MRK4 {
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       R sum = k1[d] + k4[d];
-      sum = fmaR((R)2, k3[d], sum);
-      s[d] = fmaR((R)2, k2[d], sum);
+      sum = fmaR((R)2, k2[d], sum);
+      s[d] = fmaR((R)2, k3[d], sum);
     }
     state_update<PR, D>(uh, uc, h * (R)(1.0 / 6.0), s, nh, nc);
   }

@@ -1,0 +1,80 @@
+"""The C ABI library: loads without a GPU, exports every entry point that
+include/gb300ode.h declares, and its host-side logic (Julia-range time grid,
+argument checking) behaves as specified.  No device computation here."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "gb300ode.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:int|void|const char\*)\s+(ode_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_expected_entry_points(pkg):
+    names = declared_functions()
+    assert set(names) == set(pkg._lib.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(pkg):
+    lib = pkg._lib.load()
+    out = subprocess.run(["nm", "-D", "--defined-only", pkg._lib.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (ode_\w+)", out))
+    for name in declared_functions():
+        assert name in exported, name
+        assert getattr(lib, name) is not None
+    assert lib.ode_abi_version() == 1
+
+
+def test_library_needs_no_driver_at_load_time(pkg):
+    out = subprocess.run(["ldd", pkg._lib.LIB_PATH], capture_output=True, text=True).stdout
+    assert "libcuda" not in out and "libnvrtc" not in out
+
+
+GRID_CASES = [(0, 0.01, 1), (0, 0.1, 1), (0, 0.3, 1), (0, 0.05 / 11, 0.05), (0.0, 0.1, 100.0), (1.5, 0.25, 4.0),
+              (0, 1 / 3, 2), (0, 0.013, 0.5), (-1, 0.07, 1), (0, 1e-3, 0.1), (2.0, 0.1, 1.0), (0, 0.7, 0.7),
+              (0.1, 0.2, 0.9), (0, 0.001, 1.0), (0, np.pi / 10, np.pi)]
+
+
+@pytest.mark.parametrize("t0,dt,tf", GRID_CASES)
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_fixed_grid_matches_julia_range(pkg, po, t0, dt, tf, precision):
+    """The library's C++ restatement of Julia's t0:dt:tf equals the oracle's
+    independent Python restatement (element by element)."""
+    a = pkg.fixed_grid(t0, dt, tf, precision)
+    b = po.julia_range(t0, dt, tf, precision)
+    assert len(a) == len(b)
+    assert np.array_equal(a, b)
+
+
+def test_create_without_gpu_fails_cleanly(pkg):
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        pytest.skip("a GPU is present")
+    lib = pkg._lib.load()
+    h = ctypes.c_void_p()
+    rc = lib.ode_create(ctypes.byref(h), 0)
+    assert rc in (pkg._lib.ECUDA, pkg._lib.EINVAL)
+    assert not h.value
+
+
+def test_null_handle_and_bad_arguments(pkg):
+    lib = pkg._lib.load()
+    assert lib.ode_ensemble_solve(None, None, None, None) == pkg._lib.EINVAL
+    n = ctypes.c_int64()
+    assert lib.ode_fixed_grid(0.0, 0.0, 1.0, 0, None, 0, ctypes.byref(n)) == pkg._lib.EINVAL
+    assert lib.ode_fixed_grid(0.0, float("nan"), 1.0, 0, None, 0, ctypes.byref(n)) == pkg._lib.EINVAL
+    assert lib.ode_last_error(None) == b"null handle"

@@ -1,0 +1,191 @@
+"""The CPU oracle against known answers and the reference's own tests.
+
+The reference (Julia) cannot run here, so the oracle is pinned by:
+  * analytic solutions: f(u) = -u (test/gpu_ode_regression.jl:2-9) and the
+    2x2 linear system [2 3; 4 5] (test/simpleatsit5_tests.jl:87-93);
+  * the reference's relational tests, restated: SimpleATsit5 == GPUSimpleATsit5
+    (test/gpusimpleatsit5_tests.jl:35-39,49), SimpleTsit5 == GPUSimpleTsit5 on
+    a chaotic Lorenz run to t = 100 (:59-67), the last fixed step landing on tf
+    (test/simpletsit5_tests.jl:84-90), saveat lengths (test/gpu_ode_regression.jl:60-61,84-85),
+    fixed vs adaptive agreement within the reference's tolerances (:35-36,57-58,81-82);
+  * the committed golden fixtures (tests/golden/), regenerated by make_golden.py.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import decay_inputs, lorenz_inputs
+
+ALGS = ["RK4", "Tsit5", "ATsit5", "Vern7", "AVern7", "Vern9", "AVern9"]
+
+
+@pytest.mark.parametrize("alg", ALGS)
+@pytest.mark.parametrize("rounding", ["ref", "device"])
+def test_decay_known_answer(po, alg, rounding):
+    u0, A = decay_inputs(2)
+    kw = {} if alg == "RK4" else {"saveat": [0.0, 0.4, 1.0]}
+    o = po.solve(alg, "linear", u0, A, (0, 1), 0.01, rounding=rounding, abstol=1e-10, reltol=1e-10, **kw)
+    assert np.abs(o["u_final"] - np.exp(-1)).max() < (1e-10 if alg != "RK4" else 1e-9)
+    assert (o["retcode"] == 0).all()
+    if alg != "RK4":
+        assert o["us"].shape[0] == 3  # length(sol.u) == length(saveat)
+        assert np.array_equal(o["us"][0], u0)  # saveat[1] == t0 copies u0
+        tol = 1e-4 if alg == "Vern9" else 1e-9  # fixed-step Vern9 keeps the reference's unrelabelled dense stages
+        assert np.abs(o["us"][1] - np.exp(-0.4)).max() < tol
+
+
+@pytest.mark.parametrize("adaptive,fixed", [("ATsit5", "Tsit5"), ("AVern7", "Vern7"), ("AVern9", "Vern9")])
+def test_fp32_regression_pairs(po, adaptive, fixed):
+    """test/gpu_ode_regression.jl in Float32: fixed dt=0.01 vs adaptive at 1f-7,
+    against the exact solution in place of OrdinaryDiffEq's Vern9."""
+    u0, A = decay_inputs(1)
+    exact = np.exp(-1.0)
+    s = po.solve(fixed, "linear", u0, A, (0, 1), 0.01, precision="fp32")
+    a = po.solve(adaptive, "linear", u0, A, (0, 1), 0.01, precision="fp32", abstol=1e-7, reltol=1e-7)
+    assert np.linalg.norm(s["u_final"][:, 0] - exact) < 5e-3
+    assert np.linalg.norm(a["u_final"][:, 0] - exact) < 5e-4
+    sv = np.array([0.0, 0.4], dtype=np.float32).astype(np.float64)
+    s = po.solve(fixed, "linear", u0, A, (0, 1), 0.01, precision="fp32", saveat=sv)
+    a = po.solve(adaptive, "linear", u0, A, (0, 1), 0.01, precision="fp32", abstol=1e-7, reltol=1e-7, saveat=sv)
+    ex = np.exp(-sv)[:, None, None] * np.ones((2, 3, 1))
+    assert np.linalg.norm(a["us"] - ex) < 2e-4
+    assert np.linalg.norm(s["us"] - ex) < (2e-4 if fixed != "Vern9" else 2e-3)
+
+
+def test_linear_2x2_interpolation(po):
+    """test/simpleatsit5_tests.jl:86-112: du = [2 3; 4 5] u, u0 = (1, 1),
+    abstol = reltol = 1e-6, dt = 0.1; here against the matrix exponential."""
+    from scipy.linalg import expm
+    M = np.array([[2.0, 3.0], [4.0, 5.0]])
+    u0 = np.ones((2, 1))
+    A = M.reshape(4, 1)
+    sv = np.linspace(0, 1, 21)
+    for alg in ("ATsit5", "SimpleATsit5"):
+        o = po.solve(alg, "linear", u0, A, (0, 1), 0.1, abstol=1e-6, reltol=1e-6, saveat=sv)
+        ex = np.stack([expm(M * t) @ u0[:, 0] for t in sv])
+        rel = np.abs(o["us"][:, :, 0] - ex) / np.abs(ex)
+        assert rel.max() < 2e-5
+
+
+def test_simple_vs_gpu_atsit5_identical(po):
+    """GPUSimpleATsit5 and SimpleATsit5 are the same algorithm (test/gpusimpleatsit5_tests.jl:35-39,49)."""
+    u0 = np.full((3, 1), 10.0)
+    p = np.array([[10.0], [28.0], [8 / 3]])
+    for sv in (None, np.arange(0, 1001) * 0.1):
+        a = po.solve("ATsit5", "lorenz", u0, p, (0, 100), 0.01, abstol=1e-6, reltol=1e-3, saveat=sv)
+        b = po.solve("SimpleATsit5", "lorenz", u0, p, (0, 100), 0.01, abstol=1e-6, reltol=1e-3, saveat=sv)
+        assert np.array_equal(a["u_final"], b["u_final"])
+        assert np.array_equal(a["naccept"], b["naccept"])
+        if sv is not None:
+            assert np.array_equal(a["us"], b["us"], equal_nan=True)
+
+
+def test_simple_vs_gpu_tsit5_identical_chaotic(po):
+    """test/gpusimpleatsit5_tests.jl:54-67: SimpleTsit5 and GPUSimpleTsit5 agree
+    on Lorenz over (0, 100) with dt = 0.1 although their update is grouped
+    differently; with left-to-right @muladd accumulation they are identical."""
+    u0 = np.full((3, 1), 10.0)
+    p = np.array([[10.0], [28.0], [8 / 3]])
+    a = po.solve("Tsit5", "lorenz", u0, p, (0, 100), 0.1)
+    b = po.solve("SimpleTsit5", "lorenz", u0, p, (0, 100), 0.1)
+    assert np.array_equal(a["u_final"], b["u_final"])
+    c = po.solve("Tsit5", "lorenz", u0, p, (0, 100), 0.1, saveat=[5.0, 100.0])
+    assert np.allclose(c["us"][1], a["u_final"], rtol=1e-12)  # sol.u[end] ≈ sol4.u[end] (:64-66)
+
+
+def test_last_step_lands_on_tf(po):
+    """test/simpletsit5_tests.jl:84-90: dt = 0.05/11 on (0, 0.05).  Julia's range
+    0:dt:0.05 takes the literal path (Float64(1/220) != 0.05/11) and has 11
+    points ending at 10*dt; SimpleTsit5 then adds a last partial step and its
+    solution ends exactly at 0.05."""
+    g = po.julia_range(0.0, 0.05 / 11, 0.05)
+    assert len(g) == 11 and g[-1] == 10 * (0.05 / 11)
+    u0 = np.ones((1, 1))
+    o = po.solve("SimpleTsit5", "linear", u0, np.ones((1, 1)), (0, 0.05), 0.05 / 11)
+    assert o["t_final"][0] == 0.05
+    assert o["naccept"][0] == 12
+
+
+def test_julia_ranges(po):
+    assert len(po.julia_range(0, 0.01, 1)) == 101
+    assert po.julia_range(0, 0.1, 1)[3] == 0.3          # the rational path rounds i/10 exactly
+    assert list(po.julia_range(0, 0.3, 1)) == [0.0, 0.3, 0.6, 0.9]
+    assert len(po.julia_range(0, 0.01, 1, "fp32")) == 101
+    g = po.julia_range(0.0, 0.1, 100.0)
+    assert len(g) == 1001 and g[-1] == 100.0
+
+
+def test_rounding_modes_agree_within_northstar_tolerance(po):
+    """The device rounding canon (fused multiply-adds, single-precision step-size
+    factor) stays within the benchmark spec's tolerance of the reference's rounding:
+    accepted-step counts within +/-1 and final states within 10x the error
+    scale abstol + reltol*|u| (chaotic trajectories amplify rounding, so the
+    bar is 99.9% of trajectories)."""
+    u0, p = lorenz_inputs(3000, seed=21)
+    kw = dict(abstol=1e-8, reltol=1e-6, nthreads=8)
+    a = po.solve("ATsit5", "lorenz", u0, p, (0, 10), 0.1, rounding="ref", **kw)
+    b = po.solve("ATsit5", "lorenz", u0, p, (0, 10), 0.1, rounding="device", **kw)
+    assert np.abs(a["naccept"] - b["naccept"]).max() <= 1
+    scale = 1e-8 + 1e-6 * np.abs(a["u_final"]).max(0)
+    err = np.abs(a["u_final"] - b["u_final"]).max(0) / scale
+    assert np.mean(err <= 10) >= 0.999
+
+
+def test_fixed_step_rounding_modes_1e12(po):
+    """Fixed-step FP64 final states: device canon within 1e-12 relative of the
+    reference rounding on the 8192-trajectory fixed Tsit5 Lorenz workload."""
+    n = 8192
+    rng = np.random.default_rng(11)
+    u0 = np.tile(np.array([[1.0], [0.0], [0.0]]), (1, n))
+    p = np.stack([np.full(n, 10.0), rng.uniform(0, 21, n), np.full(n, 8 / 3)])
+    a = po.solve("Tsit5", "lorenz", u0, p, (0, 1), 0.01, rounding="ref", nthreads=8)
+    b = po.solve("Tsit5", "lorenz", u0, p, (0, 1), 0.01, rounding="device", nthreads=8)
+    rel = np.abs(a["u_final"] - b["u_final"]).max(0) / np.abs(a["u_final"]).max(0)
+    assert rel.max() <= 1e-12
+
+
+def test_ctrl_pow_accuracy(po):
+    xs = np.concatenate([np.logspace(-40, 38, 400), [1.0, 0.5, 2.0, 1e-4, 3.0]]).astype(np.float32)
+    for b in (0.14, 0.08):
+        got = np.array([po.ctrl_pow(float(x), np.float32(b)) for x in xs])
+        ref = xs.astype(np.float64) ** np.float64(np.float32(b))
+        assert np.max(np.abs(got / ref - 1)) < 2e-6  # about 10 ulp across the whole float range
+    assert po.ctrl_pow(0.0, 0.14) == 0.0
+    assert np.isnan(po.ctrl_pow(float("nan"), 0.14))
+    assert po.ctrl_pow(float("inf"), 0.14) == float("inf")
+
+
+def test_dtmin_and_maxiters(po):
+    u0, p = lorenz_inputs(4, seed=2)
+    o = po.solve("ATsit5", "lorenz", u0, p, (0, 1), 0.1, abstol=0.0, reltol=1e-30)
+    assert (o["retcode"] == 1).all()
+    o = po.solve("ATsit5", "lorenz", u0, p, (0, 10), 0.1, abstol=1e-8, reltol=1e-6, maxiters=10)
+    assert (o["retcode"] == 2).all() and ((o["naccept"] + o["nreject"]) == 10).all()
+
+
+def test_nan_is_accepted_like_reference(po):
+    """A NaN error estimate is not > 1, so the reference accepts the step and
+    carries on; the trajectory finishes (flagged with retcode 3)."""
+    u0 = np.array([[np.nan], [1.0], [1.0]])
+    p = np.array([[10.0], [28.0], [8 / 3]])
+    o = po.solve("ATsit5", "lorenz", u0, p, (0, 1), 0.1)
+    assert o["retcode"][0] == 3 and o["t_final"][0] == 1.0
+    assert np.isnan(o["u_final"]).all()
+
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+sys.path.insert(0, GOLDEN)
+
+
+def test_golden_fixtures(po):
+    import make_golden
+    for name, case in make_golden.CASES.items():
+        path = os.path.join(GOLDEN, name + ".npz")
+        ref = np.load(path)
+        out = make_golden.run_case(po, case)
+        for k in ("u_final", "naccept", "nreject", "retcode"):
+            assert np.array_equal(out[k], ref[k], equal_nan=True), (name, k)
+        if "us" in ref.files:
+            assert np.array_equal(out["us"], ref["us"], equal_nan=True), name
