@@ -203,6 +203,13 @@ void ode_learn_default_opts(ode_learn_opts* o);
 int ode_learn_fit(ode_handle* h, const ode_solve_args* a, const ode_learn_opts* opts, ode_learn_report* rep);
 /* Predicted (log attempts, log dt_first) per trajectory into host arrays (either may be NULL). */
 int ode_learn_predict(ode_handle* h, const ode_solve_args* a, float* log_attempts, float* log_dt_first);
+/* One forward and backward pass of the training kernel on a batch, for
+ * verification: params in the flat layout W1[nh][nin] b1[nh] W2[nh][nh]
+ * b2[nh] W3[2][nh] b3[2] (rounded to bf16 as training uses them), x
+ * [batch][nin], y [batch][2]; writes the fp32 gradient of the loss
+ * mean_b sum_o (out - y)^2 and the loss. */
+int ode_learn_gradcheck(ode_handle* h, int nin, int nh, int64_t batch, const float* params, const float* x,
+                        const float* y, float* grad, float* loss);
 
 #ifdef __cplusplus
 }

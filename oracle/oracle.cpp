@@ -1098,3 +1098,56 @@ extern "C" int oracle_solve(const oracle_args* a, oracle_out* o) {
 }
 
 extern "C" float oracle_ctrl_pow(float x, float b) { return oracle_pow::ctrl_pow(x, b); }
+
+/* Reference forward and backward pass of the learned-schedule MLP, in double
+ * precision, for checking the device training kernel's gradients.
+ * Layout W1[nh][nin] b1[nh] W2[nh][nh] b2[nh] W3[2][nh] b3[2];
+ * loss = (1/batch) sum_b sum_o (out_bo - y_bo)^2. */
+extern "C" int oracle_mlp_forward_backward(int nin, int nh, int64_t batch, const float* prm, const float* x,
+                                           const float* y, float* grad, float* loss) {
+  if (nin < 1 || nh < 1 || batch < 1) return -1;
+  const int w1 = 0, b1 = nh * nin, w2 = b1 + nh, b2 = w2 + nh * nh, w3 = b2 + nh, b3 = w3 + 2 * nh;
+  const int np = b3 + 2;
+  std::vector<double> g(np, 0.0), a1(nh), a2(nh), d1(nh), d2(nh);
+  double L = 0;
+  for (int64_t s = 0; s < batch; ++s) {
+    const float* xs = x + s * nin;
+    for (int j = 0; j < nh; ++j) {
+      double acc = prm[b1 + j];
+      for (int f = 0; f < nin; ++f) acc += (double)prm[w1 + j * nin + f] * xs[f];
+      a1[j] = acc > 0 ? acc : 0;
+    }
+    for (int j = 0; j < nh; ++j) {
+      double acc = prm[b2 + j];
+      for (int k = 0; k < nh; ++k) acc += (double)prm[w2 + j * nh + k] * a1[k];
+      a2[j] = acc > 0 ? acc : 0;
+    }
+    double dout[2];
+    for (int q = 0; q < 2; ++q) {
+      double acc = prm[b3 + q];
+      for (int k = 0; k < nh; ++k) acc += (double)prm[w3 + q * nh + k] * a2[k];
+      const double e = acc - y[s * 2 + q];
+      L += e * e / batch;
+      dout[q] = 2 * e / batch;
+      g[b3 + q] += dout[q];
+      for (int k = 0; k < nh; ++k) g[w3 + q * nh + k] += dout[q] * a2[k];
+    }
+    for (int j = 0; j < nh; ++j) {
+      double acc = 0;
+      for (int q = 0; q < 2; ++q) acc += (double)prm[w3 + q * nh + j] * dout[q];
+      d2[j] = a2[j] > 0 ? acc : 0;
+      g[b2 + j] += d2[j];
+      for (int k = 0; k < nh; ++k) g[w2 + j * nh + k] += d2[j] * a1[k];
+    }
+    for (int k = 0; k < nh; ++k) {
+      double acc = 0;
+      for (int j = 0; j < nh; ++j) acc += (double)prm[w2 + j * nh + k] * d2[j];
+      d1[k] = a1[k] > 0 ? acc : 0;
+      g[b1 + k] += d1[k];
+      for (int f = 0; f < nin; ++f) g[w1 + k * nin + f] += d1[k] * xs[f];
+    }
+  }
+  for (int i = 0; i < np; ++i) grad[i] = (float)g[i];
+  *loss = (float)L;
+  return 0;
+}

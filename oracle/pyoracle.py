@@ -61,11 +61,32 @@ def lib():
         _lib.oracle_solve.restype = ctypes.c_int
         _lib.oracle_ctrl_pow.argtypes = [ctypes.c_float, ctypes.c_float]
         _lib.oracle_ctrl_pow.restype = ctypes.c_float
+        _lib.oracle_mlp_forward_backward.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int64] + [ctypes.c_void_p] * 5
     return _lib
 
 
 def ctrl_pow(x, b):
     return lib().oracle_ctrl_pow(x, b)
+
+
+def mlp_forward_backward(nin, nh, params, x, y):
+    """Gradient and loss of the learned-schedule MLP (double-precision reference)."""
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    grad = np.zeros_like(params)
+    loss = np.zeros(1, dtype=np.float32)
+    rc = lib().oracle_mlp_forward_backward(nin, nh, x.shape[0], params.ctypes.data, x.ctypes.data, y.ctypes.data,
+                                           grad.ctypes.data, loss.ctypes.data)
+    assert rc == 0
+    return grad, float(loss[0])
+
+
+def bf16_round(a):
+    """Round float32 values to bfloat16 (nearest, ties to even), returned as float32."""
+    u = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) >> 16 << 16
+    return u.astype(np.uint32).view(np.float32)
 
 
 # --------------------------------------------------------------------------- Julia ranges

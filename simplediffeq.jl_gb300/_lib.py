@@ -23,7 +23,8 @@ RET_DEFAULT, RET_DTMIN, RET_MAXITERS, RET_NAN = 0, 1, 2, 3
 
 # Every symbol include/gb300ode.h declares.
 EXPORTS = ["ode_abi_version", "ode_create", "ode_destroy", "ode_last_error", "ode_ensemble_solve",
-           "ode_fixed_grid", "ode_rhs_compile", "ode_learn_default_opts", "ode_learn_fit", "ode_learn_predict"]
+           "ode_fixed_grid", "ode_rhs_compile", "ode_learn_default_opts", "ode_learn_fit", "ode_learn_predict",
+           "ode_learn_gradcheck"]
 
 
 class SolveArgs(ctypes.Structure):
@@ -93,6 +94,8 @@ def load():
     lib.ode_learn_fit.argtypes = [ctypes.c_void_p, ctypes.POINTER(SolveArgs), ctypes.POINTER(LearnOpts),
                                   ctypes.POINTER(LearnReport)]
     lib.ode_learn_predict.argtypes = [ctypes.c_void_p, ctypes.POINTER(SolveArgs), ctypes.c_void_p, ctypes.c_void_p]
+    lib.ode_learn_gradcheck.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     _lib = lib
     return lib
 
@@ -160,6 +163,16 @@ class Handle:
         rep = LearnReport()
         self.check(self.lib.ode_learn_fit(self.h, ctypes.byref(args), ctypes.byref(o), ctypes.byref(rep)))
         return rep
+
+    def learn_gradcheck(self, nin, nh, params, x, y):
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        grad = np.zeros_like(params)
+        loss = np.zeros(1, dtype=np.float32)
+        self.check(self.lib.ode_learn_gradcheck(self.h, nin, nh, x.shape[0], params.ctypes.data, x.ctypes.data,
+                                                y.ctypes.data, grad.ctypes.data, loss.ctypes.data))
+        return grad, float(loss[0])
 
     def learn_predict(self, args, n):
         la = np.zeros(n, dtype=np.float32)
