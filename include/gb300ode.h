@@ -179,14 +179,16 @@ int ode_rhs_compile(ode_handle* h, const char* body, int dim, int nparams, int* 
  * trajectory's (p, u0) to (log attempts, log dt of the first accepted step).
  * It is trained on the GPU on counts the plain solver records for a training
  * ensemble, then used by ODE_SCHED_LEARNED to order trajectories by predicted
- * cost (longest first) and to seed each trajectory's initial dt. */
+ * cost (longest first) and, if asked, to seed each trajectory's initial dt. */
 typedef struct {
   int32_t hidden;      /* hidden width (default 64) */
   int32_t epochs;      /* passes over the training set (default 200) */
   int32_t batch;       /* minibatch size (default 1024) */
   float lr;            /* Adam learning rate (default 3e-3) */
   uint64_t seed;       /* initialisation and shuffling seed */
-  int32_t seed_dt0;    /* 1: use the predicted dt0 in ODE_SCHED_LEARNED (default 1) */
+  int32_t seed_dt0;    /* 1: seed each trajectory's initial dt with the prediction in
+                          ODE_SCHED_LEARNED (default 0: ordering only, results
+                          bit-identical to the plain schedule) */
   float dt0_safety;    /* predicted dt0 is multiplied by this (default 1.0) */
 } ode_learn_opts;
 
