@@ -213,6 +213,27 @@ int ode_learn_predict(ode_handle* h, const ode_solve_args* a, float* log_attempt
 int ode_learn_gradcheck(ode_handle* h, int nin, int nh, int64_t batch, const float* params, const float* x,
                         const float* y, float* grad, float* loss);
 
+/* ---- allocation-free solve ------------------------------------------------
+ * No counterpart in the reference: an entry point for callers that cannot
+ * allocate GPU memory, such as applications that own the whole device memory
+ * budget (pools sized at start-up) or real-time loops that cannot afford
+ * cudaMalloc/cudaFree synchronising the device.  The caller passes device
+ * buffers for every input and output (memory = ODE_MEM_DEVICE); the solver's
+ * own scratch (work counter, statistics, saveat times) lives in a fixed
+ * 33,024-byte array inside the library's device image, which every GPU that
+ * loads the library keeps until the process exits.
+ *
+ * Runs GPUSimpleATsit5, FP64, built-in Lorenz, persistent schedule (the
+ * kernel of ode_ensemble_solve with ODE_SCHED_PERSISTENT, identical results);
+ * other combinations return ODE_ENOTSUP, more than ODE_NOALLOC_MAX_SAVE saveat
+ * points ODE_EINVAL.  No handle: diagnostics go to `err` (may be NULL).
+ * The first call on a device (with that device current) looks the scratch
+ * array up; make it before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race, so serialise them.  Runs on
+ * a->stream (NULL: the default stream) and returns after the solve finished. */
+#define ODE_NOALLOC_MAX_SAVE 4096
+int ode_ensemble_solve_noalloc(const ode_solve_args* a, ode_solve_out* o, char* err, size_t errlen);
+
 #ifdef __cplusplus
 }
 #endif

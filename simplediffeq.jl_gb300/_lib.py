@@ -24,7 +24,7 @@ RET_DEFAULT, RET_DTMIN, RET_MAXITERS, RET_NAN = 0, 1, 2, 3
 # Every symbol include/gb300ode.h declares.
 EXPORTS = ["ode_abi_version", "ode_create", "ode_destroy", "ode_last_error", "ode_ensemble_solve",
            "ode_fixed_grid", "ode_rhs_compile", "ode_learn_default_opts", "ode_learn_fit", "ode_learn_predict",
-           "ode_learn_gradcheck"]
+           "ode_learn_gradcheck", "ode_ensemble_solve_noalloc"]
 
 
 class SolveArgs(ctypes.Structure):
@@ -96,6 +96,8 @@ def load():
     lib.ode_learn_predict.argtypes = [ctypes.c_void_p, ctypes.POINTER(SolveArgs), ctypes.c_void_p, ctypes.c_void_p]
     lib.ode_learn_gradcheck.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.ode_ensemble_solve_noalloc.argtypes = [ctypes.POINTER(SolveArgs), ctypes.POINTER(SolveOut), ctypes.c_char_p,
+                                               ctypes.c_size_t]
     _lib = lib
     return lib
 

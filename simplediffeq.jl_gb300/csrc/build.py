@@ -136,7 +136,7 @@ def build(verbose=False, jobs=None):
     os.makedirs(LIB, exist_ok=True)
     headers = [os.path.join(HERE, f) for f in ("ode_solver.cuh", "ode_kparams.h", "tableaus.h", "ode_host.h",
                                                "jlrange.h")] + [os.path.join(PKG, "..", "include", "gb300ode.h")]
-    host_tus = [os.path.join(HERE, "ode_capi.cu"), os.path.join(HERE, "learn.cu")]
+    host_tus = [os.path.join(HERE, "ode_capi.cu"), os.path.join(HERE, "learn.cu"), os.path.join(HERE, "noalloc.cu")]
     gen = [os.path.join(BUILD, "aot_registry.inc"), os.path.join(BUILD, "embedded_src.inc")]
     jobs_list = []
     for src in tus + host_tus:
