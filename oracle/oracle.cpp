@@ -22,8 +22,10 @@
  *   DEVICE  the device rounding canon the CUDA kernels implement: every
  *           multiply-add of the reference's expressions is one fused
  *           multiply-add (linear combinations accumulate left to right in
- *           both modes, see Alg::lc), and the step-size factor q is computed
- *           in single precision with ctrl_pow.h.
+ *           both modes, see Alg::lc); the error norm (when abstol >= 1e-30)
+ *           and the step-size factor q are computed in single precision, q
+ *           with ctrl_pow.h; the dense-output abscissa uses recip_dev and a
+ *           shared theta^2 (horner).
  * Build with -ffp-contract=off so that no other multiply-add is fused.
  *
  * Documented deviations from the reference, shared with the device path:
@@ -222,14 +224,26 @@ static void state_update(int D, const State<typename P::R>& a, typename P::R h,
 }
 
 /* Horner evaluation of c0 + c1 x + ... with leading zero coefficients, as
- * @evalpoly does it (scalar muladd, fused). nz = number of leading zeros. */
-template <class R>
+ * @evalpoly does it (scalar muladd, fused). nz = number of leading zeros.
+ * The device canon multiplies the polynomials that start at x^2 by one shared
+ * x*x instead of by x twice. */
+template <bool DEV, class R>
 static R horner(R x, const double* c, int n, int nz) {
   R ex = (R)c[n - 1];
   for (int i = n - 2; i >= 0; --i) ex = fmaX(x, ex, (R)c[i]);
+  if (DEV && nz == 2) return (x * x) * ex;
   for (int i = 0; i < nz; ++i) ex = x * ex;
   return ex;
 }
+
+/* 1/x of the device canon for the dense-output abscissa: a correctly rounded
+ * single-precision reciprocal refined by one Newton step in double. */
+static inline double recip_dev(double x) {
+  const double r0 = (double)(1.0f / (float)x);
+  const double e = std::fma(-x, r0, 1.0);
+  return std::fma(r0, e, r0);
+}
+static inline float recip_dev(float x) { return 1.0f / x; }
 
 /* ---------------------------------------------------------------- tableaus */
 namespace t5 = gbtab::tsit5;
@@ -252,7 +266,7 @@ const Term T5_E[] = {{t5::btilde1, 0}, {t5::btilde2, 1}, {t5::btilde3, 2}, {t5::
 const Term T5_U_IN[] = {{t5::a71, 0}, {t5::a72, 1}, {t5::a73, 2}, {t5::a74, 3}};
 
 /* bθs of src/tsit5/tsit5.jl:385-399: b1θ = poly(0, r11..r14), b_iθ = poly(0, 0, r_i2..r_i4) */
-template <class R>
+template <bool DEV, class R>
 static void tsit5_btheta(R th, R* b) {
   const double c1[] = {t5::r11, t5::r12, t5::r13, t5::r14};
   const double c2[] = {t5::r22, t5::r23, t5::r24};
@@ -261,13 +275,13 @@ static void tsit5_btheta(R th, R* b) {
   const double c5[] = {t5::r52, t5::r53, t5::r54};
   const double c6[] = {t5::r62, t5::r63, t5::r64};
   const double c7[] = {t5::r72, t5::r73, t5::r74};
-  b[0] = horner(th, c1, 4, 1);
-  b[1] = horner(th, c2, 3, 2);
-  b[2] = horner(th, c3, 3, 2);
-  b[3] = horner(th, c4, 3, 2);
-  b[4] = horner(th, c5, 3, 2);
-  b[5] = horner(th, c6, 3, 2);
-  b[6] = horner(th, c7, 3, 2);
+  b[0] = horner<DEV>(th, c1, 4, 1);
+  b[1] = horner<DEV>(th, c2, 3, 2);
+  b[2] = horner<DEV>(th, c3, 3, 2);
+  b[3] = horner<DEV>(th, c4, 3, 2);
+  b[4] = horner<DEV>(th, c5, 3, 2);
+  b[5] = horner<DEV>(th, c6, 3, 2);
+  b[6] = horner<DEV>(th, c7, 3, 2);
 }
 
 /* ---- Verner 7(6), src/verner/gpuvern7.jl:360-404 (slots 0..9 = k1..k10) */
@@ -299,7 +313,7 @@ const Term V7_X16[] = {{v7x::a1601, 0}, {v7x::a1604, 3}, {v7x::a1605, 4}, {v7x::
 const double V7_XC[] = {v7x::c11, v7x::c12, v7x::c13, v7x::c14, v7x::c15, v7x::c16};
 
 /* bθs of src/verner/verner_tableaus.jl:1337-1360; order b1,b4..b9,b11..b16 */
-template <class R>
+template <bool DEV, class R>
 static void vern7_btheta(R th, R* b) {
   const double r1[] = {v7r::r011, v7r::r012, v7r::r013, v7r::r014, v7r::r015, v7r::r016, v7r::r017};
   const double r4[] = {v7r::r042, v7r::r043, v7r::r044, v7r::r045, v7r::r046, v7r::r047};
@@ -314,9 +328,9 @@ static void vern7_btheta(R th, R* b) {
   const double r14[] = {v7r::r142, v7r::r143, v7r::r144, v7r::r145, v7r::r146, v7r::r147};
   const double r15[] = {v7r::r152, v7r::r153, v7r::r154, v7r::r155, v7r::r156, v7r::r157};
   const double r16[] = {v7r::r162, v7r::r163, v7r::r164, v7r::r165, v7r::r166, v7r::r167};
-  b[0] = horner(th, r1, 7, 1);
+  b[0] = horner<DEV>(th, r1, 7, 1);
   const double* rs[] = {r4, r5, r6, r7, r8, r9, r11, r12, r13, r14, r15, r16};
-  for (int i = 0; i < 12; ++i) b[i + 1] = horner(th, rs[i], 6, 2);
+  for (int i = 0; i < 12; ++i) b[i + 1] = horner<DEV>(th, rs[i], 6, 2);
 }
 
 /* ---- Verner 9(8), src/verner/gpuvern9.jl:468-573 (slots 0..15 = k1..k16) */
@@ -381,7 +395,7 @@ const double V9_XC[] = {v9x::c17, v9x::c18, v9x::c19, v9x::c20, v9x::c21, v9x::c
                         v9x::c25, v9x::c26};
 
 /* bθs of src/verner/verner_tableaus.jl:1362-1398; order b1,b8..b15,b17..b26 */
-template <class R>
+template <bool DEV, class R>
 static void vern9_btheta(R th, R* b) {
   const double r1[] = {v9r::r011, v9r::r012, v9r::r013, v9r::r014, v9r::r015, v9r::r016, v9r::r017, v9r::r018, v9r::r019};
 #define V9ROW(i) const double r##i[] = {v9r::r##i##2, v9r::r##i##3, v9r::r##i##4, v9r::r##i##5, \
@@ -391,9 +405,9 @@ static void vern9_btheta(R th, R* b) {
   V9ROW(10); V9ROW(11); V9ROW(12); V9ROW(13); V9ROW(14); V9ROW(15);
   V9ROW(17); V9ROW(18); V9ROW(19); V9ROW(20); V9ROW(21); V9ROW(22); V9ROW(23); V9ROW(24); V9ROW(25); V9ROW(26);
 #undef V9ROW
-  b[0] = horner(th, r1, 9, 1);
+  b[0] = horner<DEV>(th, r1, 9, 1);
   const double* rs[] = {r8, r9, r10, r11, r12, r13, r14, r15, r17, r18, r19, r20, r21, r22, r23, r24, r25, r26};
-  for (int i = 0; i < 18; ++i) b[i + 1] = horner(th, rs[i], 8, 2);
+  for (int i = 0; i < 18; ++i) b[i + 1] = horner<DEV>(th, rs[i], 8, 2);
 }
 
 /* ---------------------------------------------------------------- methods */
@@ -439,7 +453,7 @@ struct Tsit5 {
                     double* out) {
     (void)told; (void)tnew;
     R b[7], s[MAXD];
-    tsit5_btheta<R>((R)theta, b);
+    tsit5_btheta<P::DEV, R>((R)theta, b);
     for (int d = 0; d < A.D; ++d) s[d] = b[0] * k[0][d];
     for (int j = 1; j < 7; ++j)
       for (int d = 0; d < A.D; ++d) s[d] = vmadd<P::DEV>(b[j], k[j][d], s[d]);
@@ -505,7 +519,7 @@ struct Vern7 {
     (void)told;
     const R h = (R)dtold;
     R b[13], s[MAXD], tmp[MAXD];
-    vern7_btheta<R>((R)theta, b);
+    vern7_btheta<P::DEV, R>((R)theta, b);
     const Term* xs[] = {V7_X11, V7_X12, V7_X13, V7_X14, V7_X15, V7_X16};
     const int nx[] = {7, 8, 9, 10, 10, 10};
     for (int i = 0; i < 6; ++i) {
@@ -569,7 +583,7 @@ struct Vern9 {
     for (int j = 1; j <= 8; ++j)
       for (int d = 0; d < A.D; ++d) kk[j][d] = ADAPTIVE ? k[j + 6][d] : k[j][d];
     R b[19], s[MAXD], tmp[MAXD];
-    vern9_btheta<R>((R)theta, b);
+    vern9_btheta<P::DEV, R>((R)theta, b);
     const Term* xs[] = {V9_X17, V9_X18, V9_X19, V9_X20, V9_X21, V9_X22, V9_X23, V9_X24, V9_X25, V9_X26};
     const int nx[] = {9, 10, 11, 12, 13, 14, 14, 14, 14, 14};
     const T tb = ADAPTIVE ? told : tnew;
@@ -710,16 +724,28 @@ static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
       if (a->maxiters > 0 && attempts >= a->maxiters) { ret = RET_MAXITERS; goto done; }
       M::attempt(A, up, t, dt, k, un, e, true);
       ++attempts;
-      /* error norm: RMS of e ./ (abstol .+ max.(|uprev|, |u|) * reltol) */
-      R acc = 0;
-      for (int d = 0; d < D; ++d) {
-        R m = jmax(std::fabs(up.hi[d]), std::fabs(un.hi[d]));
-        R sc = P::DEV ? fmaX(m, reltol, abstol) : abstol + m * reltol;
-        R r = e[d] / sc;
-        if (d == 0) acc = r * r;
-        else acc = P::DEV ? fmaX(r, r, acc) : acc + r * r;
+      /* error norm: RMS of e ./ (abstol .+ max.(|uprev|, |u|) * reltol); the
+       * device canon evaluates it in single precision unless abstol < 1e-30 */
+      if (P::DEV && a->abstol >= 1e-30) {
+        const float fa = (float)a->abstol, fr = (float)a->reltol;
+        float acc = 0;
+        for (int d = 0; d < D; ++d) {
+          float m = jmax(std::fabs((float)up.hi[d]), std::fabs((float)un.hi[d]));
+          float r = (float)e[d] / std::fma(m, fr, fa);
+          acc = (d == 0) ? r * r : std::fma(r, r, acc);
+        }
+        EEst = (R)std::sqrt(acc / (float)D);
+      } else {
+        R acc = 0;
+        for (int d = 0; d < D; ++d) {
+          R m = jmax(std::fabs(up.hi[d]), std::fabs(un.hi[d]));
+          R sc = P::DEV ? fmaX(m, reltol, abstol) : abstol + m * reltol;
+          R r = e[d] / sc;
+          if (d == 0) acc = r * r;
+          else acc = P::DEV ? fmaX(r, r, acc) : acc + r * r;
+        }
+        EEst = std::sqrt(acc / (R)D);
       }
-      EEst = std::sqrt(acc / (R)D);
       if (EEst != EEst) saw_nan = true;
 
       if (!P::DEV) {
@@ -770,9 +796,10 @@ static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
           else t += dtold;
           if (nacc == 0) dt_first = (double)dtold;
           ++nacc;
+          const T inv_dt = recip_dev(dtold);
           while (cur < P_ && (T)a->saveat[cur] <= t) {
             const T savet = (T)a->saveat[cur];
-            const T theta = (savet - told) / dtold;
+            const T theta = (savet - told) * inv_dt;
             M::dense(A, up, told, t, dtold, theta, k, tmpv);
             put_us(a, o, i, cur, tmpv);
             ++cur;
@@ -964,7 +991,7 @@ static void solve_simple_atsit5(const oracle_args* a, oracle_out* o, int64_t i) 
       /* integ(t): θ = (t - tprev)/dt, u = uprev + dt * Σ bθ_i ks_i */
       const double theta = (a->saveat[cur] - it.tprev) / it.dt;
       double b[7], s[MAXD];
-      tsit5_btheta<double>(theta, b);
+      tsit5_btheta<P::DEV, double>(theta, b);
       for (int d = 0; d < D; ++d) s[d] = b[0] * it.ks[0][d];
       for (int j = 1; j < 7; ++j)
         for (int d = 0; d < D; ++d) s[d] = vmadd<P::DEV>(b[j], it.ks[j][d], s[d]);

@@ -141,6 +141,7 @@ extern "C" int ode_ensemble_solve_noalloc(const ode_solve_args* a, ode_solve_out
   kp.dim = 3;
   kp.nparams = 3;
   kp.maxiters = a->maxiters > 0 ? a->maxiters : kDefaultMaxIters;
+  kp.norm_fp64 = a->abstol < 1e-30 ? 1 : 0;  /* the same rule as ode_ensemble_solve */
   kp.us = o->us;
   kp.u_final = o->u_final;
   kp.t_final = o->t_final;

@@ -508,6 +508,7 @@ int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o,
   kp.dim = D;
   kp.nparams = NP;
   kp.maxiters = a->maxiters > 0 ? a->maxiters : kDefaultMaxIters;
+  kp.norm_fp64 = a->abstol < 1e-30 ? 1 : 0;
 
   const bool host = a->memory == ODE_MEM_HOST;
   const size_t nd = (size_t)n * sizeof(double);

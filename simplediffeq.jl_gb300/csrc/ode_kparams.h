@@ -20,6 +20,7 @@ struct KParams {
   int save_everystep;
   int dim, nparams;
   long long maxiters;      /* <= 0: no cap */
+  int norm_fp64;           /* 1: error norm in double (abstol below 1e-30) */
   double* us;              /* [npoints][dim][n] or 0 */
   double* u_final;         /* [dim][n] or 0 */
   double* t_final;         /* [n] or 0 */

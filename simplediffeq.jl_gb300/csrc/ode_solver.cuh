@@ -23,10 +23,14 @@
  *     are compiled with --fmad=false);
  *   - stage times t + c*dt and Horner steps of the dense-output polynomials
  *     are fused, as Julia fuses scalar muladd;
- *   - the step-size factor q (q11 = EEst^beta1, qold^beta2, the clamps and the
- *     reciprocal applied to dt) is computed in single precision with the
- *     deterministic ctrl_pow below; dt, t, the state and the error estimate
- *     keep the solver precision.
+ *   - the error norm EEst and the step-size factor q (q11 = EEst^beta1,
+ *     qold^beta2, the clamps and the reciprocal applied to dt) are computed in
+ *     single precision, q with the deterministic ctrl_pow below (the norm in
+ *     double when abstol < 1e-30); dt, t and the state keep the solver
+ *     precision;
+ *   - the dense-output abscissa theta multiplies by recip(dt) (a float
+ *     reciprocal refined by one Newton step) and the polynomials that start at
+ *     theta^2 multiply by one shared theta^2.
  */
 #pragma once
 #include "ode_kparams.h"
@@ -51,6 +55,28 @@ template <class X> __device__ __forceinline__ X jmin(X a, X b) { return (a != a 
 template <class X> __device__ __forceinline__ X jmax(X a, X b) { return (a != a || b != b) ? a + b : (b > a ? b : a); }
 template <class X> __device__ __forceinline__ X fm_min(X x, X y) { return (y > x) ? x : y; }
 template <class X> __device__ __forceinline__ X fm_max(X x, X y) { return (y > x) ? y : x; }
+
+/* min(|a|, |b|) with Julia's NaN propagation.  For doubles it compares the
+ * bit patterns as integers (for non-negative IEEE values integer order is
+ * numeric order and NaNs sort above +Inf), keeping the work off the FP64 pipe. */
+__device__ __forceinline__ double absmin(double a, double b) {
+  const unsigned long long MASK = 0x7fffffffffffffffULL, INF = 0x7ff0000000000000ULL;
+  const unsigned long long ua = (unsigned long long)__double_as_longlong(a) & MASK;
+  const unsigned long long ub = (unsigned long long)__double_as_longlong(b) & MASK;
+  const unsigned long long r = (ua > INF) ? ua : ((ub > INF) ? ub : (ua < ub ? ua : ub));
+  return __longlong_as_double((long long)r);
+}
+__device__ __forceinline__ float absmin(float a, float b) { return jmin(fabsf(a), fabsf(b)); }
+
+/* 1/x for the dense-output abscissa theta = (t_save - told) / dt: a single
+ * precision reciprocal refined by one Newton step in double (relative error
+ * below 1e-14, four FP64 operations instead of a full division). */
+__device__ __forceinline__ double recip(double x) {
+  const double r0 = (double)__frcp_rn((float)x);
+  const double e = __fma_rn(-x, r0, 1.0);
+  return __fma_rn(r0, e, r0);
+}
+__device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
 
 /* Single-precision x^b for the step-size controller (x >= 0 or NaN).
  * log2 from the atanh series of the reduced mantissa, 2^y from the Taylor
@@ -323,11 +349,12 @@ struct MTsit5 {
   __device__ static __forceinline__ void dense(const F& f, const R (&uh)[D], const R (&uc)[D], T told, T tnew,
                                                T dtold, T theta, R (&k)[NK][D], double (&out)[D]) {
     const R th = (R)theta;
+    const R th2 = th * th;
     R ex, b1, b2, b3, b4, b5, b6, b7;
     ex = C5(r14); ex = fmaR(th, ex, C5(r13)); ex = fmaR(th, ex, C5(r12)); ex = fmaR(th, ex, C5(r11)); b1 = th * ex;
 #define TSIT5_B(i, out_)                                                        \
   ex = C5(r##i##4); ex = fmaR(th, ex, C5(r##i##3)); ex = fmaR(th, ex, C5(r##i##2)); \
-  ex = th * ex; out_ = th * ex;
+  out_ = th2 * ex;
     TSIT5_B(2, b2) TSIT5_B(3, b3) TSIT5_B(4, b4) TSIT5_B(5, b5) TSIT5_B(6, b6) TSIT5_B(7, b7)
 #undef TSIT5_B
     R s[D];
@@ -418,13 +445,14 @@ struct MVern7 {
     axpy(tmp, uh, h, s); f(tmp, stime(tnew, X7T(c16), dtold), x[5]);
 
     const R th = (R)theta;
+    const R th2 = th * th;
     R b[13], ex;
     ex = R7(r017); ex = fmaR(th, ex, R7(r016)); ex = fmaR(th, ex, R7(r015)); ex = fmaR(th, ex, R7(r014));
     ex = fmaR(th, ex, R7(r013)); ex = fmaR(th, ex, R7(r012)); ex = fmaR(th, ex, R7(r011)); b[0] = th * ex;
 #define V7B(i, j)                                                                      \
   ex = R7(r##i##7); ex = fmaR(th, ex, R7(r##i##6)); ex = fmaR(th, ex, R7(r##i##5));        \
   ex = fmaR(th, ex, R7(r##i##4)); ex = fmaR(th, ex, R7(r##i##3)); ex = fmaR(th, ex, R7(r##i##2)); \
-  ex = th * ex; b[j] = th * ex;
+  b[j] = th2 * ex;
     V7B(04, 1) V7B(05, 2) V7B(06, 3) V7B(07, 4) V7B(08, 5) V7B(09, 6)
     V7B(11, 7) V7B(12, 8) V7B(13, 9) V7B(14, 10) V7B(15, 11) V7B(16, 12)
 #undef V7B
@@ -567,6 +595,7 @@ struct MVern9Impl {
     axpy(tmp, uh, h, s); f(tmp, stime(tb, X9T(c26), dtold), x[9]);
 
     const R th = (R)theta;
+    const R th2 = th * th;
     R b[19], ex;
     ex = R9(r019); ex = fmaR(th, ex, R9(r018)); ex = fmaR(th, ex, R9(r017)); ex = fmaR(th, ex, R9(r016));
     ex = fmaR(th, ex, R9(r015)); ex = fmaR(th, ex, R9(r014)); ex = fmaR(th, ex, R9(r013));
@@ -574,7 +603,7 @@ struct MVern9Impl {
 #define V9B(i, j)                                                                             \
   ex = R9(r##i##9); ex = fmaR(th, ex, R9(r##i##8)); ex = fmaR(th, ex, R9(r##i##7));               \
   ex = fmaR(th, ex, R9(r##i##6)); ex = fmaR(th, ex, R9(r##i##5)); ex = fmaR(th, ex, R9(r##i##4)); \
-  ex = fmaR(th, ex, R9(r##i##3)); ex = fmaR(th, ex, R9(r##i##2)); ex = th * ex; b[j] = th * ex;
+  ex = fmaR(th, ex, R9(r##i##3)); ex = fmaR(th, ex, R9(r##i##2)); b[j] = th2 * ex;
     V9B(08, 1) V9B(09, 2) V9B(10, 3) V9B(11, 4) V9B(12, 5) V9B(13, 6) V9B(14, 7) V9B(15, 8)
     V9B(17, 9) V9B(18, 10) V9B(19, 11) V9B(20, 12) V9B(21, 13) V9B(22, 14) V9B(23, 15) V9B(24, 16)
     V9B(25, 17) V9B(26, 18)
@@ -742,39 +771,64 @@ __device__ __forceinline__ bool adaptive_iter(const KParams& P, Lane<PR, D, F, N
   M::attempt(l.f, l.uh, l.uc, l.t, l.dt, l.k, nh, nc, e, true);
   l.att += 1;
   /* EEst = sqrt(sum((e ./ (abstol .+ max.(|uprev|, |u|) .* reltol)).^2) / D) */
-  const R abstol = (R)P.abstol, reltol = (R)P.reltol;
-  R acc = (R)0;
+  /* EEst = sqrt(mean((e ./ (abstol .+ max.(|uprev|, |u|) .* reltol)).^2)), in
+   * single precision (converting doubles to float is as cheap as an FP32 op on
+   * this GPU, FP64 division and square root are not); double when abstol is so
+   * small that the scale could leave the float range (P.norm_fp64). */
+  float Ef;
+  bool reject, is_zero;
+  if (sizeof(R) == sizeof(float) || !P.norm_fp64) {
+    const float abstol = (float)P.abstol, reltol = (float)P.reltol;
+    float acc = 0.f;
 #pragma unroll
-  for (int d = 0; d < D; ++d) {
-    const R m = jmax(absR(l.uh[d]), absR(nh[d]));
-    const R r = e[d] / fmaR(m, reltol, abstol);
-    acc = (d == 0) ? r * r : fmaR(r, r, acc);
+    for (int d = 0; d < D; ++d) {
+      const float m = jmax(fabsf((float)l.uh[d]), fabsf((float)nh[d]));
+      const float r = __fdiv_rn((float)e[d], __fmaf_rn(m, reltol, abstol));
+      acc = (d == 0) ? r * r : __fmaf_rn(r, r, acc);
+    }
+    Ef = __fsqrt_rn(__fdiv_rn(acc, (float)D));
+    reject = Ef > 1.0f;
+    is_zero = Ef == 0.0f;
+  } else {
+    const R abstol = (R)P.abstol, reltol = (R)P.reltol;
+    R acc = (R)0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const R m = jmax(absR(l.uh[d]), absR(nh[d]));
+      const R r = e[d] / fmaR(m, reltol, abstol);
+      acc = (d == 0) ? r * r : fmaR(r, r, acc);
+    }
+    const R EEst = sqrtR(acc / (R)D);
+    Ef = (float)EEst;
+    reject = EEst > (R)1;
+    is_zero = EEst == (R)0;
   }
-  const R EEst = sqrtR(acc / (R)D);
-  if (EEst != EEst) l.nan_seen = true;
+  if (Ef != Ef) l.nan_seen = true;
   const float B1 = (float)(7.0 / 50.0), B2 = (float)(2.0 / 25.0), GAM = (float)(9.0 / 10.0);
   const float QMAXI = 0.1f, QMINI = 5.0f, QOLDINIT = (float)1.0e-4;
-  const float Ef = (float)EEst;
   const float q11 = ctrl_pow(Ef, B1);
-  if (EEst > (R)1) {
+  if (reject) {
     const float fac = jmin(QMINI, __fdiv_rn(q11, GAM));
     l.dt = l.dt * (T)__fdiv_rn(1.0f, fac);
     l.nrej += 1;
     return false;
   }
-  float q = (EEst == (R)0) ? QMAXI : __fdiv_rn(q11, l.qoldp);
+  float q = is_zero ? QMAXI : __fdiv_rn(q11, l.qoldp);
   q = fm_max(QMAXI, fm_min(QMINI, __fdiv_rn(q, GAM)));
   l.qoldp = ctrl_pow(jmax(Ef, QOLDINIT), B2);
   const T tf = (T)P.tf;
   const T dtold = l.dt;
   const T dtn = l.dt * (T)__fdiv_rn(1.0f, q);
-  l.dt = jmin(absR(dtn), absR(tf - l.t - dtold));
+  const T rest = tf - l.t - dtold;
+  l.dt = absmin(dtn, rest);
   const T told = l.t;
-  l.t = ((double)(tf - l.t - dtold) < dtmin) ? tf : l.t + dtold;
+  l.t = ((double)rest < dtmin) ? tf : l.t + dtold;
   if (l.nacc == 0) l.dt_first = (double)dtold;
   l.nacc += 1;
+  T inv_dt = (T)0;
+  if (l.cur < P.nsave && (T)P.saveat[l.cur] <= l.t) inv_dt = recip(dtold);
   while (l.cur < P.nsave && (T)P.saveat[l.cur] <= l.t) {
-    const T theta = ((T)P.saveat[l.cur] - told) / dtold;
+    const T theta = ((T)P.saveat[l.cur] - told) * inv_dt;
     double v[D];
     M::dense(l.f, l.uh, l.uc, told, l.t, dtold, theta, l.k, v);
     store_point<PR, D>(P, l.idx, l.cur, v);
