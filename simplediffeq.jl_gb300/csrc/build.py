@@ -52,8 +52,10 @@ GROUPS = {
     "lorenz": [("tsit5", "fixed", "lorenz", 3, "fp64"),
                ("atsit5", "plain", "lorenz", 3, "fp64"),
                ("atsit5", "persistent", "lorenz", 3, "fp64")],
+    "lorenz_staged": [("atsit5", "staged", "lorenz", 3, "fp64")],
     "vdp": [("avern7", "plain", "vanderpol", 2, "fp64"),
-            ("avern7", "persistent", "vanderpol", 2, "fp64")],
+            ("avern7", "persistent", "vanderpol", 2, "fp64"),
+            ("avern7", "staged", "vanderpol", 2, "fp64")],
     "r3bp64": [("avern9", "plain", "r3bp", 4, "fp64"),
                ("avern9", "persistent", "r3bp", 4, "fp64")],
     "r3bp32": [("avern9", "plain", "r3bp", 4, "fp32k"),

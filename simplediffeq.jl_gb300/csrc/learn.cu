@@ -46,7 +46,7 @@ constexpr int NBINS = 1024;
 
 struct Model {
   int nin = 0, nh = 0, rhs = -1, alg = -1, dim = 0, nparams = 0;
-  int seed_dt0 = 1;
+  int seed_dt0 = 0;
   float dt0_safety = 1.0f;
   std::vector<float> xmean, xstd, ymean, ystd;  /* standardisation */
   float lo = 0.f, hi = 1.f;                      /* binning range of log attempts */
@@ -406,7 +406,7 @@ void ode_learn_default_opts(ode_learn_opts* o) {
   o->batch = 1024;
   o->lr = 3e-3f;
   o->seed = 1;
-  o->seed_dt0 = 1;
+  o->seed_dt0 = 0;
   o->dt0_safety = 1.0f;
 }
 

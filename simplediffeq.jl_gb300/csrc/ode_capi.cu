@@ -239,16 +239,19 @@ std::string rhs_type_expr(ode_handle* h, const ode_solve_args* a) {
   return b;
 }
 
-/* kind of entry point: plain | persistent | fixed | rk4 */
-const char* entry_kind(int alg, int sched) {
+/* kind of entry point: plain | persistent | staged | fixed | rk4.  The
+ * persistent schedules use the staged driver (saveat interpolation batched
+ * per warp through shared memory) when there are saveat points. */
+const char* entry_kind(int alg, int sched, int64_t nsave) {
   if (alg == ODE_ALG_RK4) return "rk4";
   if (is_fixed(alg)) return "fixed";
-  return sched == ODE_SCHED_PLAIN ? "plain" : "persistent";
+  if (sched == ODE_SCHED_PLAIN) return "plain";
+  return nsave > 0 ? "staged" : "persistent";
 }
 
 std::string kernel_key(ode_handle* h, const ode_solve_args* a, int sched) {
   char b[160];
-  snprintf(b, sizeof b, "%s|%s|%d|%d|%s", alg_name(a->alg), entry_kind(a->alg, sched), a->rhs, a->dim,
+  snprintf(b, sizeof b, "%s|%s|%d|%d|%s", alg_name(a->alg), entry_kind(a->alg, sched, a->nsave), a->rhs, a->dim,
            prec_name(a->precision));
   return b;
 }
@@ -271,7 +274,7 @@ int compile_jit(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* f
            "    user_rhs<R>(du, u, p, (R)t);\n  }\n};\n";
   }
   src += "typedef " + rhs_type_expr(h, a) + " RHS_T;\n";
-  src += std::string("GBODE_ENTRY(gbode_jit, ") + entry_kind(a->alg, sched) + ", " + method_type(a->alg) + ", " +
+  src += std::string("GBODE_ENTRY(gbode_jit, ") + entry_kind(a->alg, sched, a->nsave) + ", " + method_type(a->alg) + ", " +
          prec_type(a->precision) + ", RHS_T)\n";
 
   if (!load_nvrtc()) return fail(h, ODE_ENVRTC, "libnvrtc.so.13 could not be loaded");
@@ -315,7 +318,7 @@ int get_kernel(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn
     *jit = h->kjit[key];
     return ODE_OK;
   }
-  const char* kind = entry_kind(a->alg, sched);
+  const char* kind = entry_kind(a->alg, sched, a->nsave);
   for (const AotEntry& e : kAotEntries) {
     if (e.alg == a->alg && e.rhs == a->rhs && e.dim == a->dim && e.precision == a->precision &&
         std::strcmp(e.kind, kind) == 0) {

@@ -758,19 +758,32 @@ __device__ __forceinline__ void lane_finish(const KParams& P, Lane<PR, D, F, NK>
   tot.sav += (unsigned long long)l.ninterp;
 }
 
-/* One attempt of an adaptive method plus its accept/reject decision.
- * Returns true when the trajectory has finished (outputs written). */
+enum { TRY_REJECTED = 0, TRY_ACCEPTED = 1, TRY_STOPPED = 2 };
+
+/* What an accepted step leaves for its dense output and commit. */
+template <class T>
+struct Accepted {
+  T told, dtold;
+};
+
+/* One attempt of an adaptive method and its accept/reject decision: the
+ * stages, the error norm and the controller; on acceptance t, dt and the
+ * counters advance, while the saveat points of the step and the commit of the
+ * new state are left to the caller (the state before the step, the stage
+ * values and the proposal nh/nc are still intact).  TRY_STOPPED: dt fell
+ * below dtmin or the attempt cap was reached; the outputs are written. */
 template <class M, class PR, int D, class F, int NK>
-__device__ __forceinline__ bool adaptive_iter(const KParams& P, Lane<PR, D, F, NK>& l, Totals& tot) {
+__device__ __forceinline__ int adaptive_try(const KParams& P, Lane<PR, D, F, NK>& l, Totals& tot,
+                                            typename PR::R (&nh)[D], typename PR::R (&nc)[D],
+                                            Accepted<typename PR::T>& acc_out) {
   typedef typename PR::R R;
   typedef typename PR::T T;
   const double dtmin = M::DTMIN_1F7 ? (double)1.0e-7f : 1.0e-14;
-  if ((double)l.dt < dtmin) { lane_finish(P, l, RET_DTMIN, tot); return true; }
-  if (P.maxiters > 0 && l.att >= P.maxiters) { lane_finish(P, l, RET_MAXITERS, tot); return true; }
-  R nh[D], nc[D], e[D];
+  if ((double)l.dt < dtmin) { lane_finish(P, l, RET_DTMIN, tot); return TRY_STOPPED; }
+  if (P.maxiters > 0 && l.att >= P.maxiters) { lane_finish(P, l, RET_MAXITERS, tot); return TRY_STOPPED; }
+  R e[D];
   M::attempt(l.f, l.uh, l.uc, l.t, l.dt, l.k, nh, nc, e, true);
   l.att += 1;
-  /* EEst = sqrt(sum((e ./ (abstol .+ max.(|uprev|, |u|) .* reltol)).^2) / D) */
   /* EEst = sqrt(mean((e ./ (abstol .+ max.(|uprev|, |u|) .* reltol)).^2)), in
    * single precision (converting doubles to float is as cheap as an FP32 op on
    * this GPU, FP64 division and square root are not); double when abstol is so
@@ -811,7 +824,7 @@ __device__ __forceinline__ bool adaptive_iter(const KParams& P, Lane<PR, D, F, N
     const float fac = jmin(QMINI, __fdiv_rn(q11, GAM));
     l.dt = l.dt * (T)__fdiv_rn(1.0f, fac);
     l.nrej += 1;
-    return false;
+    return TRY_REJECTED;
   }
   float q = is_zero ? QMAXI : __fdiv_rn(q11, l.qoldp);
   q = fm_max(QMAXI, fm_min(QMINI, __fdiv_rn(q, GAM)));
@@ -825,6 +838,38 @@ __device__ __forceinline__ bool adaptive_iter(const KParams& P, Lane<PR, D, F, N
   l.t = ((double)rest < dtmin) ? tf : l.t + dtold;
   if (l.nacc == 0) l.dt_first = (double)dtold;
   l.nacc += 1;
+  acc_out.told = told;
+  acc_out.dtold = dtold;
+  return TRY_ACCEPTED;
+}
+
+/* Replace the state by the accepted proposal (and the FSAL stage). */
+template <class M, class PR, int D, class F, int NK>
+__device__ __forceinline__ void adaptive_commit(Lane<PR, D, F, NK>& l, const typename PR::R (&nh)[D],
+                                                const typename PR::R (&nc)[D]) {
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    l.uh[d] = nh[d];
+    l.uc[d] = nc[d];
+  }
+  if (M::FSAL) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) l.k[0][d] = l.k[NK - 1][d];
+  }
+}
+
+/* One attempt with the saveat points of an accepted step interpolated at once
+ * by this lane.  Returns true when the trajectory has finished (outputs written). */
+template <class M, class PR, int D, class F, int NK>
+__device__ __forceinline__ bool adaptive_iter(const KParams& P, Lane<PR, D, F, NK>& l, Totals& tot) {
+  typedef typename PR::R R;
+  typedef typename PR::T T;
+  R nh[D], nc[D];
+  Accepted<T> st;
+  const int r = adaptive_try<M>(P, l, tot, nh, nc, st);
+  if (r == TRY_STOPPED) return true;
+  if (r == TRY_REJECTED) return false;
+  const T told = st.told, dtold = st.dtold;
   T inv_dt = (T)0;
   if (l.cur < P.nsave && (T)P.saveat[l.cur] <= l.t) inv_dt = recip(dtold);
   while (l.cur < P.nsave && (T)P.saveat[l.cur] <= l.t) {
@@ -835,16 +880,8 @@ __device__ __forceinline__ bool adaptive_iter(const KParams& P, Lane<PR, D, F, N
     l.cur += 1;
     l.ninterp += 1;
   }
-#pragma unroll
-  for (int d = 0; d < D; ++d) {
-    l.uh[d] = nh[d];
-    l.uc[d] = nc[d];
-  }
-  if (M::FSAL) {
-#pragma unroll
-    for (int d = 0; d < D; ++d) l.k[0][d] = l.k[NK - 1][d];
-  }
-  if (!(l.t < tf)) { lane_finish(P, l, RET_DEFAULT, tot); return true; }
+  adaptive_commit<M>(l, nh, nc);
+  if (!(l.t < (T)P.tf)) { lane_finish(P, l, RET_DEFAULT, tot); return true; }
   return false;
 }
 
@@ -909,6 +946,178 @@ __device__ __forceinline__ void run_adaptive_persistent(const KParams& P) {
     if (active && adaptive_iter<M>(P, l, tot)) active = false;
   }
   flush_totals(P, tot);
+}
+
+/* ------------------------------------------------------------------ staged dense output */
+/* Persistent schedule with the saveat interpolation staged through shared
+ * memory.  In the plain and persistent drivers a lane interpolates its saveat
+ * points as soon as its step is accepted, and the other lanes of the warp
+ * idle meanwhile (about one step in three has a save point, so nearly every
+ * warp iteration pays for a full interpolation on a few lanes).  Here an
+ * accepted step only appends a job per saveat point to a per-warp ring in
+ * shared memory (a snapshot of what the interpolation reads: the state before
+ * the step, the stage values, the parameters, t, dt and theta); whenever 32
+ * jobs are waiting the whole warp interpolates 32 points at once, one per
+ * lane.  Each point is computed by the same M::dense call on the same values,
+ * so the results are bit-identical to the other drivers. */
+constexpr int kStageBytesPerWarp = 12288;  /* 4 warps per block: 48 KB of static shared memory */
+
+template <class M, class PR, int D, class F>
+struct StageLayout {
+  typedef typename PR::R R;
+  typedef typename PR::T T;
+  enum { NREC = D * (PR::KAHAN ? 2 : 1) + M::NK * D + F::NP };
+  enum { JOB = 4 * (int)sizeof(T) + 8 + NREC * (int)sizeof(R) + 4 };
+  enum { CAP = (kStageBytesPerWarp / JOB) & ~7 };
+};
+
+template <class M, class PR, int D, class F>
+__device__ __forceinline__ void run_adaptive_staged(const KParams& P) {
+  typedef typename PR::R R;
+  typedef typename PR::T T;
+  typedef StageLayout<M, PR, D, F> SL;
+  enum { CAP = SL::CAP, NK = M::NK, KOFF = D * (PR::KAHAN ? 2 : 1), POFF = KOFF + NK * D };
+  __shared__ __align__(16) unsigned char qmem[4][kStageBytesPerWarp];
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  unsigned char* qb = qmem[(threadIdx.x >> 5) & 3];
+  T* tv = (T*)qb;                                            /* told, tnew, dtold, theta: [4][CAP] */
+  long long* iv = (long long*)(qb + 4 * CAP * sizeof(T));    /* trajectory: [CAP] */
+  R* rv = (R*)(qb + 4 * CAP * sizeof(T) + 8 * CAP);          /* record values: [NREC][CAP] */
+  int* jv = (int*)(qb + 4 * CAP * sizeof(T) + 8 * CAP + SL::NREC * CAP * sizeof(R)); /* saveat index */
+  int qhead = 0, qcount = 0; /* warp-uniform */
+
+  Lane<PR, D, F, NK> l;
+  Totals tot = {0, 0, 0};
+  bool active = false, exhausted = false;
+
+  /* interpolate the m oldest jobs, one per lane */
+  auto round = [&](int m) {
+    __syncwarp();
+    if (lane < m) {
+      const int slot = (qhead + lane) % CAP;
+      R uh[D], uc[D], kk[NK][D];
+      F f2;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        uh[d] = rv[d * CAP + slot];
+        uc[d] = PR::KAHAN ? rv[(D + d) * CAP + slot] : (R)0;
+      }
+#pragma unroll
+      for (int q = 0; q < NK; ++q)
+#pragma unroll
+        for (int d = 0; d < D; ++d) kk[q][d] = rv[(KOFF + q * D + d) * CAP + slot];
+#pragma unroll
+      for (int q = 0; q < F::NP; ++q) f2.p[q] = rv[(POFF + q) * CAP + slot];
+      double v[D];
+      M::dense(f2, uh, uc, tv[slot], tv[CAP + slot], tv[2 * CAP + slot], tv[3 * CAP + slot], kk, v);
+      store_point<PR, D>(P, iv[slot], jv[slot], v);
+    }
+    __syncwarp();
+    qhead = (qhead + m) % CAP;
+    qcount -= m;
+  };
+
+  for (;;) {
+    const bool want = !active && !exhausted;
+    const unsigned need = __ballot_sync(FULL, want);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(P.counter, (unsigned long long)__popc(need));
+      base = __shfl_sync(FULL, base, leader);
+      if (want) {
+        const unsigned long long w = base + (unsigned long long)__popc(need & ((1u << lane) - 1u));
+        if (w < (unsigned long long)P.n) {
+          const long long idx = P.order ? (long long)P.order[w] : (long long)w;
+          active = !adaptive_start<M>(P, idx, l, tot);
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (!__any_sync(FULL, active)) {
+      if (!__any_sync(FULL, !exhausted)) break;
+      continue;
+    }
+    R nh[D], nc[D];
+    Accepted<T> st;
+    int r = TRY_REJECTED, njobs = 0;
+    if (active) {
+      r = adaptive_try<M>(P, l, tot, nh, nc, st);
+      if (r == TRY_STOPPED) active = false;
+      if (r == TRY_ACCEPTED)
+        while (l.cur + njobs < P.nsave && (T)P.saveat[l.cur + njobs] <= l.t) ++njobs;
+    }
+    /* slots for this iteration's jobs: exclusive prefix sum over the warp */
+    int incl = njobs;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(FULL, incl, 31);
+    const int excl = incl - njobs;
+    const int space = CAP - qcount;
+    if (njobs) {
+      const T inv_dt = recip(st.dtold);
+      for (int q = 0; q < njobs; ++q) {
+        const long long j = l.cur + q;
+        const T theta = ((T)P.saveat[j] - st.told) * inv_dt;
+        if (excl + q < space) {
+          const int slot = (qhead + qcount + excl + q) % CAP;
+          tv[slot] = st.told;
+          tv[CAP + slot] = l.t;
+          tv[2 * CAP + slot] = st.dtold;
+          tv[3 * CAP + slot] = theta;
+          iv[slot] = l.idx;
+          jv[slot] = (int)j;
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            rv[d * CAP + slot] = l.uh[d];
+            if (PR::KAHAN) rv[(D + d) * CAP + slot] = l.uc[d];
+          }
+#pragma unroll
+          for (int k = 0; k < NK; ++k)
+#pragma unroll
+            for (int d = 0; d < D; ++d) rv[(KOFF + k * D + d) * CAP + slot] = l.k[k][d];
+#pragma unroll
+          for (int k = 0; k < F::NP; ++k) rv[(POFF + k) * CAP + slot] = l.f.p[k];
+        } else {
+          /* the ring is full: interpolate here */
+          double v[D];
+          M::dense(l.f, l.uh, l.uc, st.told, l.t, st.dtold, theta, l.k, v);
+          store_point<PR, D>(P, l.idx, j, v);
+        }
+      }
+      l.cur += njobs;
+      l.ninterp += njobs;
+    }
+    qcount += total < space ? total : space;
+    if (r == TRY_ACCEPTED) {
+      adaptive_commit<M>(l, nh, nc);
+      if (!(l.t < (T)P.tf)) {
+        lane_finish(P, l, RET_DEFAULT, tot);
+        active = false;
+      }
+    }
+    while (qcount >= 32) round(32);
+  }
+  while (qcount > 0) round(qcount < 32 ? qcount : 32);
+  flush_totals(P, tot);
+}
+
+/* Staged when a full round of jobs fits the ring, the unstaged persistent
+ * driver otherwise (large states: Verner 9 with dim 4, Kuramoto-12). */
+template <class M, class PR, int D, class F>
+__device__ __forceinline__ void run_adaptive_staged_or_persistent(const KParams& P) {
+  if constexpr (StageLayout<M, PR, D, F>::CAP >= 32) {
+    if (P.nsave > 0) {
+      run_adaptive_staged<M, PR, D, F>(P);
+      return;
+    }
+  }
+  run_adaptive_persistent<M, PR, D, F>(P);
 }
 
 /* Fixed-step methods: thread i, the grid of Julia's t0:dt:tf shared by all. */
@@ -1009,7 +1218,7 @@ __device__ __forceinline__ void run_rk4(const KParams& P) {
 }  // namespace gbode
 
 /* Entry-point generator: GBODE_ENTRY(name, kind, Method, Prec, Rhs) defines
- * extern "C" __global__ name(KParams).  kind: plain | persistent | fixed | rk4. */
+ * extern "C" __global__ name(KParams).  kind: plain | persistent | staged | fixed | rk4. */
 #define GBODE_ENTRY_plain(NAME, M, PR, RHS)                                                  \
   extern "C" __global__ void __launch_bounds__(128) NAME(gbode::KParams P) {                \
     gbode::run_adaptive_plain<M<PR, RHS::D, RHS>, PR, RHS::D, RHS>(P);                      \
@@ -1017,6 +1226,10 @@ __device__ __forceinline__ void run_rk4(const KParams& P) {
 #define GBODE_ENTRY_persistent(NAME, M, PR, RHS)                                             \
   extern "C" __global__ void __launch_bounds__(128) NAME(gbode::KParams P) {                \
     gbode::run_adaptive_persistent<M<PR, RHS::D, RHS>, PR, RHS::D, RHS>(P);                 \
+  }
+#define GBODE_ENTRY_staged(NAME, M, PR, RHS)                                                 \
+  extern "C" __global__ void __launch_bounds__(128) NAME(gbode::KParams P) {                \
+    gbode::run_adaptive_staged_or_persistent<M<PR, RHS::D, RHS>, PR, RHS::D, RHS>(P);       \
   }
 #define GBODE_ENTRY_fixed(NAME, M, PR, RHS)                                                  \
   extern "C" __global__ void __launch_bounds__(128) NAME(gbode::KParams P) {                \

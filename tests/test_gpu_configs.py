@@ -1,0 +1,82 @@
+"""GPU checks of the remaining ensemble workloads: Kuramoto-12 (whose sin/cos
+come from CUDA's libdevice on the GPU and from glibc in the oracle, so parity
+is a tolerance), the single-precision modes' accuracy against the FP64
+oracle at abstol = reltol = 1e-14, and the staged saveat path in the
+compensated single-precision mode."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from test_gpu_parity import T_ARENSTORF, assert_bitexact, gpu, r3bp_inputs
+
+pytestmark = pytest.mark.gpu
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+import make_golden  # noqa: E402  (input generators shared with the golden fixtures)
+
+
+@pytest.mark.parametrize("schedule", ["plain", "persistent"])
+def test_kuramoto12_matches_oracle_within_tolerance(pkg, po, schedule):
+    u0, p = make_golden.kuramoto(2048, 9)
+    sv = np.linspace(0, 50, 50)
+    kw = dict(abstol=1e-8, reltol=1e-6)
+    sol = gpu(pkg, pkg.GPUSimpleATsit5(), "kuramoto", u0, p, (0.0, 50.0), 0.1, saveat=sv, schedule=schedule, **kw)
+    ref = po.solve("ATsit5", "kuramoto", u0, p, (0, 50), 0.1, rounding="device", saveat=sv, nthreads=8, **kw)
+    scale = 1e-8 + 1e-6 * np.abs(ref["u_final"]).max(0)
+    err = np.abs(sol.u_final - ref["u_final"]).max(0) / scale
+    assert np.mean(err <= 10) >= 0.999
+    assert np.mean(sol.naccept == ref["naccept"]) >= 0.99
+    assert np.abs(sol.naccept - ref["naccept"]).max() <= 2
+    es = np.abs(sol.us - ref["us"]).max(axis=(0, 1)) / scale
+    assert np.mean(es <= 10) >= 0.999
+
+
+def test_fp32_modes_error_against_fp64_oracle(pkg, po):
+    """Arenstorf ensemble: FP32 and FP32-Kahan (tol 1e-7) against the FP64
+    oracle at abstol = reltol = 1e-14 (trajectories the oracle finishes;
+    Vern9's 1f-7 dtmin stops a few, as in the reference)."""
+    u0, mu = r3bp_inputs(1024, seed=21)
+    ref = po.solve("AVern9", "r3bp", u0, mu, (0, T_ARENSTORF), 0.1, rounding="ref", abstol=1e-14, reltol=1e-14,
+                   nthreads=8)
+    out = {}
+    for prec in ("fp32", "fp32_kahan"):
+        sol = gpu(pkg, pkg.GPUSimpleAVern9(), "r3bp", u0, mu, (0.0, T_ARENSTORF), 0.1, abstol=1e-7, reltol=1e-7,
+                  precision=prec, throw=False)
+        ok = (ref["retcode"] == 0) & (sol.retcode == 0)
+        assert ok.mean() > 0.97
+        err = np.abs(sol.u_final[:, ok] - ref["u_final"][:, ok]).max(0)
+        out[prec] = (np.median(err), err.max())
+        print("%s: max error vs FP64 oracle at 1e-14: %.3e (median %.3e) over %d trajectories"
+              % (prec, err.max(), np.median(err), ok.sum()))
+    assert out["fp32_kahan"][0] < 1e-3
+    assert out["fp32"][0] > 2 * out["fp32_kahan"][0]  # the compensated update is what buys the accuracy
+
+
+def test_staged_saveat_fp32_kahan_bitexact(pkg, po):
+    rng = np.random.default_rng(12)
+    n = 2048
+    mu = np.exp(rng.uniform(np.log(0.1), np.log(10), n))[None, :]
+    u0 = rng.uniform(-2, 2, (2, n))
+    sv = np.linspace(0, 20, 200)
+    sol = gpu(pkg, pkg.GPUSimpleAVern7(), "vanderpol", u0, mu, (0.0, 20.0), 0.1, abstol=1e-6, reltol=1e-6,
+              saveat=sv, precision="fp32_kahan", schedule="persistent")
+    ref = po.solve("AVern7", "vanderpol", u0, mu, (0, 20), 0.1, rounding="device", precision="fp32_kahan",
+                   abstol=1e-6, reltol=1e-6, saveat=sv, nthreads=8)
+    assert_bitexact(sol, ref)
+
+
+def test_learned_default_is_ordering_only(pkg):
+    """With the default options the learned schedule only reorders: every
+    trajectory's result equals the plain schedule's."""
+    from conftest import lorenz_inputs
+    kw = dict(dt=0.1, abstol=1e-8, reltol=1e-6)
+    tr = lorenz_inputs(8192, seed=111)
+    ens = lambda u0, p: pkg.EnsembleProblem(pkg.ODEProblem("lorenz", u0[:, 0], (0.0, 10.0), p[:, 0]), u0s=u0, ps=p)
+    pkg.learn_fit(ens(*tr), pkg.GPUSimpleATsit5(), 8192, **kw)
+    u0, p = lorenz_inputs(8192, seed=112)
+    sv = np.linspace(0, 10, 100)
+    a = pkg.solve(ens(u0, p), pkg.GPUSimpleATsit5(), trajectories=8192, schedule="learned", saveat=sv, **kw)
+    b = pkg.solve(ens(u0, p), pkg.GPUSimpleATsit5(), trajectories=8192, schedule="plain", saveat=sv, **kw)
+    assert a.stats.schedule_used == 2
+    assert np.array_equal(a.u_final, b.u_final) and np.array_equal(a.us, b.us, equal_nan=True)
