@@ -91,6 +91,14 @@ enum {
 
 enum { ODE_MEM_HOST = 0, ODE_MEM_DEVICE = 1 };
 
+/* what the saveat outputs hold */
+enum {
+  ODE_OUTPUT_STATE = 0,      /* us[nsave][dim][n]: the interpolated state (the reference's sol.u) */
+  ODE_OUTPUT_KURAMOTO_R = 1  /* us[nsave][1][n]: r(t) = |(1/dim) sum_k exp(i u_k(t))|, the Kuramoto order
+                                parameter of the interpolated state, reduced in the kernel (an ensemble
+                                output_func fused into the solve) */
+};
+
 /* per-trajectory return codes */
 enum {
   ODE_RET_DEFAULT = 0,  /* finished at tf (ReturnCode.Default in the reference) */
@@ -122,11 +130,13 @@ typedef struct {
   const double* p;      /* [nparams][n] */
   const double* dt0;    /* optional [n] per-trajectory initial dt (adaptive), or NULL */
   void* stream;         /* cudaStream_t, or NULL for the handle's stream */
+  int32_t output;       /* ODE_OUTPUT_* (0: the state) */
 } ode_solve_args;
 
 typedef struct {
-  double* us;           /* [npoints][dim][n]: npoints = nsave, or the grid length when
-                           save_everystep applies; NULL to skip */
+  double* us;           /* [npoints][dim][n] (ODE_OUTPUT_STATE) or [npoints][1][n]
+                           (ODE_OUTPUT_KURAMOTO_R): npoints = nsave, or the grid length
+                           when save_everystep applies; NULL to skip */
   double* u_final;      /* [dim][n] state at the end, or NULL */
   double* t_final;      /* [n], or NULL */
   int8_t* retcode;      /* [n] ODE_RET_*, or NULL */

@@ -652,8 +652,20 @@ static void load_traj(const oracle_args* a, int64_t i, Alg<P>& A, State<typename
   }
 }
 
+/* Saveat point j of trajectory i: the state, or the Kuramoto order parameter
+ * r = |(1/D) sum_k exp(i v_k)| (an ensemble output function: SciMLBase would
+ * apply it to each solution on the host). */
 static inline void put_us(const oracle_args* a, oracle_out* o, int64_t i, int64_t j, const double* v) {
   if (!o->us) return;
+  if (a->output == 1) {
+    double C = 0, S = 0;
+    for (int d = 0; d < a->dim; ++d) {
+      C += std::cos(v[d]);
+      S += std::sin(v[d]);
+    }
+    o->us[j * a->n + i] = std::sqrt(C * C + S * S) / a->dim;
+    return;
+  }
   for (int d = 0; d < a->dim; ++d) o->us[(j * a->dim + d) * a->n + i] = v[d];
 }
 

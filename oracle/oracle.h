@@ -47,6 +47,7 @@ typedef struct {
   const double* p;       /* SoA [nparams][n] */
   const double* dt0;     /* optional per-trajectory initial dt [n] */
   int nthreads;
+  int output;            /* 0: state at saveat points; 1: Kuramoto order parameter r(t) of it */
 } oracle_args;
 
 typedef struct {

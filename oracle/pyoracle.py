@@ -35,7 +35,7 @@ class _Args(ctypes.Structure):
                 ("saveat", ctypes.c_void_p), ("nsave", ctypes.c_int64), ("save_everystep", ctypes.c_int),
                 ("grid", ctypes.c_void_p), ("ngrid", ctypes.c_int64), ("maxiters", ctypes.c_int64),
                 ("u0", ctypes.c_void_p), ("p", ctypes.c_void_p), ("dt0", ctypes.c_void_p),
-                ("nthreads", ctypes.c_int)]
+                ("nthreads", ctypes.c_int), ("output", ctypes.c_int)]
 
 
 class _Out(ctypes.Structure):
@@ -176,7 +176,7 @@ def _ptr(a):
 
 
 def solve(alg, rhs, u0, p, tspan, dt, precision="fp64", rounding="ref", abstol=1e-6, reltol=1e-3,
-          saveat=None, save_everystep=False, maxiters=0, dt0=None, nthreads=1, grid=None):
+          saveat=None, save_everystep=False, maxiters=0, dt0=None, nthreads=1, grid=None, output="state"):
     """Solve n trajectories.  u0: (dim, n) float64, p: (nparams, n) float64.
     Returns a dict of numpy arrays (us is (npoints, dim, n))."""
     u0 = np.ascontiguousarray(u0, dtype=np.float64)
@@ -195,8 +195,9 @@ def solve(alg, rhs, u0, p, tspan, dt, precision="fp64", rounding="ref", abstol=1
         npts = len(grid)
     else:
         npts = 0
+    width = 1 if output == "kuramoto_r" else dim
     out = {
-        "us": np.full((npts, dim, n), np.nan) if npts else None,
+        "us": np.full((npts, width, n), np.nan) if npts else None,
         "u_final": np.zeros((dim, n)),
         "t_final": np.zeros(n),
         "retcode": np.zeros(n, dtype=np.int8),
@@ -208,7 +209,7 @@ def solve(alg, rhs, u0, p, tspan, dt, precision="fp64", rounding="ref", abstol=1
     args = _Args(ALG[alg], RHS[rhs], PREC[precision], ROUND[rounding], n, dim, nparams, t0, tf, float(dt),
                  float(abstol), float(reltol), _ptr(sv), 0 if sv is None else len(sv), int(bool(save_everystep)),
                  _ptr(grid), 0 if grid is None else len(grid), int(maxiters), _ptr(u0), _ptr(p), _ptr(d0),
-                 int(nthreads))
+                 int(nthreads), 1 if output == "kuramoto_r" else 0)
     o = _Out(_ptr(out["us"]), _ptr(out["u_final"]), _ptr(out["t_final"]), _ptr(out["retcode"]),
              _ptr(out["naccept"]), _ptr(out["nreject"]), _ptr(out["dt_first"]))
     rc = lib().oracle_solve(ctypes.byref(args), ctypes.byref(o))

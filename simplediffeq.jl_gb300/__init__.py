@@ -218,7 +218,7 @@ def _stack(eprob, trajectories):
 
 
 def make_args(alg, f_id, u0s, ps, tspan, dt, abstol, reltol, saveat, save_everystep, precision, schedule,
-              maxiters, memory=_lib.MEM_HOST, dt0=None):
+              maxiters, memory=_lib.MEM_HOST, dt0=None, output="state"):
     a = _lib.SolveArgs()
     a.alg = _lib.ALG[alg.name]
     a.rhs = f_id
@@ -235,11 +235,13 @@ def make_args(alg, f_id, u0s, ps, tspan, dt, abstol, reltol, saveat, save_everys
     a.maxiters = int(maxiters)
     a.u0, a.p = u0s.ctypes.data, ps.ctypes.data
     a.dt0 = None if dt0 is None else dt0.ctypes.data
+    a.output = _lib.OUTPUT[output]
     return a
 
 
 def solve(prob, alg, trajectories=None, dt=0.1, abstol=1e-6, reltol=1e-3, saveat=None, save_everystep=None,
-          precision="fp64", schedule="persistent", maxiters=0, device=0, dt0=None, throw=True, **kwargs):
+          precision="fp64", schedule="persistent", maxiters=0, device=0, dt0=None, throw=True, output="state",
+          **kwargs):
     """Solve an EnsembleProblem (or a single ODEProblem as an ensemble of one).
 
     Unknown keyword arguments are accepted and ignored, as the reference's
@@ -272,8 +274,10 @@ def solve(prob, alg, trajectories=None, dt=0.1, abstol=1e-6, reltol=1e-3, saveat
     if not alg.adaptive:
         schedule = "plain"
     args = make_args(alg, fid, u0s, ps, base.tspan, dt, abstol, reltol, sv, save_everystep, precision, schedule,
-                     maxiters, dt0=None if dt0 is None else np.ascontiguousarray(dt0, dtype=np.float64))
+                     maxiters, dt0=None if dt0 is None else np.ascontiguousarray(dt0, dtype=np.float64),
+                     output=output)
     dim = u0s.shape[0]
+    width = 1 if output == "kuramoto_r" else dim
     if sv is not None:
         npts = len(sv)
         tpts = sv
@@ -282,7 +286,7 @@ def solve(prob, alg, trajectories=None, dt=0.1, abstol=1e-6, reltol=1e-3, saveat
         npts = len(tpts)
     else:
         npts, tpts = 0, None
-    us = np.empty((npts, dim, n)) if npts else None
+    us = np.empty((npts, width, n)) if npts else None
     out = {"u_final": np.empty((dim, n)), "t_final": np.empty(n), "retcode": np.empty(n, dtype=np.int8),
            "naccept": np.empty(n, dtype=np.int32), "nreject": np.empty(n, dtype=np.int32),
            "dt_first": np.empty(n)}

@@ -19,6 +19,7 @@ RHS = {"lorenz": 0, "vanderpol": 1, "r3bp": 2, "kuramoto": 3, "linear": 4}
 PREC = {"fp64": 0, "fp32": 1, "fp32_kahan": 2}
 SCHED = {"plain": 0, "persistent": 1, "learned": 2}
 MEM_HOST, MEM_DEVICE = 0, 1
+OUTPUT = {"state": 0, "kuramoto_r": 1}
 RET_DEFAULT, RET_DTMIN, RET_MAXITERS, RET_NAN = 0, 1, 2, 3
 
 # Every symbol include/gb300ode.h declares.
@@ -34,7 +35,8 @@ class SolveArgs(ctypes.Structure):
                 ("dt", ctypes.c_double), ("abstol", ctypes.c_double), ("reltol", ctypes.c_double),
                 ("saveat", ctypes.c_void_p), ("nsave", ctypes.c_int64), ("save_everystep", ctypes.c_int32),
                 ("memory", ctypes.c_int32), ("maxiters", ctypes.c_int64), ("u0", ctypes.c_void_p),
-                ("p", ctypes.c_void_p), ("dt0", ctypes.c_void_p), ("stream", ctypes.c_void_p)]
+                ("p", ctypes.c_void_p), ("dt0", ctypes.c_void_p), ("stream", ctypes.c_void_p),
+                ("output", ctypes.c_int32)]
 
 
 class SolveOut(ctypes.Structure):

@@ -30,6 +30,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <random>
 #include <vector>
@@ -42,7 +43,7 @@ constexpr int MAXIN = 40;   /* nparams + dim */
 constexpr int HMAX = 64;
 constexpr int NOUT = 2;
 constexpr int TILE = 32;    /* samples per block in training */
-constexpr int NBINS = 1024;
+constexpr int NBINS = kCostBins;
 
 struct Model {
   int nin = 0, nh = 0, rhs = -1, alg = -1, dim = 0, nparams = 0;
@@ -294,11 +295,17 @@ int model_predict_device(ode_handle* h, const ode_solve_args* a, const KParams& 
   return e == cudaSuccess ? ODE_OK : cuda_fail(h, e, "mlp_predict");
 }
 
-int order_by_cost(ode_handle* h, const float* log_att, int64_t n, int* order, cudaStream_t s, int* launches) {
+std::string model_key(const Model* m) {
+  if (!m) return "nomodel";
+  char b[256];
+  snprintf(b, sizeof b, "%p|%p|%a|%a|%a|%d|%d|%d", (void*)m->d_w, (void*)m->d_norm, m->lo, m->hi, m->dt0_safety,
+           m->seed_dt0, m->nin, m->nh);
+  return b;
+}
+
+int order_by_cost(ode_handle* h, const float* log_att, int64_t n, int* order, unsigned* cnt, cudaStream_t s,
+                  int* launches) {
   Model* m = h->model;
-  int rc;
-  unsigned* cnt = (unsigned*)buf(h, "bins", NBINS * sizeof(unsigned), &rc);
-  if (!cnt) return rc;
   cudaError_t e = cudaMemsetAsync(cnt, 0, NBINS * sizeof(unsigned), s);
   if (e != cudaSuccess) return cuda_fail(h, e, "memset bins");
   const float inv_w = (float)NBINS / std::max(1e-6f, m->hi - m->lo);

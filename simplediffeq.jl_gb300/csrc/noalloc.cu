@@ -88,6 +88,8 @@ extern "C" int ode_ensemble_solve_noalloc(const ode_solve_args* a, ode_solve_out
       a->precision != ODE_FP64)
     return say(err, errlen, ODE_ENOTSUP,
                "the allocation-free solve runs GPUSimpleATsit5, FP64, built-in Lorenz (dim 3, 3 parameters) only");
+  if (a->output != ODE_OUTPUT_STATE)
+    return say(err, errlen, ODE_ENOTSUP, "the allocation-free solve stores the state at saveat points only");
   if (a->schedule != ODE_SCHED_PERSISTENT)
     return say(err, errlen, ODE_ENOTSUP, "the allocation-free solve runs the persistent schedule only");
   if (a->memory != ODE_MEM_DEVICE)

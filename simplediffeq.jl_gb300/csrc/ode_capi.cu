@@ -15,6 +15,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -465,6 +466,10 @@ int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o,
   if (!(a->t0 == a->t0) || !(a->tf == a->tf) || !(a->dt == a->dt))
     return fail(h, ODE_EINVAL, "t0, tf and dt must not be NaN");
   if (a->nsave < 0 || (a->nsave > 0 && !a->saveat)) return fail(h, ODE_EINVAL, "saveat missing");
+  if (a->output != ODE_OUTPUT_STATE && a->output != ODE_OUTPUT_KURAMOTO_R)
+    return fail(h, ODE_EINVAL, "unknown output kind");
+  if (a->output == ODE_OUTPUT_KURAMOTO_R && (a->save_everystep || a->alg == ODE_ALG_RK4))
+    return fail(h, ODE_EINVAL, "the order-parameter output applies to saveat points");
   if (a->alg == ODE_ALG_RK4 && a->nsave > 0)
     return fail(h, ODE_EINVAL, "GPUSimpleRK4 has no saveat (it saves every step; use save_everystep)");
   int rc = check_rhs(h, a);
@@ -512,6 +517,7 @@ int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o,
   kp.nparams = NP;
   kp.maxiters = a->maxiters > 0 ? a->maxiters : kDefaultMaxIters;
   kp.norm_fp64 = a->abstol < 1e-30 ? 1 : 0;
+  kp.output = a->output;
 
   const bool host = a->memory == ODE_MEM_HOST;
   const size_t nd = (size_t)n * sizeof(double);
@@ -553,7 +559,7 @@ int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o,
   /* outputs */
   struct OutMap { void* host; const char* name; size_t bytes; void** dev; };
   OutMap outs[] = {
-      {o->us, "us", (size_t)npoints * D * nd, (void**)&kp.us},
+      {o->us, "us", (size_t)npoints * (a->output == ODE_OUTPUT_KURAMOTO_R ? 1 : D) * nd, (void**)&kp.us},
       {o->u_final, "u_final", nd * D, (void**)&kp.u_final},
       {o->t_final, "t_final", nd, (void**)&kp.t_final},
       {o->retcode, "retcode", (size_t)n, (void**)&kp.retcode},
@@ -590,32 +596,83 @@ int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o,
     gridx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(resident, (n + 127) / 128));
   }
 
-  CK(cudaMemsetAsync(stats, 0, 4 * sizeof(unsigned long long), s), "memset stats");
+  /* device buffers of the learned schedule, allocated before any capture */
+  float *latt = nullptr, *ldt = nullptr;
+  int* order = nullptr;
+  unsigned* bins = nullptr;
+  double* dseed = nullptr;
+  const bool seeding = sched == ODE_SCHED_LEARNED && !a->dt0 && model_seed_dt0(h->model);
   if (sched == ODE_SCHED_LEARNED) {
-    float* latt = (float*)buf(h, "pred_att", (size_t)n * 4, &rc);
-    if (!latt) return rc;
-    float* ldt = (float*)buf(h, "pred_dt", (size_t)n * 4, &rc);
-    if (!ldt) return rc;
-    int* order = (int*)buf(h, "order", (size_t)n * 4 + 16, &rc);
-    if (!order) return rc;
-    rc = model_predict_device(h, a, kp, latt, ldt, s, &launches);
-    if (rc != ODE_OK) return rc;
-    rc = order_by_cost(h, latt, n, order, s, &launches);
-    if (rc != ODE_OK) return rc;
+    if (!(latt = (float*)buf(h, "pred_att", (size_t)n * 4, &rc))) return rc;
+    if (!(ldt = (float*)buf(h, "pred_dt", (size_t)n * 4, &rc))) return rc;
+    if (!(order = (int*)buf(h, "order", (size_t)n * 4 + 16, &rc))) return rc;
+    if (!(bins = (unsigned*)buf(h, "bins", kCostBins * sizeof(unsigned), &rc))) return rc;
+    if (seeding && !(dseed = (double*)buf(h, "dt0_seed", nd, &rc))) return rc;
     kp.order = order;
-    if (!a->dt0 && model_seed_dt0(h->model)) {
-      double* dd = (double*)buf(h, "dt0_seed", nd, &rc);
-      if (!dd) return rc;
-      rc = seed_dt0(h, ldt, n, model_dt0_safety(h->model), dd, s, &launches);
-      if (rc != ODE_OK) return rc;
-      kp.dt0 = dd;
-    }
+    if (seeding) kp.dt0 = dseed;
   }
+
+  /* The device-side sequence of a solve (statistics reset, cost prediction,
+   * binning, dt0 seeding, the solver kernel) is captured once into a CUDA
+   * graph and replayed while the launch parameters stay the same. */
+  auto enqueue = [&](int* nl) -> int {
+    CK(cudaMemsetAsync(stats, 0, 4 * sizeof(unsigned long long), s), "memset stats");
+    if (sched == ODE_SCHED_LEARNED && n > 0) {
+      int r = model_predict_device(h, a, kp, latt, ldt, s, nl);
+      if (r == ODE_OK) r = order_by_cost(h, latt, n, order, bins, s, nl);
+      if (r == ODE_OK && seeding) r = seed_dt0(h, ldt, n, model_dt0_safety(h->model), dseed, s, nl);
+      if (r != ODE_OK) return r;
+    }
+    if (n > 0) {
+      const int r = launch(h, fn, gridx, &kp, s);
+      if (r != ODE_OK) return r;
+      ++*nl;
+    }
+    return ODE_OK;
+  };
+  std::string key((const char*)&kp, sizeof kp);
+  {
+    char extra[256];
+    snprintf(extra, sizeof extra, "|%p|%u|%d|%d|", (void*)fn, gridx, sched, (int)seeding);
+    key += extra;
+    if (sched == ODE_SCHED_LEARNED) key += model_key(h->model);
+  }
+  const bool use_graph = s != 0 && !std::getenv("GBODE_NO_GRAPH");
+  int replayed = 0;
   CK(cudaEventRecord(h->ev0, s), "event");
-  if (n > 0) {
-    rc = launch(h, fn, gridx, &kp, s);
+  if (use_graph && h->graph.exec && h->graph.key == key) {
+    CK(cudaGraphLaunch(h->graph.exec, s), "cudaGraphLaunch");
+    launches = h->graph.launches;
+    replayed = 1;
+  } else if (use_graph) {
+    if (h->graph.exec) cudaGraphExecDestroy(h->graph.exec);
+    if (h->graph.graph) cudaGraphDestroy(h->graph.graph);
+    h->graph = GraphEntry();
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    int nl = 0;
+    const int r = enqueue(&nl);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(s, &g);
+    if (r != ODE_OK) {
+      if (g) cudaGraphDestroy(g);
+      return r;
+    }
+    if (ce != cudaSuccess) return cuda_fail(h, ce, "cudaStreamEndCapture");
+    cudaGraphExec_t ex = nullptr;
+    cudaError_t ie = cudaGraphInstantiate(&ex, g, 0);
+    if (ie != cudaSuccess) {
+      cudaGraphDestroy(g);
+      return cuda_fail(h, ie, "cudaGraphInstantiate");
+    }
+    h->graph.graph = g;
+    h->graph.exec = ex;
+    h->graph.key = key;
+    h->graph.launches = nl;
+    CK(cudaGraphLaunch(ex, s), "cudaGraphLaunch");
+    launches = nl;
+  } else {
+    rc = enqueue(&launches);
     if (rc != ODE_OK) return rc;
-    ++launches;
   }
   CK(cudaEventRecord(h->ev1, s), "event");
 
@@ -635,7 +692,7 @@ int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o,
     st->saves = (int64_t)hs[1];
     st->launches = launches;
     st->schedule_used = sched;
-    st->graph_replayed = 0;
+    st->graph_replayed = replayed;
     st->jit = jit;
     st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
   }

@@ -30,7 +30,10 @@ struct GraphEntry {
   std::string key;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  int launches = 0;
 };
+
+constexpr int kCostBins = 1024;  /* bins of the learned schedule's counting sort */
 
 }  // namespace gbode
 
@@ -66,8 +69,12 @@ void model_free(Model* m);
  * dt0_out is non-null, the seeded initial dt.  Enqueued on `s`. */
 int model_predict_device(ode_handle* h, const ode_solve_args* a, const KParams& kp, float* log_att,
                          float* log_dt, cudaStream_t s, int* launches);
-/* Order trajectories by predicted cost, longest first: order[n] on the device. */
-int order_by_cost(ode_handle* h, const float* log_att, int64_t n, int* order, cudaStream_t s, int* launches);
+/* Order trajectories by predicted cost, longest first: order[n] on the device;
+ * bins: kCostBins counters of device scratch. */
+int order_by_cost(ode_handle* h, const float* log_att, int64_t n, int* order, unsigned* bins, cudaStream_t s,
+                  int* launches);
+/* Everything about the model that a captured launch sequence depends on. */
+std::string model_key(const Model* m);
 /* dt0[i] = safety * exp(log_dt[i]) */
 int seed_dt0(ode_handle* h, const float* log_dt, int64_t n, float safety, double* dt0, cudaStream_t s,
              int* launches);

@@ -21,6 +21,7 @@ struct KParams {
   int dim, nparams;
   long long maxiters;      /* <= 0: no cap */
   int norm_fp64;           /* 1: error norm in double (abstol below 1e-30) */
+  int output;              /* 0: store the state at saveat points; 1: store the Kuramoto order parameter */
   double* us;              /* [npoints][dim][n] or 0 */
   double* u_final;         /* [dim][n] or 0 */
   double* t_final;         /* [n] or 0 */

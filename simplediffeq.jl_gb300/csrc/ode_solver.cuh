@@ -667,9 +667,24 @@ struct Lane {
   bool nan_seen;
 };
 
+/* Write saveat point j of trajectory idx: the state, or (P.output == 1) the
+ * Kuramoto order parameter r = |(1/D) sum_k exp(i v_k)| = sqrt(C^2 + S^2) / D
+ * of it, so a phase ensemble keeps one number per save point. */
 template <class PR, int D>
 __device__ __forceinline__ void store_point(const KParams& P, long long idx, long long j, const double (&v)[D]) {
   if (!P.us) return;
+  if (P.output == 1) {
+    double C = 0.0, S = 0.0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      double sn, cs;
+      sincos(v[d], &sn, &cs);
+      C = C + cs;
+      S = S + sn;
+    }
+    P.us[j * P.n + idx] = __dsqrt_rn(__fma_rn(C, C, S * S)) / (double)D;
+    return;
+  }
 #pragma unroll
   for (int d = 0; d < D; ++d) P.us[(j * D + d) * P.n + idx] = v[d];
 }
@@ -750,9 +765,9 @@ __device__ __forceinline__ void lane_finish(const KParams& P, Lane<PR, D, F, NK>
   if (P.dt_first) P.dt_first[idx] = l.dt_first;
   if (P.us) {
     const double qnan = __longlong_as_double(0x7ff8000000000000LL);
+    const int width = P.output == 1 ? 1 : D;
     for (long long j = l.cur; j < P.nsave; ++j)
-#pragma unroll
-      for (int d = 0; d < D; ++d) P.us[(j * D + d) * P.n + idx] = qnan;
+      for (int d = 0; d < width; ++d) P.us[(j * width + d) * P.n + idx] = qnan;
   }
   tot.att += (unsigned long long)l.att;
   tot.sav += (unsigned long long)l.ninterp;

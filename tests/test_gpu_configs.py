@@ -80,3 +80,37 @@ def test_learned_default_is_ordering_only(pkg):
     b = pkg.solve(ens(u0, p), pkg.GPUSimpleATsit5(), trajectories=8192, schedule="plain", saveat=sv, **kw)
     assert a.stats.schedule_used == 2
     assert np.array_equal(a.u_final, b.u_final) and np.array_equal(a.us, b.us, equal_nan=True)
+
+
+@pytest.mark.parametrize("schedule", ["plain", "persistent"])
+def test_kuramoto_order_parameter_output(pkg, po, schedule):
+    """4,194,304-trajectory workload shape, small n: final state plus the order
+    parameter r(t) at 50 saveat times, reduced inside the kernel."""
+    u0, p = make_golden.kuramoto(1024, 19)
+    sv = np.linspace(0, 50, 50)
+    kw = dict(abstol=1e-8, reltol=1e-6)
+    sol = gpu(pkg, pkg.GPUSimpleATsit5(), "kuramoto", u0, p, (0.0, 50.0), 0.1, saveat=sv, schedule=schedule,
+              output="kuramoto_r", **kw)
+    full = gpu(pkg, pkg.GPUSimpleATsit5(), "kuramoto", u0, p, (0.0, 50.0), 0.1, saveat=sv, schedule=schedule, **kw)
+    ref = po.solve("ATsit5", "kuramoto", u0, p, (0, 50), 0.1, rounding="device", saveat=sv, nthreads=8,
+                   output="kuramoto_r", **kw)
+    assert sol.us.shape == (50, 1, 1024)
+    # the kernel's reduction equals the order parameter of its own full-state output
+    r_full = np.abs(np.exp(1j * full.us).mean(1))
+    assert np.abs(sol.us[:, 0, :] - r_full).max() < 1e-12
+    assert np.array_equal(sol.u_final, full.u_final)
+    # and agrees with the oracle's
+    assert np.mean(np.abs(sol.us - ref["us"]).max(axis=(0, 1)) < 1e-6) >= 0.999
+
+
+def test_repeated_solve_replays_the_captured_graph(pkg):
+    from conftest import lorenz_inputs
+    u0, p = lorenz_inputs(4096, seed=31)
+    sv = np.linspace(0, 10, 20)
+    e = pkg.EnsembleProblem(pkg.ODEProblem("lorenz", u0[:, 0], (0.0, 10.0), p[:, 0]), u0s=u0, ps=p)
+    kw = dict(dt=0.1, abstol=1e-8, reltol=1e-6, saveat=sv, schedule="persistent")
+    a = pkg.solve(e, pkg.GPUSimpleATsit5(), trajectories=4096, **kw)
+    b = pkg.solve(e, pkg.GPUSimpleATsit5(), trajectories=4096, **kw)
+    assert b.stats.graph_replayed == 1
+    assert np.array_equal(a.u_final, b.u_final) and np.array_equal(a.us, b.us)
+    assert a.stats.attempts == b.stats.attempts
