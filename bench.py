@@ -166,6 +166,7 @@ def main():
     ap.add_argument("--schedule", default=os.environ.get("GBODE_BENCH_SCHEDULE", "learned"))
     ap.add_argument("--n", type=int, default=N_TRAJ)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -225,6 +226,18 @@ def main():
         except L.GB300ODEError as e:
             fit_report = {"unavailable": str(e)}
             schedule = "persistent"
+
+    # pick the launch shape of the solver kernel on a 65,536-trajectory sample (excluded from timing)
+    tune = None
+    if not args.no_tune:
+        try:
+            rep = h.autotune(args_for(schedule if schedule != "learned" else "persistent", L.MEM_DEVICE,
+                                      du0.data_ptr(), dp.data_ptr()), 65536)
+            tune = {"block": rep.block, "max_registers": rep.max_registers, "stage_bytes": rep.stage_bytes,
+                    "variants": rep.variants, "sample_ms_default": rep.default_ms, "sample_ms_best": rep.best_ms,
+                    "tune_ms": rep.tune_ms}
+        except L.GB300ODEError as e:
+            tune = {"unavailable": str(e)}
 
     def device_step(sched):
         a = args_for(sched, L.MEM_DEVICE, du0.data_ptr(), dp.data_ptr())
@@ -324,6 +337,8 @@ def main():
     }
     if fit_report is not None:
         line["learned_fit"] = fit_report
+    if tune is not None:
+        line["autotune"] = tune
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     print(json.dumps(line))

@@ -184,6 +184,27 @@ int ode_fixed_grid(double t0, double dt, double tf, int precision, double* out, 
  * Compiler diagnostics go to `log` (may be NULL). */
 int ode_rhs_compile(ode_handle* h, const char* body, int dim, int nparams, int* rhs_id, char* log, size_t loglen);
 
+/* ---- autotuner ----------------------------------------------------------
+ * Times launch-shape variants of the solver kernel (threads per block,
+ * register cap, bytes of the per-warp saveat staging ring) on the first
+ * `sample` trajectories of `a` (<= 0: 65,536) and keeps the fastest for later
+ * solves of the same algorithm / rhs / precision / dim / schedule kind on this
+ * handle.  Variants differ only in launch shape: results are unchanged.  The
+ * persistent kernel hands trajectories to lanes dynamically, so there is no
+ * fixed trajectories-per-thread parameter to tune. */
+typedef struct {
+  int32_t variants;       /* variants timed */
+  int32_t block;          /* chosen threads per block */
+  int32_t max_registers;  /* chosen register cap (0: the compiler's choice) */
+  int32_t stage_bytes;    /* chosen staging-ring bytes per warp */
+  double default_ms;      /* kernel time of the default kernel on the sample */
+  double best_ms;         /* kernel time of the chosen kernel on the sample */
+  int64_t sample;         /* trajectories timed */
+  double tune_ms;         /* wall time of the tuning */
+} ode_tune_report;
+
+int ode_autotune(ode_handle* h, const ode_solve_args* a, int64_t sample, ode_tune_report* rep);
+
 /* ---- learned schedule ---------------------------------------------------
  * A 2-hidden-layer ReLU MLP (bf16 weights, fp32 accumulation) maps each
  * trajectory's (p, u0) to (log attempts, log dt of the first accepted step).

@@ -25,7 +25,7 @@ RET_DEFAULT, RET_DTMIN, RET_MAXITERS, RET_NAN = 0, 1, 2, 3
 # Every symbol include/gb300ode.h declares.
 EXPORTS = ["ode_abi_version", "ode_create", "ode_destroy", "ode_last_error", "ode_ensemble_solve",
            "ode_fixed_grid", "ode_rhs_compile", "ode_learn_default_opts", "ode_learn_fit", "ode_learn_predict",
-           "ode_learn_gradcheck", "ode_ensemble_solve_noalloc"]
+           "ode_learn_gradcheck", "ode_ensemble_solve_noalloc", "ode_autotune"]
 
 
 class SolveArgs(ctypes.Structure):
@@ -60,6 +60,12 @@ class LearnOpts(ctypes.Structure):
 class LearnReport(ctypes.Structure):
     _fields_ = [("loss_first", ctypes.c_float), ("loss_last", ctypes.c_float), ("r2_attempts", ctypes.c_float),
                 ("train_solve_ms", ctypes.c_double), ("train_fit_ms", ctypes.c_double)]
+
+
+class TuneReport(ctypes.Structure):
+    _fields_ = [("variants", ctypes.c_int32), ("block", ctypes.c_int32), ("max_registers", ctypes.c_int32),
+                ("stage_bytes", ctypes.c_int32), ("default_ms", ctypes.c_double), ("best_ms", ctypes.c_double),
+                ("sample", ctypes.c_int64), ("tune_ms", ctypes.c_double)]
 
 
 class GB300ODEError(RuntimeError):
@@ -98,6 +104,7 @@ def load():
     lib.ode_learn_predict.argtypes = [ctypes.c_void_p, ctypes.POINTER(SolveArgs), ctypes.c_void_p, ctypes.c_void_p]
     lib.ode_learn_gradcheck.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.ode_autotune.argtypes = [ctypes.c_void_p, ctypes.POINTER(SolveArgs), ctypes.c_int64, ctypes.POINTER(TuneReport)]
     lib.ode_ensemble_solve_noalloc.argtypes = [ctypes.POINTER(SolveArgs), ctypes.POINTER(SolveOut), ctypes.c_char_p,
                                                ctypes.c_size_t]
     _lib = lib
@@ -166,6 +173,11 @@ class Handle:
             setattr(o, k, v)
         rep = LearnReport()
         self.check(self.lib.ode_learn_fit(self.h, ctypes.byref(args), ctypes.byref(o), ctypes.byref(rep)))
+        return rep
+
+    def autotune(self, args, sample=0):
+        rep = TuneReport()
+        self.check(self.lib.ode_autotune(self.h, ctypes.byref(args), int(sample), ctypes.byref(rep)))
         return rep
 
     def learn_gradcheck(self, nin, nh, params, x, y):

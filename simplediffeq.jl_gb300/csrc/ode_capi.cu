@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <thread>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -257,7 +258,9 @@ std::string kernel_key(ode_handle* h, const ode_solve_args* a, int sched) {
   return b;
 }
 
-int compile_jit(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn, std::string* log_out) {
+/* Source of the one-kernel translation unit for (algorithm, rhs, precision,
+ * dim, schedule kind). */
+std::string jit_source(ode_handle* h, const ode_solve_args* a, int sched) {
   std::string src = "#include \"ode_solver.cuh\"\n";
   if (a->rhs >= ODE_RHS_USER) {
     const UserRhs& u = h->users[a->rhs - ODE_RHS_USER];
@@ -275,44 +278,77 @@ int compile_jit(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* f
            "    user_rhs<R>(du, u, p, (R)t);\n  }\n};\n";
   }
   src += "typedef " + rhs_type_expr(h, a) + " RHS_T;\n";
-  src += std::string("GBODE_ENTRY(gbode_jit, ") + entry_kind(a->alg, sched, a->nsave) + ", " + method_type(a->alg) + ", " +
-         prec_type(a->precision) + ", RHS_T)\n";
+  src += std::string("GBODE_ENTRY(gbode_jit, ") + entry_kind(a->alg, sched, a->nsave) + ", " + method_type(a->alg) +
+         ", " + prec_type(a->precision) + ", RHS_T)\n";
+  return src;
+}
 
-  if (!load_nvrtc()) return fail(h, ODE_ENVRTC, "libnvrtc.so.13 could not be loaded");
+/* NVRTC: source -> CUBIN for sm_103a.  Thread-safe (no handle state);
+ * extra_opts carries the launch-shape variants of the autotuner. */
+int nvrtc_cubin(const std::string& src, const std::vector<std::string>& extra_opts, std::vector<char>* cubin,
+                std::string* log, std::string* err) {
+  if (!load_nvrtc()) {
+    *err = "libnvrtc.so.13 could not be loaded";
+    return ODE_ENVRTC;
+  }
   nvrtcProgram prog;
   const char* hdrs[] = {kSrc_ode_solver_cuh, kSrc_ode_kparams_h, kSrc_tableaus_h};
   const char* names[] = {"ode_solver.cuh", "ode_kparams.h", "tableaus.h"};
   nvrtcResult r = g_nvrtc.create(&prog, src.c_str(), "gbode_jit.cu", 3, hdrs, names);
-  if (r != NVRTC_SUCCESS) return fail(h, ODE_ENVRTC, std::string("nvrtcCreateProgram: ") + g_nvrtc.errstr(r));
-  const char* opts[] = {"--gpu-architecture=sm_103a", "--fmad=false", "-std=c++17", "-lineinfo",
-                        "-default-device"};
-  r = g_nvrtc.compile(prog, 5, opts);
+  if (r != NVRTC_SUCCESS) {
+    *err = std::string("nvrtcCreateProgram: ") + g_nvrtc.errstr(r);
+    return ODE_ENVRTC;
+  }
+  std::vector<const char*> opts = {"--gpu-architecture=sm_103a", "--fmad=false", "-std=c++17", "-lineinfo",
+                                   "-default-device"};
+  for (const std::string& o : extra_opts) opts.push_back(o.c_str());
+  r = g_nvrtc.compile(prog, (int)opts.size(), opts.data());
   size_t loglen = 0;
   g_nvrtc.logsize(prog, &loglen);
-  std::string log(loglen, '\0');
-  if (loglen) g_nvrtc.log(prog, &log[0]);
-  if (log_out) *log_out = log;
+  std::string lg(loglen, '\0');
+  if (loglen) g_nvrtc.log(prog, &lg[0]);
+  if (log) *log = lg;
   if (r != NVRTC_SUCCESS) {
     g_nvrtc.destroy(&prog);
-    return fail(h, ODE_ENVRTC, "run-time compilation failed:\n" + log);
+    *err = "run-time compilation failed:\n" + lg;
+    return ODE_ENVRTC;
   }
   size_t n = 0;
   g_nvrtc.cubinsize(prog, &n);
-  std::vector<char> cubin(n);
-  g_nvrtc.cubin(prog, cubin.data());
+  cubin->resize(n);
+  g_nvrtc.cubin(prog, cubin->data());
   g_nvrtc.destroy(&prog);
+  return ODE_OK;
+}
+
+int load_cubin(ode_handle* h, const std::vector<char>& cubin, int block, CUfunction* fn) {
   CUmodule mod;
   CUresult cr = g_drv.cuModuleLoadData(&mod, cubin.data());
   if (cr != CUDA_SUCCESS) return cu_fail(h, cr, "cuModuleLoadData");
   h->modules.push_back(mod);
   cr = g_drv.cuModuleGetFunction(fn, mod, "gbode_jit");
   if (cr != CUDA_SUCCESS) return cu_fail(h, cr, "cuModuleGetFunction");
+  h->fblock[*fn] = block;
   return ODE_OK;
+}
+
+int compile_jit(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn, std::string* log_out) {
+  std::vector<char> cubin;
+  std::string err;
+  const int rc = nvrtc_cubin(jit_source(h, a, sched), {}, &cubin, log_out, &err);
+  if (rc != ODE_OK) return fail(h, rc, err);
+  return load_cubin(h, cubin, 128, fn);
 }
 
 /* Find (or build) the kernel for this solve. */
 int get_kernel(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn, int* jit) {
   const std::string key = kernel_key(h, a, sched);
+  auto tt = h->tuned.find(key);
+  if (tt != h->tuned.end()) {
+    *fn = tt->second;
+    *jit = 1;
+    return ODE_OK;
+  }
   auto it = h->kcache.find(key);
   if (it != h->kcache.end()) {
     *fn = it->second;
@@ -341,9 +377,14 @@ int get_kernel(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn
   return ODE_OK;
 }
 
+int block_of(ode_handle* h, CUfunction fn) {
+  auto it = h->fblock.find(fn);
+  return it == h->fblock.end() ? 128 : it->second;
+}
+
 int launch(ode_handle* h, CUfunction fn, unsigned grid, KParams* kp, cudaStream_t s) {
   void* params[] = {kp};
-  CUresult r = g_drv.cuLaunchKernel(fn, grid, 1, 1, 128, 1, 1, 0, (CUstream)s, params, nullptr);
+  CUresult r = g_drv.cuLaunchKernel(fn, grid, 1, 1, (unsigned)block_of(h, fn), 1, 1, 0, (CUstream)s, params, nullptr);
   if (r != CUDA_SUCCESS) return cu_fail(h, r, "cuLaunchKernel");
   return ODE_OK;
 }
@@ -585,15 +626,16 @@ int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o,
   /* schedule */
   int launches = 0;
   unsigned gridx;
+  const int block = block_of(h, fn);
   if (sched == ODE_SCHED_PLAIN) {
-    gridx = (unsigned)((n + 127) / 128);
+    gridx = (unsigned)((n + block - 1) / block);
   } else {
     int nb = 0;
-    CUresult cr = g_drv.cuOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, 0);
+    CUresult cr = g_drv.cuOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, block, 0);
     if (cr != CUDA_SUCCESS) return cu_fail(h, cr, "occupancy");
     if (nb < 1) nb = 1;
     const int64_t resident = (int64_t)nb * h->nsm;
-    gridx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(resident, (n + 127) / 128));
+    gridx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(resident, (n + block - 1) / block));
   }
 
   /* device buffers of the learned schedule, allocated before any capture */
@@ -700,6 +742,129 @@ int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o,
     char m[128];
     snprintf(m, sizeof m, "%llu trajectories stopped early (dt<dtmin or maxiters); see retcode", hs[2]);
     return fail(h, ODE_ETRAJ, m);
+  }
+  return ODE_OK;
+}
+
+/* Autotuner: time launch-shape variants of the solver kernel on a sample of
+ * the caller's ensemble and keep the fastest for this handle.  Variants are
+ * compiled with NVRTC in parallel; they differ in threads per block, register
+ * cap (which sets how many warps an SM holds) and the bytes of each warp's
+ * saveat staging ring, never in arithmetic, so results do not change. */
+int ode_autotune(ode_handle* h, const ode_solve_args* a, int64_t sample, ode_tune_report* rep) {
+  if (!h) return ODE_EINVAL;
+  if (!a) return fail(h, ODE_EINVAL, "null arguments");
+  if (is_fixed(a->alg)) return fail(h, ODE_EINVAL, "autotuning applies to the adaptive algorithms");
+  if (a->n < 1 || (a->memory != ODE_MEM_HOST && a->memory != ODE_MEM_DEVICE))
+    return fail(h, ODE_EINVAL, "bad ensemble");
+  int rc = check_rhs(h, a);
+  if (rc != ODE_OK) return rc;
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  const auto t0 = std::chrono::steady_clock::now();
+  const int64_t n = a->n;
+  const int64_t m = std::min<int64_t>(n, sample > 0 ? std::max<int64_t>(sample, 1024) : 65536);
+  const int D = a->dim, NP = a->nparams;
+  cudaStream_t s = h->stream;
+  const cudaMemcpyKind kind = a->memory == ODE_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  /* the first m trajectories, gathered from the [rows][n] arrays by strided copies */
+  double* du0 = (double*)buf(h, "tune_u0", (size_t)m * D * 8, &rc);
+  if (!du0) return rc;
+  double* dp = (double*)buf(h, "tune_p", (size_t)m * (NP > 0 ? NP : 1) * 8, &rc);
+  if (!dp) return rc;
+  CK(cudaMemcpy2DAsync(du0, m * 8, a->u0, n * 8, m * 8, D, kind, s), "copy sample u0");
+  if (NP > 0) CK(cudaMemcpy2DAsync(dp, m * 8, a->p, n * 8, m * 8, NP, kind, s), "copy sample p");
+  double* ddt0 = nullptr;
+  if (a->dt0) {
+    if (!(ddt0 = (double*)buf(h, "tune_dt0", (size_t)m * 8, &rc))) return rc;
+    CK(cudaMemcpyAsync(ddt0, a->dt0, m * 8, kind, s), "copy sample dt0");
+  }
+  const int width = a->output == ODE_OUTPUT_KURAMOTO_R ? 1 : D;
+  double* dus = nullptr;
+  if (a->nsave > 0 && !(dus = (double*)buf(h, "tune_us", (size_t)a->nsave * width * m * 8, &rc))) return rc;
+  double* duf = (double*)buf(h, "tune_uf", (size_t)m * D * 8, &rc);
+  if (!duf) return rc;
+  CK(cudaStreamSynchronize(s), "sample copies");
+  ode_solve_args ta = *a;
+  ta.n = m;
+  ta.memory = ODE_MEM_DEVICE;
+  ta.u0 = du0;
+  ta.p = dp;
+  ta.dt0 = ddt0;
+  ta.stream = nullptr;
+  ta.schedule = a->schedule == ODE_SCHED_PLAIN ? ODE_SCHED_PLAIN : ODE_SCHED_PERSISTENT;
+  ode_solve_out to;
+  std::memset(&to, 0, sizeof to);
+  to.us = dus;
+  to.u_final = duf;
+  const std::string key = kernel_key(h, &ta, ta.schedule);
+  h->tuned.erase(key);
+  auto time_solve = [&](double* ms) -> int {
+    double best = 1e300;
+    for (int r = 0; r < 2; ++r) {
+      ode_solve_stats st;
+      const int rr = ode_ensemble_solve(h, &ta, &to, &st);
+      if (rr != ODE_OK && rr != ODE_ETRAJ) return rr;
+      best = std::min(best, st.kernel_ms);
+    }
+    *ms = best;
+    return ODE_OK;
+  };
+  double base_ms = 0;
+  rc = time_solve(&base_ms);
+  if (rc != ODE_OK) return rc;
+
+  struct Variant {
+    int block, regs, stage;
+  };
+  const Variant vars[] = {{128, 0, 12288}, {128, 0, 8192},  {128, 112, 12288}, {128, 96, 12288},
+                          {128, 96, 8192}, {128, 80, 8192}, {64, 0, 12288},    {64, 96, 24576}};
+  const int nv = (int)(sizeof vars / sizeof vars[0]);
+  const std::string src = jit_source(h, &ta, ta.schedule);
+  std::vector<std::vector<char>> cubins(nv);
+  std::vector<int> ok(nv, 0);
+  {
+    std::vector<std::thread> th;
+    for (int v = 0; v < nv; ++v) {
+      th.emplace_back([&, v]() {
+        std::vector<std::string> o = {"-DGBODE_BLOCK=" + std::to_string(vars[v].block),
+                                      "-DGBODE_STAGE_BYTES=" + std::to_string(vars[v].stage)};
+        if (vars[v].regs) o.push_back("--maxrregcount=" + std::to_string(vars[v].regs));
+        std::string lg, err;
+        ok[v] = nvrtc_cubin(src, o, &cubins[v], &lg, &err) == ODE_OK;
+      });
+    }
+    for (auto& t : th) t.join();
+  }
+  double best_ms = base_ms;
+  int best = -1, tried = 0;
+  CUfunction best_fn = nullptr;
+  for (int v = 0; v < nv; ++v) {
+    if (!ok[v]) continue;
+    CUfunction fn;
+    rc = load_cubin(h, cubins[v], vars[v].block, &fn);
+    if (rc != ODE_OK) return rc;
+    h->tuned[key] = fn;
+    double ms = 0;
+    rc = time_solve(&ms);
+    h->tuned.erase(key);
+    if (rc != ODE_OK) return rc;
+    ++tried;
+    if (ms < 0.99 * best_ms) {
+      best_ms = ms;
+      best = v;
+      best_fn = fn;
+    }
+  }
+  if (best >= 0) h->tuned[key] = best_fn;
+  if (rep) {
+    rep->variants = tried;
+    rep->block = best >= 0 ? vars[best].block : 128;
+    rep->max_registers = best >= 0 ? vars[best].regs : 0;
+    rep->stage_bytes = best >= 0 ? vars[best].stage : 12288;
+    rep->default_ms = base_ms;
+    rep->best_ms = best_ms;
+    rep->sample = m;
+    rep->tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   }
   return ODE_OK;
 }

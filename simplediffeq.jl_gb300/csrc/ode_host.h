@@ -46,6 +46,8 @@ struct ode_handle {
   std::map<std::string, gbode::DevBuf> bufs;
   std::map<std::string, CUfunction> kcache;
   std::map<std::string, int> kjit;  /* 1 if the cached function was compiled at run time */
+  std::map<std::string, CUfunction> tuned;  /* autotuned variant per kernel key */
+  std::map<CUfunction, int> fblock;         /* threads per block of run-time compiled functions */
   std::vector<CUmodule> modules;
   std::vector<gbode::UserRhs> users;
   gbode::GraphEntry graph;

@@ -975,7 +975,17 @@ __device__ __forceinline__ void run_adaptive_persistent(const KParams& P) {
  * jobs are waiting the whole warp interpolates 32 points at once, one per
  * lane.  Each point is computed by the same M::dense call on the same values,
  * so the results are bit-identical to the other drivers. */
-constexpr int kStageBytesPerWarp = 12288;  /* 4 warps per block: 48 KB of static shared memory */
+/* Launch shape: threads per block and the bytes of each warp's staging ring.
+ * Both can be set at compile time (the autotuner compiles variants); the
+ * defaults give 4 warps x 12 KB = 48 KB of static shared memory per block. */
+#ifndef GBODE_BLOCK
+#define GBODE_BLOCK 128
+#endif
+#ifndef GBODE_STAGE_BYTES
+#define GBODE_STAGE_BYTES 12288
+#endif
+constexpr int kStageBytesPerWarp = GBODE_STAGE_BYTES;
+constexpr int kWarpsPerBlock = GBODE_BLOCK / 32;
 
 template <class M, class PR, int D, class F>
 struct StageLayout {
@@ -992,10 +1002,10 @@ __device__ __forceinline__ void run_adaptive_staged(const KParams& P) {
   typedef typename PR::T T;
   typedef StageLayout<M, PR, D, F> SL;
   enum { CAP = SL::CAP, NK = M::NK, KOFF = D * (PR::KAHAN ? 2 : 1), POFF = KOFF + NK * D };
-  __shared__ __align__(16) unsigned char qmem[4][kStageBytesPerWarp];
+  __shared__ __align__(16) unsigned char qmem[kWarpsPerBlock][kStageBytesPerWarp];
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  unsigned char* qb = qmem[(threadIdx.x >> 5) & 3];
+  unsigned char* qb = qmem[threadIdx.x >> 5];
   T* tv = (T*)qb;                                            /* told, tnew, dtold, theta: [4][CAP] */
   long long* iv = (long long*)(qb + 4 * CAP * sizeof(T));    /* trajectory: [CAP] */
   R* rv = (R*)(qb + 4 * CAP * sizeof(T) + 8 * CAP);          /* record values: [NREC][CAP] */
@@ -1235,23 +1245,23 @@ __device__ __forceinline__ void run_rk4(const KParams& P) {
 /* Entry-point generator: GBODE_ENTRY(name, kind, Method, Prec, Rhs) defines
  * extern "C" __global__ name(KParams).  kind: plain | persistent | staged | fixed | rk4. */
 #define GBODE_ENTRY_plain(NAME, M, PR, RHS)                                                  \
-  extern "C" __global__ void __launch_bounds__(128) NAME(gbode::KParams P) {                \
+  extern "C" __global__ void __launch_bounds__(GBODE_BLOCK) NAME(gbode::KParams P) {                \
     gbode::run_adaptive_plain<M<PR, RHS::D, RHS>, PR, RHS::D, RHS>(P);                      \
   }
 #define GBODE_ENTRY_persistent(NAME, M, PR, RHS)                                             \
-  extern "C" __global__ void __launch_bounds__(128) NAME(gbode::KParams P) {                \
+  extern "C" __global__ void __launch_bounds__(GBODE_BLOCK) NAME(gbode::KParams P) {                \
     gbode::run_adaptive_persistent<M<PR, RHS::D, RHS>, PR, RHS::D, RHS>(P);                 \
   }
 #define GBODE_ENTRY_staged(NAME, M, PR, RHS)                                                 \
-  extern "C" __global__ void __launch_bounds__(128) NAME(gbode::KParams P) {                \
+  extern "C" __global__ void __launch_bounds__(GBODE_BLOCK) NAME(gbode::KParams P) {                \
     gbode::run_adaptive_staged_or_persistent<M<PR, RHS::D, RHS>, PR, RHS::D, RHS>(P);       \
   }
 #define GBODE_ENTRY_fixed(NAME, M, PR, RHS)                                                  \
-  extern "C" __global__ void __launch_bounds__(128) NAME(gbode::KParams P) {                \
+  extern "C" __global__ void __launch_bounds__(GBODE_BLOCK) NAME(gbode::KParams P) {                \
     gbode::run_fixed<M<PR, RHS::D, RHS>, PR, RHS::D, RHS>(P);                               \
   }
 #define GBODE_ENTRY_rk4(NAME, M, PR, RHS)                                                    \
-  extern "C" __global__ void __launch_bounds__(128) NAME(gbode::KParams P) {                \
+  extern "C" __global__ void __launch_bounds__(GBODE_BLOCK) NAME(gbode::KParams P) {                \
     gbode::run_rk4<PR, RHS::D, RHS>(P);                                                      \
   }
 #define GBODE_ENTRY(NAME, KIND, M, PR, RHS) GBODE_ENTRY_##KIND(NAME, M, PR, RHS)

@@ -114,3 +114,24 @@ def test_repeated_solve_replays_the_captured_graph(pkg):
     assert b.stats.graph_replayed == 1
     assert np.array_equal(a.u_final, b.u_final) and np.array_equal(a.us, b.us)
     assert a.stats.attempts == b.stats.attempts
+
+
+def test_autotuner_keeps_results(pkg):
+    """The tuned kernel differs only in launch shape: results are unchanged."""
+    from conftest import lorenz_inputs
+    n = 32768
+    u0, p = lorenz_inputs(n, seed=41)
+    sv = np.linspace(0, 10, 100)
+    e = pkg.EnsembleProblem(pkg.ODEProblem("lorenz", u0[:, 0], (0.0, 10.0), p[:, 0]), u0s=u0, ps=p)
+    kw = dict(dt=0.1, abstol=1e-8, reltol=1e-6, saveat=sv, schedule="persistent")
+    before = pkg.solve(e, pkg.GPUSimpleATsit5(), trajectories=n, **kw)
+    h = pkg._handle(0)
+    args = pkg.make_args(pkg.GPUSimpleATsit5(), 0, u0, p, (0.0, 10.0), 0.1, 1e-8, 1e-6, sv, False, "fp64",
+                         "persistent", 0)
+    rep = h.autotune(args, sample=16384)
+    assert rep.variants >= 4 and rep.sample == 16384
+    assert rep.best_ms <= rep.default_ms
+    print("autotune: block %d, regs %d, stage %d B: %.2f ms vs default %.2f ms (%d variants, %.0f ms)"
+          % (rep.block, rep.max_registers, rep.stage_bytes, rep.best_ms, rep.default_ms, rep.variants, rep.tune_ms))
+    after = pkg.solve(e, pkg.GPUSimpleATsit5(), trajectories=n, **kw)
+    assert np.array_equal(before.u_final, after.u_final) and np.array_equal(before.us, after.us)
