@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <mutex>
 #include <thread>
 #include <cmath>
 #include <cstdio>
@@ -45,7 +46,7 @@ struct DriverApi {
   CUresult (*cuFuncGetAttribute)(int*, CUfunction_attribute, CUfunction) = nullptr;
 };
 struct NvrtcApi {
-  bool tried = false, ok = false;
+  bool ok = false;
   nvrtcResult (*create)(nvrtcProgram*, const char*, const char*, int, const char* const*, const char* const*);
   nvrtcResult (*compile)(nvrtcProgram, int, const char* const*);
   nvrtcResult (*logsize)(nvrtcProgram, size_t*);
@@ -82,14 +83,14 @@ static bool load_driver_api() {
   return ok;
 }
 
-static bool load_nvrtc() {
-  if (g_nvrtc.tried) return g_nvrtc.ok;
-  g_nvrtc.tried = true;
+static std::once_flag g_nvrtc_once;
+
+static void load_nvrtc_once() {
   const char* names[] = {"libnvrtc.so.13", "libnvrtc.so", "/usr/local/cuda/lib64/libnvrtc.so.13"};
   void* h = nullptr;
   for (const char* n : names)
     if ((h = dlopen(n, RTLD_NOW | RTLD_LOCAL))) break;
-  if (!h) return false;
+  if (!h) return;
 #define NV(field, sym) g_nvrtc.field = (decltype(g_nvrtc.field))dlsym(h, sym)
   NV(create, "nvrtcCreateProgram");
   NV(compile, "nvrtcCompileProgram");
@@ -102,6 +103,11 @@ static bool load_nvrtc() {
 #undef NV
   g_nvrtc.ok = g_nvrtc.create && g_nvrtc.compile && g_nvrtc.logsize && g_nvrtc.log && g_nvrtc.cubinsize &&
                g_nvrtc.cubin && g_nvrtc.destroy && g_nvrtc.errstr;
+}
+
+/* NVRTC is loaded on first use, once, safely from several threads. */
+static bool load_nvrtc() {
+  std::call_once(g_nvrtc_once, load_nvrtc_once);
   return g_nvrtc.ok;
 }
 
