@@ -20,6 +20,12 @@ roofline   FP64 pipe: algorithmic FLOPs per launch (263 per step attempt, 101 pe
 cpu_baseline  the oracle's SimpleATsit5 (CPU restatement, reference rounding)
            on all host cores over a bounded sample of the same workload.
 With --impl reference only the CPU restatement runs (rank 0).
+
+--config N measures another ensemble workload of the same solver family
+(1: fixed-step Tsit5; 3: AVern7 Van der Pol; 4: AVern9 restricted three-body
+in FP32 with Kahan-compensated state; 5: ATsit5 Kuramoto-12 with the order
+parameter reduced in the kernel).  The default is the 1M adaptive Lorenz
+workload above (config 2).
 """
 import argparse
 import json
@@ -53,6 +59,64 @@ def inputs(n, seed=2024):
     u0[2] += 20
     p = np.stack([np.full(n, 10.0), rng.uniform(0, 30, n), np.full(n, 8 / 3)])
     return np.ascontiguousarray(u0), np.ascontiguousarray(p)
+
+
+def inputs_fixed_lorenz(n, seed):
+    rng = np.random.default_rng(seed)
+    u0 = np.tile(np.array([[1.0], [0.0], [0.0]]), (1, n))
+    p = np.stack([np.full(n, 10.0), rng.uniform(0, 21, n), np.full(n, 8 / 3)])
+    return np.ascontiguousarray(u0), np.ascontiguousarray(p)
+
+
+def inputs_vdp(n, seed):
+    rng = np.random.default_rng(seed)
+    mu = np.exp(rng.uniform(np.log(0.1), np.log(10.0), n))[None, :]
+    return np.ascontiguousarray(rng.uniform(-2, 2, (2, n))), np.ascontiguousarray(mu)
+
+
+def inputs_r3bp(n, seed):
+    rng = np.random.default_rng(seed)
+    u0 = np.array([0.994, 0.0, 0.0, -2.00158510637908])[:, None] + rng.normal(0, 1e-4, (4, n))
+    return np.ascontiguousarray(u0), np.full((1, n), 0.012277471)
+
+
+def inputs_kuramoto(n, seed, D=12):
+    rng = np.random.default_rng(seed)
+    th = rng.uniform(0, 2 * np.pi, (D, n))
+    p = np.vstack([rng.normal(0, 1, (D, n)), rng.uniform(0, 4, (1, n))])
+    return np.ascontiguousarray(th), np.ascontiguousarray(p)
+
+
+T_ARENSTORF = 17.0652165601579625588917206249
+# Per-unit algorithmic work (FMA = 2 flops): per step attempt and per saveat point.
+CONFIGS = {
+    1: dict(workload="fixed-step GPUSimpleTsit5 FP64, 8192 Lorenz trajectories, u0=(1,0,0), rho~U[0,21], "
+                     "tspan (0,1), dt 0.01, final state only",
+            alg="Tsit5", rhs="lorenz", n=8192, tspan=(0.0, 1.0), dt=0.01, abstol=1e-6, reltol=1e-3, nsave=0,
+            precision="fp64", output="state", inputs=inputs_fixed_lorenz, flops_attempt=192, flops_save=0,
+            rhs_per_attempt=6, oracle_alg="SimpleTsit5", dtype="f64"),
+    2: dict(workload=WORKLOAD, alg="ATsit5", rhs="lorenz", n=N_TRAJ, tspan=TSPAN, dt=DT0, abstol=ABSTOL,
+            reltol=RELTOL, nsave=NSAVE, precision="fp64", output="state", inputs=inputs,
+            flops_attempt=FLOPS_PER_ATTEMPT, flops_save=FLOPS_PER_SAVE, rhs_per_attempt=6,
+            oracle_alg="SimpleATsit5", dtype="f64"),
+    3: dict(workload="adaptive GPUSimpleAVern7 FP64, 524,288 Van der Pol trajectories, mu~LogUniform[0.1,10], "
+                     "(x,v)(0)~U[-2,2]^2, tspan (0,20), abstol 1e-10, reltol 1e-8, saveat 200 uniform times",
+            alg="AVern7", rhs="vanderpol", n=524288, tspan=(0.0, 20.0), dt=0.1, abstol=1e-10, reltol=1e-8,
+            nsave=200, precision="fp64", output="state", inputs=inputs_vdp, flops_attempt=298, flops_save=494,
+            rhs_per_attempt=10, oracle_alg="AVern7", dtype="f64"),
+    4: dict(workload="adaptive GPUSimpleAVern9, FP32 stages with Kahan-compensated state and FP64 t, 262,144 "
+                     "planar restricted three-body trajectories (mu=0.012277471, Arenstorf u0 + N(0,1e-4)), "
+                     "one Arenstorf period, abstol = reltol = 1e-7, final state",
+            alg="AVern9", rhs="r3bp", n=262144, tspan=(0.0, T_ARENSTORF), dt=0.1, abstol=1e-7, reltol=1e-7,
+            nsave=0, precision="fp32_kahan", output="state", inputs=inputs_r3bp, flops_attempt=1290,
+            flops_save=0, rhs_per_attempt=16, oracle_alg="AVern9", dtype="f32 (Kahan state, f64 t)"),
+    5: dict(workload="adaptive GPUSimpleATsit5 FP64, 4,194,304 Kuramoto-12 trajectories, omega~N(0,1), "
+                     "K~U[0,4], theta(0)~U[0,2pi)^12, tspan (0,50), abstol 1e-8, reltol 1e-6, final state + "
+                     "order parameter at 50 saveat times (reduced in the kernel)",
+            alg="ATsit5", rhs="kuramoto", n=4194304, tspan=(0.0, 50.0), dt=0.1, abstol=1e-8, reltol=1e-6,
+            nsave=50, precision="fp64", output="kuramoto_r", inputs=inputs_kuramoto, flops_attempt=1310,
+            flops_save=266, rhs_per_attempt=6, oracle_alg="ATsit5", dtype="f64"),
+}
 
 
 class ClockSampler:
@@ -98,21 +162,25 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_baseline(n_sample=65536, threads=None):
-    """SimpleATsit5 restated in C++ (reference rounding) over a bounded sample."""
+def cpu_baseline(cfg, n_sample=65536, threads=None):
+    """The oracle's CPU restatement of the reference solver (reference rounding)
+    over a bounded sample of the same workload, on all host cores."""
     import __graft_entry__ as g
     po = g.oracle()
     threads = threads or os.cpu_count()
-    u0, p = inputs(N_TRAJ)
-    u0, p = np.ascontiguousarray(u0[:, :n_sample]), np.ascontiguousarray(p[:, :n_sample])
-    sv = np.linspace(*TSPAN, NSAVE)
+    n_sample = min(n_sample, cfg["n"])
+    u0, p = cfg["inputs"](n_sample, 2024)
+    sv = np.linspace(*cfg["tspan"], cfg["nsave"]) if cfg["nsave"] else None
+    prec = "fp32" if cfg["precision"] == "fp32_kahan" else cfg["precision"]
     t = time.perf_counter()
-    po.solve("SimpleATsit5", "lorenz", u0, p, TSPAN, DT0, rounding="ref", abstol=ABSTOL, reltol=RELTOL, saveat=sv,
-             nthreads=threads)
+    po.solve(cfg["oracle_alg"], cfg["rhs"], u0, p, cfg["tspan"], cfg["dt"], rounding="ref", abstol=cfg["abstol"],
+             reltol=cfg["reltol"], saveat=sv, nthreads=threads, precision=prec, output=cfg["output"])
     dt = time.perf_counter() - t
     return {"value": n_sample / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "first %d trajectories of the 1,048,576-trajectory workload, SimpleATsit5 C++ restatement "
-                      "(reference rounding, libm pow), one std::thread per core, static chunks" % n_sample,
+            "sample": "the first %d trajectories of the workload, %s restated in C++ (reference rounding, libm "
+                      "pow%s), one std::thread per core, static chunks"
+                      % (n_sample, cfg["oracle_alg"], ", FP32 as the reference with Float32 state"
+                         if prec == "fp32" else ""),
             "seconds": dt}
 
 
@@ -126,8 +194,10 @@ def run_reference(args, rank):
     u0, p = inputs(N_TRAJ)
     u0, p = np.ascontiguousarray(u0[:, :n_sample]), np.ascontiguousarray(p[:, :n_sample])
     sv = np.linspace(*TSPAN, NSAVE)
-    run = lambda: po.solve("SimpleATsit5", "lorenz", u0, p, TSPAN, DT0, rounding="ref", abstol=ABSTOL,
-                           reltol=RELTOL, saveat=sv, nthreads=threads)
+
+    def run():
+        po.solve("SimpleATsit5", "lorenz", u0, p, TSPAN, DT0, rounding="ref", abstol=ABSTOL, reltol=RELTOL,
+                 saveat=sv, nthreads=threads)
     for _ in range(args.warmup):
         run()
     t = time.perf_counter()
@@ -163,8 +233,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", type=int, default=2, choices=sorted(CONFIGS))
     ap.add_argument("--schedule", default=os.environ.get("GBODE_BENCH_SCHEDULE", "learned"))
-    ap.add_argument("--n", type=int, default=N_TRAJ)
+    ap.add_argument("--n", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     args = ap.parse_args()
@@ -174,6 +245,8 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference(args, rank)
+    cfg = CONFIGS[args.config]
+    fixed = cfg["alg"] in ("Tsit5", "Vern7", "Vern9", "RK4")
 
     import torch
     dist = None
@@ -185,24 +258,29 @@ def main():
     pkg = g.package()
     L = pkg._lib
     h = L.Handle(local)
+    alg = getattr(pkg, "GPUSimple" + cfg["alg"])()
 
-    n = args.n
-    u0, p = inputs(n, seed=2024 + rank)
-    sv = np.linspace(*TSPAN, NSAVE)
+    n = args.n or cfg["n"]
+    u0, p = cfg["inputs"](n, 2024 + rank)
+    dim, nparams = u0.shape[0], p.shape[0]
+    nsave = cfg["nsave"]
+    sv = np.linspace(*cfg["tspan"], nsave) if nsave else None
+    width = 1 if cfg["output"] == "kuramoto_r" else dim
     dev = torch.device("cuda", local)
     du0 = torch.from_numpy(u0).to(dev)
     dp = torch.from_numpy(p).to(dev)
-    outs = {"us": torch.empty((NSAVE, 3, n), dtype=torch.float64, device=dev),
-            "u_final": torch.empty((3, n), dtype=torch.float64, device=dev),
+    outs = {"u_final": torch.empty((dim, n), dtype=torch.float64, device=dev),
             "t_final": torch.empty(n, dtype=torch.float64, device=dev),
             "retcode": torch.empty(n, dtype=torch.int8, device=dev),
             "naccept": torch.empty(n, dtype=torch.int32, device=dev),
             "nreject": torch.empty(n, dtype=torch.int32, device=dev)}
+    if nsave:
+        outs["us"] = torch.empty((nsave, width, n), dtype=torch.float64, device=dev)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
 
-    def args_for(schedule, memory, u0p, pp):
-        a = pkg.make_args(pkg.GPUSimpleATsit5(), L.RHS["lorenz"], u0, p, TSPAN, DT0, ABSTOL, RELTOL, sv, False,
-                          "fp64", schedule, 0, memory=memory)
+    def args_for(schedule, memory, u0p, pp, uu=u0, ppp=p):
+        a = pkg.make_args(alg, L.RHS[cfg["rhs"]], uu, ppp, cfg["tspan"], cfg["dt"], cfg["abstol"], cfg["reltol"],
+                          sv, False, cfg["precision"], schedule, 0, memory=memory, output=cfg["output"])
         a.u0, a.p = u0p, pp
         return a
 
@@ -212,13 +290,13 @@ def main():
             setattr(o, k, v.data_ptr())
         return o
 
-    schedule = args.schedule
+    schedule = "plain" if fixed else args.schedule
     fit_report = None
     if schedule == "learned":
         # fit the cost model on a separate 65,536-trajectory training ensemble solved by the plain kernel
-        tu0, tp = inputs(65536, seed=777 + rank)
-        ta = pkg.make_args(pkg.GPUSimpleATsit5(), L.RHS["lorenz"], tu0, tp, TSPAN, DT0, ABSTOL, RELTOL, sv, False,
-                           "fp64", "plain", 0)
+        tu0, tp = cfg["inputs"](65536, 777 + rank)
+        ta = pkg.make_args(alg, L.RHS[cfg["rhs"]], tu0, tp, cfg["tspan"], cfg["dt"], cfg["abstol"], cfg["reltol"],
+                           None, False, cfg["precision"], "plain", 0)
         try:
             rep = h.learn_fit(ta)
             fit_report = {"loss_first": rep.loss_first, "loss_last": rep.loss_last, "r2_log_attempts": rep.r2_attempts,
@@ -229,7 +307,7 @@ def main():
 
     # pick the launch shape of the solver kernel on a 65,536-trajectory sample (excluded from timing)
     tune = None
-    if not args.no_tune:
+    if not args.no_tune and not fixed:
         try:
             rep = h.autotune(args_for(schedule if schedule != "learned" else "persistent", L.MEM_DEVICE,
                                       du0.data_ptr(), dp.data_ptr()), 65536)
@@ -242,7 +320,7 @@ def main():
     def device_step(sched):
         a = args_for(sched, L.MEM_DEVICE, du0.data_ptr(), dp.data_ptr())
         st = L.SolveStats()
-        h.check(h.solve_raw(a, out_dev(), st))
+        h.check(h.solve_raw(a, out_dev(), st), allow=(L.ETRAJ,))
         return st
 
     def timed(sched, steps, warmup):
@@ -275,11 +353,15 @@ def main():
     value = n * world / (step_ms * 1e-3)
 
     # plain one-thread-per-trajectory kernel on the same inputs, same timing rules
-    pk, patt, psav, _ = timed("plain", max(1, min(args.steps, 3)), 1)
-    plain_ms = sum(pk) / len(pk)
+    if schedule != "plain":
+        pk, _, _, _ = timed("plain", max(1, min(args.steps, 3)), 1)
+        plain_ms = sum(pk) / len(pk)
+    else:
+        plain_ms = step_ms
     uf_plain = outs["u_final"].cpu().numpy()
-    scale = ABSTOL + RELTOL * np.abs(uf_plain).max(0)
+    scale = cfg["abstol"] + cfg["reltol"] * np.abs(uf_plain).max(0)
     dev_err = np.abs(uf_measured - uf_plain).max(0) / scale
+    dev_err = dev_err[np.isfinite(dev_err)] if np.isfinite(dev_err).any() else np.zeros(1)
 
     # end to end through the C ABI with pinned host buffers
     hu0 = torch.from_numpy(u0).pin_memory()
@@ -289,36 +371,38 @@ def main():
     for k, v in hout.items():
         setattr(ho, k, v.data_ptr())
     ha = args_for(schedule, L.MEM_HOST, hu0.data_ptr(), hp.data_ptr())
-    for _ in range(1):
-        h.check(h.solve_raw(ha, ho, L.SolveStats()))
+    h.check(h.solve_raw(ha, ho, L.SolveStats()), allow=(L.ETRAJ,))
     torch.cuda.synchronize()
     e2e_t = []
     for _ in range(max(1, min(args.steps, 3))):
         t0 = time.perf_counter()
-        h.check(h.solve_raw(ha, ho, L.SolveStats()))
+        h.check(h.solve_raw(ha, ho, L.SolveStats()), allow=(L.ETRAJ,))
         e2e_t.append(time.perf_counter() - t0)
     e2e_s = sum(e2e_t) / len(e2e_t)
-    h2d = u0.nbytes + p.nbytes + sv.nbytes
+    h2d = u0.nbytes + p.nbytes + (sv.nbytes if sv is not None else 0)
     d2h = sum(v.numel() * v.element_size() for v in hout.values())
 
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return
-    # FP64 pipe peak, measured live
-    peak = L.probe_rates(local, 2000)["dfma"][0] * 2 / 1e12
-    flops = (att / args.steps) * FLOPS_PER_ATTEMPT + (sav / args.steps) * FLOPS_PER_SAVE
+    # pipe peak, measured live: FP64 FMA (or FP32 FMA for the single-precision mode)
+    rates = L.probe_rates(local, 2000)
+    fp32 = cfg["precision"] != "fp64"
+    peak = (rates["ffma"][0] if fp32 else rates["dfma"][0]) * 2 / 1e12
+    flops = (att / args.steps) * cfg["flops_attempt"] + (sav / args.steps) * cfg["flops_save"]
     achieved = flops / (step_ms * 1e-3) / 1e12
     traffic = load_traffic()
     tr = None
-    if traffic and "atsit5_lorenz" in traffic:
+    if args.config == 2 and traffic and "atsit5_lorenz" in traffic:
         tr = traffic["atsit5_lorenz"]["bytes_per_trajectory"] * n
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "metric": METRIC if args.config == 2 else "ensemble trajectories/s (workload %d)" % args.config,
+        "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; no public dataset involved)",
-        "config": {"workload": WORKLOAD, "trajectories_per_gpu": n, "schedule": schedule,
-                   "l2": "flushed between steps by a 512 MB device write; outputs (2.5 GB) exceed L2",
+        "vs_baseline": None, "dtype": cfg["dtype"], "data": "synthetic (seeded; no public dataset involved)",
+        "config": {"workload": cfg["workload"], "trajectories_per_gpu": n, "schedule": schedule,
+                   "l2": "flushed between steps by a 512 MB device write",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "plain": {"value": n * world / (plain_ms * 1e-3), "ms_per_step": plain_ms},
         "speedup_vs_plain": plain_ms / step_ms,
@@ -326,11 +410,11 @@ def main():
                           "frac_within_10x": float(np.mean(dev_err <= 10)),
                           "error_scale": "abstol + reltol*max|u_final|"},
         "attempts_per_step": att / args.steps, "saves_per_step": sav / args.steps,
-        "rhs_evals_per_s": (att / args.steps) * 6 / (step_ms * 1e-3),
-        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+        "rhs_evals_per_s": (att / args.steps) * cfg["rhs_per_attempt"] / (step_ms * 1e-3),
+        "roofline": {"bound": "fp32" if fp32 else "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": tr,
-                     "peak_source": "FP64 FMA lane rate measured by this run's probe (libgb300ode_probe.so); "
-                                    "MEASURED_PEAKS.json carries no FP64 figure"},
+                     "peak_source": "%s FMA lane rate measured by this run's probe (libgb300ode_probe.so); "
+                                    "MEASURED_PEAKS.json carries no FP64/FP32-pipe figure" % ("FP32" if fp32 else "FP64")},
         "e2e": {"value": n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clocks,
@@ -339,8 +423,18 @@ def main():
         line["learned_fit"] = fit_report
     if tune is not None:
         line["autotune"] = tune
+    if args.config == 4:
+        # accuracy of the single-precision result against the FP64 oracle at abstol = reltol = 1e-14
+        po = g.oracle()
+        m = 2048
+        ref = po.solve("AVern9", "r3bp", np.ascontiguousarray(u0[:, :m]), np.ascontiguousarray(p[:, :m]),
+                       cfg["tspan"], cfg["dt"], rounding="ref", abstol=1e-14, reltol=1e-14, nthreads=os.cpu_count())
+        ok = ref["retcode"] == 0
+        err = np.abs(uf_measured[:, :m][:, ok] - ref["u_final"][:, ok]).max(0)
+        line["error_vs_fp64_oracle_1e-14"] = {"max": float(err.max()), "median": float(np.median(err)),
+                                              "trajectories": int(ok.sum())}
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline()
+        line["cpu_baseline"] = cpu_baseline(cfg, n_sample=65536 if args.config != 5 else 16384)
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
