@@ -45,10 +45,9 @@ __device__ __forceinline__ double sqrtR(double x) { return __dsqrt_rn(x); }
 __device__ __forceinline__ float sqrtR(float x) { return __fsqrt_rn(x); }
 __device__ __forceinline__ double absR(double x) { return fabs(x); }
 __device__ __forceinline__ float absR(float x) { return fabsf(x); }
-__device__ __forceinline__ double sinR(double x) { return sin(x); }
-__device__ __forceinline__ float sinR(float x) { return sinf(x); }
-__device__ __forceinline__ double cosR(double x) { return cos(x); }
-__device__ __forceinline__ float cosR(float x) { return cosf(x); }
+/* sine and cosine of one argument with a single argument reduction */
+__device__ __forceinline__ void sincosR(double x, double* s, double* c) { sincos(x, s, c); }
+__device__ __forceinline__ void sincosR(float x, float* s, float* c) { sincosf(x, s, c); }
 
 /* Julia's min/max propagate NaN; @fastmath min/max are compare-and-select. */
 template <class X> __device__ __forceinline__ X jmin(X a, X b) { return (a != a || b != b) ? a + b : (b < a ? b : a); }
@@ -278,8 +277,7 @@ struct RhsKuramoto {
     R sn[DD], cs[DD], S = 0, C = 0;
 #pragma unroll
     for (int j = 0; j < DD; ++j) {
-      sn[j] = sinR(u[j]);
-      cs[j] = cosR(u[j]);
+      sincosR(u[j], &sn[j], &cs[j]);
       S = S + sn[j];
       C = C + cs[j];
     }

@@ -147,3 +147,54 @@ def test_maxiters_stops(pkg):
               throw=False)
     assert (sol.retcode == 2).all()
     assert ((sol.naccept + sol.nreject) == 10).all()
+
+
+def test_bad_arguments_return_einval(pkg):
+    L = pkg._lib
+    h = pkg._handle(0)
+    u0, p = lorenz_inputs(8, seed=1)
+    out = L.SolveOut()
+    a = pkg.make_args(pkg.GPUSimpleATsit5(), L.RHS["lorenz"], u0, p, (0.0, 1.0), 0.1, 1e-6, 1e-3, None, False,
+                      "fp64", "plain", 0)
+    a.dim = 4  # Lorenz is 3-dimensional
+    assert h.solve_raw(a, out) == L.EINVAL and "Lorenz" in h.error()
+    a.dim, a.alg = 3, 17
+    assert h.solve_raw(a, out) == L.EINVAL
+    a.alg, a.dt = L.ALG["ATsit5"], float("nan")
+    assert h.solve_raw(a, out) == L.EINVAL
+
+
+def test_allocation_failure_is_reported_and_the_handle_survives(pkg):
+    """A workspace request far beyond the device's memory fails cleanly with
+    ODE_ENOMEM.  The failing request is the first one a solve makes (the
+    device copy of u0: 2^31 - 1 trajectories x 32 components x 8 bytes =
+    550 GB), so nothing is copied or launched."""
+    L = pkg._lib
+    h = pkg._handle(0)
+    n = (1 << 31) - 1
+    D = 32
+    u0 = np.zeros((D, 1))
+    p = np.zeros((D + 1, 1))
+    a = pkg.make_args(pkg.GPUSimpleRK4(), L.RHS["kuramoto"], u0, p, (0.0, 1.0), 0.1, 1e-6, 1e-3, None, False,
+                      "fp64", "plain", 0)
+    a.n = n  # the host arrays above are never read: the allocation fails first
+    o = L.SolveOut()
+    rc = h.solve_raw(a, o)
+    assert rc == L.ENOMEM, (rc, h.error())
+    assert "cudaMalloc" in h.error()
+    # the handle still works
+    u0, p = lorenz_inputs(64, seed=3)
+    sol = gpu(pkg, pkg.GPUSimpleATsit5(), "lorenz", u0, p, (0.0, 1.0), 0.1)
+    assert (sol.retcode == 0).all()
+
+
+def test_nan_state_finishes_like_the_reference(pkg, po):
+    """NaN > 1 is false: the reference accepts a NaN error estimate and the
+    trajectory runs to tf with NaN state (retcode 3 flags it)."""
+    u0, p = lorenz_inputs(32, seed=4)
+    u0[0, :5] = np.nan
+    sol = gpu(pkg, pkg.GPUSimpleATsit5(), "lorenz", u0, p, (0.0, 1.0), 0.1, schedule="persistent")
+    ref = po.solve("ATsit5", "lorenz", u0, p, (0, 1), 0.1, rounding="device")
+    assert (sol.retcode[:5] == 3).all() and (sol.retcode[5:] == 0).all()
+    assert (sol.t_final[:5] == 1.0).all() and np.isnan(sol.u_final[:, :5]).all()
+    assert_bitexact(sol, ref)
