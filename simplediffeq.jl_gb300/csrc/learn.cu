@@ -347,8 +347,9 @@ static int train(ode_handle* h, Model* m, const std::vector<float>& X, const std
   float* dL = (float*)buf(h, "learn_loss", 4, &rc);
   if (!dL) return rc;
   cudaStream_t s = h->stream;
-  if (!m->d_master && cudaMalloc(&m->d_master, np * 4) != cudaSuccess) return fail(h, ODE_ENOMEM, "model alloc");
-  if (!m->d_w && cudaMalloc(&m->d_w, np * 2) != cudaSuccess) return fail(h, ODE_ENOMEM, "model alloc");
+  cudaError_t ae;
+  if (!m->d_master && (ae = cudaMalloc(&m->d_master, np * 4)) != cudaSuccess) return cuda_fail(h, ae, "model alloc");
+  if (!m->d_w && (ae = cudaMalloc(&m->d_w, np * 2)) != cudaSuccess) return cuda_fail(h, ae, "model alloc");
   /* He initialisation, seeded */
   std::mt19937_64 rng(o.seed);
   std::vector<float> w(np, 0.f);
@@ -525,7 +526,8 @@ int ode_learn_fit(ode_handle* h, const ode_solve_args* a, const ode_learn_opts* 
   nrm[2 * MAXIN + 1] = m->ymean[1];
   nrm[2 * MAXIN + 2] = m->ystd[0];
   nrm[2 * MAXIN + 3] = m->ystd[1];
-  if (!m->d_norm && cudaMalloc(&m->d_norm, nrm.size() * 4) != cudaSuccess) return fail(h, ODE_ENOMEM, "model alloc");
+  cudaError_t ae = cudaSuccess;
+  if (!m->d_norm && (ae = cudaMalloc(&m->d_norm, nrm.size() * 4)) != cudaSuccess) return cuda_fail(h, ae, "model alloc");
   cudaMemcpy(m->d_norm, nrm.data(), nrm.size() * 4, cudaMemcpyHostToDevice);
   float lf = 0, ll = 0;
   rc = train(h, m, Xs, Ys, nb, o, &lf, &ll);

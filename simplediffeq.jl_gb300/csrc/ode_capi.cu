@@ -116,6 +116,10 @@ int fail(ode_handle* h, int code, const std::string& msg) {
   return code;
 }
 int cuda_fail(ode_handle* h, cudaError_t e, const char* what) {
+  /* the error is reported here: reset the runtime's per-thread last error so
+   * that a later cudaGetLastError() check does not see it again (errors that
+   * leave the context unusable stay sticky regardless) */
+  cudaGetLastError();
   return fail(h, e == cudaErrorMemoryAllocation ? ODE_ENOMEM : ODE_ECUDA,
               std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
 }
