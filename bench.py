@@ -238,6 +238,7 @@ def main():
     ap.add_argument("--n", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--tune-sample", type=int, default=262144, help="trajectories the autotuner times each variant on")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -305,15 +306,17 @@ def main():
             fit_report = {"unavailable": str(e)}
             schedule = "persistent"
 
-    # pick the launch shape of the solver kernel on a 65,536-trajectory sample (excluded from timing)
+    # pick the launch shape of the solver kernel on a sample (default 262,144 trajectories: smaller samples
+    # are dominated by the end-of-kernel tail and mislead), timed in the order the
+    # schedule uses (excluded from timing)
     tune = None
     if not args.no_tune and not fixed:
         try:
-            rep = h.autotune(args_for(schedule if schedule != "learned" else "persistent", L.MEM_DEVICE,
-                                      du0.data_ptr(), dp.data_ptr()), 65536)
+            rep = h.autotune(args_for(schedule, L.MEM_DEVICE, du0.data_ptr(), dp.data_ptr()), args.tune_sample)
             tune = {"block": rep.block, "max_registers": rep.max_registers, "stage_bytes": rep.stage_bytes,
-                    "variants": rep.variants, "sample_ms_default": rep.default_ms, "sample_ms_best": rep.best_ms,
-                    "tune_ms": rep.tune_ms}
+                    "variants": rep.variants, "sample": rep.sample, "sample_ms_default": rep.default_ms,
+                    "sample_ms_best": rep.best_ms, "tune_ms": rep.tune_ms,
+                    "table": [[b, r, s, round(ms, 3)] for b, r, s, ms in rep.rows()]}
         except L.GB300ODEError as e:
             tune = {"unavailable": str(e)}
 

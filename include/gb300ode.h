@@ -42,7 +42,7 @@
 extern "C" {
 #endif
 
-#define ODE_ABI_VERSION 1
+#define ODE_ABI_VERSION 2
 
 /* status codes */
 enum {
@@ -191,7 +191,17 @@ int ode_rhs_compile(ode_handle* h, const char* body, int dim, int nparams, int* 
  * solves of the same algorithm / rhs / precision / dim / schedule kind on this
  * handle.  Variants differ only in launch shape: results are unchanged.  The
  * persistent kernel hands trajectories to lanes dynamically, so there is no
- * fixed trajectories-per-thread parameter to tune. */
+ * fixed trajectories-per-thread parameter to tune.  With ODE_SCHED_LEARNED
+ * and a fitted model the sample is timed in the learned order.  The search
+ * covers threads per block {128, 64, 32} x register caps {none, 128, 112,
+ * 96, 80} x staging-ring bytes that hold at least 32 saveat jobs and fit the
+ * 48 KB of static shared memory a block may have. */
+#define ODE_TUNE_MAX_VARIANTS 64
+typedef struct {
+  int32_t block, max_registers, stage_bytes;
+  float ms;               /* best kernel time on the sample; < 0: did not compile or load */
+} ode_tune_variant;
+
 typedef struct {
   int32_t variants;       /* variants timed */
   int32_t block;          /* chosen threads per block */
@@ -201,6 +211,8 @@ typedef struct {
   double best_ms;         /* kernel time of the chosen kernel on the sample */
   int64_t sample;         /* trajectories timed */
   double tune_ms;         /* wall time of the tuning */
+  int32_t ntable;         /* rows of `table` filled */
+  ode_tune_variant table[ODE_TUNE_MAX_VARIANTS];  /* every variant tried, in search order */
 } ode_tune_report;
 
 int ode_autotune(ode_handle* h, const ode_solve_args* a, int64_t sample, ode_tune_report* rep);

@@ -62,10 +62,23 @@ class LearnReport(ctypes.Structure):
                 ("train_solve_ms", ctypes.c_double), ("train_fit_ms", ctypes.c_double)]
 
 
+TUNE_MAX_VARIANTS = 64
+
+
+class TuneVariant(ctypes.Structure):
+    _fields_ = [("block", ctypes.c_int32), ("max_registers", ctypes.c_int32), ("stage_bytes", ctypes.c_int32),
+                ("ms", ctypes.c_float)]
+
+
 class TuneReport(ctypes.Structure):
     _fields_ = [("variants", ctypes.c_int32), ("block", ctypes.c_int32), ("max_registers", ctypes.c_int32),
                 ("stage_bytes", ctypes.c_int32), ("default_ms", ctypes.c_double), ("best_ms", ctypes.c_double),
-                ("sample", ctypes.c_int64), ("tune_ms", ctypes.c_double)]
+                ("sample", ctypes.c_int64), ("tune_ms", ctypes.c_double), ("ntable", ctypes.c_int32),
+                ("table", TuneVariant * TUNE_MAX_VARIANTS)]
+
+    def rows(self):
+        """(block, max_registers, stage_bytes, ms) of every variant tried; ms < 0: not compiled."""
+        return [(v.block, v.max_registers, v.stage_bytes, v.ms) for v in self.table[:self.ntable]]
 
 
 class GB300ODEError(RuntimeError):

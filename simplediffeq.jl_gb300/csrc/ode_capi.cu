@@ -12,6 +12,7 @@
 #include <nvrtc.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <mutex>
 #include <thread>
@@ -259,6 +260,17 @@ const char* entry_kind(int alg, int sched, int64_t nsave) {
   if (is_fixed(alg)) return "fixed";
   if (sched == ODE_SCHED_PLAIN) return "plain";
   return nsave > 0 ? "staged" : "persistent";
+}
+
+/* Bytes of one saveat job in the staged kernel's ring: the host-side copy of
+ * StageLayout<M, PR, D, F>::JOB in ode_solver.cuh (4 times of type T, the
+ * trajectory index, the saveat index, and D (x2 with Kahan) state values,
+ * NK x D stage values and the parameters of type R). */
+int stage_job_bytes(const ode_solve_args* a) {
+  const int nk = a->alg == ODE_ALG_AVERN9 ? 16 : a->alg == ODE_ALG_AVERN7 ? 10 : 7;
+  const int r = a->precision == ODE_FP64 ? 8 : 4, t = a->precision == ODE_FP32 ? 4 : 8;
+  const int nrec = a->dim * (a->precision == ODE_FP32_KAHAN ? 2 : 1) + nk * a->dim + a->nparams;
+  return 4 * t + 8 + nrec * r + 4;
 }
 
 std::string kernel_key(ode_handle* h, const ode_solve_args* a, int sched) {
@@ -801,7 +813,10 @@ int ode_autotune(ode_handle* h, const ode_solve_args* a, int64_t sample, ode_tun
   ta.p = dp;
   ta.dt0 = ddt0;
   ta.stream = nullptr;
-  ta.schedule = a->schedule == ODE_SCHED_PLAIN ? ODE_SCHED_PLAIN : ODE_SCHED_PERSISTENT;
+  /* time in the order the solves will use: learned when a model fits these arguments */
+  ta.schedule = a->schedule == ODE_SCHED_PLAIN                                      ? ODE_SCHED_PLAIN
+                : (a->schedule == ODE_SCHED_LEARNED && model_ready(h->model, &ta)) ? ODE_SCHED_LEARNED
+                                                                                    : ODE_SCHED_PERSISTENT;
   ode_solve_out to;
   std::memset(&to, 0, sizeof to);
   to.us = dus;
@@ -810,7 +825,7 @@ int ode_autotune(ode_handle* h, const ode_solve_args* a, int64_t sample, ode_tun
   h->tuned.erase(key);
   auto time_solve = [&](double* ms) -> int {
     double best = 1e300;
-    for (int r = 0; r < 2; ++r) {
+    for (int r = 0; r < 3; ++r) {
       ode_solve_stats st;
       const int rr = ode_ensemble_solve(h, &ta, &to, &st);
       if (rr != ODE_OK && rr != ODE_ETRAJ) return rr;
@@ -823,24 +838,44 @@ int ode_autotune(ode_handle* h, const ode_solve_args* a, int64_t sample, ode_tun
   rc = time_solve(&base_ms);
   if (rc != ODE_OK) return rc;
 
+  /* Search space.  The staging ring only exists in the staged kernel (saveat
+   * with a persistent schedule) and only when it holds a full round of 32
+   * jobs; a block's rings share its 48 KB of static shared memory. */
   struct Variant {
     int block, regs, stage;
   };
-  const Variant vars[] = {{128, 0, 12288}, {128, 0, 8192},  {128, 112, 12288}, {128, 96, 12288},
-                          {128, 96, 8192}, {128, 80, 8192}, {64, 0, 12288},    {64, 96, 24576}};
-  const int nv = (int)(sizeof vars / sizeof vars[0]);
+  const bool staged = std::strcmp(entry_kind(ta.alg, ta.schedule, ta.nsave), "staged") == 0;
+  const int job = stage_job_bytes(&ta);
+  std::vector<Variant> vars;
+  for (int block : {128, 64, 32}) {
+    std::vector<int> rings;
+    if (staged) {
+      for (int ring : {12288, 16384, 24576, 36864, 49152})
+        if (ring / 32 * block <= 49152 && (ring / job & ~7) >= 32) rings.push_back(ring);
+    }
+    if (rings.empty()) rings.push_back(12288);
+    for (int regs : {0, 128, 112, 96, 80})
+      for (int ring : rings) vars.push_back({block, regs, ring});
+  }
+  if ((int)vars.size() > ODE_TUNE_MAX_VARIANTS) vars.resize(ODE_TUNE_MAX_VARIANTS);
+  const int nv = (int)vars.size();
   const std::string src = jit_source(h, &ta, ta.schedule);
   std::vector<std::vector<char>> cubins(nv);
   std::vector<int> ok(nv, 0);
   {
+    /* compile on the host's cores, one variant per worker at a time */
+    std::atomic<int> next(0);
+    const int nworkers = std::max(1, std::min<int>(nv, (int)std::thread::hardware_concurrency()));
     std::vector<std::thread> th;
-    for (int v = 0; v < nv; ++v) {
-      th.emplace_back([&, v]() {
-        std::vector<std::string> o = {"-DGBODE_BLOCK=" + std::to_string(vars[v].block),
-                                      "-DGBODE_STAGE_BYTES=" + std::to_string(vars[v].stage)};
-        if (vars[v].regs) o.push_back("--maxrregcount=" + std::to_string(vars[v].regs));
-        std::string lg, err;
-        ok[v] = nvrtc_cubin(src, o, &cubins[v], &lg, &err) == ODE_OK;
+    for (int w = 0; w < nworkers; ++w) {
+      th.emplace_back([&]() {
+        for (int v = next++; v < nv; v = next++) {
+          std::vector<std::string> o = {"-DGBODE_BLOCK=" + std::to_string(vars[v].block),
+                                        "-DGBODE_STAGE_BYTES=" + std::to_string(vars[v].stage)};
+          if (vars[v].regs) o.push_back("--maxrregcount=" + std::to_string(vars[v].regs));
+          std::string lg, err;
+          ok[v] = nvrtc_cubin(src, o, &cubins[v], &lg, &err) == ODE_OK;
+        }
       });
     }
     for (auto& t : th) t.join();
@@ -848,6 +883,7 @@ int ode_autotune(ode_handle* h, const ode_solve_args* a, int64_t sample, ode_tun
   double best_ms = base_ms;
   int best = -1, tried = 0;
   CUfunction best_fn = nullptr;
+  std::vector<double> ms_of(nv, -1.0);
   for (int v = 0; v < nv; ++v) {
     if (!ok[v]) continue;
     CUfunction fn;
@@ -859,6 +895,7 @@ int ode_autotune(ode_handle* h, const ode_solve_args* a, int64_t sample, ode_tun
     h->tuned.erase(key);
     if (rc != ODE_OK) return rc;
     ++tried;
+    ms_of[v] = ms;
     if (ms < 0.99 * best_ms) {
       best_ms = ms;
       best = v;
@@ -875,6 +912,9 @@ int ode_autotune(ode_handle* h, const ode_solve_args* a, int64_t sample, ode_tun
     rep->best_ms = best_ms;
     rep->sample = m;
     rep->tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    rep->ntable = nv;
+    for (int v = 0; v < nv; ++v)
+      rep->table[v] = ode_tune_variant{vars[v].block, vars[v].regs, vars[v].stage, (float)ms_of[v]};
   }
   return ODE_OK;
 }

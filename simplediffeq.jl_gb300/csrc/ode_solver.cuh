@@ -1081,7 +1081,14 @@ __device__ __forceinline__ void run_adaptive_staged(const KParams& P) {
     }
     const int total = __shfl_sync(FULL, incl, 31);
     const int excl = incl - njobs;
-    const int space = CAP - qcount;
+    int space = CAP - qcount;
+    if (total > space && qcount > 0) {
+      /* this iteration's jobs do not all fit: interpolate the waiting ones
+       * (fewer than 32) now, so that the new jobs go to the ring instead of
+       * being interpolated in place by their lanes one after another */
+      round(qcount < 32 ? qcount : 32);
+      space = CAP - qcount;
+    }
     if (njobs) {
       const T inv_dt = recip(st.dtold);
       for (int q = 0; q < njobs; ++q) {

@@ -32,7 +32,7 @@ def test_library_exports_every_declared_symbol(pkg):
     for name in declared_functions():
         assert name in exported, name
         assert getattr(lib, name) is not None
-    assert lib.ode_abi_version() == 1
+    assert lib.ode_abi_version() == 2
 
 
 def test_library_needs_no_driver_at_load_time(pkg):
@@ -78,3 +78,29 @@ def test_null_handle_and_bad_arguments(pkg):
     assert lib.ode_fixed_grid(0.0, 0.0, 1.0, 0, None, 0, ctypes.byref(n)) == pkg._lib.EINVAL
     assert lib.ode_fixed_grid(0.0, float("nan"), 1.0, 0, None, 0, ctypes.byref(n)) == pkg._lib.EINVAL
     assert lib.ode_last_error(None) == b"null handle"
+
+
+STRUCTS = [("SolveArgs", "ode_solve_args"), ("SolveOut", "ode_solve_out"), ("SolveStats", "ode_solve_stats"),
+           ("LearnOpts", "ode_learn_opts"), ("LearnReport", "ode_learn_report"), ("TuneVariant", "ode_tune_variant"),
+           ("TuneReport", "ode_tune_report")]
+
+
+def test_ctypes_structs_match_the_c_layout(pkg, tmp_path):
+    """Every struct of the Python binding has the size and field offsets that
+    a C compiler gives the header's struct."""
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "gb300ode.h"', "int main(void) {"]
+    expect = []
+    for py, c in STRUCTS:
+        cls = getattr(pkg._lib, py)
+        lines.append('printf("%%zu\\n", sizeof(%s));' % c)
+        expect.append(ctypes.sizeof(cls))
+        for f in cls._fields_:
+            lines.append('printf("%%zu\\n", offsetof(%s, %s));' % (c, f[0]))
+            expect.append(getattr(cls, f[0]).offset)
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert got == expect
