@@ -114,8 +114,11 @@ CONFIGS = {
                      "K~U[0,4], theta(0)~U[0,2pi)^12, tspan (0,50), abstol 1e-8, reltol 1e-6, final state + "
                      "order parameter at 50 saveat times (reduced in the kernel)",
             alg="ATsit5", rhs="kuramoto", n=4194304, tspan=(0.0, 50.0), dt=0.1, abstol=1e-8, reltol=1e-6,
-            nsave=50, precision="fp64", output="kuramoto_r", inputs=inputs_kuramoto, flops_attempt=1310,
-            flops_save=266, rhs_per_attempt=6, oracle_alg="ATsit5", dtype="f64"),
+            nsave=50, precision="fp64", output="kuramoto_r", inputs=inputs_kuramoto,
+            # 1310 stage/RHS/controller flops + 6 RHS x 12 sin/cos pairs x 33 flops of the kernel's
+            # sincos_cw (15 FMA + 2 multiplies + 1 add); per save 266 + 12 pairs x 33
+            flops_attempt=1310 + 6 * 12 * 33, flops_save=266 + 12 * 33, rhs_per_attempt=6, oracle_alg="ATsit5",
+            dtype="f64"),
 }
 
 

@@ -2,7 +2,7 @@
  *
  * TEST INFRASTRUCTURE COPY: the oracle's own implementation of the controller
  * power used by the device rounding canon.  It is written independently of
- * the kernels' copy (simplediffeq.jl_gb300/csrc/ode_math.cuh); the two must
+ * the kernels' copy (ctrl_pow in simplediffeq.jl_gb300/csrc/ode_solver.cuh); the two must
  * agree bit for bit, which the parity tests check through whole solves.
  *
  * Method (textbook, no vendor code): x = m * 2^e with m in [sqrt(1/2), sqrt(2));

@@ -88,6 +88,63 @@ template <class X> static inline X jmax(X a, X b) {
 template <class X> static inline X fmin_(X x, X y) { return (y > x) ? x : y; }
 template <class X> static inline X fmax_(X x, X y) { return (y > x) ? y : x; }
 
+/* Sine and cosine in the device canon (double precision): Cody-Waite
+ * reduction modulo pi/2 (Cody & Waite, Software Manual for the Elementary
+ * Functions, 1980) in fused form, r = fma(-k, C2, fma(-k, C1, x)) with C1 the
+ * double nearest pi/2 and C2 the double nearest pi/2 - C1; k is x * 2/pi
+ * rounded to the nearest integer by adding 1.5 * 2^52 in one fused
+ * multiply-add (the quadrant k mod 4 is then the low bits of that sum);
+ * sin r = r + r^3 P(r^2), cos r = 1 + r^2 Q(r^2) with the near-minimax
+ * coefficients printed by simplediffeq.jl_gb300/csrc/gen_sincos.py, Horner
+ * form, one rounding per operation.  Outside |x| < 2^19 (and for NaN/Inf)
+ * libm is used. */
+static void sincos_dev(double x, double* s, double* c) {
+  if (!(std::fabs(x) < 524288.0)) {
+    *s = std::sin(x);
+    *c = std::cos(x);
+    return;
+  }
+  static const double P[6] = {-0x1.5555555555548p-3, 0x1.111111110f7d0p-7, -0x1.a01a019bfde60p-13,
+                              0x1.71de3567ccfe8p-19, -0x1.ae5e5a8d61ce7p-26, 0x1.5d8fd0a40698ep-33};
+  static const double Q[6] = {-0x1.fffffffffff96p-2, 0x1.555555554f0a9p-5, -0x1.6c16c1640a98bp-10,
+                              0x1.a019f81ca810ap-16, -0x1.27df4604d6713p-22, 0x1.1b8b9800ee7dap-29};
+  const double shifter = 6755399441055744.0;  /* 1.5 * 2^52 */
+  const double kb = std::fma(x, 0x1.45f306dc9c883p-1, shifter);
+  const double k = kb - shifter;
+  uint64_t bits;
+  std::memcpy(&bits, &kb, 8);
+  const unsigned quadrant = (unsigned)(bits & 3u);
+  double r = std::fma(-k, 0x1.921fb54442d18p+0, x);
+  r = std::fma(-k, 0x1.1a62633145c07p-54, r);
+  const double z = r * r;
+  double ps = P[5], pc = Q[5];
+  for (int m = 4; m >= 0; --m) {
+    ps = std::fma(ps, z, P[m]);
+    pc = std::fma(pc, z, Q[m]);
+  }
+  const double sr = std::fma(z * r, ps, r);
+  const double cr = std::fma(z, pc, 1.0);
+  switch (quadrant) {
+    case 0: *s = sr; *c = cr; break;
+    case 1: *s = cr; *c = -sr; break;
+    case 2: *s = -sr; *c = -cr; break;
+    default: *s = -cr; *c = sr; break;
+  }
+}
+
+template <class R, bool DEV>
+static inline void sincos_of(R x, R* s, R* c) {
+  if (DEV && sizeof(R) == sizeof(double)) {
+    double sd, cd;
+    sincos_dev((double)x, &sd, &cd);
+    *s = (R)sd;
+    *c = (R)cd;
+  } else {
+    *s = std::sin(x);
+    *c = std::cos(x);
+  }
+}
+
 /* ---------------------------------------------------------------- problems */
 /* Built-in right-hand sides.  The REF form is the plain Julia expression; the
  * DEV form fuses the products the device functors fuse. */
@@ -144,8 +201,7 @@ static void rhs_eval(int id, int D, const R* u, const R* p, double t, R* du) {
     case ORACLE_KURAMOTO: {  /* theta_i' = w_i + (K/D) sum_j sin(theta_j - theta_i); p = (w_1..w_D, K) */
       R S = 0, C = 0, sn[MAXD], cs[MAXD];
       for (int j = 0; j < D; ++j) {
-        sn[j] = std::sin(u[j]);
-        cs[j] = std::cos(u[j]);
+        sincos_of<R, DEV>(u[j], &sn[j], &cs[j]);
         S += sn[j];
         C += cs[j];
       }
@@ -658,12 +714,21 @@ static void load_traj(const oracle_args* a, int64_t i, Alg<P>& A, State<typename
 static inline void put_us(const oracle_args* a, oracle_out* o, int64_t i, int64_t j, const double* v) {
   if (!o->us) return;
   if (a->output == 1) {
+    /* device canon: sincos_dev and a fused C*C + S*S; reference rounding: libm and two roundings */
+    const bool dev = a->rounding == ORACLE_ROUND_DEVICE;
     double C = 0, S = 0;
     for (int d = 0; d < a->dim; ++d) {
-      C += std::cos(v[d]);
-      S += std::sin(v[d]);
+      double sn, cs;
+      if (dev) {
+        sincos_dev(v[d], &sn, &cs);
+      } else {
+        sn = std::sin(v[d]);
+        cs = std::cos(v[d]);
+      }
+      C = C + cs;
+      S = S + sn;
     }
-    o->us[j * a->n + i] = std::sqrt(C * C + S * S) / a->dim;
+    o->us[j * a->n + i] = std::sqrt(dev ? std::fma(C, C, S * S) : C * C + S * S) / a->dim;
     return;
   }
   for (int d = 0; d < a->dim; ++d) o->us[(j * a->dim + d) * a->n + i] = v[d];
@@ -1137,6 +1202,7 @@ extern "C" int oracle_solve(const oracle_args* a, oracle_out* o) {
 }
 
 extern "C" float oracle_ctrl_pow(float x, float b) { return oracle_pow::ctrl_pow(x, b); }
+extern "C" void oracle_sincos(double x, double* s, double* c) { sincos_dev(x, s, c); }
 
 /* Reference forward and backward pass of the learned-schedule MLP, in double
  * precision, for checking the device training kernel's gradients.

@@ -62,6 +62,8 @@ typedef struct {
 
 int oracle_solve(const oracle_args* a, oracle_out* o);
 float oracle_ctrl_pow(float x, float b);
+/* the device canon's double sine and cosine (Cody-Waite reduction, Taylor polynomials) */
+void oracle_sincos(double x, double* s, double* c);
 int oracle_mlp_forward_backward(int nin, int nh, int64_t batch, const float* params, const float* x,
                                 const float* y, float* grad, float* loss);
 

@@ -61,12 +61,21 @@ def lib():
         _lib.oracle_solve.restype = ctypes.c_int
         _lib.oracle_ctrl_pow.argtypes = [ctypes.c_float, ctypes.c_float]
         _lib.oracle_ctrl_pow.restype = ctypes.c_float
+        _lib.oracle_sincos.argtypes = [ctypes.c_double, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+        _lib.oracle_sincos.restype = None
         _lib.oracle_mlp_forward_backward.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int64] + [ctypes.c_void_p] * 5
     return _lib
 
 
 def ctrl_pow(x, b):
     return lib().oracle_ctrl_pow(x, b)
+
+
+def sincos(x):
+    """The device canon's double (sin x, cos x)."""
+    s, c = ctypes.c_double(), ctypes.c_double()
+    lib().oracle_sincos(float(x), ctypes.byref(s), ctypes.byref(c))
+    return s.value, c.value
 
 
 def mlp_forward_backward(nin, nh, params, x, y):

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <cstdint>
 #include <mutex>
 #include <thread>
 #include <cmath>
@@ -265,11 +266,12 @@ const char* entry_kind(int alg, int sched, int64_t nsave) {
 /* Bytes of one saveat job in the staged kernel's ring: the host-side copy of
  * StageLayout<M, PR, D, F>::JOB in ode_solver.cuh (4 times of type T, the
  * trajectory index, the saveat index, and D (x2 with Kahan) state values,
- * NK x D stage values and the parameters of type R). */
+ * NK x D stage values and, for the Verner methods, the parameters, of type R). */
 int stage_job_bytes(const ode_solve_args* a) {
   const int nk = a->alg == ODE_ALG_AVERN9 ? 16 : a->alg == ODE_ALG_AVERN7 ? 10 : 7;
   const int r = a->precision == ODE_FP64 ? 8 : 4, t = a->precision == ODE_FP32 ? 4 : 8;
-  const int nrec = a->dim * (a->precision == ODE_FP32_KAHAN ? 2 : 1) + nk * a->dim + a->nparams;
+  const bool dense_f = a->alg != ODE_ALG_ATSIT5;  /* Verner dense output evaluates f: parameters ride along */
+  const int nrec = a->dim * (a->precision == ODE_FP32_KAHAN ? 2 : 1) + nk * a->dim + (dense_f ? a->nparams : 0);
   return 4 * t + 8 + nrec * r + 4;
 }
 
@@ -404,9 +406,28 @@ int block_of(ode_handle* h, CUfunction fn) {
   return it == h->fblock.end() ? 128 : it->second;
 }
 
-int launch(ode_handle* h, CUfunction fn, unsigned grid, KParams* kp, cudaStream_t s) {
+/* Threads per block of a one-thread-per-trajectory launch: of the compiled
+ * block size and its halves down to one warp, the one that puts the fewest
+ * warps on the busiest SM (ties go to the larger block).  A small ensemble
+ * then spreads over every SM: 8,192 trajectories in blocks of 128 would fill
+ * 64 of 152 SMs with 4 warps each, in blocks of 64 they give 128 SMs 2 warps. */
+int plain_block(int64_t n, int nsm, int maxb) {
+  int best = maxb;
+  int64_t best_w = INT64_MAX;
+  for (int b = maxb; b >= 32; b /= 2) {
+    const int64_t blocks = (n + b - 1) / b;
+    const int64_t w = (blocks + nsm - 1) / nsm * (b / 32);
+    if (w < best_w) {
+      best_w = w;
+      best = b;
+    }
+  }
+  return best;
+}
+
+int launch(ode_handle* h, CUfunction fn, unsigned grid, int block, KParams* kp, cudaStream_t s) {
   void* params[] = {kp};
-  CUresult r = g_drv.cuLaunchKernel(fn, grid, 1, 1, (unsigned)block_of(h, fn), 1, 1, 0, (CUstream)s, params, nullptr);
+  CUresult r = g_drv.cuLaunchKernel(fn, grid, 1, 1, (unsigned)block, 1, 1, 0, (CUstream)s, params, nullptr);
   if (r != CUDA_SUCCESS) return cu_fail(h, r, "cuLaunchKernel");
   return ODE_OK;
 }
@@ -648,8 +669,9 @@ int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o,
   /* schedule */
   int launches = 0;
   unsigned gridx;
-  const int block = block_of(h, fn);
+  int block = block_of(h, fn);
   if (sched == ODE_SCHED_PLAIN) {
+    block = plain_block(n, h->nsm, block);
     gridx = (unsigned)((n + block - 1) / block);
   } else {
     int nb = 0;
@@ -688,7 +710,7 @@ int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o,
       if (r != ODE_OK) return r;
     }
     if (n > 0) {
-      const int r = launch(h, fn, gridx, &kp, s);
+      const int r = launch(h, fn, gridx, block, &kp, s);
       if (r != ODE_OK) return r;
       ++*nl;
     }
@@ -697,7 +719,7 @@ int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o,
   std::string key((const char*)&kp, sizeof kp);
   {
     char extra[256];
-    snprintf(extra, sizeof extra, "|%p|%u|%d|%d|", (void*)fn, gridx, sched, (int)seeding);
+    snprintf(extra, sizeof extra, "|%p|%u|%d|%d|%d|", (void*)fn, gridx, block, sched, (int)seeding);
     key += extra;
     if (sched == ODE_SCHED_LEARNED) key += model_key(h->model);
   }

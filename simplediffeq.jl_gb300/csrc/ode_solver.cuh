@@ -45,8 +45,49 @@ __device__ __forceinline__ double sqrtR(double x) { return __dsqrt_rn(x); }
 __device__ __forceinline__ float sqrtR(float x) { return __fsqrt_rn(x); }
 __device__ __forceinline__ double absR(double x) { return fabs(x); }
 __device__ __forceinline__ float absR(float x) { return fabsf(x); }
+/* Sine and cosine of a double with one argument reduction, in 18 double
+ * operations.  Method: Cody and Waite's reduction modulo pi/2 (W. J. Cody and
+ * W. Waite, Software Manual for the Elementary Functions, 1980) in its fused
+ * form: k = x * 2/pi rounded to the nearest integer (one fused multiply-add
+ * with 1.5 * 2^52, whose low bits then hold k), r = (x - k*C1) - k*C2 with
+ * C1 = pi/2 rounded to double and C2 the rounded remainder, each term one
+ * fused multiply-add; then sin r = r + r^3 P(r^2) and cos r = 1 + r^2 Q(r^2)
+ * with near-minimax P and Q of degree 5 from csrc/gen_sincos.py, in Horner
+ * form.  Within 1.5 ulp (1.7e-16 absolute) of the exact values below 2^19
+ * (checked against 40-digit values), except that results below 1e-15 in
+ * magnitude (x within 1e-15 of a multiple of pi/2) keep an absolute error
+ * below 1e-30 instead of a relative one.  Every step is one IEEE double operation, so the oracle reproduces it
+ * bit for bit.  |x| >= 2^19 and non-finite x go to CUDA's sincos. */
+__device__ __forceinline__ void sincos_cw(double x, double* s, double* c) {
+  if (!(fabs(x) < 524288.0)) {
+    sincos(x, s, c);
+    return;
+  }
+  const double kb = __fma_rn(x, 0x1.45f306dc9c883p-1, 0x1.8p52);  /* 2/pi; 1.5 * 2^52 */
+  const double k = kb - 0x1.8p52;
+  const int q = __double2loint(kb) & 3;
+  double r = __fma_rn(-k, 0x1.921fb54442d18p+0, x);
+  r = __fma_rn(-k, 0x1.1a62633145c07p-54, r);
+  const double z = r * r;
+  double ps = 0x1.5d8fd0a40698ep-33;
+  ps = __fma_rn(ps, z, -0x1.ae5e5a8d61ce7p-26);
+  ps = __fma_rn(ps, z, 0x1.71de3567ccfe8p-19);
+  ps = __fma_rn(ps, z, -0x1.a01a019bfde60p-13);
+  ps = __fma_rn(ps, z, 0x1.111111110f7d0p-7);
+  ps = __fma_rn(ps, z, -0x1.5555555555548p-3);
+  const double sr = __fma_rn(z * r, ps, r);
+  double pc = 0x1.1b8b9800ee7dap-29;
+  pc = __fma_rn(pc, z, -0x1.27df4604d6713p-22);
+  pc = __fma_rn(pc, z, 0x1.a019f81ca810ap-16);
+  pc = __fma_rn(pc, z, -0x1.6c16c1640a98bp-10);
+  pc = __fma_rn(pc, z, 0x1.555555554f0a9p-5);
+  pc = __fma_rn(pc, z, -0x1.fffffffffff96p-2);
+  const double cr = __fma_rn(z, pc, 1.0);
+  *s = q == 0 ? sr : q == 1 ? cr : q == 2 ? -sr : -cr;
+  *c = q == 0 ? cr : q == 1 ? -sr : q == 2 ? -cr : sr;
+}
 /* sine and cosine of one argument with a single argument reduction */
-__device__ __forceinline__ void sincosR(double x, double* s, double* c) { sincos(x, s, c); }
+__device__ __forceinline__ void sincosR(double x, double* s, double* c) { sincos_cw(x, s, c); }
 __device__ __forceinline__ void sincosR(float x, float* s, float* c) { sincosf(x, s, c); }
 
 /* Julia's min/max propagate NaN; @fastmath min/max are compare-and-select. */
@@ -309,7 +350,7 @@ template <class PR, int D, class F>
 struct MTsit5 {
   typedef typename PR::R R;
   typedef typename PR::T T;
-  enum { NK = 7, FSAL = 1, DTMIN_1F7 = 0 };
+  enum { NK = 7, FSAL = 1, DTMIN_1F7 = 0, DENSE_F = 0 };  /* DENSE_F: dense output evaluates f */
 
   __device__ static __forceinline__ void attempt(const F& f, const R (&uh)[D], const R (&uc)[D], T t, T dt,
                                                  R (&k)[NK][D], R (&nh)[D], R (&nc)[D], R (&e)[D], bool want_err) {
@@ -371,7 +412,7 @@ template <class PR, int D, class F>
 struct MVern7 {
   typedef typename PR::R R;
   typedef typename PR::T T;
-  enum { NK = 10, FSAL = 0, DTMIN_1F7 = 0 };
+  enum { NK = 10, FSAL = 0, DTMIN_1F7 = 0, DENSE_F = 1 };
 
   __device__ static __forceinline__ void attempt(const F& f, const R (&uh)[D], const R (&uc)[D], T t, T dt,
                                                  R (&k)[NK][D], R (&nh)[D], R (&nc)[D], R (&e)[D], bool want_err) {
@@ -472,7 +513,7 @@ template <class PR, int D, class F, bool ADAPTIVE>
 struct MVern9Impl {
   typedef typename PR::R R;
   typedef typename PR::T T;
-  enum { NK = 16, FSAL = 0, DTMIN_1F7 = 1 };
+  enum { NK = 16, FSAL = 0, DTMIN_1F7 = 1, DENSE_F = 1 };
 
   __device__ static __forceinline__ void attempt(const F& f, const R (&uh)[D], const R (&uc)[D], T t, T dt,
                                                  R (&k)[NK][D], R (&nh)[D], R (&nc)[D], R (&e)[D], bool want_err) {
@@ -676,7 +717,7 @@ __device__ __forceinline__ void store_point(const KParams& P, long long idx, lon
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       double sn, cs;
-      sincos(v[d], &sn, &cs);
+      sincos_cw(v[d], &sn, &cs);
       C = C + cs;
       S = S + sn;
     }
@@ -989,7 +1030,8 @@ template <class M, class PR, int D, class F>
 struct StageLayout {
   typedef typename PR::R R;
   typedef typename PR::T T;
-  enum { NREC = D * (PR::KAHAN ? 2 : 1) + M::NK * D + F::NP };
+  /* the parameters ride along only when the dense output evaluates f (Verner's extra stages) */
+  enum { NREC = D * (PR::KAHAN ? 2 : 1) + M::NK * D + (M::DENSE_F ? F::NP : 0) };
   enum { JOB = 4 * (int)sizeof(T) + 8 + NREC * (int)sizeof(R) + 4 };
   enum { CAP = (kStageBytesPerWarp / JOB) & ~7 };
 };
@@ -1030,8 +1072,10 @@ __device__ __forceinline__ void run_adaptive_staged(const KParams& P) {
       for (int q = 0; q < NK; ++q)
 #pragma unroll
         for (int d = 0; d < D; ++d) kk[q][d] = rv[(KOFF + q * D + d) * CAP + slot];
+      if (M::DENSE_F) {
 #pragma unroll
-      for (int q = 0; q < F::NP; ++q) f2.p[q] = rv[(POFF + q) * CAP + slot];
+        for (int q = 0; q < F::NP; ++q) f2.p[q] = rv[(POFF + q) * CAP + slot];
+      }
       double v[D];
       M::dense(f2, uh, uc, tv[slot], tv[CAP + slot], tv[2 * CAP + slot], tv[3 * CAP + slot], kk, v);
       store_point<PR, D>(P, iv[slot], jv[slot], v);
@@ -1111,8 +1155,10 @@ __device__ __forceinline__ void run_adaptive_staged(const KParams& P) {
           for (int k = 0; k < NK; ++k)
 #pragma unroll
             for (int d = 0; d < D; ++d) rv[(KOFF + k * D + d) * CAP + slot] = l.k[k][d];
+          if (M::DENSE_F) {
 #pragma unroll
-          for (int k = 0; k < F::NP; ++k) rv[(POFF + k) * CAP + slot] = l.f.p[k];
+            for (int k = 0; k < F::NP; ++k) rv[(POFF + k) * CAP + slot] = l.f.p[k];
+          }
         } else {
           /* the ring is full: interpolate here */
           double v[D];

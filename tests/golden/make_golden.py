@@ -62,6 +62,11 @@ CASES = {
                               abstol=1e-7, reltol=1e-7, precision="fp32_kahan", rounding="device"),
     "atsit5_kuramoto_ref": dict(alg="ATsit5", rhs="kuramoto", inputs=("kuramoto", 8, 5), tspan=(0, 50), dt=0.1,
                                 abstol=1e-8, reltol=1e-6, saveat=np.linspace(0, 50, 50), rounding="ref"),
+    "atsit5_kuramoto_dev": dict(alg="ATsit5", rhs="kuramoto", inputs=("kuramoto", 8, 5), tspan=(0, 50), dt=0.1,
+                                abstol=1e-8, reltol=1e-6, saveat=np.linspace(0, 50, 50), rounding="device"),
+    "atsit5_kuramoto_r_dev": dict(alg="ATsit5", rhs="kuramoto", inputs=("kuramoto", 8, 5), tspan=(0, 50), dt=0.1,
+                                  abstol=1e-8, reltol=1e-6, saveat=np.linspace(0, 50, 50), rounding="device",
+                                  output="kuramoto_r"),
 }
 
 
@@ -76,9 +81,12 @@ def make_inputs(spec):
     return kuramoto(spec[1], spec[2])
 
 
-def run_case(po, case):
+def run_case(po, case, inputs=None):
+    """Solve a case with the oracle; `inputs` = (u0, p) overrides the generated inputs."""
     c = dict(case)
-    u0, p = make_inputs(c.pop("inputs"))
+    u0, p = make_inputs(c.pop("inputs")) if inputs is None else inputs
+    if inputs is not None:
+        c.pop("inputs")
     alg, rhs, tspan, dt = c.pop("alg"), c.pop("rhs"), c.pop("tspan"), c.pop("dt")
     return po.solve(alg, rhs, u0, p, tspan, dt, **c)
 
@@ -87,10 +95,14 @@ def main():
     sys.path.insert(0, os.path.join(HERE, "..", "..", "oracle"))
     import pyoracle as po
     for name, case in CASES.items():
-        out = run_case(po, case)
+        # the inputs are stored with the outputs: numpy's exp/log (used for log-uniform parameters
+        # and normal samples) may round differently on other machines, so consumers use these
+        u0, p = make_inputs(case["inputs"])
+        out = run_case(po, case, (u0, p))
         keep = {k: out[k] for k in ("u_final", "naccept", "nreject", "retcode")}
         if out["us"] is not None:
             keep["us"] = out["us"]
+        keep["u0"], keep["p"] = u0, p
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **keep)
         print(name, {k: v.shape for k, v in keep.items()})
 

@@ -1,8 +1,9 @@
-"""GPU checks of the remaining ensemble workloads: Kuramoto-12 (whose sin/cos
-come from CUDA's libdevice on the GPU and from glibc in the oracle, so parity
-is a tolerance), the single-precision modes' accuracy against the FP64
-oracle at abstol = reltol = 1e-14, and the staged saveat path in the
-compensated single-precision mode."""
+"""GPU checks of the remaining ensemble workloads: Kuramoto-12 (bit-identical
+to the oracle's device canon, whose double sine and cosine are the kernels'
+own Cody-Waite/Taylor routine, and within tolerance of the reference
+rounding with libm), the single-precision modes' accuracy against the FP64
+oracle at abstol = reltol = 1e-14, the staged saveat path in the compensated
+single-precision mode, and every committed device-canon golden fixture."""
 import os
 import sys
 
@@ -17,12 +18,15 @@ import make_golden  # noqa: E402  (input generators shared with the golden fixtu
 
 
 @pytest.mark.parametrize("schedule", ["plain", "persistent"])
-def test_kuramoto12_matches_oracle_within_tolerance(pkg, po, schedule):
+def test_kuramoto12_bitexact_and_within_reference_tolerance(pkg, po, schedule):
     u0, p = make_golden.kuramoto(2048, 9)
     sv = np.linspace(0, 50, 50)
     kw = dict(abstol=1e-8, reltol=1e-6)
     sol = gpu(pkg, pkg.GPUSimpleATsit5(), "kuramoto", u0, p, (0.0, 50.0), 0.1, saveat=sv, schedule=schedule, **kw)
-    ref = po.solve("ATsit5", "kuramoto", u0, p, (0, 50), 0.1, rounding="device", saveat=sv, nthreads=8, **kw)
+    dev = po.solve("ATsit5", "kuramoto", u0, p, (0, 50), 0.1, rounding="device", saveat=sv, nthreads=8, **kw)
+    assert_bitexact(sol, dev)
+    # against the reference rounding (libm sin/cos, unfused products): the adaptive tolerance
+    ref = po.solve("ATsit5", "kuramoto", u0, p, (0, 50), 0.1, rounding="ref", saveat=sv, nthreads=8, **kw)
     scale = 1e-8 + 1e-6 * np.abs(ref["u_final"]).max(0)
     err = np.abs(sol.u_final - ref["u_final"]).max(0) / scale
     assert np.mean(err <= 10) >= 0.999
@@ -30,6 +34,27 @@ def test_kuramoto12_matches_oracle_within_tolerance(pkg, po, schedule):
     assert np.abs(sol.naccept - ref["naccept"]).max() <= 2
     es = np.abs(sol.us - ref["us"]).max(axis=(0, 1)) / scale
     assert np.mean(es <= 10) >= 0.999
+
+
+@pytest.mark.parametrize("name", [k for k, c in make_golden.CASES.items() if c["rounding"] == "device"])
+def test_committed_device_golden_fixtures(pkg, name):
+    """Each committed device-canon fixture, reproduced bit for bit by the GPU
+    (plain and persistent schedules) from the same seeded inputs."""
+    case = dict(make_golden.CASES[name])
+    fx = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", name + ".npz"))
+    case.pop("inputs")
+    u0, p = fx["u0"], fx["p"]  # stored: regenerating them here could round differently
+    alg, rhs, tspan, dt = case.pop("alg"), case.pop("rhs"), case.pop("tspan"), case.pop("dt")
+    case.pop("rounding")
+    scheds = ["plain"] if alg in ("Tsit5", "Vern7", "Vern9", "RK4") else ["plain", "persistent"]
+    for sched in scheds:
+        sol = gpu(pkg, getattr(pkg, "GPUSimple" + alg)(), rhs, u0, p, (float(tspan[0]), float(tspan[1])), dt,
+                  schedule=sched, throw=False, **case)
+        assert np.array_equal(sol.u_final, fx["u_final"], equal_nan=True), (name, sched)
+        assert np.array_equal(sol.naccept, fx["naccept"]) and np.array_equal(sol.nreject, fx["nreject"])
+        assert np.array_equal(sol.retcode, fx["retcode"])
+        if "us" in fx.files:
+            assert np.array_equal(sol.us, fx["us"], equal_nan=True), (name, sched)
 
 
 def test_fp32_modes_error_against_fp64_oracle(pkg, po):
@@ -99,8 +124,8 @@ def test_kuramoto_order_parameter_output(pkg, po, schedule):
     r_full = np.abs(np.exp(1j * full.us).mean(1))
     assert np.abs(sol.us[:, 0, :] - r_full).max() < 1e-12
     assert np.array_equal(sol.u_final, full.u_final)
-    # and agrees with the oracle's
-    assert np.mean(np.abs(sol.us - ref["us"]).max(axis=(0, 1)) < 1e-6) >= 0.999
+    # and is the oracle's, bit for bit
+    assert np.array_equal(sol.us, ref["us"])
 
 
 def test_repeated_solve_replays_the_captured_graph(pkg):
