@@ -4,6 +4,7 @@
  * per-trajectory solve methods of SimpleDiffEq.jl's GPU-crutch solvers:
  *
  *   DiffEqBase.solve(prob, GPUSimpleRK4(); dt)                 src/rk4/gpurk4.jl:53-98
+ *   DiffEqBase.solve(prob, GPUSimpleEuler(); dt)               src/euler/gpueuler.jl:53-90
  *   DiffEqBase.solve(prob, GPUSimpleTsit5(); dt, saveat, ...)  src/tsit5/gpuatsit5.jl:55-147
  *   DiffEqBase.solve(prob, GPUSimpleATsit5(); dt, abstol, reltol, saveat, ...)
  *                                                              src/tsit5/gpuatsit5.jl:205-336
@@ -64,7 +65,8 @@ enum {
   ODE_ALG_VERN7 = 3,   /* GPUSimpleVern7  (fixed step) */
   ODE_ALG_AVERN7 = 4,  /* GPUSimpleAVern7 (adaptive)   */
   ODE_ALG_VERN9 = 5,   /* GPUSimpleVern9  (fixed step) */
-  ODE_ALG_AVERN9 = 6   /* GPUSimpleAVern9 (adaptive)   */
+  ODE_ALG_AVERN9 = 6,  /* GPUSimpleAVern9 (adaptive)   */
+  ODE_ALG_EULER = 7    /* GPUSimpleEuler  (fixed step) */
 };
 
 /* built-in right-hand sides f(u, p, t); ids >= ODE_RHS_USER come from ode_rhs_compile */

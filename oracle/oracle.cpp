@@ -8,6 +8,7 @@
  *   GPUSimpleVern7 / GPUSimpleAVern7   src/verner/gpuvern7.jl:55-242, :300-536
  *   GPUSimpleVern9 / GPUSimpleAVern9   src/verner/gpuvern9.jl:55-353, :411-779
  *   GPUSimpleRK4                       src/rk4/gpurk4.jl:53-98
+ *   GPUSimpleEuler                     src/euler/gpueuler.jl:53-90
  *   SimpleATsit5 (integrator form)     src/tsit5/atsit5.jl:117-179, :322-413, :705-732
  *   SimpleTsit5 (integrator form)      src/tsit5/tsit5.jl:84-122, :303-352, :358-399
  *   PI controller constants            src/SimpleDiffEq.jl:67-77, src/tsit5/atsit5.jl:57-62
@@ -945,9 +946,31 @@ static void solve_fixed(const oracle_args* a, oracle_out* o, int64_t i) {
   finish<P>(a, o, i, st, t, RET_DEFAULT, steps, 0, steps > 0 ? (double)dt : NAN);
 }
 
-/* GPUSimpleRK4, gpurk4.jl:53-98: saves every grid point (us[1] = u0). */
+/* GPUSimpleEuler, src/euler/gpueuler.jl:67-76: k1 = f(u, p, ts[i]) (the END
+ * of the step, as in GPUSimpleRK4) and u = uprev + dt*k1, @muladd of a
+ * vector: fused in the device canon, a multiply and an add in the reference. */
 template <class P>
-static void solve_rk4(const oracle_args* a, oracle_out* o, int64_t i) {
+struct Euler {
+  typedef typename P::R R;
+  typedef typename P::T T;
+  static void step(const Alg<P>& A, const State<R>& up, T t, T dt, State<R>& u) {
+    R k1[MAXD];
+    const R h = (R)dt;
+    A.f(up.hi, (double)t, k1);
+    if (P::DEV) {
+      State<R> tmpu;
+      state_update<P>(A.D, up, h, k1, tmpu);
+      u = tmpu;
+    } else {
+      for (int d = 0; d < A.D; ++d) { u.hi[d] = h * k1[d] + up.hi[d]; u.c[d] = 0; }
+    }
+  }
+};
+
+/* GPUSimpleRK4, gpurk4.jl:53-98, and GPUSimpleEuler, gpueuler.jl:53-90 (S =
+ * RK4 or Euler): one step per grid point, every grid point saved (us[1] = u0). */
+template <class P, class S>
+static void solve_onestep(const oracle_args* a, oracle_out* o, int64_t i) {
   typedef typename P::R R;
   typedef typename P::T T;
   Alg<P> A;
@@ -960,7 +983,7 @@ static void solve_rk4(const oracle_args* a, oracle_out* o, int64_t i) {
   T t = (T)a->t0;
   for (int64_t g = 1; g < a->ngrid; ++g) {
     t = (T)a->grid[g];
-    RK4<P>::step(A, st, t, dt, un);
+    S::step(A, st, t, dt, un);
     st = un;
     if (every) { value_of(st, a->dim, P::KAHAN, tmpv); put_us(a, o, i, g, tmpv); }
   }
@@ -1140,7 +1163,8 @@ template <class P>
 static void solve_range(const oracle_args* a, oracle_out* o, int64_t i0, int64_t i1) {
   for (int64_t i = i0; i < i1; ++i) {
     switch (a->alg) {
-      case ORACLE_RK4: solve_rk4<P>(a, o, i); break;
+      case ORACLE_RK4: solve_onestep<P, RK4<P>>(a, o, i); break;
+      case ORACLE_EULER: solve_onestep<P, Euler<P>>(a, o, i); break;
       case ORACLE_TSIT5: solve_fixed<P, Tsit5<P>>(a, o, i); break;
       case ORACLE_ATSIT5: solve_adaptive<P, Tsit5<P>>(a, o, i); break;
       case ORACLE_VERN7: solve_fixed<P, Vern7<P>>(a, o, i); break;
@@ -1171,11 +1195,11 @@ static void solve_range_prec(const oracle_args* a, oracle_out* o, int64_t i0, in
 
 extern "C" int oracle_solve(const oracle_args* a, oracle_out* o) {
   if (!a || !o || a->n < 0 || a->dim < 1 || a->dim > MAXD || a->nparams < 0 || a->nparams > MAXP) return -1;
-  if (a->alg < 0 || a->alg > ORACLE_SIMPLE_TSIT5) return -1;
+  if (a->alg < 0 || a->alg > ORACLE_EULER) return -1;
   if (a->alg == ORACLE_SIMPLE_ATSIT5 && a->precision != ORACLE_FP64) return -1;
   if (a->precision == ORACLE_FP32_KAHAN && a->rounding != ORACLE_ROUND_DEVICE) return -1;
   const bool fixed = a->alg == ORACLE_RK4 || a->alg == ORACLE_TSIT5 || a->alg == ORACLE_VERN7 ||
-                     a->alg == ORACLE_VERN9 || a->alg == ORACLE_SIMPLE_TSIT5;
+                     a->alg == ORACLE_VERN9 || a->alg == ORACLE_SIMPLE_TSIT5 || a->alg == ORACLE_EULER;
   if (fixed && (!a->grid || a->ngrid < 1)) return -1;
   if (a->rhs == ORACLE_R3BP && a->dim != 4) return -1;
   if (a->rhs == ORACLE_LORENZ && a->dim != 3) return -1;

@@ -21,7 +21,8 @@ enum oracle_alg {
   ORACLE_VERN9 = 5,        /* GPUSimpleVern9         src/verner/gpuvern9.jl:55-353 */
   ORACLE_AVERN9 = 6,       /* GPUSimpleAVern9        src/verner/gpuvern9.jl:411-779 */
   ORACLE_SIMPLE_ATSIT5 = 7,/* SimpleATsit5 integrator src/tsit5/atsit5.jl:117-179,322-413,705-732 */
-  ORACLE_SIMPLE_TSIT5 = 8  /* SimpleTsit5 integrator  src/tsit5/tsit5.jl:84-122,303-352 */
+  ORACLE_SIMPLE_TSIT5 = 8, /* SimpleTsit5 integrator  src/tsit5/tsit5.jl:84-122,303-352 */
+  ORACLE_EULER = 9         /* GPUSimpleEuler         src/euler/gpueuler.jl:53-90 */
 };
 
 enum oracle_rhs { ORACLE_LORENZ = 0, ORACLE_VDP = 1, ORACLE_R3BP = 2, ORACLE_KURAMOTO = 3, ORACLE_LINEAR = 4 };

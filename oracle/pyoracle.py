@@ -20,8 +20,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
 ALG = {"RK4": 0, "Tsit5": 1, "ATsit5": 2, "Vern7": 3, "AVern7": 4, "Vern9": 5, "AVern9": 6,
-       "SimpleATsit5": 7, "SimpleTsit5": 8}
-FIXED = {"RK4", "Tsit5", "Vern7", "Vern9", "SimpleTsit5"}
+       "SimpleATsit5": 7, "SimpleTsit5": 8, "Euler": 9}
+FIXED = {"RK4", "Tsit5", "Vern7", "Vern9", "SimpleTsit5", "Euler"}
 RHS = {"lorenz": 0, "vanderpol": 1, "r3bp": 2, "kuramoto": 3, "linear": 4}
 PREC = {"fp64": 0, "fp32": 1, "fp32_kahan": 2}
 ROUND = {"ref": 0, "device": 1}

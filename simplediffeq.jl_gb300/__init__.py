@@ -51,6 +51,11 @@ class GPUSimpleRK4(_Alg):
     name = "RK4"
 
 
+class GPUSimpleEuler(_Alg):
+    """Fixed-step forward Euler (src/euler/gpueuler.jl:50). Saves every step."""
+    name = "Euler"
+
+
 class GPUSimpleTsit5(_Alg):
     """Fixed-step Tsitouras 5(4) (src/tsit5/gpuatsit5.jl:52)."""
     name = "Tsit5"
@@ -262,8 +267,10 @@ def solve(prob, alg, trajectories=None, dt=0.1, abstol=1e-6, reltol=1e-3, saveat
     u0s, ps = _stack(eprob, n)
     if ps.shape[0] == 0:
         ps = np.zeros((0, n))
-    if alg.name == "RK4":
-        saveat = None  # GPUSimpleRK4 has no saveat keyword (gpurk4.jl:53-58); it saves every step
+    if alg.name in ("RK4", "Euler"):
+        # GPUSimpleRK4 and GPUSimpleEuler have no saveat keyword (gpurk4.jl:53-58, gpueuler.jl:53-58);
+        # they save every step
+        saveat = None
         if save_everystep is None:
             save_everystep = True
     if save_everystep is None:
@@ -320,6 +327,6 @@ def learn_fit(prob, alg, trajectories, device=0, opts=None, **kw):
 
 
 __all__ = ["ODEProblem", "EnsembleProblem", "EnsembleSolution", "ODESolution", "UserRHS", "solve", "learn_fit",
-           "GPUSimpleRK4", "GPUSimpleTsit5", "GPUSimpleATsit5", "GPUSimpleVern7", "GPUSimpleAVern7",
+           "GPUSimpleRK4", "GPUSimpleEuler", "GPUSimpleTsit5", "GPUSimpleATsit5", "GPUSimpleVern7", "GPUSimpleAVern7",
            "GPUSimpleVern9", "GPUSimpleAVern9", "isadaptive", "DtLessThanMin", "GB300ODEError", "Handle",
            "fixed_grid"]

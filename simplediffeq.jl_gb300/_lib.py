@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(HERE, "lib", "libgb300ode.so")
 PROBE_PATH = os.path.join(HERE, "lib", "libgb300ode_probe.so")
 
 OK, EINVAL, ECUDA, ENOMEM, ENOTSUP, ENVRTC, ETRAJ, ENOMODEL = 0, -1, -2, -3, -4, -5, -6, -7
-ALG = {"RK4": 0, "Tsit5": 1, "ATsit5": 2, "Vern7": 3, "AVern7": 4, "Vern9": 5, "AVern9": 6}
+ALG = {"RK4": 0, "Tsit5": 1, "ATsit5": 2, "Vern7": 3, "AVern7": 4, "Vern9": 5, "AVern9": 6, "Euler": 7}
 RHS = {"lorenz": 0, "vanderpol": 1, "r3bp": 2, "kuramoto": 3, "linear": 4}
 PREC = {"fp64": 0, "fp32": 1, "fp32_kahan": 2}
 SCHED = {"plain": 0, "persistent": 1, "learned": 2}

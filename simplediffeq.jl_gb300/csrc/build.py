@@ -29,9 +29,9 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC
 
 # Kernels compiled ahead of time: (alg, kind, rhs, dim, precision, rhs C++ type).
 # Everything else is compiled on first use with NVRTC from the same headers.
-ALG = {"rk4": 0, "tsit5": 1, "atsit5": 2, "vern7": 3, "avern7": 4, "vern9": 5, "avern9": 6}
-METHOD = {"rk4": "gbode::MTsit5", "tsit5": "gbode::MTsit5", "atsit5": "gbode::MTsit5", "vern7": "gbode::MVern7",
-          "avern7": "gbode::MVern7", "vern9": "gbode::MVern9", "avern9": "gbode::MAVern9"}
+ALG = {"rk4": 0, "tsit5": 1, "atsit5": 2, "vern7": 3, "avern7": 4, "vern9": 5, "avern9": 6, "euler": 7}
+METHOD = {"rk4": "gbode::MRK4", "tsit5": "gbode::MTsit5", "atsit5": "gbode::MTsit5", "vern7": "gbode::MVern7",
+          "avern7": "gbode::MVern7", "vern9": "gbode::MVern9", "avern9": "gbode::MAVern9", "euler": "gbode::MEuler"}
 RHS = {"lorenz": 0, "vanderpol": 1, "r3bp": 2, "kuramoto": 3, "linear": 4}
 PREC = {"fp64": (0, "gbode::PFP64", "double", "double"), "fp32": (1, "gbode::PFP32", "float", "float"),
         "fp32k": (2, "gbode::PFP32K", "float", "double")}

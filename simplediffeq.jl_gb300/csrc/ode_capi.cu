@@ -171,11 +171,16 @@ namespace {
  * device must end, and the reference's loop has no cap of its own. */
 const int64_t kDefaultMaxIters = 1000000;
 
-bool is_fixed(int alg) { return alg == ODE_ALG_RK4 || alg == ODE_ALG_TSIT5 || alg == ODE_ALG_VERN7 || alg == ODE_ALG_VERN9; }
+bool is_fixed(int alg) {
+  return alg == ODE_ALG_RK4 || alg == ODE_ALG_TSIT5 || alg == ODE_ALG_VERN7 || alg == ODE_ALG_VERN9 ||
+         alg == ODE_ALG_EULER;
+}
+/* the one-step methods without saveat (they save every grid point) */
+bool is_onestep(int alg) { return alg == ODE_ALG_RK4 || alg == ODE_ALG_EULER; }
 
 const char* alg_name(int alg) {
-  static const char* n[] = {"rk4", "tsit5", "atsit5", "vern7", "avern7", "vern9", "avern9"};
-  return (alg >= 0 && alg <= 6) ? n[alg] : "?";
+  static const char* n[] = {"rk4", "tsit5", "atsit5", "vern7", "avern7", "vern9", "avern9", "euler"};
+  return (alg >= 0 && alg <= 7) ? n[alg] : "?";
 }
 const char* prec_name(int p) {
   static const char* n[] = {"fp64", "fp32", "fp32k"};
@@ -185,7 +190,8 @@ const char* prec_name(int p) {
 /* C++ names used to assemble a kernel for NVRTC */
 const char* method_type(int alg) {
   switch (alg) {
-    case ODE_ALG_RK4: return "gbode::MTsit5";  /* unused by the rk4 entry */
+    case ODE_ALG_RK4: return "gbode::MRK4";
+    case ODE_ALG_EULER: return "gbode::MEuler";
     case ODE_ALG_TSIT5:
     case ODE_ALG_ATSIT5: return "gbode::MTsit5";
     case ODE_ALG_VERN7:
@@ -257,7 +263,7 @@ std::string rhs_type_expr(ode_handle* h, const ode_solve_args* a) {
  * persistent schedules use the staged driver (saveat interpolation batched
  * per warp through shared memory) when there are saveat points. */
 const char* entry_kind(int alg, int sched, int64_t nsave) {
-  if (alg == ODE_ALG_RK4) return "rk4";
+  if (is_onestep(alg)) return "onestep";
   if (is_fixed(alg)) return "fixed";
   if (sched == ODE_SCHED_PLAIN) return "plain";
   return nsave > 0 ? "staged" : "persistent";
@@ -541,7 +547,7 @@ int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o,
   if (!h) return ODE_EINVAL;
   if (!a || !o) return fail(h, ODE_EINVAL, "null argument");
   h->err.clear();
-  if (a->alg < ODE_ALG_RK4 || a->alg > ODE_ALG_AVERN9) return fail(h, ODE_EINVAL, "unknown algorithm");
+  if (a->alg < ODE_ALG_RK4 || a->alg > ODE_ALG_EULER) return fail(h, ODE_EINVAL, "unknown algorithm");
   if (a->precision < ODE_FP64 || a->precision > ODE_FP32_KAHAN) return fail(h, ODE_EINVAL, "unknown precision");
   if (a->schedule < ODE_SCHED_PLAIN || a->schedule > ODE_SCHED_LEARNED) return fail(h, ODE_EINVAL, "unknown schedule");
   if (a->memory != ODE_MEM_HOST && a->memory != ODE_MEM_DEVICE) return fail(h, ODE_EINVAL, "unknown memory kind");
@@ -552,10 +558,10 @@ int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o,
   if (a->nsave < 0 || (a->nsave > 0 && !a->saveat)) return fail(h, ODE_EINVAL, "saveat missing");
   if (a->output != ODE_OUTPUT_STATE && a->output != ODE_OUTPUT_KURAMOTO_R)
     return fail(h, ODE_EINVAL, "unknown output kind");
-  if (a->output == ODE_OUTPUT_KURAMOTO_R && (a->save_everystep || a->alg == ODE_ALG_RK4))
+  if (a->output == ODE_OUTPUT_KURAMOTO_R && (a->save_everystep || is_onestep(a->alg)))
     return fail(h, ODE_EINVAL, "the order-parameter output applies to saveat points");
-  if (a->alg == ODE_ALG_RK4 && a->nsave > 0)
-    return fail(h, ODE_EINVAL, "GPUSimpleRK4 has no saveat (it saves every step; use save_everystep)");
+  if (is_onestep(a->alg) && a->nsave > 0)
+    return fail(h, ODE_EINVAL, "GPUSimpleRK4 and GPUSimpleEuler have no saveat (they save every step; use save_everystep)");
   int rc = check_rhs(h, a);
   if (rc != ODE_OK) return rc;
   const bool fixed = is_fixed(a->alg);

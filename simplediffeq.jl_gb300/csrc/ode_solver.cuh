@@ -690,6 +690,21 @@ struct MRK4 {
   }
 };
 
+/* Forward Euler, src/euler/gpueuler.jl:67-76: k1 = f(u, p, t) with t the END
+ * of the step (t = ts[i], the same quirk as GPUSimpleRK4), u = uprev + dt*k1
+ * (one fused multiply-add; the compensated sum in the Kahan mode). */
+template <class PR, int D, class F>
+struct MEuler {
+  typedef typename PR::R R;
+  typedef typename PR::T T;
+  __device__ static __forceinline__ void step(const F& f, const R (&uh)[D], const R (&uc)[D], T t, T dt,
+                                              R (&nh)[D], R (&nc)[D]) {
+    R k1[D];
+    f(uh, t, k1);
+    state_update<PR, D>(uh, uc, (R)dt, k1, nh, nc);
+  }
+};
+
 /* ------------------------------------------------------------------ per-lane trajectory state */
 template <class PR, int D, class F, int NK>
 struct Lane {
@@ -1250,9 +1265,10 @@ __device__ __forceinline__ void run_fixed(const KParams& P) {
   flush_totals(P, tot);
 }
 
-/* GPUSimpleRK4: saves every grid point when asked (us[1] = u0). */
-template <class PR, int D, class F>
-__device__ __forceinline__ void run_rk4(const KParams& P) {
+/* GPUSimpleRK4 and GPUSimpleEuler (M = MRK4 or MEuler): one step per grid
+ * point, every grid point saved when asked (us[1] = u0). */
+template <class M, class PR, int D, class F>
+__device__ __forceinline__ void run_onestep(const KParams& P) {
   typedef typename PR::R R;
   typedef typename PR::T T;
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1271,7 +1287,7 @@ __device__ __forceinline__ void run_rk4(const KParams& P) {
   R nh[D], nc[D];
   for (long long g = 1; g < P.ngrid; ++g) {
     l.t = (T)P.grid[g];
-    MRK4<PR, D, F>::step(l.f, l.uh, l.uc, l.t, dt, nh, nc);
+    M::step(l.f, l.uh, l.uc, l.t, dt, nh, nc);
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       l.uh[d] = nh[d];
@@ -1294,7 +1310,7 @@ __device__ __forceinline__ void run_rk4(const KParams& P) {
 }  // namespace gbode
 
 /* Entry-point generator: GBODE_ENTRY(name, kind, Method, Prec, Rhs) defines
- * extern "C" __global__ name(KParams).  kind: plain | persistent | staged | fixed | rk4. */
+ * extern "C" __global__ name(KParams).  kind: plain | persistent | staged | fixed | onestep. */
 #define GBODE_ENTRY_plain(NAME, M, PR, RHS)                                                  \
   extern "C" __global__ void __launch_bounds__(GBODE_BLOCK) NAME(gbode::KParams P) {                \
     gbode::run_adaptive_plain<M<PR, RHS::D, RHS>, PR, RHS::D, RHS>(P);                      \
@@ -1311,8 +1327,8 @@ __device__ __forceinline__ void run_rk4(const KParams& P) {
   extern "C" __global__ void __launch_bounds__(GBODE_BLOCK) NAME(gbode::KParams P) {                \
     gbode::run_fixed<M<PR, RHS::D, RHS>, PR, RHS::D, RHS>(P);                               \
   }
-#define GBODE_ENTRY_rk4(NAME, M, PR, RHS)                                                    \
+#define GBODE_ENTRY_onestep(NAME, M, PR, RHS)                                                \
   extern "C" __global__ void __launch_bounds__(GBODE_BLOCK) NAME(gbode::KParams P) {                \
-    gbode::run_rk4<PR, RHS::D, RHS>(P);                                                      \
+    gbode::run_onestep<M<PR, RHS::D, RHS>, PR, RHS::D, RHS>(P);                              \
   }
 #define GBODE_ENTRY(NAME, KIND, M, PR, RHS) GBODE_ENTRY_##KIND(NAME, M, PR, RHS)

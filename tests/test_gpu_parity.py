@@ -70,22 +70,28 @@ def test_tsit5_fixed_lorenz_config1(pkg, po):
     assert (sol.naccept == 100).all()
 
 
-@pytest.mark.parametrize("alg", ["RK4", "Tsit5", "ATsit5", "Vern7", "AVern7", "Vern9", "AVern9"])
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("alg", ["Euler", "RK4", "Tsit5", "ATsit5", "Vern7", "AVern7", "Vern9", "AVern9"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "fp32_kahan"])
 def test_decay_all_algorithms_bitexact(pkg, po, alg, precision):
-    """f(u) = -u, u0 = ones, tspan (0,1) as test/gpu_ode_regression.jl, with saveat."""
+    """f(u) = -u, u0 = ones, tspan (0,1) as test/gpu_ode_regression.jl, with saveat
+    (every step for the one-step methods, which have no saveat)."""
     u0, A = decay_inputs(64)
     algo = getattr(pkg, "GPUSimple" + alg)()
     kw = dict(abstol=1e-7, reltol=1e-7, precision=precision)
-    if alg != "RK4":
+    onestep = alg in ("RK4", "Euler")
+    if not onestep:
         kw["saveat"] = np.array([0.0, 0.4, 1.0])
     dt = 0.01
     sol = gpu(pkg, algo, "linear", u0, A, (0.0, 1.0), dt, **kw)
     ref = po.solve(alg, "linear", u0, A, (0, 1), dt, rounding="device", precision=precision,
-                   abstol=1e-7, reltol=1e-7, saveat=kw.get("saveat"), save_everystep=(alg == "RK4"))
+                   abstol=1e-7, reltol=1e-7, saveat=kw.get("saveat"), save_everystep=onestep)
     assert_bitexact(sol, ref)
-    tol = 5e-3 if precision == "fp32" else 1e-5
-    assert np.abs(sol.u_final - np.exp(-1.0)).max() < tol
+    if alg == "Euler":  # the discrete solution (1 - dt)^k
+        assert np.abs(sol.u_final - 0.99 ** 100).max() < (1e-13 if precision == "fp64" else 1e-5)
+        assert sol.us.shape == (101, 3, 64)
+    else:
+        tol = 5e-3 if precision == "fp32" else 1e-5
+        assert np.abs(sol.u_final - np.exp(-1.0)).max() < tol
 
 
 def test_avern7_vanderpol(pkg, po):

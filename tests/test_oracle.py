@@ -215,3 +215,20 @@ def test_device_canon_sincos_accuracy(po):
         assert ((err <= 2 * np.spacing(np.abs(want))) | (err <= 1e-30)).all()
     assert po.sincos(1e6) == (np.sin(1e6), np.cos(1e6))
     assert all(np.isnan(po.sincos(float("nan"))))
+
+
+@pytest.mark.parametrize("rounding", ["ref", "device"])
+def test_euler_known_answer_and_lorenz_stability(po, rounding):
+    """GPUSimpleEuler (src/euler/gpueuler.jl): on f(u) = -u the discrete solution
+    is (1 - dt)^k at every grid point; and the stability test of
+    test/simpleeuler_tests.jl:40-60 (Lorenz from u0 = 10 ones, dt = 0.01,
+    10,000 steps, no NaN)."""
+    u0, A = decay_inputs(2)
+    o = po.solve("Euler", "linear", u0, A, (0, 1), 0.01, rounding=rounding, save_everystep=True)
+    k = np.arange(101)
+    assert np.abs(o["us"][:, 0, 0] - 0.99 ** k).max() < 1e-14
+    assert o["naccept"][0] == 100
+    u0 = np.full((3, 1), 10.0)
+    p = np.array([[10.0], [28.0], [8 / 3]])
+    o = po.solve("Euler", "lorenz", u0, p, (0, 100.0), 0.01, rounding=rounding)
+    assert np.isfinite(o["u_final"]).all() and o["naccept"][0] == 10000
