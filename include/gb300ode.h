@@ -54,7 +54,8 @@ enum {
   ODE_ENOTSUP = -4,  /* valid but unsupported combination */
   ODE_ENVRTC = -5,   /* run-time compilation of a kernel failed (log in ode_last_error) */
   ODE_ETRAJ = -6,    /* the solve completed but some trajectory ended with retcode DTMIN or MAXITERS */
-  ODE_ENOMODEL = -7  /* learned schedule requested without a fitted model */
+  ODE_ENOMODEL = -7, /* learned schedule requested without a fitted model */
+  ODE_ESMALL = -8    /* output buffers too small: the size needed is reported (ode_ensemble_solve_everystep) */
 };
 
 /* algorithms: the GPUSimple* solver types */
@@ -96,9 +97,10 @@ enum { ODE_MEM_HOST = 0, ODE_MEM_DEVICE = 1 };
 /* what the saveat outputs hold */
 enum {
   ODE_OUTPUT_STATE = 0,      /* us[nsave][dim][n]: the interpolated state (the reference's sol.u) */
-  ODE_OUTPUT_KURAMOTO_R = 1  /* us[nsave][1][n]: r(t) = |(1/dim) sum_k exp(i u_k(t))|, the Kuramoto order
+  ODE_OUTPUT_KURAMOTO_R = 1, /* us[nsave][1][n]: r(t) = |(1/dim) sum_k exp(i u_k(t))|, the Kuramoto order
                                 parameter of the interpolated state, reduced in the kernel (an ensemble
                                 output_func fused into the solve) */
+  ODE_OUTPUT_USER = 1000     /* ids >= ODE_OUTPUT_USER come from ode_output_compile: us[npoints][width][n] */
 };
 
 /* per-trajectory return codes */
@@ -185,6 +187,48 @@ int ode_fixed_grid(double t0, double dt, double tf, int precision, double* out, 
  * float.  On success *rhs_id receives an id usable in ode_solve_args.rhs.
  * Compiler diagnostics go to `log` (may be NULL). */
 int ode_rhs_compile(ode_handle* h, const char* body, int dim, int nparams, int* rhs_id, char* log, size_t loglen);
+
+/* ---- every-step output of the adaptive solvers ---------------------------
+ * The reference's default for GPUSimpleATsit5 / AVern7 / AVern9 without
+ * saveat is save_everystep = true: sol.t and sol.u hold t0, u0 and the time
+ * and state after every accepted step (src/tsit5/gpuatsit5.jl:225-229,
+ * :301-303; gpuvern7.jl:320-324, :428-430; gpuvern9.jl:431-435, :597-599),
+ * a different length for every trajectory.  This call returns that ragged output for the whole ensemble in
+ * two passes: the first counts each trajectory's accepted steps, the second
+ * (same solve, bit-identical) writes the points.  Trajectory i's points are
+ * rows offsets[i] .. offsets[i+1]-1 of ts[rows] and us[rows][dim].
+ * Buffers are host or device memory as a->memory says; `a` must name an
+ * adaptive algorithm, no saveat and the state output.  If ts or us is NULL or
+ * capacity < total, only offsets and total are written and ODE_ESMALL is
+ * returned: allocate total rows and call again.  No counterpart in the
+ * reference beyond the per-trajectory push! it replaces. */
+typedef struct {
+  int64_t* offsets;   /* [n+1] first row of each trajectory; offsets[n] = total */
+  double* ts;         /* [capacity] */
+  double* us;         /* [capacity][dim] */
+  int64_t capacity;   /* rows the ts / us buffers hold */
+  int64_t total;      /* out: rows needed (sum over trajectories of accepted steps + 1) */
+  double* u_final;    /* [dim][n], or NULL */
+  double* t_final;    /* [n], or NULL */
+  int8_t* retcode;    /* [n], or NULL */
+  int32_t* naccept;   /* [n], or NULL */
+  int32_t* nreject;   /* [n], or NULL */
+} ode_everystep_out;
+
+int ode_ensemble_solve_everystep(ode_handle* h, const ode_solve_args* a, ode_everystep_out* o,
+                                 ode_solve_stats* stats);
+
+/* Compile a saveat output function with NVRTC: an ensemble output_func fused
+ * into the solve, applied to every saved point on the device instead of on the
+ * host afterwards.  `body` is the body of
+ *   __device__ void output(double* out, const double* u, const double* p, double t)
+ * which writes `width` values from the saved state u (dim values), the
+ * trajectory's parameters p (nparams values) and the save time t.  With
+ * ode_solve_args.output = *output_id, us holds [npoints][width][n].  Compiler
+ * diagnostics go to `log` (may be NULL).  No counterpart in the reference:
+ * SciMLBase's EnsembleProblem applies output_func on the host, per trajectory. */
+int ode_output_compile(ode_handle* h, const char* body, int dim, int nparams, int width, int* output_id, char* log,
+                       size_t loglen);
 
 /* ---- autotuner ----------------------------------------------------------
  * Times launch-shape variants of the solver kernel (threads per block,

@@ -756,6 +756,19 @@ static void finish(const oracle_args* a, oracle_out* o, int64_t i, const State<t
 
 /* Adaptive driver: the loop of gpuatsit5.jl:250-320 / gpuvern7.jl:353-520 /
  * gpuvern9.jl:461-763 with the controller of :279-299. */
+/* Row k of trajectory i's every-step output (gpuatsit5.jl:225-229, :301-303:
+ * push!(us, u); push!(ts, t) after each accepted step, u0 first). */
+template <class R>
+static void put_step(const oracle_args* a, oracle_out* o, int64_t i, int64_t k, double t, const State<R>& st,
+                     bool kahan) {
+  if (!o->ev_t) return;
+  double v[MAXD];
+  value_of(st, a->dim, kahan, v);
+  const int64_t r = o->ev_off[i] + k;
+  o->ev_t[r] = t;
+  for (int d = 0; d < a->dim; ++d) o->ev_u[r * a->dim + d] = v[d];
+}
+
 template <class P, class M>
 static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
   typedef typename P::R R;
@@ -790,6 +803,7 @@ static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
   if (M::FSAL) A.f(st.hi, (double)t, k[0]);
   int ret = RET_DEFAULT;
   int32_t nacc = 0, nrej = 0;
+  put_step(a, o, i, 0, (double)t, st, P::KAHAN);
   int64_t attempts = 0;
   double dt_first = NAN;
   bool saw_nan = false;
@@ -851,6 +865,7 @@ static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
             ++cur;
           }
           st = un;
+          put_step(a, o, i, nacc, (double)t, st, P::KAHAN);
           if (M::FSAL)
             for (int d = 0; d < D; ++d) k[0][d] = k[6][d];
         }
@@ -883,6 +898,7 @@ static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
             ++cur;
           }
           st = un;
+          put_step(a, o, i, nacc, (double)t, st, P::KAHAN);
           if (M::FSAL)
             for (int d = 0; d < D; ++d) k[0][d] = k[6][d];
         }

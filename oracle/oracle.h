@@ -59,6 +59,12 @@ typedef struct {
   int32_t* naccept;  /* [n]; may be NULL */
   int32_t* nreject;  /* [n]; may be NULL */
   double* dt_first;  /* [n] dt of the first accepted step; may be NULL */
+  /* every-step output of the adaptive solvers (save_everystep without saveat):
+   * trajectory i's rows start at ev_off[i]; row k holds the time and state
+   * after its k-th accepted step (k = 0: t0, u0).  NULL to skip. */
+  const int64_t* ev_off;
+  double* ev_t;      /* [rows] */
+  double* ev_u;      /* [rows][dim] */
 } oracle_out;
 
 int oracle_solve(const oracle_args* a, oracle_out* o);

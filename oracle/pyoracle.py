@@ -41,7 +41,8 @@ class _Args(ctypes.Structure):
 class _Out(ctypes.Structure):
     _fields_ = [("us", ctypes.c_void_p), ("u_final", ctypes.c_void_p), ("t_final", ctypes.c_void_p),
                 ("retcode", ctypes.c_void_p), ("naccept", ctypes.c_void_p), ("nreject", ctypes.c_void_p),
-                ("dt_first", ctypes.c_void_p)]
+                ("dt_first", ctypes.c_void_p), ("ev_off", ctypes.c_void_p), ("ev_t", ctypes.c_void_p),
+                ("ev_u", ctypes.c_void_p)]
 
 
 _lib = None
@@ -220,8 +221,19 @@ def solve(alg, rhs, u0, p, tspan, dt, precision="fp64", rounding="ref", abstol=1
                  _ptr(grid), 0 if grid is None else len(grid), int(maxiters), _ptr(u0), _ptr(p), _ptr(d0),
                  int(nthreads), 1 if output == "kuramoto_r" else 0)
     o = _Out(_ptr(out["us"]), _ptr(out["u_final"]), _ptr(out["t_final"]), _ptr(out["retcode"]),
-             _ptr(out["naccept"]), _ptr(out["nreject"]), _ptr(out["dt_first"]))
+             _ptr(out["naccept"]), _ptr(out["nreject"]), _ptr(out["dt_first"]), None, None, None)
     rc = lib().oracle_solve(ctypes.byref(args), ctypes.byref(o))
     if rc != 0:
         raise ValueError("oracle_solve rejected the arguments (rc=%d)" % rc)
+    if save_everystep and sv is None and alg not in FIXED:
+        # every-step output (ragged): count accepted steps, then solve again writing the rows
+        off = np.zeros(n + 1, dtype=np.int64)
+        off[1:] = np.cumsum(out["naccept"].astype(np.int64) + 1)
+        ts = np.full(off[-1], np.nan)
+        us = np.full((off[-1], dim), np.nan)
+        o.ev_off, o.ev_t, o.ev_u = _ptr(off), _ptr(ts), _ptr(us)
+        rc = lib().oracle_solve(ctypes.byref(args), ctypes.byref(o))
+        if rc != 0:
+            raise ValueError("oracle_solve rejected the arguments (rc=%d)" % rc)
+        out.update(offsets=off, ts_rows=ts, us_rows=us)
     return out

@@ -104,6 +104,16 @@ class UserRHS:
         self.body, self.dim, self.nparams = body, int(dim), int(nparams)
 
 
+class UserOutput:
+    """An ensemble output function fused into the solve: the C++ body of
+    ``__device__ void output(double* out, const double* u, const double* p, double t)``
+    writing ``width`` values per saved point, compiled with NVRTC on first use.
+    SciMLBase's ``output_func`` would run on the host for every trajectory."""
+
+    def __init__(self, body, width):
+        self.body, self.width = body, int(width)
+
+
 _BUILTIN_DIMS = {"lorenz": (3, 3), "vanderpol": (2, 1), "r3bp": (4, 1)}
 
 
@@ -157,17 +167,27 @@ class EnsembleSolution:
     """Results of an ensemble solve, kept as structure-of-arrays:
     ``us`` (npoints, dim, n), ``u_final`` (dim, n), ``t_final`` (n,),
     ``retcode``, ``naccept``, ``nreject`` (n,), ``t`` (the save times).
+    With every-step output of an adaptive solver the points are ragged:
+    trajectory i's times and states are rows ``offsets[i]:offsets[i+1]`` of
+    ``ts_rows`` (rows,) and ``us_rows`` (rows, dim).
     ``sol[i]`` builds the ODESolution of trajectory i (0-based)."""
 
-    def __init__(self, t, us, u_final, t_final, retcode, naccept, nreject, dt_first, stats):
+    def __init__(self, t, us, u_final, t_final, retcode, naccept, nreject, dt_first, stats, offsets=None,
+                 ts_rows=None, us_rows=None):
         self.t, self.us, self.u_final, self.t_final = t, us, u_final, t_final
         self.retcode, self.naccept, self.nreject, self.dt_first = retcode, naccept, nreject, dt_first
         self.stats = stats
+        self.offsets, self.ts_rows, self.us_rows = offsets, ts_rows, us_rows
 
     def __len__(self):
         return self.u_final.shape[1]
 
     def __getitem__(self, i):
+        if self.offsets is not None:
+            a, b = int(self.offsets[i]), int(self.offsets[i + 1])
+            return ODESolution(self.ts_rows[a:b].copy(), [self.us_rows[r].copy() for r in range(a, b)],
+                               _RETNAMES.get(int(self.retcode[i]), "Failure"), int(self.naccept[i]),
+                               int(self.nreject[i]))
         if self.us is not None:
             u = [self.us[j, :, i].copy() for j in range(self.us.shape[0])]
             t = self.t
@@ -201,6 +221,18 @@ def _rhs_id(h, f):
             cache[key] = h.compile_rhs(f.body, f.dim, f.nparams)
         return cache[key]
     raise TypeError("f must be a built-in name or a UserRHS (Python callables cannot run on the GPU)")
+
+
+def _output_id(h, output, dim, nparams):
+    if isinstance(output, UserOutput):
+        cache = h.__dict__.setdefault("_output_ids", {})
+        key = (output.body, output.width, dim, nparams)
+        if key not in cache:
+            cache[key] = h.compile_output(output.body, dim, nparams, output.width)
+        return cache[key]
+    if output not in _lib.OUTPUT:
+        raise ValueError("output must be 'state', 'kuramoto_r' or a UserOutput")
+    return _lib.OUTPUT[output]
 
 
 def _stack(eprob, trajectories):
@@ -240,7 +272,7 @@ def make_args(alg, f_id, u0s, ps, tspan, dt, abstol, reltol, saveat, save_everys
     a.maxiters = int(maxiters)
     a.u0, a.p = u0s.ctypes.data, ps.ctypes.data
     a.dt0 = None if dt0 is None else dt0.ctypes.data
-    a.output = _lib.OUTPUT[output]
+    a.output = output if isinstance(output, int) else _lib.OUTPUT[output]
     return a
 
 
@@ -251,9 +283,11 @@ def solve(prob, alg, trajectories=None, dt=0.1, abstol=1e-6, reltol=1e-3, saveat
 
     Unknown keyword arguments are accepted and ignored, as the reference's
     ``kwargs...`` swallows them.  ``save_everystep`` defaults to False for
-    ensembles (adaptive per-step output is ragged and not produced) and applies
-    to the fixed-step algorithms; GPUSimpleRK4 ignores ``saveat`` as the
-    reference does."""
+    ensembles; with ``save_everystep=True`` and no ``saveat`` an adaptive
+    solver returns every accepted step, a different number per trajectory
+    (ragged output, as the reference's default for one trajectory); for the
+    fixed-step algorithms it saves every grid point.  GPUSimpleRK4 and
+    GPUSimpleEuler ignore ``saveat`` as the reference does."""
     single = isinstance(prob, ODEProblem)
     eprob = EnsembleProblem(prob) if single else prob
     base = eprob.prob
@@ -275,16 +309,15 @@ def solve(prob, alg, trajectories=None, dt=0.1, abstol=1e-6, reltol=1e-3, saveat
             save_everystep = True
     if save_everystep is None:
         save_everystep = False
-    if save_everystep and saveat is None and alg.adaptive:
-        raise NotImplementedError("save_everystep=true for adaptive ensembles (ragged output) is not produced")
+    ragged = bool(save_everystep) and saveat is None and alg.adaptive
     sv = None if saveat is None else np.ascontiguousarray(np.asarray(saveat, dtype=np.float64))
     if not alg.adaptive:
         schedule = "plain"
+    dim = u0s.shape[0]
     args = make_args(alg, fid, u0s, ps, base.tspan, dt, abstol, reltol, sv, save_everystep, precision, schedule,
                      maxiters, dt0=None if dt0 is None else np.ascontiguousarray(dt0, dtype=np.float64),
-                     output=output)
-    dim = u0s.shape[0]
-    width = 1 if output == "kuramoto_r" else dim
+                     output=_output_id(h, output, dim, ps.shape[0]))
+    width = output.width if isinstance(output, UserOutput) else (1 if output == "kuramoto_r" else dim)
     if sv is not None:
         npts = len(sv)
         tpts = sv
@@ -293,10 +326,12 @@ def solve(prob, alg, trajectories=None, dt=0.1, abstol=1e-6, reltol=1e-3, saveat
         npts = len(tpts)
     else:
         npts, tpts = 0, None
-    us = np.empty((npts, width, n)) if npts else None
     out = {"u_final": np.empty((dim, n)), "t_final": np.empty(n), "retcode": np.empty(n, dtype=np.int8),
            "naccept": np.empty(n, dtype=np.int32), "nreject": np.empty(n, dtype=np.int32),
            "dt_first": np.empty(n)}
+    if ragged:
+        return _solve_everystep(h, args, out, n, dim, throw, single)
+    us = np.empty((npts, width, n)) if npts else None
     o = _lib.SolveOut()
     o.us = None if us is None else us.ctypes.data
     for k, v in out.items():
@@ -306,6 +341,34 @@ def solve(prob, alg, trajectories=None, dt=0.1, abstol=1e-6, reltol=1e-3, saveat
     h.check(rc, allow=(_lib.ETRAJ,))
     sol = EnsembleSolution(tpts, us, out["u_final"], out["t_final"], out["retcode"], out["naccept"],
                            out["nreject"], out["dt_first"], st)
+    if rc == _lib.ETRAJ and throw:
+        if (out["retcode"] == _lib.RET_DTMIN).any():
+            raise DtLessThanMin("dt<dtmin")
+        raise RuntimeError("maxiters reached")
+    return sol[0] if single else sol
+
+
+def _solve_everystep(h, args, out, n, dim, throw, single):
+    """save_everystep = true without saveat for an adaptive solver: ragged
+    output through ode_ensemble_solve_everystep (count, then fill)."""
+    args.save_everystep = 0
+    offsets = np.empty(n + 1, dtype=np.int64)
+    eo = _lib.EverystepOut()
+    eo.offsets = offsets.ctypes.data
+    for k in ("u_final", "t_final", "retcode", "naccept", "nreject"):
+        setattr(eo, k, out[k].ctypes.data)
+    st = _lib.SolveStats()
+    rc = h.solve_everystep(args, eo, st)
+    if rc != _lib.ESMALL:
+        h.check(rc, allow=(_lib.ETRAJ,))
+    ts = np.empty(eo.total)
+    us = np.empty((eo.total, dim))
+    eo.ts, eo.us, eo.capacity = ts.ctypes.data, us.ctypes.data, eo.total
+    rc = h.solve_everystep(args, eo, st)
+    h.check(rc, allow=(_lib.ETRAJ,))
+    out["dt_first"][:] = np.nan
+    sol = EnsembleSolution(None, None, out["u_final"], out["t_final"], out["retcode"], out["naccept"],
+                           out["nreject"], out["dt_first"], st, offsets=offsets, ts_rows=ts, us_rows=us)
     if rc == _lib.ETRAJ and throw:
         if (out["retcode"] == _lib.RET_DTMIN).any():
             raise DtLessThanMin("dt<dtmin")
@@ -326,7 +389,7 @@ def learn_fit(prob, alg, trajectories, device=0, opts=None, **kw):
     return h.learn_fit(args, opts)
 
 
-__all__ = ["ODEProblem", "EnsembleProblem", "EnsembleSolution", "ODESolution", "UserRHS", "solve", "learn_fit",
-           "GPUSimpleRK4", "GPUSimpleEuler", "GPUSimpleTsit5", "GPUSimpleATsit5", "GPUSimpleVern7", "GPUSimpleAVern7",
+__all__ = ["ODEProblem", "EnsembleProblem", "EnsembleSolution", "ODESolution", "UserRHS", "UserOutput", "solve",
+           "learn_fit", "GPUSimpleRK4", "GPUSimpleEuler", "GPUSimpleTsit5", "GPUSimpleATsit5", "GPUSimpleVern7", "GPUSimpleAVern7",
            "GPUSimpleVern9", "GPUSimpleAVern9", "isadaptive", "DtLessThanMin", "GB300ODEError", "Handle",
            "fixed_grid"]

@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libgb300ode.so")
 PROBE_PATH = os.path.join(HERE, "lib", "libgb300ode_probe.so")
 
-OK, EINVAL, ECUDA, ENOMEM, ENOTSUP, ENVRTC, ETRAJ, ENOMODEL = 0, -1, -2, -3, -4, -5, -6, -7
+OK, EINVAL, ECUDA, ENOMEM, ENOTSUP, ENVRTC, ETRAJ, ENOMODEL, ESMALL = 0, -1, -2, -3, -4, -5, -6, -7, -8
 ALG = {"RK4": 0, "Tsit5": 1, "ATsit5": 2, "Vern7": 3, "AVern7": 4, "Vern9": 5, "AVern9": 6, "Euler": 7}
 RHS = {"lorenz": 0, "vanderpol": 1, "r3bp": 2, "kuramoto": 3, "linear": 4}
 PREC = {"fp64": 0, "fp32": 1, "fp32_kahan": 2}
@@ -24,8 +24,9 @@ RET_DEFAULT, RET_DTMIN, RET_MAXITERS, RET_NAN = 0, 1, 2, 3
 
 # Every symbol include/gb300ode.h declares.
 EXPORTS = ["ode_abi_version", "ode_create", "ode_destroy", "ode_last_error", "ode_ensemble_solve",
-           "ode_fixed_grid", "ode_rhs_compile", "ode_learn_default_opts", "ode_learn_fit", "ode_learn_predict",
-           "ode_learn_gradcheck", "ode_ensemble_solve_noalloc", "ode_autotune"]
+           "ode_fixed_grid", "ode_rhs_compile", "ode_output_compile", "ode_learn_default_opts", "ode_learn_fit",
+           "ode_learn_predict", "ode_learn_gradcheck", "ode_ensemble_solve_noalloc", "ode_autotune",
+           "ode_ensemble_solve_everystep"]
 
 
 class SolveArgs(ctypes.Structure):
@@ -43,6 +44,13 @@ class SolveOut(ctypes.Structure):
     _fields_ = [("us", ctypes.c_void_p), ("u_final", ctypes.c_void_p), ("t_final", ctypes.c_void_p),
                 ("retcode", ctypes.c_void_p), ("naccept", ctypes.c_void_p), ("nreject", ctypes.c_void_p),
                 ("dt_first", ctypes.c_void_p)]
+
+
+class EverystepOut(ctypes.Structure):
+    _fields_ = [("offsets", ctypes.c_void_p), ("ts", ctypes.c_void_p), ("us", ctypes.c_void_p),
+                ("capacity", ctypes.c_int64), ("total", ctypes.c_int64), ("u_final", ctypes.c_void_p),
+                ("t_final", ctypes.c_void_p), ("retcode", ctypes.c_void_p), ("naccept", ctypes.c_void_p),
+                ("nreject", ctypes.c_void_p)]
 
 
 class SolveStats(ctypes.Structure):
@@ -106,10 +114,14 @@ def load():
     lib.ode_last_error.restype = ctypes.c_char_p
     lib.ode_ensemble_solve.argtypes = [ctypes.c_void_p, ctypes.POINTER(SolveArgs), ctypes.POINTER(SolveOut),
                                        ctypes.POINTER(SolveStats)]
+    lib.ode_ensemble_solve_everystep.argtypes = [ctypes.c_void_p, ctypes.POINTER(SolveArgs),
+                                                 ctypes.POINTER(EverystepOut), ctypes.POINTER(SolveStats)]
     lib.ode_fixed_grid.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                    ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
     lib.ode_rhs_compile.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(ctypes.c_int), ctypes.c_char_p, ctypes.c_size_t]
+    lib.ode_output_compile.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.POINTER(ctypes.c_int), ctypes.c_char_p, ctypes.c_size_t]
     lib.ode_learn_default_opts.argtypes = [ctypes.POINTER(LearnOpts)]
     lib.ode_learn_default_opts.restype = None
     lib.ode_learn_fit.argtypes = [ctypes.c_void_p, ctypes.POINTER(SolveArgs), ctypes.POINTER(LearnOpts),
@@ -171,6 +183,10 @@ class Handle:
         return self.lib.ode_ensemble_solve(self.h, ctypes.byref(args), ctypes.byref(out),
                                            ctypes.byref(stats) if stats is not None else None)
 
+    def solve_everystep(self, args, out, stats=None):
+        return self.lib.ode_ensemble_solve_everystep(self.h, ctypes.byref(args), ctypes.byref(out),
+                                                     ctypes.byref(stats) if stats is not None else None)
+
     def compile_rhs(self, body, dim, nparams):
         rid = ctypes.c_int(0)
         log = ctypes.create_string_buffer(8192)
@@ -178,6 +194,15 @@ class Handle:
         if rc != OK:
             raise GB300ODEError(rc, self.error())
         return rid.value
+
+    def compile_output(self, body, dim, nparams, width):
+        oid = ctypes.c_int(0)
+        log = ctypes.create_string_buffer(8192)
+        rc = self.lib.ode_output_compile(self.h, body.encode(), int(dim), int(nparams), int(width), ctypes.byref(oid),
+                                         log, 8192)
+        if rc != OK:
+            raise GB300ODEError(rc, self.error() + "\n" + log.value.decode(errors="replace"))
+        return oid.value
 
     def learn_fit(self, args, opts=None):
         o = LearnOpts()

@@ -281,17 +281,37 @@ int stage_job_bytes(const ode_solve_args* a) {
   return 4 * t + 8 + nrec * r + 4;
 }
 
+/* values stored per saveat point and trajectory */
+int output_width(ode_handle* h, const ode_solve_args* a) {
+  if (a->output == ODE_OUTPUT_KURAMOTO_R) return 1;
+  if (a->output >= ODE_OUTPUT_USER) return h->outputs[a->output - ODE_OUTPUT_USER].width;
+  return a->dim;
+}
+
 std::string kernel_key(ode_handle* h, const ode_solve_args* a, int sched) {
   char b[160];
-  snprintf(b, sizeof b, "%s|%s|%d|%d|%s", alg_name(a->alg), entry_kind(a->alg, sched, a->nsave), a->rhs, a->dim,
-           prec_name(a->precision));
+  snprintf(b, sizeof b, "%s|%s|%d|%d|%s|%d", alg_name(a->alg), entry_kind(a->alg, sched, a->nsave), a->rhs, a->dim,
+           prec_name(a->precision), a->output >= ODE_OUTPUT_USER ? a->output : 0);
   return b;
 }
 
 /* Source of the one-kernel translation unit for (algorithm, rhs, precision,
  * dim, schedule kind). */
 std::string jit_source(ode_handle* h, const ode_solve_args* a, int sched) {
-  std::string src = "#include \"ode_solver.cuh\"\n";
+  std::string src;
+  if (a->output >= ODE_OUTPUT_USER) {
+    /* the output function goes before the solver header, whose store_point calls it */
+    const UserOutput& u = h->outputs[a->output - ODE_OUTPUT_USER];
+    char hdr[256];
+    snprintf(hdr, sizeof hdr, "#define GBODE_USER_OUTPUT 1\n#define GBODE_OUTPUT_WIDTH %d\n#define GBODE_OUTPUT_NP %d\n",
+             u.width, u.nparams);
+    src += hdr;
+    src += "__device__ __forceinline__ void gbode_user_output(double* out, const double* u, const double* p, "
+           "double t) {\n";
+    src += u.body;
+    src += "\n}\n";
+  }
+  src += "#include \"ode_solver.cuh\"\n";
   if (a->rhs >= ODE_RHS_USER) {
     const UserRhs& u = h->users[a->rhs - ODE_RHS_USER];
     char hdr[256];
@@ -387,8 +407,8 @@ int get_kernel(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn
   }
   const char* kind = entry_kind(a->alg, sched, a->nsave);
   for (const AotEntry& e : kAotEntries) {
-    if (e.alg == a->alg && e.rhs == a->rhs && e.dim == a->dim && e.precision == a->precision &&
-        std::strcmp(e.kind, kind) == 0) {
+    if (a->output < ODE_OUTPUT_USER && e.alg == a->alg && e.rhs == a->rhs && e.dim == a->dim &&
+        e.precision == a->precision && std::strcmp(e.kind, kind) == 0) {
       cudaFunction_t f;
       cudaError_t ce = cudaGetFuncBySymbol(&f, e.fn);
       if (ce != cudaSuccess) return cuda_fail(h, ce, "cudaGetFuncBySymbol");
@@ -542,7 +562,50 @@ int ode_rhs_compile(ode_handle* h, const char* body, int dim, int nparams, int* 
   return ODE_OK;
 }
 
-int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_solve_stats* st) {
+int ode_output_compile(ode_handle* h, const char* body, int dim, int nparams, int width, int* output_id, char* log,
+                       size_t loglen) {
+  if (!h) return ODE_EINVAL;
+  if (!body || !output_id || dim < 1 || dim > 32 || nparams < 0 || nparams > 256 || width < 1 || width > 64)
+    return fail(h, ODE_EINVAL, "ode_output_compile: bad arguments");
+  /* compile the function alone now so that syntax errors surface here; the
+   * solver kernels that use it are compiled on first use */
+  char hdr[160];
+  snprintf(hdr, sizeof hdr, "#define GBODE_OUTPUT_WIDTH %d\n#define GBODE_OUTPUT_NP %d\n", width, nparams);
+  std::string src = hdr;
+  src += "__device__ __forceinline__ void gbode_user_output(double* out, const double* u, const double* p, double t) {\n";
+  src += body;
+  src += "\n}\nextern \"C\" __global__ void gbode_output_probe(double* out, const double* u, const double* p, "
+         "double t) {\n  gbode_user_output(out, u, p, t);\n}\n";
+  std::vector<char> cubin;
+  std::string lg, err;
+  const int rc = nvrtc_cubin(src, {}, &cubin, &lg, &err);
+  if (log && loglen) {
+    std::strncpy(log, lg.c_str(), loglen - 1);
+    log[loglen - 1] = '\0';
+  }
+  if (rc != ODE_OK) return fail(h, rc, err.empty() ? "output function did not compile (see log)" : err);
+  UserOutput u;
+  u.body = body;
+  u.dim = dim;
+  u.nparams = nparams;
+  u.width = width;
+  h->outputs.push_back(u);
+  *output_id = ODE_OUTPUT_USER + (int)h->outputs.size() - 1;
+  return ODE_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+/* Device pointers of the every-step output (ode_ensemble_solve_everystep). */
+struct EveryStep {
+  const long long* off;
+  double* t;
+  double* u;
+};
+
+int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_solve_stats* st, const EveryStep* ev) {
   const auto wall0 = std::chrono::steady_clock::now();
   if (!h) return ODE_EINVAL;
   if (!a || !o) return fail(h, ODE_EINVAL, "null argument");
@@ -556,8 +619,14 @@ int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o,
   if (!(a->t0 == a->t0) || !(a->tf == a->tf) || !(a->dt == a->dt))
     return fail(h, ODE_EINVAL, "t0, tf and dt must not be NaN");
   if (a->nsave < 0 || (a->nsave > 0 && !a->saveat)) return fail(h, ODE_EINVAL, "saveat missing");
-  if (a->output != ODE_OUTPUT_STATE && a->output != ODE_OUTPUT_KURAMOTO_R)
+  if (a->output >= ODE_OUTPUT_USER) {
+    if (a->output >= ODE_OUTPUT_USER + (int)h->outputs.size()) return fail(h, ODE_EINVAL, "unknown output function");
+    const UserOutput& u = h->outputs[a->output - ODE_OUTPUT_USER];
+    if (u.dim != a->dim || u.nparams != a->nparams)
+      return fail(h, ODE_EINVAL, "the output function was compiled for another dim / nparams");
+  } else if (a->output != ODE_OUTPUT_STATE && a->output != ODE_OUTPUT_KURAMOTO_R) {
     return fail(h, ODE_EINVAL, "unknown output kind");
+  }
   if (a->output == ODE_OUTPUT_KURAMOTO_R && (a->save_everystep || is_onestep(a->alg)))
     return fail(h, ODE_EINVAL, "the order-parameter output applies to saveat points");
   if (is_onestep(a->alg) && a->nsave > 0)
@@ -649,7 +718,7 @@ int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o,
   /* outputs */
   struct OutMap { void* host; const char* name; size_t bytes; void** dev; };
   OutMap outs[] = {
-      {o->us, "us", (size_t)npoints * (a->output == ODE_OUTPUT_KURAMOTO_R ? 1 : D) * nd, (void**)&kp.us},
+      {o->us, "us", (size_t)npoints * output_width(h, a) * nd, (void**)&kp.us},
       {o->u_final, "u_final", nd * D, (void**)&kp.u_final},
       {o->t_final, "t_final", nd, (void**)&kp.t_final},
       {o->retcode, "retcode", (size_t)n, (void**)&kp.retcode},
@@ -666,6 +735,11 @@ int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o,
     } else {
       *m.dev = m.host;
     }
+  }
+  if (ev) {
+    kp.ev_off = ev->off;
+    kp.ev_t = ev->t;
+    kp.ev_u = ev->u;
   }
   unsigned long long* stats = (unsigned long long*)buf(h, "stats", 4 * sizeof(unsigned long long), &rc);
   if (!stats) return rc;
@@ -796,6 +870,101 @@ int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o,
   return ODE_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_solve_stats* st) {
+  return solve_impl(h, a, o, st, nullptr);
+}
+
+/* Ragged every-step output in two passes: count, prefix-sum on the host,
+ * solve again writing each accepted step at its row. */
+int ode_ensemble_solve_everystep(ode_handle* h, const ode_solve_args* a, ode_everystep_out* o,
+                                 ode_solve_stats* st) {
+  if (!h) return ODE_EINVAL;
+  if (!a || !o || !o->offsets) return fail(h, ODE_EINVAL, "null argument");
+  if (is_fixed(a->alg)) return fail(h, ODE_EINVAL, "every-step output is for the adaptive algorithms");
+  if (a->nsave != 0 || a->output != ODE_OUTPUT_STATE)
+    return fail(h, ODE_EINVAL, "every-step output takes no saveat and the state output");
+  if (a->memory != ODE_MEM_HOST && a->memory != ODE_MEM_DEVICE) return fail(h, ODE_EINVAL, "unknown memory kind");
+  if (a->n < 0 || a->n > 0x7fffffffLL) return fail(h, ODE_EINVAL, "n must be in [0, 2^31)");
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  const int64_t n = a->n;
+  const int D = a->dim;
+  const bool host = a->memory == ODE_MEM_HOST;
+  cudaStream_t s = a->stream ? (cudaStream_t)a->stream : h->stream;
+  int rc = ODE_OK;
+
+  /* pass 1: accepted steps per trajectory */
+  std::vector<int32_t> counts((size_t)n);
+  {
+    ode_solve_args a1 = *a;
+    a1.save_everystep = 0;
+    ode_solve_out o1;
+    std::memset(&o1, 0, sizeof o1);
+    int32_t* dcount = nullptr;
+    if (host) {
+      o1.naccept = counts.data();
+    } else {
+      if (!(dcount = (int32_t*)buf(h, "ev_count", (size_t)n * 4, &rc))) return rc;
+      o1.naccept = dcount;
+    }
+    rc = solve_impl(h, &a1, &o1, nullptr, nullptr);
+    if (rc != ODE_OK && rc != ODE_ETRAJ) return rc;
+    if (!host && n > 0) {
+      CK(cudaMemcpyAsync(counts.data(), dcount, (size_t)n * 4, cudaMemcpyDeviceToHost, s), "copy counts");
+      CK(cudaStreamSynchronize(s), "sync counts");
+    }
+  }
+  std::vector<long long> off((size_t)n + 1);
+  off[0] = 0;
+  for (int64_t i = 0; i < n; ++i) off[(size_t)i + 1] = off[(size_t)i] + (long long)counts[(size_t)i] + 1;
+  const int64_t total = off[(size_t)n];
+  o->total = total;
+  const size_t offbytes = ((size_t)n + 1) * sizeof(long long);
+  if (host) {
+    std::memcpy(o->offsets, off.data(), offbytes);
+  } else {
+    CK(cudaMemcpyAsync(o->offsets, off.data(), offbytes, cudaMemcpyHostToDevice, s), "copy offsets");
+    CK(cudaStreamSynchronize(s), "sync offsets");
+  }
+  if (!o->ts || !o->us || o->capacity < total)
+    return fail(h, ODE_ESMALL, "every-step buffers too small: total rows needed are in ode_everystep_out.total");
+
+  /* pass 2: the same solve, writing each accepted step */
+  EveryStep ev;
+  if (host) {
+    long long* doff = (long long*)buf(h, "ev_off", offbytes, &rc);
+    if (!doff) return rc;
+    double* dt = (double*)buf(h, "ev_t", (size_t)total * sizeof(double), &rc);
+    if (!dt) return rc;
+    double* du = (double*)buf(h, "ev_u", (size_t)total * D * sizeof(double), &rc);
+    if (!du) return rc;
+    CK(cudaMemcpyAsync(doff, off.data(), offbytes, cudaMemcpyHostToDevice, s), "copy offsets");
+    ev = EveryStep{doff, dt, du};
+  } else {
+    ev = EveryStep{(const long long*)o->offsets, o->ts, o->us};
+  }
+  ode_solve_args a2 = *a;
+  a2.save_everystep = 0;
+  ode_solve_out o2;
+  std::memset(&o2, 0, sizeof o2);
+  o2.u_final = o->u_final;
+  o2.t_final = o->t_final;
+  o2.retcode = o->retcode;
+  o2.naccept = o->naccept;
+  o2.nreject = o->nreject;
+  rc = solve_impl(h, &a2, &o2, st, &ev);
+  if (rc != ODE_OK && rc != ODE_ETRAJ) return rc;
+  if (host && total > 0) {
+    CK(cudaMemcpyAsync(o->ts, ev.t, (size_t)total * sizeof(double), cudaMemcpyDeviceToHost, s), "copy ts");
+    CK(cudaMemcpyAsync(o->us, ev.u, (size_t)total * D * sizeof(double), cudaMemcpyDeviceToHost, s), "copy us");
+    CK(cudaStreamSynchronize(s), "sync every-step output");
+  }
+  return rc;
+}
+
 /* Autotuner: time launch-shape variants of the solver kernel on a sample of
  * the caller's ensemble and keep the fastest for this handle.  Variants are
  * compiled with NVRTC in parallel; they differ in threads per block, register
@@ -828,7 +997,7 @@ int ode_autotune(ode_handle* h, const ode_solve_args* a, int64_t sample, ode_tun
     if (!(ddt0 = (double*)buf(h, "tune_dt0", (size_t)m * 8, &rc))) return rc;
     CK(cudaMemcpyAsync(ddt0, a->dt0, m * 8, kind, s), "copy sample dt0");
   }
-  const int width = a->output == ODE_OUTPUT_KURAMOTO_R ? 1 : D;
+  const int width = output_width(h, a);
   double* dus = nullptr;
   if (a->nsave > 0 && !(dus = (double*)buf(h, "tune_us", (size_t)a->nsave * width * m * 8, &rc))) return rc;
   double* duf = (double*)buf(h, "tune_uf", (size_t)m * D * 8, &rc);

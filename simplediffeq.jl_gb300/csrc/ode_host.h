@@ -24,6 +24,12 @@ struct UserRhs {
   int dim = 0, nparams = 0;
 };
 
+/* a saveat output function compiled into the solver kernel */
+struct UserOutput {
+  std::string body;
+  int dim = 0, nparams = 0, width = 0;
+};
+
 struct Model;  /* learned-schedule model, defined in learn.cu */
 
 struct GraphEntry {
@@ -50,6 +56,7 @@ struct ode_handle {
   std::map<CUfunction, int> fblock;         /* threads per block of run-time compiled functions */
   std::vector<CUmodule> modules;
   std::vector<gbode::UserRhs> users;
+  std::vector<gbode::UserOutput> outputs;
   gbode::GraphEntry graph;
   gbode::Model* model = nullptr;
 };

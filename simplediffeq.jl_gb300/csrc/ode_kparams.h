@@ -29,6 +29,9 @@ struct KParams {
   int* naccept;            /* [n] or 0 */
   int* nreject;            /* [n] or 0 */
   double* dt_first;        /* [n] or 0 */
+  const long long* ev_off; /* every-step output: trajectory i's points are rows ev_off[i].., or 0 */
+  double* ev_t;            /* [rows] time of each accepted step (t0 first) */
+  double* ev_u;            /* [rows][dim] state after each accepted step (u0 first) */
   const int* order;        /* persistent: position -> trajectory, or 0 for identity */
   unsigned long long* counter;   /* persistent: next position to hand out (zeroed before launch) */
   unsigned long long* stats;     /* [2] attempts and saves summed over trajectories, or 0 */

@@ -727,6 +727,22 @@ struct Lane {
 template <class PR, int D>
 __device__ __forceinline__ void store_point(const KParams& P, long long idx, long long j, const double (&v)[D]) {
   if (!P.us) return;
+#ifdef GBODE_USER_OUTPUT
+  /* a user output function (ode_output_compile), defined before this header by
+   * the run-time compiled translation unit together with GBODE_OUTPUT_WIDTH and
+   * GBODE_OUTPUT_NP */
+  if (P.output >= 1000) {
+    double pv[GBODE_OUTPUT_NP > 0 ? GBODE_OUTPUT_NP : 1];
+#pragma unroll
+    for (int q = 0; q < GBODE_OUTPUT_NP; ++q) pv[q] = P.p[(long long)q * P.n + idx];
+    const double t = P.saveat ? P.saveat[j] : P.grid[j];
+    double o[GBODE_OUTPUT_WIDTH];
+    gbode_user_output(o, v, pv, t);
+#pragma unroll
+    for (int w = 0; w < GBODE_OUTPUT_WIDTH; ++w) P.us[(j * GBODE_OUTPUT_WIDTH + w) * P.n + idx] = o[w];
+    return;
+  }
+#endif
   if (P.output == 1) {
     double C = 0.0, S = 0.0;
 #pragma unroll
@@ -747,6 +763,20 @@ template <class PR, int D, class L>
 __device__ __forceinline__ void state_value(const L& l, double (&v)[D]) {
 #pragma unroll
   for (int d = 0; d < D; ++d) v[d] = PR::KAHAN ? (double)l.uh[d] - (double)l.uc[d] : (double)l.uh[d];
+}
+
+/* Every-step output (save_everystep = true without saveat, the reference's
+ * push!(us, u); push!(ts, t) after each accepted step, gpuatsit5.jl:301-303):
+ * row k of trajectory l.idx is the state after its k-th accepted step. */
+template <class PR, int D, class L>
+__device__ __forceinline__ void store_step(const KParams& P, const L& l, long long k) {
+  if (!P.ev_t) return;
+  const long long r = P.ev_off[l.idx] + k;
+  double v[D];
+  state_value<PR, D>(l, v);
+  P.ev_t[r] = (double)l.t;
+#pragma unroll
+  for (int d = 0; d < D; ++d) P.ev_u[r * D + d] = v[d];
 }
 
 /* Load trajectory idx: parameters, u0, t0, dt; first saveat point if it is t0. */
@@ -778,6 +808,7 @@ __device__ __forceinline__ void lane_load(const KParams& P, long long idx, Lane<
     store_point<PR, D>(P, idx, 0, v);
     l.cur = 1;
   }
+  store_step<PR, D>(P, l, 0);
 }
 
 /* Attempts, dense-output points and early stops summed over the trajectories
@@ -950,6 +981,7 @@ __device__ __forceinline__ bool adaptive_iter(const KParams& P, Lane<PR, D, F, N
     l.ninterp += 1;
   }
   adaptive_commit<M>(l, nh, nc);
+  store_step<PR, D>(P, l, l.nacc);
   if (!(l.t < (T)P.tf)) { lane_finish(P, l, RET_DEFAULT, tot); return true; }
   return false;
 }
@@ -1187,6 +1219,7 @@ __device__ __forceinline__ void run_adaptive_staged(const KParams& P) {
     qcount += total < space ? total : space;
     if (r == TRY_ACCEPTED) {
       adaptive_commit<M>(l, nh, nc);
+      store_step<PR, D>(P, l, l.nacc);
       if (!(l.t < (T)P.tf)) {
         lane_finish(P, l, RET_DEFAULT, tot);
         active = false;

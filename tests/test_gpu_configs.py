@@ -160,3 +160,92 @@ def test_autotuner_keeps_results(pkg):
           % (rep.block, rep.max_registers, rep.stage_bytes, rep.best_ms, rep.default_ms, rep.variants, rep.tune_ms))
     after = pkg.solve(e, pkg.GPUSimpleATsit5(), trajectories=n, **kw)
     assert np.array_equal(before.u_final, after.u_final) and np.array_equal(before.us, after.us)
+
+
+@pytest.mark.parametrize("schedule", ["plain", "persistent"])
+def test_user_output_function_fused_into_the_solve(pkg, schedule):
+    """An ensemble output function compiled with NVRTC (ode_output_compile):
+    at every saved point the kernel stores (|u|^2, sigma*u0*u1 + t) instead of
+    the state.  It equals the same arithmetic applied to the kernel's own
+    full-state output, bit for bit (the body has no fusable multiply-add pairs
+    that the host evaluates differently), for adaptive saveat and for the
+    fixed-step save-every-step grid."""
+    from conftest import lorenz_inputs
+    u0, p = lorenz_inputs(3000, seed=51)
+    e = pkg.EnsembleProblem(pkg.ODEProblem("lorenz", u0[:, 0], (0.0, 10.0), p[:, 0]), u0s=u0, ps=p)
+    out = pkg.UserOutput("double s = u[0] * u[0];\n s = s + u[1] * u[1];\n out[0] = s + u[2] * u[2];\n"
+                         " double q = p[0] * u[0];\n out[1] = q * u[1] + t;", width=2)
+    sv = np.linspace(0, 10, 37)
+    kw = dict(dt=0.1, abstol=1e-8, reltol=1e-6, saveat=sv, schedule=schedule)
+    a = pkg.solve(e, pkg.GPUSimpleATsit5(), trajectories=3000, output=out, **kw)
+    b = pkg.solve(e, pkg.GPUSimpleATsit5(), trajectories=3000, **kw)
+    assert a.us.shape == (37, 2, 3000)
+    s = b.us[:, 0, :] * b.us[:, 0, :]
+    s = s + b.us[:, 1, :] * b.us[:, 1, :]
+    assert np.array_equal(a.us[:, 0, :], s + b.us[:, 2, :] * b.us[:, 2, :])
+    q = p[0][None, :] * b.us[:, 0, :]
+    assert np.array_equal(a.us[:, 1, :], q * b.us[:, 1, :] + sv[:, None])
+    assert np.array_equal(a.u_final, b.u_final)
+    # fixed step, every grid point
+    c = pkg.solve(e, pkg.GPUSimpleTsit5(), trajectories=3000, dt=0.05, save_everystep=True, output=out)
+    d = pkg.solve(e, pkg.GPUSimpleTsit5(), trajectories=3000, dt=0.05, save_everystep=True)
+    assert c.us.shape == (201, 2, 3000)
+    q = p[0][None, :] * d.us[:, 0, :]
+    assert np.array_equal(c.us[:, 1, :], q * d.us[:, 1, :] + pkg.fixed_grid(0.0, 0.05, 10.0)[:, None])
+
+
+def test_user_output_compile_errors_are_reported(pkg):
+    h = pkg._handle(0)
+    with pytest.raises(pkg.GB300ODEError) as e:
+        h.compile_output("out[0] = u[0] +;", 3, 3, 1)
+    assert e.value.code == -5  # ODE_ENVRTC
+
+
+@pytest.mark.parametrize("schedule", ["plain", "persistent"])
+def test_every_step_output_bitexact(pkg, po, schedule):
+    """Ragged every-step output of the adaptive solvers (two passes: count, then
+    fill) against the oracle's rows, through the Python API (host buffers) and
+    the C ABI with device buffers, including the ODE_ESMALL size protocol."""
+    from conftest import lorenz_inputs
+    import torch
+    u0, p = lorenz_inputs(1500, seed=61)
+    e = pkg.EnsembleProblem(pkg.ODEProblem("lorenz", u0[:, 0], (0.0, 5.0), p[:, 0]), u0s=u0, ps=p)
+    kw = dict(abstol=1e-8, reltol=1e-6)
+    sol = pkg.solve(e, pkg.GPUSimpleATsit5(), trajectories=1500, dt=0.1, save_everystep=True, schedule=schedule,
+                    **kw)
+    ref = po.solve("ATsit5", "lorenz", u0, p, (0, 5), 0.1, rounding="device", save_everystep=True, nthreads=8, **kw)
+    assert np.array_equal(sol.offsets, ref["offsets"])
+    assert np.array_equal(sol.ts_rows, ref["ts_rows"]) and np.array_equal(sol.us_rows, ref["us_rows"])
+    assert np.array_equal(sol.u_final, ref["u_final"]) and np.array_equal(sol.naccept, ref["naccept"])
+    tr = sol[7]
+    assert tr.t[0] == 0.0 and tr.t[-1] == 5.0 and len(tr.u) == sol.naccept[7] + 1
+    # the C ABI with device buffers: first call reports the size, second fills
+    L = pkg._lib
+    h = pkg._handle(0)
+    du0 = torch.tensor(u0, device="cuda")
+    dp = torch.tensor(p, device="cuda")
+    a = pkg.make_args(pkg.GPUSimpleATsit5(), 0, u0, p, (0.0, 5.0), 0.1, 1e-8, 1e-6, None, False, "fp64", schedule,
+                      0, memory=L.MEM_DEVICE)
+    a.u0, a.p = du0.data_ptr(), dp.data_ptr()
+    off = torch.empty(1501, dtype=torch.int64, device="cuda")
+    o = L.EverystepOut()
+    o.offsets = off.data_ptr()
+    assert h.solve_everystep(a, o) == L.ESMALL
+    assert o.total == ref["offsets"][-1]
+    ts = torch.empty(o.total, dtype=torch.float64, device="cuda")
+    us = torch.empty((o.total, 3), dtype=torch.float64, device="cuda")
+    o.ts, o.us, o.capacity = ts.data_ptr(), us.data_ptr(), o.total
+    h.check(h.solve_everystep(a, o))
+    assert np.array_equal(off.cpu().numpy(), ref["offsets"])
+    assert np.array_equal(ts.cpu().numpy(), ref["ts_rows"]) and np.array_equal(us.cpu().numpy(), ref["us_rows"])
+
+
+def test_every_step_output_verner_fp32_kahan(pkg, po):
+    u0, mu = make_golden.r3bp(256, 5)
+    sol = pkg.solve(pkg.EnsembleProblem(pkg.ODEProblem("r3bp", u0[:, 0], (0.0, 2.0), mu[:, 0]), u0s=u0, ps=mu),
+                    pkg.GPUSimpleAVern9(), trajectories=256, dt=0.1, save_everystep=True, precision="fp32_kahan",
+                    abstol=1e-7, reltol=1e-7, throw=False)
+    ref = po.solve("AVern9", "r3bp", u0, mu, (0, 2), 0.1, rounding="device", precision="fp32_kahan",
+                   save_everystep=True, abstol=1e-7, reltol=1e-7, nthreads=8)
+    assert np.array_equal(sol.offsets, ref["offsets"])
+    assert np.array_equal(sol.ts_rows, ref["ts_rows"]) and np.array_equal(sol.us_rows, ref["us_rows"])

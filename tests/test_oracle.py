@@ -232,3 +232,31 @@ def test_euler_known_answer_and_lorenz_stability(po, rounding):
     p = np.array([[10.0], [28.0], [8 / 3]])
     o = po.solve("Euler", "lorenz", u0, p, (0, 100.0), 0.01, rounding=rounding)
     assert np.isfinite(o["u_final"]).all() and o["naccept"][0] == 10000
+
+
+def test_every_step_output_rows(po):
+    """GPUSimpleATsit5's default save_everystep = true without saveat
+    (src/tsit5/gpuatsit5.jl:225-229, :301-303): t0/u0, then the time and state
+    after each accepted step.  Restated from test/gpusimpleatsit5_tests.jl:28-39:
+    the last time equals the save_everystep = false solve's final time."""
+    u0 = np.full((3, 1), 10.0)
+    p = np.array([[10.0], [28.0], [8 / 3]])
+    kw = dict(abstol=1e-6, reltol=1e-3)
+    ev = po.solve("ATsit5", "lorenz", u0, p, (0, 100), 1e-2, save_everystep=True, **kw)
+    fin = po.solve("ATsit5", "lorenz", u0, p, (0, 100), 1e-2, **kw)
+    off, ts, us = ev["offsets"], ev["ts_rows"], ev["us_rows"]
+    assert off[1] == ev["naccept"][0] + 1
+    assert ts[0] == 0.0 and np.array_equal(us[0], u0[:, 0])
+    assert ts[-1] == fin["t_final"][0] == 100.0
+    assert np.array_equal(us[-1], fin["u_final"][:, 0])
+    assert (np.diff(ts) > 0).all()
+    # the Verner solvers too (gpuvern7.jl:428-430, gpuvern9.jl:597-599), in both rounding modes:
+    # one row per accepted step plus u0, the last row the final state
+    for alg, rhs, u, pp, tsp in (("AVern7", "vanderpol", np.array([[2.0], [0.0]]), np.array([[1.5]]), (0, 5)),
+                                 ("AVern9", "r3bp", np.array([[0.994], [0.0], [0.0], [-2.00158510637908]]),
+                                  np.array([[0.012277471]]), (0, 1))):
+        for rounding in ("ref", "device"):
+            e = po.solve(alg, rhs, u, pp, tsp, 0.1, rounding=rounding, save_everystep=True, abstol=1e-9, reltol=1e-9)
+            f = po.solve(alg, rhs, u, pp, tsp, 0.1, rounding=rounding, abstol=1e-9, reltol=1e-9)
+            assert len(e["ts_rows"]) == f["naccept"][0] + 1
+            assert np.array_equal(e["us_rows"][-1], f["u_final"][:, 0])
