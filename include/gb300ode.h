@@ -230,6 +230,51 @@ int ode_ensemble_solve_everystep(ode_handle* h, const ode_solve_args* a, ode_eve
 int ode_output_compile(ode_handle* h, const char* body, int dim, int nparams, int width, int* output_id, char* log,
                        size_t loglen);
 
+/* ---- SimpleEM: Euler-Maruyama SDE ensembles ---------------------------------
+ * DiffEqBase.solve(prob::SDEProblem, SimpleEM(); dt), src/euler_maruyama.jl:48-98
+ * (out-of-place, diagonal noise), for a whole ensemble:
+ *   n = Int((tf - t0)/dt) + 1 points t_k = t0 + k*dt,
+ *   u_{k+1} = u_k + f(u_k, p, t_k)*dt + sqrt(dt)*g(u_k, p, t_k) .* xi_k.
+ * The reference draws xi_k with Julia's randn; here xi_k comes from a
+ * counter-based generator (Philox4x32-10 keyed by `seed`, counter = step,
+ * component pair, trajectory; Box-Muller with the library's own log and
+ * sin/cos), so results depend only on (seed, trajectory index, step) and are
+ * reproducible on the CPU.  Non-diagonal noise (a noise_rate_prototype
+ * matrix) is not supported. */
+enum {
+  ODE_SDE_GBM = 0,     /* geometric Brownian motion: f = mu u, g = sigma u (any dim), p = (mu, sigma) */
+  ODE_SDE_OU = 1,      /* Ornstein-Uhlenbeck: f = theta (mu - u), g = sigma (any dim), p = (theta, mu, sigma) */
+  ODE_SDE_LORENZ = 2,  /* Lorenz drift, additive noise: dim 3, p = (sigma, rho, beta, noise) */
+  ODE_SDE_USER = 1000
+};
+
+typedef struct {
+  int32_t sde;            /* ODE_SDE_* or an id from ode_sde_compile */
+  int64_t n;              /* trajectories */
+  int32_t dim, nparams;
+  double t0, tf, dt;      /* (tf - t0)/dt must be an integer (the reference's Int(...) throws otherwise) */
+  uint64_t seed;
+  int32_t save_everystep; /* 1: every grid point (what the reference returns); 0: final state only */
+  int32_t memory;         /* ODE_MEM_HOST or ODE_MEM_DEVICE */
+  const double* u0;       /* [dim][n] */
+  const double* p;        /* [nparams][n] */
+  void* stream;           /* cudaStream_t, or NULL */
+} ode_sde_args;
+
+typedef struct {
+  double* us;             /* [npoints][dim][n] (save_everystep), or NULL */
+  double* u_final;        /* [dim][n], or NULL */
+} ode_sde_out;
+
+int ode_sde_solve(ode_handle* h, const ode_sde_args* a, ode_sde_out* o, ode_solve_stats* stats);
+
+/* Compile a user SDE with NVRTC: `drift` and `diffusion` are the bodies of
+ *   __device__ void drift(double* f, const double* u, const double* p, double t)
+ *   __device__ void diffusion(double* g, const double* u, const double* p, double t)
+ * (diagonal noise: g has dim components). */
+int ode_sde_compile(ode_handle* h, const char* drift, const char* diffusion, int dim, int nparams, int* sde_id,
+                    char* log, size_t loglen);
+
 /* ---- autotuner ----------------------------------------------------------
  * Times launch-shape variants of the solver kernel (threads per block,
  * register cap, bytes of the per-warp saveat staging ring) on the first

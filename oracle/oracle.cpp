@@ -9,6 +9,7 @@
  *   GPUSimpleVern9 / GPUSimpleAVern9   src/verner/gpuvern9.jl:55-353, :411-779
  *   GPUSimpleRK4                       src/rk4/gpurk4.jl:53-98
  *   GPUSimpleEuler                     src/euler/gpueuler.jl:53-90
+ *   SimpleEM (SDE, diagonal noise)     src/euler_maruyama.jl:48-98
  *   SimpleATsit5 (integrator form)     src/tsit5/atsit5.jl:117-179, :322-413, :705-732
  *   SimpleTsit5 (integrator form)      src/tsit5/tsit5.jl:84-122, :303-352, :358-399
  *   PI controller constants            src/SimpleDiffEq.jl:67-77, src/tsit5/atsit5.jl:57-62
@@ -1239,6 +1240,147 @@ extern "C" int oracle_solve(const oracle_args* a, oracle_out* o) {
   }
   for (auto& x : th) x.join();
   return 0;
+}
+
+/* ---------------------------------------------------------------- SimpleEM */
+namespace {
+
+/* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy
+ * as 1, 2, 3", SC'11): 10 rounds of two 32x32->64 multiplies and a key bump. */
+void philox(const uint32_t* cin, const uint32_t* kin, uint32_t* out) {
+  uint32_t c0 = cin[0], c1 = cin[1], c2 = cin[2], c3 = cin[3], k0 = kin[0], k1 = kin[1];
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0, n1 = (uint32_t)p1;
+    const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1, n3 = (uint32_t)p0;
+    c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+/* log of a positive normal double, device canon: x = m 2^e with m in
+ * [sqrt(1/2), sqrt(2)), log m = 2 atanh(s) = 2 (s + s^3/3 + ... + s^23/23),
+ * s = (m-1)/(m+1), plus e (LN2_HI + LN2_LO) with LN2_HI of 42 bits. */
+double log_dev(double x) {
+  uint64_t b;
+  std::memcpy(&b, &x, 8);
+  int e = (int)((b >> 52) & 0x7ff) - 1023;
+  const uint64_t mb = (b & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL;
+  double m;
+  std::memcpy(&m, &mb, 8);
+  if (m > 0x1.6a09e667f3bcdp+0) {
+    m = m * 0.5;
+    e += 1;
+  }
+  const double s = (m - 1.0) / (m + 1.0);
+  const double z = s * s;
+  double q = 1.0 / 23.0;
+  for (int k = 10; k >= 1; --k) q = std::fma(q, z, 1.0 / (double)(2 * k + 1));
+  const double t2 = s + s;
+  const double lm = std::fma(t2 * z, q, t2);
+  const double de = (double)e;
+  return std::fma(de, 0x1.62e42fefa38p-1, std::fma(de, 0x1.ef35793c7673p-45, lm));
+}
+
+void normal_pair(uint64_t seed, int64_t k, int j, int64_t idx, double* z0, double* z1) {
+  const uint32_t c[4] = {(uint32_t)k, (uint32_t)j, (uint32_t)idx, (uint32_t)((uint64_t)idx >> 32)};
+  const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  uint32_t r[4];
+  philox(c, key, r);
+  const uint64_t a = ((uint64_t)(r[0] >> 5) << 26) | (r[1] >> 6);
+  const uint64_t cc = ((uint64_t)(r[2] >> 5) << 26) | (r[3] >> 6);
+  const double u1 = (double)(a + 1) * 0x1.0p-53;
+  const double u2 = (double)cc * 0x1.0p-53;
+  const double rad = std::sqrt(-2.0 * log_dev(u1));
+  double sn, cs;
+  sincos_dev(u2 * 0x1.921fb54442d18p+2, &sn, &cs);
+  *z0 = rad * cs;
+  *z1 = rad * sn;
+}
+
+/* drift and diffusion of the built-in SDEs; the Lorenz drift in the REF/DEV
+ * forms of rhs_eval */
+void sde_fg(const oracle_sde_args* a, bool dev, const double* u, const double* p, double* f, double* g) {
+  const int D = a->dim;
+  switch (a->sde) {
+    case ORACLE_SDE_GBM:
+      for (int d = 0; d < D; ++d) { f[d] = p[0] * u[d]; g[d] = p[1] * u[d]; }
+      break;
+    case ORACLE_SDE_OU:
+      for (int d = 0; d < D; ++d) { f[d] = p[0] * (p[1] - u[d]); g[d] = p[2]; }
+      break;
+    default:
+      f[0] = p[0] * (u[1] - u[0]);
+      if (dev) {
+        f[1] = std::fma(u[0], p[1] - u[2], -u[1]);
+        f[2] = std::fma(u[0], u[1], -(p[2] * u[2]));
+      } else {
+        f[1] = u[0] * (p[1] - u[2]) - u[1];
+        f[2] = u[0] * u[1] - p[2] * u[2];
+      }
+      for (int d = 0; d < 3; ++d) g[d] = p[3];
+  }
+}
+
+/* src/euler_maruyama.jl:66-91 for trajectory i: t_k = t0 + k dt (scalar
+ * muladd), u += f dt + sqrt(dt) g .* xi; REF rounds (u + f dt) + (sqdt g) xi
+ * with a separate multiply and add each, DEV fuses both. */
+void solve_em(const oracle_sde_args* a, int64_t i) {
+  const int D = a->dim;
+  const bool dev = a->rounding == ORACLE_ROUND_DEVICE;
+  double u[MAXD], p[MAXP], f[MAXD], g[MAXD], xi[MAXD + 1];
+  for (int q = 0; q < a->nparams; ++q) p[q] = a->p[q * a->n + i];
+  for (int d = 0; d < D; ++d) u[d] = a->u0[d * a->n + i];
+  if (a->us)
+    for (int d = 0; d < D; ++d) a->us[d * a->n + i] = u[d];
+  const double sqdt = std::sqrt(a->dt);
+  for (int64_t k = 0; k < a->nsteps; ++k) {
+    const double t = std::fma((double)k, a->dt, a->t0);
+    (void)t;  /* the built-in SDEs are autonomous */
+    sde_fg(a, dev, u, p, f, g);
+    for (int j = 0; j < (D + 1) / 2; ++j) normal_pair(a->seed, k, j, i, &xi[2 * j], &xi[2 * j + 1]);
+    for (int d = 0; d < D; ++d) {
+      const double sg = sqdt * g[d];
+      u[d] = dev ? std::fma(sg, xi[d], std::fma(f[d], a->dt, u[d])) : (u[d] + f[d] * a->dt) + sg * xi[d];
+    }
+    if (a->us)
+      for (int d = 0; d < D; ++d) a->us[((k + 1) * D + d) * a->n + i] = u[d];
+  }
+  if (a->u_final)
+    for (int d = 0; d < D; ++d) a->u_final[d * a->n + i] = u[d];
+}
+
+}  // namespace
+
+extern "C" int oracle_sde_solve(const oracle_sde_args* a) {
+  if (!a || a->n < 0 || a->dim < 1 || a->dim > MAXD || a->nparams < 0 || a->nparams > MAXP || a->nsteps < 0)
+    return -1;
+  if (a->sde == ORACLE_SDE_GBM && a->nparams != 2) return -1;
+  if (a->sde == ORACLE_SDE_OU && a->nparams != 3) return -1;
+  if (a->sde == ORACLE_SDE_LORENZ && (a->dim != 3 || a->nparams != 4)) return -1;
+  if (a->sde < 0 || a->sde > ORACLE_SDE_LORENZ) return -1;
+  int nt = a->nthreads > 0 ? a->nthreads : 1;
+  if ((int64_t)nt > a->n) nt = (int)std::max<int64_t>(1, a->n);
+  auto run = [&](int64_t i0, int64_t i1) {
+    for (int64_t i = i0; i < i1; ++i) solve_em(a, i);
+  };
+  std::vector<std::thread> th;
+  const int64_t chunk = (a->n + nt - 1) / nt;
+  for (int w = 0; w < nt; ++w) {
+    const int64_t i0 = w * chunk, i1 = std::min<int64_t>(a->n, i0 + chunk);
+    if (i0 >= i1) break;
+    th.emplace_back(run, i0, i1);
+  }
+  for (auto& x : th) x.join();
+  return 0;
+}
+
+extern "C" void oracle_philox(const uint32_t* c, const uint32_t* k, uint32_t* out) { philox(c, k, out); }
+extern "C" double oracle_log(double x) { return log_dev(x); }
+extern "C" void oracle_normal_pair(uint64_t seed, int64_t k, int j, int64_t idx, double* z0, double* z1) {
+  normal_pair(seed, k, j, idx, z0, z1);
 }
 
 extern "C" float oracle_ctrl_pow(float x, float b) { return oracle_pow::ctrl_pow(x, b); }

@@ -68,6 +68,30 @@ typedef struct {
 } oracle_out;
 
 int oracle_solve(const oracle_args* a, oracle_out* o);
+
+/* SimpleEM (src/euler_maruyama.jl:48-98), diagonal noise, with the counter-based
+ * normals of the device canon (Philox4x32-10 + Box-Muller). */
+enum oracle_sde { ORACLE_SDE_GBM = 0, ORACLE_SDE_OU = 1, ORACLE_SDE_LORENZ = 2 };
+typedef struct {
+  int sde, rounding;
+  int64_t n;
+  int dim, nparams;
+  double t0, dt;
+  int64_t nsteps;
+  uint64_t seed;
+  const double* u0;  /* [dim][n] */
+  const double* p;   /* [nparams][n] */
+  double* us;        /* [nsteps+1][dim][n] or NULL */
+  double* u_final;   /* [dim][n] or NULL */
+  int nthreads;
+} oracle_sde_args;
+int oracle_sde_solve(const oracle_sde_args* a);
+/* Philox4x32-10 of counter c[4] under key k[2] into out[4] */
+void oracle_philox(const uint32_t* c, const uint32_t* k, uint32_t* out);
+/* the device canon's double logarithm */
+double oracle_log(double x);
+/* components 2j, 2j+1 of the step-k normal vector of trajectory idx */
+void oracle_normal_pair(uint64_t seed, int64_t k, int j, int64_t idx, double* z0, double* z1);
 float oracle_ctrl_pow(float x, float b);
 /* the device canon's double sine and cosine (Cody-Waite reduction, Taylor polynomials) */
 void oracle_sincos(double x, double* s, double* c);

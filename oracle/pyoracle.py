@@ -45,6 +45,16 @@ class _Out(ctypes.Structure):
                 ("ev_u", ctypes.c_void_p)]
 
 
+class _SdeArgs(ctypes.Structure):
+    _fields_ = [("sde", ctypes.c_int), ("rounding", ctypes.c_int), ("n", ctypes.c_int64), ("dim", ctypes.c_int),
+                ("nparams", ctypes.c_int), ("t0", ctypes.c_double), ("dt", ctypes.c_double),
+                ("nsteps", ctypes.c_int64), ("seed", ctypes.c_uint64), ("u0", ctypes.c_void_p),
+                ("p", ctypes.c_void_p), ("us", ctypes.c_void_p), ("u_final", ctypes.c_void_p),
+                ("nthreads", ctypes.c_int)]
+
+
+SDE = {"gbm": 0, "ou": 1, "lorenz": 2}
+
 _lib = None
 
 
@@ -64,6 +74,14 @@ def lib():
         _lib.oracle_ctrl_pow.restype = ctypes.c_float
         _lib.oracle_sincos.argtypes = [ctypes.c_double, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         _lib.oracle_sincos.restype = None
+        _lib.oracle_sde_solve.argtypes = [ctypes.POINTER(_SdeArgs)]
+        _lib.oracle_philox.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        _lib.oracle_philox.restype = None
+        _lib.oracle_log.argtypes = [ctypes.c_double]
+        _lib.oracle_log.restype = ctypes.c_double
+        _lib.oracle_normal_pair.argtypes = [ctypes.c_uint64, ctypes.c_int64, ctypes.c_int, ctypes.c_int64,
+                                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+        _lib.oracle_normal_pair.restype = None
         _lib.oracle_mlp_forward_backward.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int64] + [ctypes.c_void_p] * 5
     return _lib
 
@@ -237,3 +255,48 @@ def solve(alg, rhs, u0, p, tspan, dt, precision="fp64", rounding="ref", abstol=1
             raise ValueError("oracle_solve rejected the arguments (rc=%d)" % rc)
         out.update(offsets=off, ts_rows=ts, us_rows=us)
     return out
+
+
+def sde_grid_steps(t0, tf, dt):
+    """n - 1 of SimpleEM's n = Int((tf - t0)/dt) + 1; ValueError where Julia's Int() throws."""
+    q = (float(tf) - float(t0)) / float(dt)
+    if q != np.floor(q) or q < 0:
+        raise ValueError("InexactError: (tf - t0)/dt = %r is not an integer" % q)
+    return int(q)
+
+
+def sde_solve(sde, u0, p, tspan, dt, seed, rounding="device", save_everystep=True, nthreads=1):
+    """SimpleEM (src/euler_maruyama.jl:48-98) for n trajectories with the device
+    canon's counter-based normals.  Returns u_final (dim, n) and, with
+    save_everystep, us (npoints, dim, n) and the grid t."""
+    u0 = np.ascontiguousarray(u0, dtype=np.float64)
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    dim, n = u0.shape
+    nsteps = sde_grid_steps(tspan[0], tspan[1], dt)
+    us = np.full((nsteps + 1, dim, n), np.nan) if save_everystep else None
+    uf = np.zeros((dim, n))
+    a = _SdeArgs(SDE[sde], ROUND[rounding], n, dim, p.shape[0], float(tspan[0]), float(dt), nsteps, int(seed),
+                 _ptr(u0), _ptr(p), _ptr(us), _ptr(uf), int(nthreads))
+    if lib().oracle_sde_solve(ctypes.byref(a)) != 0:
+        raise ValueError("oracle_sde_solve rejected the arguments")
+    # t_k = fma(k, dt, t0): one rounding of the exact value
+    t = np.array([float(Fraction(k) * Fraction(float(dt)) + Fraction(float(tspan[0]))) for k in range(nsteps + 1)])
+    return {"u_final": uf, "us": us, "t": t}
+
+
+def philox(counter, key):
+    c = (ctypes.c_uint32 * 4)(*counter)
+    k = (ctypes.c_uint32 * 2)(*key)
+    out = (ctypes.c_uint32 * 4)()
+    lib().oracle_philox(c, k, out)
+    return list(out)
+
+
+def log_dev(x):
+    return lib().oracle_log(float(x))
+
+
+def normal_pair(seed, k, j, idx):
+    z0, z1 = ctypes.c_double(), ctypes.c_double()
+    lib().oracle_normal_pair(int(seed), int(k), int(j), int(idx), ctypes.byref(z0), ctypes.byref(z1))
+    return z0.value, z1.value

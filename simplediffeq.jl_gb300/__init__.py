@@ -137,6 +137,36 @@ class ODEProblem:
                           self.p if p is None else p, self.inplace)
 
 
+class SimpleEM(_Alg):
+    """Fixed-step Euler-Maruyama for SDEProblems (src/euler_maruyama.jl:48).
+    The noise comes from a counter-based generator keyed by ``seed``."""
+    name = "EM"
+
+
+class UserSDE:
+    """A user SDE with diagonal noise: the C++ bodies of
+    ``__device__ void drift(double* f, const double* u, const double* p, double t)`` and
+    ``__device__ void diffusion(double* g, const double* u, const double* p, double t)``,
+    compiled with NVRTC on first use."""
+
+    def __init__(self, drift, diffusion, dim, nparams):
+        self.drift, self.diffusion, self.dim, self.nparams = drift, diffusion, int(dim), int(nparams)
+
+
+class SDEProblem:
+    """Out-of-place SDE du = f(u, p, t) dt + g(u, p, t) .* dW with diagonal noise.
+    ``sde`` is "gbm" (f = mu u, g = sigma u; p = (mu, sigma)), "ou"
+    (f = theta (mu - u), g = sigma; p = (theta, mu, sigma)), "lorenz"
+    (Lorenz drift, additive noise; p = (sigma, rho, beta, noise)) or a UserSDE."""
+
+    def __init__(self, sde, u0, tspan, p=(), inplace=False):
+        self.f = sde
+        self.u0 = np.atleast_1d(np.asarray(u0, dtype=np.float64))
+        self.tspan = (float(tspan[0]), float(tspan[1]))
+        self.p = np.atleast_1d(np.asarray(p, dtype=np.float64)) if np.size(p) else np.zeros(0)
+        self.inplace = bool(inplace)
+
+
 class EnsembleProblem:
     """SciMLBase.EnsembleProblem: ``prob_func(prob, i, repeat)`` returns the
     problem of trajectory i (1-based, as in Julia), or pass the stacked initial
@@ -288,8 +318,11 @@ def solve(prob, alg, trajectories=None, dt=0.1, abstol=1e-6, reltol=1e-3, saveat
     (ragged output, as the reference's default for one trajectory); for the
     fixed-step algorithms it saves every grid point.  GPUSimpleRK4 and
     GPUSimpleEuler ignore ``saveat`` as the reference does."""
-    single = isinstance(prob, ODEProblem)
+    single = isinstance(prob, (ODEProblem, SDEProblem))
     eprob = EnsembleProblem(prob) if single else prob
+    if isinstance(eprob.prob, SDEProblem) or isinstance(alg, SimpleEM):
+        return _solve_sde(eprob, alg, 1 if single else trajectories, dt, save_everystep, device, single,
+                          kwargs.get("seed", 0))
     base = eprob.prob
     if base.inplace:
         raise AssertionError("!isinplace(prob)")  # @assert !isinplace(prob) in every GPUSimple solve
@@ -376,6 +409,55 @@ def _solve_everystep(h, args, out, n, dim, throw, single):
     return sol[0] if single else sol
 
 
+def _solve_sde(eprob, alg, n, dt, save_everystep, device, single, seed):
+    """SimpleEM over the ensemble (ode_sde_solve); saves every grid point by
+    default, as the reference does."""
+    base = eprob.prob
+    if not isinstance(base, SDEProblem) or not isinstance(alg, SimpleEM):
+        raise TypeError("SimpleEM solves SDEProblems, and SDEProblems need SimpleEM")
+    if base.inplace:
+        raise NotImplementedError("in-place SDE functions: give the out-of-place form")
+    if n is None:
+        n = eprob.u0s.shape[1] if eprob.u0s is not None else 1
+    h = _handle(device)
+    u0s, ps = _stack(eprob, n)
+    dim, nparams = u0s.shape[0], ps.shape[0]
+    if ps.shape[0] == 0:
+        ps = np.zeros((0, n))
+    if isinstance(base.f, UserSDE):
+        cache = h.__dict__.setdefault("_sde_ids", {})
+        key = (base.f.drift, base.f.diffusion, base.f.dim, base.f.nparams)
+        if key not in cache:
+            cache[key] = h.compile_sde(base.f.drift, base.f.diffusion, base.f.dim, base.f.nparams)
+        sid = cache[key]
+    else:
+        sid = _lib.SDE[base.f]
+    every = True if save_everystep is None else bool(save_everystep)
+    t0, tf = base.tspan
+    q = (tf - t0) / float(dt)
+    if q != np.floor(q) or q < 0:
+        raise ValueError("InexactError: (tf - t0)/dt = %r is not an integer" % q)
+    nsteps = int(q)
+    a = _lib.SdeArgs()
+    a.sde, a.n, a.dim, a.nparams = sid, n, dim, nparams
+    a.t0, a.tf, a.dt, a.seed = t0, tf, float(dt), int(seed)
+    a.save_everystep, a.memory = int(every), _lib.MEM_HOST
+    a.u0, a.p = u0s.ctypes.data, ps.ctypes.data
+    us = np.empty((nsteps + 1, dim, n)) if every else None
+    uf = np.empty((dim, n))
+    o = _lib.SdeOut()
+    o.us = None if us is None else us.ctypes.data
+    o.u_final = uf.ctypes.data
+    st = _lib.SolveStats()
+    h.check(h.sde_solve(a, o, st))
+    from fractions import Fraction
+    t = np.array([float(Fraction(k) * Fraction(float(dt)) + Fraction(t0)) for k in range(nsteps + 1)])
+    zeros = np.zeros(n, dtype=np.int32)
+    sol = EnsembleSolution(t if every else None, us, uf, np.full(n, t[-1]), np.zeros(n, dtype=np.int8),
+                           np.full(n, nsteps, dtype=np.int32), zeros, np.full(n, float(dt)), st)
+    return sol[0] if single else sol
+
+
 def learn_fit(prob, alg, trajectories, device=0, opts=None, **kw):
     """Fit the learned-schedule model of the device handle on a training
     ensemble (solved with the plain schedule) — see ode_learn_fit."""
@@ -389,7 +471,7 @@ def learn_fit(prob, alg, trajectories, device=0, opts=None, **kw):
     return h.learn_fit(args, opts)
 
 
-__all__ = ["ODEProblem", "EnsembleProblem", "EnsembleSolution", "ODESolution", "UserRHS", "UserOutput", "solve",
-           "learn_fit", "GPUSimpleRK4", "GPUSimpleEuler", "GPUSimpleTsit5", "GPUSimpleATsit5", "GPUSimpleVern7", "GPUSimpleAVern7",
+__all__ = ["ODEProblem", "SDEProblem", "EnsembleProblem", "EnsembleSolution", "ODESolution", "UserRHS", "UserOutput",
+           "UserSDE", "SimpleEM", "solve", "learn_fit", "GPUSimpleRK4", "GPUSimpleEuler", "GPUSimpleTsit5", "GPUSimpleATsit5", "GPUSimpleVern7", "GPUSimpleAVern7",
            "GPUSimpleVern9", "GPUSimpleAVern9", "isadaptive", "DtLessThanMin", "GB300ODEError", "Handle",
            "fixed_grid"]

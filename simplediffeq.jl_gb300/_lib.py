@@ -26,7 +26,8 @@ RET_DEFAULT, RET_DTMIN, RET_MAXITERS, RET_NAN = 0, 1, 2, 3
 EXPORTS = ["ode_abi_version", "ode_create", "ode_destroy", "ode_last_error", "ode_ensemble_solve",
            "ode_fixed_grid", "ode_rhs_compile", "ode_output_compile", "ode_learn_default_opts", "ode_learn_fit",
            "ode_learn_predict", "ode_learn_gradcheck", "ode_ensemble_solve_noalloc", "ode_autotune",
-           "ode_ensemble_solve_everystep"]
+           "ode_ensemble_solve_everystep", "ode_sde_solve", "ode_sde_compile"]
+SDE = {"gbm": 0, "ou": 1, "lorenz": 2}
 
 
 class SolveArgs(ctypes.Structure):
@@ -51,6 +52,17 @@ class EverystepOut(ctypes.Structure):
                 ("capacity", ctypes.c_int64), ("total", ctypes.c_int64), ("u_final", ctypes.c_void_p),
                 ("t_final", ctypes.c_void_p), ("retcode", ctypes.c_void_p), ("naccept", ctypes.c_void_p),
                 ("nreject", ctypes.c_void_p)]
+
+
+class SdeArgs(ctypes.Structure):
+    _fields_ = [("sde", ctypes.c_int32), ("n", ctypes.c_int64), ("dim", ctypes.c_int32), ("nparams", ctypes.c_int32),
+                ("t0", ctypes.c_double), ("tf", ctypes.c_double), ("dt", ctypes.c_double), ("seed", ctypes.c_uint64),
+                ("save_everystep", ctypes.c_int32), ("memory", ctypes.c_int32), ("u0", ctypes.c_void_p),
+                ("p", ctypes.c_void_p), ("stream", ctypes.c_void_p)]
+
+
+class SdeOut(ctypes.Structure):
+    _fields_ = [("us", ctypes.c_void_p), ("u_final", ctypes.c_void_p)]
 
 
 class SolveStats(ctypes.Structure):
@@ -116,6 +128,10 @@ def load():
                                        ctypes.POINTER(SolveStats)]
     lib.ode_ensemble_solve_everystep.argtypes = [ctypes.c_void_p, ctypes.POINTER(SolveArgs),
                                                  ctypes.POINTER(EverystepOut), ctypes.POINTER(SolveStats)]
+    lib.ode_sde_solve.argtypes = [ctypes.c_void_p, ctypes.POINTER(SdeArgs), ctypes.POINTER(SdeOut),
+                                  ctypes.POINTER(SolveStats)]
+    lib.ode_sde_compile.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
+                                    ctypes.POINTER(ctypes.c_int), ctypes.c_char_p, ctypes.c_size_t]
     lib.ode_fixed_grid.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                    ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
     lib.ode_rhs_compile.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
@@ -186,6 +202,19 @@ class Handle:
     def solve_everystep(self, args, out, stats=None):
         return self.lib.ode_ensemble_solve_everystep(self.h, ctypes.byref(args), ctypes.byref(out),
                                                      ctypes.byref(stats) if stats is not None else None)
+
+    def sde_solve(self, args, out, stats=None):
+        return self.lib.ode_sde_solve(self.h, ctypes.byref(args), ctypes.byref(out),
+                                      ctypes.byref(stats) if stats is not None else None)
+
+    def compile_sde(self, drift, diffusion, dim, nparams):
+        sid = ctypes.c_int(0)
+        log = ctypes.create_string_buffer(8192)
+        rc = self.lib.ode_sde_compile(self.h, drift.encode(), diffusion.encode(), int(dim), int(nparams),
+                                      ctypes.byref(sid), log, 8192)
+        if rc != OK:
+            raise GB300ODEError(rc, self.error() + "\n" + log.value.decode(errors="replace"))
+        return sid.value
 
     def compile_rhs(self, body, dim, nparams):
         rid = ctypes.c_int(0)

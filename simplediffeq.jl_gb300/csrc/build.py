@@ -81,7 +81,7 @@ def gen_sources():
     # 1. embedded headers
     parts = ["/* generated by build.py: device headers for NVRTC */\n"]
     for fname, var in (("ode_solver.cuh", "kSrc_ode_solver_cuh"), ("ode_kparams.h", "kSrc_ode_kparams_h"),
-                       ("tableaus.h", "kSrc_tableaus_h")):
+                       ("tableaus.h", "kSrc_tableaus_h"), ("sde_solver.cuh", "kSrc_sde_solver_cuh")):
         text = open(os.path.join(HERE, fname)).read()
         assert ")GBSRC\"" not in text
         parts.append('static const char* %s = R"GBSRC(%s)GBSRC";\n' % (var, text))
@@ -137,8 +137,9 @@ def build(verbose=False, jobs=None):
     tus = gen_sources()
     os.makedirs(LIB, exist_ok=True)
     headers = [os.path.join(HERE, f) for f in ("ode_solver.cuh", "ode_kparams.h", "tableaus.h", "ode_host.h",
-                                               "jlrange.h")] + [os.path.join(PKG, "..", "include", "gb300ode.h")]
-    host_tus = [os.path.join(HERE, "ode_capi.cu"), os.path.join(HERE, "learn.cu"), os.path.join(HERE, "noalloc.cu")]
+                                               "jlrange.h", "sde_solver.cuh")] + [
+        os.path.join(PKG, "..", "include", "gb300ode.h")]
+    host_tus = [os.path.join(HERE, f) for f in ("ode_capi.cu", "learn.cu", "noalloc.cu", "sde_capi.cu")]
     gen = [os.path.join(BUILD, "aot_registry.inc"), os.path.join(BUILD, "embedded_src.inc")]
     jobs_list = []
     for src in tus + host_tus:

@@ -342,9 +342,9 @@ int nvrtc_cubin(const std::string& src, const std::vector<std::string>& extra_op
     return ODE_ENVRTC;
   }
   nvrtcProgram prog;
-  const char* hdrs[] = {kSrc_ode_solver_cuh, kSrc_ode_kparams_h, kSrc_tableaus_h};
-  const char* names[] = {"ode_solver.cuh", "ode_kparams.h", "tableaus.h"};
-  nvrtcResult r = g_nvrtc.create(&prog, src.c_str(), "gbode_jit.cu", 3, hdrs, names);
+  const char* hdrs[] = {kSrc_ode_solver_cuh, kSrc_ode_kparams_h, kSrc_tableaus_h, kSrc_sde_solver_cuh};
+  const char* names[] = {"ode_solver.cuh", "ode_kparams.h", "tableaus.h", "sde_solver.cuh"};
+  nvrtcResult r = g_nvrtc.create(&prog, src.c_str(), "gbode_jit.cu", 4, hdrs, names);
   if (r != NVRTC_SUCCESS) {
     *err = std::string("nvrtcCreateProgram: ") + g_nvrtc.errstr(r);
     return ODE_ENVRTC;
@@ -467,6 +467,25 @@ int grid_for(double t0, double dt, double tf, std::vector<double>* out, int64_t*
 }
 
 }  // namespace
+
+namespace gbode {
+
+int jit_function(ode_handle* h, const std::string& src, int block, CUfunction* fn, std::string* log) {
+  std::vector<char> cubin;
+  std::string err;
+  const int rc = nvrtc_cubin(src, {}, &cubin, log, &err);
+  if (rc != ODE_OK) return fail(h, rc, err);
+  return load_cubin(h, cubin, block, fn);
+}
+
+int launch_params(ode_handle* h, CUfunction fn, unsigned grid, unsigned block, void* params, cudaStream_t s) {
+  void* args[] = {params};
+  const CUresult r = g_drv.cuLaunchKernel(fn, grid, 1, 1, block, 1, 1, 0, (CUstream)s, args, nullptr);
+  if (r != CUDA_SUCCESS) return cu_fail(h, r, "cuLaunchKernel");
+  return ODE_OK;
+}
+
+}  // namespace gbode
 
 extern "C" {
 

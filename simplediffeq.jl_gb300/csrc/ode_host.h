@@ -30,6 +30,12 @@ struct UserOutput {
   int dim = 0, nparams = 0, width = 0;
 };
 
+/* a user SDE: drift and diffusion bodies compiled into the Euler-Maruyama kernel */
+struct UserSde {
+  std::string drift, diffusion;
+  int dim = 0, nparams = 0;
+};
+
 struct Model;  /* learned-schedule model, defined in learn.cu */
 
 struct GraphEntry {
@@ -57,6 +63,8 @@ struct ode_handle {
   std::vector<CUmodule> modules;
   std::vector<gbode::UserRhs> users;
   std::vector<gbode::UserOutput> outputs;
+  std::vector<gbode::UserSde> sdes;
+  std::map<std::string, CUfunction> sde_kernels;
   gbode::GraphEntry graph;
   gbode::Model* model = nullptr;
 };
@@ -70,6 +78,12 @@ int cu_fail(ode_handle* h, CUresult r, const char* what);
 
 /* device buffer of at least `bytes` bytes under `name` (contents not kept on growth) */
 void* buf(ode_handle* h, const std::string& name, size_t bytes, int* rc);
+
+/* run-time compilation of a translation unit whose kernel is named gbode_jit
+ * (NVRTC with the solver headers), loaded into the handle's modules */
+int jit_function(ode_handle* h, const std::string& src, int block, CUfunction* fn, std::string* log);
+/* launch fn(params) on s through the driver API */
+int launch_params(ode_handle* h, CUfunction fn, unsigned grid, unsigned block, void* params, cudaStream_t s);
 
 /* learned schedule hooks (learn.cu) */
 void model_free(Model* m);

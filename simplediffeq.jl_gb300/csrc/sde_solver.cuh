@@ -1,0 +1,188 @@
+/* Device side of the SimpleEM ensemble solver (src/euler_maruyama.jl:48-98):
+ * fixed-step Euler-Maruyama for SDEs with diagonal noise, one trajectory per
+ * thread.
+ *
+ *   n = Int((tf - t0) / dt) + 1 points, t_k = t0 + k*dt (a scalar muladd),
+ *   u_{k+1} = u_k + f(u_k, p, t_k)*dt + sqrt(dt)*g(u_k, p, t_k) .* xi_k
+ *
+ * The reference draws xi_k with Julia's randn; this solver draws them from a
+ * counter-based generator so that every trajectory's noise is reproducible
+ * from (seed, trajectory, step) alone, on any thread and on the CPU:
+ *   - Philox4x32-10 (J. K. Salmon, M. A. Moraes, R. O. Dror, D. E. Shaw,
+ *     "Parallel random numbers: as easy as 1, 2, 3", SC'11), counter
+ *     (step k, pair j, trajectory low word, trajectory high word), key = seed;
+ *   - each Philox output gives two 53-bit uniforms u1 in (0, 1], u2 in [0, 1)
+ *     and the Box-Muller pair (G. E. P. Box, M. E. Muller, 1958)
+ *     r = sqrt(-2 log u1), (r cos 2 pi u2, r sin 2 pi u2) for components 2j, 2j+1,
+ *     with this file's log_dev and ode_solver.cuh's sincos_cw, so that the
+ *     oracle reproduces every normal bit for bit.
+ * Update rounding (device canon): u = fma(sqdt*g, xi, fma(f, dt, u)). */
+#pragma once
+#include "ode_solver.cuh"
+
+namespace gbode {
+
+struct SParams {
+  long long n;           /* trajectories */
+  long long nsteps;      /* steps (points - 1) */
+  double t0, dt;
+  unsigned long long seed;
+  int dim, nparams;
+  int save_everystep;
+  const double* u0;      /* [dim][n] */
+  const double* p;       /* [nparams][n] */
+  double* us;            /* [nsteps + 1][dim][n], or 0 */
+  double* u_final;       /* [dim][n], or 0 */
+};
+
+/* ------------------------------------------------------------------ Philox4x32-10 */
+struct U4 {
+  unsigned x, y, z, w;
+};
+
+__device__ __forceinline__ U4 philox4x32_10(U4 c, unsigned k0, unsigned k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const unsigned hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    const unsigned hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+/* Natural logarithm of a positive normal double: x = m * 2^e with m in
+ * [sqrt(1/2), sqrt(2)), log m = 2 atanh(s), s = (m - 1)/(m + 1), from the odd
+ * series 2(s + s^3/3 + ... + s^23/23) (|s| <= 0.1716, truncation below 1e-19
+ * relative), and e*ln 2 added in two parts (ln 2 = LN2_HI + LN2_LO, LN2_HI of
+ * 42 significant bits so that e*LN2_HI is exact).  Every step is one IEEE
+ * double operation. */
+__device__ __forceinline__ double log_dev(double x) {
+  long long b = __double_as_longlong(x);
+  int e = (int)((b >> 52) & 0x7ff) - 1023;
+  double m = __longlong_as_double((b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
+  if (m > 0x1.6a09e667f3bcdp+0) {  /* sqrt(2) */
+    m = m * 0.5;
+    e += 1;
+  }
+  const double s = (m - 1.0) / (m + 1.0);
+  const double z = s * s;
+  double q = 0x1.642c8590b2164p-5;     /* 1/23 */
+  q = __fma_rn(q, z, 0x1.8618618618618p-5);   /* 1/21 */
+  q = __fma_rn(q, z, 0x1.af286bca1af28p-5);   /* 1/19 */
+  q = __fma_rn(q, z, 0x1.e1e1e1e1e1e1ep-5);   /* 1/17 */
+  q = __fma_rn(q, z, 0x1.1111111111111p-4);   /* 1/15 */
+  q = __fma_rn(q, z, 0x1.3b13b13b13b14p-4);   /* 1/13 */
+  q = __fma_rn(q, z, 0x1.745d1745d1746p-4);   /* 1/11 */
+  q = __fma_rn(q, z, 0x1.c71c71c71c71cp-4);   /* 1/9 */
+  q = __fma_rn(q, z, 0x1.2492492492492p-3);   /* 1/7 */
+  q = __fma_rn(q, z, 0x1.999999999999ap-3);   /* 1/5 */
+  q = __fma_rn(q, z, 0x1.5555555555555p-2);   /* 1/3 */
+  const double t2 = s + s;
+  const double lm = __fma_rn(t2 * z, q, t2);
+  const double de = (double)e;
+  return __fma_rn(de, 0x1.62e42fefa38p-1, __fma_rn(de, 0x1.ef35793c7673p-45, lm));
+}
+
+/* Components 2j and 2j+1 of the step-k normal vector of trajectory idx. */
+__device__ __forceinline__ void normal_pair(unsigned long long seed, long long k, int j, long long idx, double* z0,
+                                            double* z1) {
+  const U4 r = philox4x32_10(U4{(unsigned)k, (unsigned)j, (unsigned)idx, (unsigned)((unsigned long long)idx >> 32)},
+                             (unsigned)seed, (unsigned)(seed >> 32));
+  const unsigned long long a = ((unsigned long long)(r.x >> 5) << 26) | (r.y >> 6);
+  const unsigned long long c = ((unsigned long long)(r.z >> 5) << 26) | (r.w >> 6);
+  const double u1 = (double)(a + 1) * 0x1.0p-53;  /* (0, 1] */
+  const double u2 = (double)c * 0x1.0p-53;        /* [0, 1) */
+  const double rad = __dsqrt_rn(-2.0 * log_dev(u1));
+  double sn, cs;
+  sincos_cw(u2 * 0x1.921fb54442d18p+2, &sn, &cs);  /* 2 pi */
+  *z0 = rad * cs;
+  *z1 = rad * sn;
+}
+
+/* ------------------------------------------------------------------ built-in SDEs (diagonal noise) */
+/* geometric Brownian motion: f = mu u, g = sigma u; p = (mu, sigma) */
+template <int DD>
+struct SdeGBM {
+  enum { D = DD, NP = 2 };
+  double p[2];
+  __device__ __forceinline__ void drift(const double (&u)[DD], double t, double (&f)[DD]) const {
+#pragma unroll
+    for (int d = 0; d < DD; ++d) f[d] = p[0] * u[d];
+  }
+  __device__ __forceinline__ void diffusion(const double (&u)[DD], double t, double (&g)[DD]) const {
+#pragma unroll
+    for (int d = 0; d < DD; ++d) g[d] = p[1] * u[d];
+  }
+};
+
+/* Ornstein-Uhlenbeck: f = theta (mu - u), g = sigma; p = (theta, mu, sigma) */
+template <int DD>
+struct SdeOU {
+  enum { D = DD, NP = 3 };
+  double p[3];
+  __device__ __forceinline__ void drift(const double (&u)[DD], double t, double (&f)[DD]) const {
+#pragma unroll
+    for (int d = 0; d < DD; ++d) f[d] = p[0] * (p[1] - u[d]);
+  }
+  __device__ __forceinline__ void diffusion(const double (&u)[DD], double t, double (&g)[DD]) const {
+#pragma unroll
+    for (int d = 0; d < DD; ++d) g[d] = p[2];
+  }
+};
+
+/* Lorenz drift with additive noise of strength p[3]; p = (sigma, rho, beta, noise) */
+struct SdeLorenz {
+  enum { D = 3, NP = 4 };
+  double p[4];
+  __device__ __forceinline__ void drift(const double (&u)[3], double t, double (&f)[3]) const {
+    f[0] = p[0] * (u[1] - u[0]);
+    f[1] = fmaR(u[0], p[1] - u[2], -u[1]);
+    f[2] = fmaR(u[0], u[1], -(p[2] * u[2]));
+  }
+  __device__ __forceinline__ void diffusion(const double (&u)[3], double t, double (&g)[3]) const {
+    g[0] = p[3];
+    g[1] = p[3];
+    g[2] = p[3];
+  }
+};
+
+/* ------------------------------------------------------------------ the Euler-Maruyama loop */
+template <class S>
+__device__ __forceinline__ void run_em(const SParams& P) {
+  enum { D = S::D };
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.n) return;
+  S sde;
+#pragma unroll
+  for (int q = 0; q < S::NP; ++q) sde.p[q] = P.p[(long long)q * P.n + i];
+  double u[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) u[d] = P.u0[(long long)d * P.n + i];
+  if (P.save_everystep && P.us)
+#pragma unroll
+    for (int d = 0; d < D; ++d) P.us[(long long)d * P.n + i] = u[d];
+  const double dt = P.dt, sqdt = __dsqrt_rn(P.dt);
+  for (long long k = 0; k < P.nsteps; ++k) {
+    const double t = __fma_rn((double)k, dt, P.t0);
+    double f[D], g[D], xi[D + 1];
+    sde.drift(u, t, f);
+    sde.diffusion(u, t, g);
+#pragma unroll
+    for (int j = 0; j < (D + 1) / 2; ++j) normal_pair(P.seed, k, j, i, &xi[2 * j], &xi[2 * j + 1]);
+#pragma unroll
+    for (int d = 0; d < D; ++d) u[d] = __fma_rn(sqdt * g[d], xi[d], __fma_rn(f[d], dt, u[d]));
+    if (P.save_everystep && P.us)
+#pragma unroll
+      for (int d = 0; d < D; ++d) P.us[((k + 1) * D + d) * P.n + i] = u[d];
+  }
+  if (P.u_final)
+#pragma unroll
+    for (int d = 0; d < D; ++d) P.u_final[(long long)d * P.n + i] = u[d];
+}
+
+}  // namespace gbode
+
+#define GBODE_SDE_ENTRY(NAME, S) \
+  extern "C" __global__ void __launch_bounds__(128) NAME(gbode::SParams P) { gbode::run_em<S>(P); }

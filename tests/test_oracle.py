@@ -260,3 +260,67 @@ def test_every_step_output_rows(po):
             f = po.solve(alg, rhs, u, pp, tsp, 0.1, rounding=rounding, abstol=1e-9, reltol=1e-9)
             assert len(e["ts_rows"]) == f["naccept"][0] + 1
             assert np.array_equal(e["us_rows"][-1], f["u_final"][:, 0])
+
+
+# ---------------------------------------------------------------- SimpleEM
+def test_philox_known_answers(po):
+    """Philox4x32-10 against the known-answer vectors published with the
+    Random123 library (Salmon et al., SC'11): zero, all-ones and pi-digit
+    counter/key pairs."""
+    assert po.philox([0, 0, 0, 0], [0, 0]) == [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]
+    assert po.philox([0xffffffff] * 4, [0xffffffff] * 2) == [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]
+    assert po.philox([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344], [0xa4093822, 0x299f31d0]) == \
+        [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]
+
+
+def test_device_canon_log_accuracy(po):
+    rng = np.random.default_rng(2)
+    x = np.concatenate([rng.uniform(2.0 ** -53, 1.0, 4000), np.exp(rng.uniform(-700, 700, 2000)),
+                        [2.0 ** -53, 0.5, 1.0 - 2.0 ** -53, np.sqrt(2.0), 2.0 ** -1022]])
+    got = np.array([po.log_dev(v) for v in x])
+    want = np.log(x)
+    assert po.log_dev(1.0) == 0.0
+    nz = want != 0
+    assert (np.abs(got[nz] - want[nz]) / np.spacing(np.abs(want[nz]))).max() <= 3
+
+
+def test_counter_based_normals(po):
+    """Box-Muller pairs from Philox: standard normal moments, uncorrelated
+    components, and a stream that depends only on (seed, step, pair, trajectory)."""
+    z = np.array([po.normal_pair(7, k, j, i) for k in range(100) for j in range(2) for i in range(250)])
+    for col in (z[:, 0], z[:, 1]):
+        assert abs(col.mean()) < 0.02 and abs(col.var() - 1) < 0.03
+        assert abs(((col - col.mean()) ** 4).mean() / col.var() ** 2 - 3) < 0.15
+    assert abs(np.corrcoef(z[:, 0], z[:, 1])[0, 1]) < 0.02
+    assert po.normal_pair(7, 3, 1, 9) == po.normal_pair(7, 3, 1, 9) != po.normal_pair(8, 3, 1, 9)
+
+
+def test_simple_em_weak_moments(po):
+    """The reference's example SDE du = 0.1u dt + 0.2u dW, u0 = 1 on (0, 1),
+    dt = 0.01 (src/euler_maruyama.jl docstring): Euler-Maruyama's exact mean
+    is (1 + 0.1 dt)^100; and an Ornstein-Uhlenbeck ensemble's variance against
+    the EM recursion's exact value sigma^2 dt sum (1 - theta dt)^(2k)."""
+    n = 20000
+    o = po.sde_solve("gbm", np.ones((1, n)), np.tile([[0.1], [0.2]], (1, n)), (0.0, 1.0), 0.01, seed=1,
+                     save_everystep=False, nthreads=8)
+    m = o["u_final"].mean()
+    sd = np.sqrt(np.exp(0.2) * (np.exp(0.04) - 1) / n)
+    assert abs(m - 1.001 ** 100) < 4 * sd
+    th, sig, dt = 1.0, 0.5, 0.01
+    o = po.sde_solve("ou", np.zeros((1, n)), np.tile([[th], [0.0], [sig]], (1, n)), (0.0, 10.0), dt, seed=2,
+                     save_everystep=True, nthreads=8)
+    exact = sig ** 2 * dt * sum((1 - th * dt) ** (2 * k) for k in range(1000))
+    v = o["u_final"].var()
+    assert abs(v - exact) < 5 * exact * np.sqrt(2.0 / n)
+    assert o["us"].shape == (1001, 1, n) and np.array_equal(o["us"][0], np.zeros((1, n)))
+    assert o["t"][-1] == 10.0
+
+
+def test_simple_em_rounding_modes_and_grid(po):
+    u0 = np.array([[1.0], [1.0], [1.0]])
+    p = np.array([[10.0], [28.0], [8 / 3], [0.1]])
+    a = po.sde_solve("lorenz", u0, p, (0.0, 0.5), 0.001, seed=3, rounding="ref", save_everystep=False)
+    b = po.sde_solve("lorenz", u0, p, (0.0, 0.5), 0.001, seed=3, rounding="device", save_everystep=False)
+    assert np.abs(a["u_final"] - b["u_final"]).max() < 1e-9
+    with pytest.raises(ValueError):
+        po.sde_grid_steps(0.0, 1.0, 0.3)  # Int((tf - t0)/dt) throws InexactError in the reference
