@@ -87,6 +87,14 @@ def inputs_kuramoto(n, seed, D=12):
     return np.ascontiguousarray(th), np.ascontiguousarray(p)
 
 
+def inputs_sde_lorenz(n, seed):
+    rng = np.random.default_rng(seed)
+    u = rng.uniform(-1, 1, (3, n))
+    u[2] += 20
+    p = np.stack([np.full(n, 10.0), rng.uniform(0, 30, n), np.full(n, 8 / 3), np.full(n, 0.5)])
+    return np.ascontiguousarray(u), np.ascontiguousarray(p)
+
+
 T_ARENSTORF = 17.0652165601579625588917206249
 # Per-unit algorithmic work (FMA = 2 flops): per step attempt and per saveat point.
 CONFIGS = {
@@ -119,6 +127,13 @@ CONFIGS = {
             # sincos_cw (15 FMA + 2 multiplies + 1 add); per save 266 + 12 pairs x 33
             flops_attempt=1310 + 6 * 12 * 33, flops_save=266 + 12 * 33, rhs_per_attempt=6, oracle_alg="ATsit5",
             dtype="f64"),
+    6: dict(kind="sde", workload="SimpleEM (Euler-Maruyama) FP64, 1,048,576 stochastic Lorenz trajectories "
+                                 "(drift sigma=10, rho~U[0,30], beta=8/3; additive noise 0.5 per component), "
+                                 "u0~U[-1,1]^3+(0,0,20), tspan (0,1), dt 1e-3, final state; Philox4x32-10 normals",
+            sde="lorenz", n=1048576, tspan=(0.0, 1.0), dt=1e-3, inputs=inputs_sde_lorenz, dtype="f64",
+            # per step: drift 8, two Box-Muller pairs x 69 (log 31, sqrt, 2 pi u2, sin/cos 33, 2 products),
+            # update 3 x 5, grid time 2
+            flops_step=8 + 2 * 69 + 15 + 2),
 }
 
 
@@ -230,6 +245,113 @@ def load_traffic():
     return None
 
 
+def run_sde(args, cfg, rank, world, local):
+    """SimpleEM workload: device-timed solves (L2 flushed between steps), the
+    C ABI end to end with pinned host buffers, the FP64 roofline and the
+    oracle's CPU restatement on a sample."""
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    import __graft_entry__ as g
+    pkg = g.package()
+    L = pkg._lib
+    h = L.Handle(local)
+    n = args.n or cfg["n"]
+    u0, p = cfg["inputs"](n, 2024 + rank)
+    dim, nparams = u0.shape[0], p.shape[0]
+    nsteps = int(round((cfg["tspan"][1] - cfg["tspan"][0]) / cfg["dt"]))
+    dev = torch.device("cuda", local)
+    du0, dp = torch.from_numpy(u0).to(dev), torch.from_numpy(p).to(dev)
+    uf = torch.empty((dim, n), dtype=torch.float64, device=dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+
+    def sargs(memory, u0p, pp):
+        a = L.SdeArgs()
+        a.sde, a.n, a.dim, a.nparams = L.SDE[cfg["sde"]], n, dim, nparams
+        a.t0, a.tf, a.dt, a.seed = cfg["tspan"][0], cfg["tspan"][1], cfg["dt"], 1234 + rank
+        a.save_everystep, a.memory, a.u0, a.p = 0, memory, u0p, pp
+        return a
+
+    a = sargs(L.MEM_DEVICE, du0.data_ptr(), dp.data_ptr())
+    o = L.SdeOut()
+    o.u_final = uf.data_ptr()
+    for _ in range(args.warmup):
+        h.check(h.sde_solve(a, o, L.SolveStats()))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    kms, launches = [], 0
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            st = L.SolveStats()
+            h.check(h.sde_solve(a, o, st))
+            kms.append(st.kernel_ms)
+            launches += st.launches
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    step_ms = sum(kms) / len(kms)
+    if dist:
+        t = torch.tensor([step_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_ms = float(t.item())
+    hu0, hp = torch.from_numpy(u0).pin_memory(), torch.from_numpy(p).pin_memory()
+    huf = torch.empty((dim, n), dtype=torch.float64).pin_memory()
+    ha = sargs(L.MEM_HOST, hu0.data_ptr(), hp.data_ptr())
+    ho = L.SdeOut()
+    ho.u_final = huf.data_ptr()
+    h.check(h.sde_solve(ha, ho))
+    e2e_t = []
+    for _ in range(max(1, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        h.check(h.sde_solve(ha, ho))
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_t) / len(e2e_t)
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    rates = L.probe_rates(local, 2000)
+    peak = rates["dfma"][0] * 2 / 1e12
+    achieved = n * nsteps * cfg["flops_step"] / (step_ms * 1e-3) / 1e12
+    line = {
+        "metric": "ensemble trajectories/s (workload 6, SimpleEM)", "value": n * world / (step_ms * 1e-3),
+        "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": cfg["dtype"],
+        "data": "synthetic (seeded; no public dataset involved)",
+        "config": {"workload": cfg["workload"], "trajectories_per_gpu": n, "steps_per_trajectory": nsteps,
+                   "l2": "flushed between steps by a 512 MB device write",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "trajectory_steps_per_s": n * world * nsteps / (step_ms * 1e-3),
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                     "traffic": None,
+                     "peak_source": "FP64 FMA lane rate measured by this run's probe (libgb300ode_probe.so)"},
+        "e2e": {"value": n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": u0.nbytes + p.nbytes,
+                "d2h_bytes_per_step": huf.numel() * 8},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        po = g.oracle()
+        m = min(n, 16384)
+        threads = os.cpu_count()
+        t = time.perf_counter()
+        po.sde_solve(cfg["sde"], np.ascontiguousarray(u0[:, :m]), np.ascontiguousarray(p[:, :m]), cfg["tspan"],
+                     cfg["dt"], seed=1234, rounding="ref", save_everystep=False, nthreads=threads)
+        el = time.perf_counter() - t
+        line["cpu_baseline"] = {"value": m / el, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": "the first %d trajectories, SimpleEM restated in C++ with the same "
+                                          "counter-based normals, one std::thread per core" % m, "seconds": el}
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -250,6 +372,8 @@ def main():
     if args.impl == "reference":
         return run_reference(args, rank)
     cfg = CONFIGS[args.config]
+    if cfg.get("kind") == "sde":
+        return run_sde(args, cfg, rank, world, local)
     fixed = cfg["alg"] in ("Tsit5", "Vern7", "Vern9", "RK4")
 
     import torch
