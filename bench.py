@@ -245,6 +245,23 @@ def load_traffic():
     return None
 
 
+def max_over_ranks(value, dist, device):
+    """The slowest replica's step time: with one process per GPU (replicas of
+    the workload, no collective on the data path) the job takes as long as its
+    slowest rank, and whole-job throughput = trajectories of all ranks / that."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_seed(rank):
+    """Each rank solves its own replica of the workload (weak scaling)."""
+    return 2024 + rank
+
+
 def run_sde(args, cfg, rank, world, local):
     """SimpleEM workload: device-timed solves (L2 flushed between steps), the
     C ABI end to end with pinned host buffers, the FP64 roofline and the
@@ -260,7 +277,7 @@ def run_sde(args, cfg, rank, world, local):
     L = pkg._lib
     h = L.Handle(local)
     n = args.n or cfg["n"]
-    u0, p = cfg["inputs"](n, 2024 + rank)
+    u0, p = cfg["inputs"](n, replica_seed(rank))
     dim, nparams = u0.shape[0], p.shape[0]
     nsteps = int(round((cfg["tspan"][1] - cfg["tspan"][0]) / cfg["dt"]))
     dev = torch.device("cuda", local)
@@ -295,11 +312,7 @@ def run_sde(args, cfg, rank, world, local):
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
-    step_ms = sum(kms) / len(kms)
-    if dist:
-        t = torch.tensor([step_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_ms = float(t.item())
+    step_ms = max_over_ranks(sum(kms) / len(kms), dist, dev)
     hu0, hp = torch.from_numpy(u0).pin_memory(), torch.from_numpy(p).pin_memory()
     huf = torch.empty((dim, n), dtype=torch.float64).pin_memory()
     ha = sargs(L.MEM_HOST, hu0.data_ptr(), hp.data_ptr())
@@ -389,7 +402,7 @@ def main():
     alg = getattr(pkg, "GPUSimple" + cfg["alg"])()
 
     n = args.n or cfg["n"]
-    u0, p = cfg["inputs"](n, 2024 + rank)
+    u0, p = cfg["inputs"](n, replica_seed(rank))
     dim, nparams = u0.shape[0], p.shape[0]
     nsave = cfg["nsave"]
     sv = np.linspace(*cfg["tspan"], nsave) if nsave else None
@@ -474,11 +487,7 @@ def main():
     with ClockSampler(local) as clk:
         kms, att, sav, launches = timed(schedule, args.steps, args.warmup)
     clocks = clk.summary()
-    step_ms = sum(kms) / len(kms)
-    if dist:
-        t = torch.tensor([step_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_ms = float(t.item())
+    step_ms = max_over_ranks(sum(kms) / len(kms), dist, dev)
     uf_measured = outs["u_final"].cpu().numpy()
     value = n * world / (step_ms * 1e-3)
 
