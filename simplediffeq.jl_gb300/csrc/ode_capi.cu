@@ -270,7 +270,7 @@ const char* entry_kind(int alg, int sched, int64_t nsave) {
 }
 
 /* Bytes of one saveat job in the staged kernel's ring: the host-side copy of
- * StageLayout<M, PR, D, F>::JOB in ode_solver.cuh (4 times of type T, the
+ * StageLayout<M, PR, D, F>::JOB in ode_solver.cuh (3 times of type T, the
  * trajectory index, the saveat index, and D (x2 with Kahan) state values,
  * NK x D stage values and, for the Verner methods, the parameters, of type R). */
 int stage_job_bytes(const ode_solve_args* a) {
@@ -278,7 +278,7 @@ int stage_job_bytes(const ode_solve_args* a) {
   const int r = a->precision == ODE_FP64 ? 8 : 4, t = a->precision == ODE_FP32 ? 4 : 8;
   const bool dense_f = a->alg != ODE_ALG_ATSIT5;  /* Verner dense output evaluates f: parameters ride along */
   const int nrec = a->dim * (a->precision == ODE_FP32_KAHAN ? 2 : 1) + nk * a->dim + (dense_f ? a->nparams : 0);
-  return 4 * t + 8 + nrec * r + 4;
+  return 3 * t + 8 + nrec * r + 4;
 }
 
 /* values stored per saveat point and trajectory */
@@ -504,6 +504,7 @@ int ode_create(ode_handle** out, int device) {
   if (e == cudaSuccess) e = cudaFree(0);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&h->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&h->ev1);
   if (e != cudaSuccess) {
@@ -522,8 +523,10 @@ void ode_destroy(ode_handle* h) {
   if (!h) return;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
-  if (h->graph.exec) cudaGraphExecDestroy(h->graph.exec);
-  if (h->graph.graph) cudaGraphDestroy(h->graph.graph);
+  for (GraphEntry& g : h->graphs) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    if (g.graph) cudaGraphDestroy(g.graph);
+  }
   for (auto& kv : h->bufs)
     if (kv.second.ptr) cudaFree(kv.second.ptr);
   for (CUmodule m : h->modules) g_drv.cuModuleUnload(m);
@@ -531,6 +534,7 @@ void ode_destroy(ode_handle* h) {
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   delete h;
 }
 
@@ -825,14 +829,24 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
   const bool use_graph = s != 0 && !std::getenv("GBODE_NO_GRAPH");
   int replayed = 0;
   CK(cudaEventRecord(h->ev0, s), "event");
-  if (use_graph && h->graph.exec && h->graph.key == key) {
-    CK(cudaGraphLaunch(h->graph.exec, s), "cudaGraphLaunch");
-    launches = h->graph.launches;
+  GraphEntry* cached = nullptr;
+  for (GraphEntry& g : h->graphs)
+    if (g.exec && g.key == key) cached = &g;
+  if (use_graph && cached) {
+    cached->last_use = ++h->graph_tick;
+    CK(cudaGraphLaunch(cached->exec, s), "cudaGraphLaunch");
+    launches = cached->launches;
     replayed = 1;
   } else if (use_graph) {
-    if (h->graph.exec) cudaGraphExecDestroy(h->graph.exec);
-    if (h->graph.graph) cudaGraphDestroy(h->graph.graph);
-    h->graph = GraphEntry();
+    if ((int)h->graphs.size() >= kGraphCache) {
+      /* evict the least recently used captured solve */
+      size_t lru = 0;
+      for (size_t i = 1; i < h->graphs.size(); ++i)
+        if (h->graphs[i].last_use < h->graphs[lru].last_use) lru = i;
+      if (h->graphs[lru].exec) cudaGraphExecDestroy(h->graphs[lru].exec);
+      if (h->graphs[lru].graph) cudaGraphDestroy(h->graphs[lru].graph);
+      h->graphs.erase(h->graphs.begin() + (long)lru);
+    }
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
     int nl = 0;
     const int r = enqueue(&nl);
@@ -849,10 +863,13 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
       cudaGraphDestroy(g);
       return cuda_fail(h, ie, "cudaGraphInstantiate");
     }
-    h->graph.graph = g;
-    h->graph.exec = ex;
-    h->graph.key = key;
-    h->graph.launches = nl;
+    GraphEntry ge;
+    ge.graph = g;
+    ge.exec = ex;
+    ge.key = key;
+    ge.launches = nl;
+    ge.last_use = ++h->graph_tick;
+    h->graphs.push_back(ge);
     CK(cudaGraphLaunch(ex, s), "cudaGraphLaunch");
     launches = nl;
   } else {
@@ -889,11 +906,152 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
   return ODE_OK;
 }
 
+/* Host buffers, large adaptive ensembles: the solve runs in chunks of
+ * trajectories so that copying one chunk's outputs to the host (copy stream)
+ * overlaps the next chunk's kernel (compute stream).  Chunks are contiguous
+ * trajectory ranges, each a complete solve of its own (learned order, graph
+ * capture) on double-buffered device slots; rows of the [rows][n] host arrays
+ * move with 2D copies.  Results are those of the unchunked solve: every
+ * trajectory is solved by the same kernel from the same inputs. */
+constexpr int64_t kChunk = 262144;
+
+int solve_chunked(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_solve_stats* st) {
+  const auto wall0 = std::chrono::steady_clock::now();
+  CK(cudaSetDevice(h->device), "cudaSetDevice");
+  const int64_t n = a->n;
+  const int D = a->dim, NP = a->nparams;
+  const int64_t nchunks = (n + kChunk - 1) / kChunk;
+  const int64_t m = (n + nchunks - 1) / nchunks;
+  cudaStream_t s = a->stream ? (cudaStream_t)a->stream : h->stream;
+  cudaStream_t cs = h->copy_stream;
+  int rc = ODE_OK;
+  if (a->output >= ODE_OUTPUT_USER && a->output >= ODE_OUTPUT_USER + (int)h->outputs.size())
+    return fail(h, ODE_EINVAL, "unknown output function");
+  const int W = output_width(h, a);
+  struct Rows {
+    const void* host_in;
+    void* host_out;
+    int64_t rows;
+    size_t elem;
+    const char* name;
+  };
+  const Rows ins[] = {{a->u0, nullptr, D, 8, "ck_u0"}, {a->p, nullptr, NP, 8, "ck_p"}, {a->dt0, nullptr, 1, 8, "ck_dt0"}};
+  const Rows outs[] = {{nullptr, o->us, a->nsave * W, 8, "ck_us"}, {nullptr, o->u_final, D, 8, "ck_uf"},
+                       {nullptr, o->t_final, 1, 8, "ck_tf"},       {nullptr, o->retcode, 1, 1, "ck_ret"},
+                       {nullptr, o->naccept, 1, 4, "ck_nacc"},     {nullptr, o->nreject, 1, 4, "ck_nrej"},
+                       {nullptr, o->dt_first, 1, 8, "ck_dtf"}};
+  void* din[2][3] = {};
+  void* dout[2][7] = {};
+  for (int b = 0; b < 2; ++b) {
+    for (int k = 0; k < 3; ++k) {
+      if (!ins[k].host_in || ins[k].rows == 0) continue;
+      if (!(din[b][k] = buf(h, std::string(ins[k].name) + (b ? "1" : "0"), (size_t)(m * ins[k].rows) * ins[k].elem,
+                            &rc)))
+        return rc;
+    }
+    for (int k = 0; k < 7; ++k) {
+      if (!outs[k].host_out || outs[k].rows == 0) continue;
+      if (!(dout[b][k] = buf(h, std::string(outs[k].name) + (b ? "1" : "0"),
+                             (size_t)(m * outs[k].rows) * outs[k].elem, &rc)))
+        return rc;
+    }
+  }
+  cudaEvent_t ready[2] = {nullptr, nullptr};
+  for (int b = 0; b < 2; ++b) CK(cudaEventCreateWithFlags(&ready[b], cudaEventDisableTiming), "event");
+  auto release = [&]() {
+    for (int b = 0; b < 2; ++b)
+      if (ready[b]) cudaEventDestroy(ready[b]);
+  };
+  /* chunk c's inputs to slot c % 2, then an event the compute stream waits on */
+  auto upload = [&](int64_t c) -> int {
+    const int b = (int)(c & 1);
+    const int64_t i0 = c * m, mc = std::min(m, n - i0);
+    for (int k = 0; k < 3; ++k) {
+      if (!din[b][k]) continue;
+      const size_t e = ins[k].elem;
+      CK(cudaMemcpy2DAsync(din[b][k], mc * e, (const char*)ins[k].host_in + i0 * e, n * e, mc * e, ins[k].rows,
+                           cudaMemcpyHostToDevice, cs),
+         "copy chunk inputs");
+    }
+    CK(cudaEventRecord(ready[b], cs), "event");
+    return ODE_OK;
+  };
+  ode_solve_stats total;
+  std::memset(&total, 0, sizeof total);
+  bool early = false;
+  rc = upload(0);
+  if (rc != ODE_OK) {
+    release();
+    return rc;
+  }
+  for (int64_t c = 0; c < nchunks && rc == ODE_OK; ++c) {
+    const int b = (int)(c & 1);
+    const int64_t i0 = c * m, mc = std::min(m, n - i0);
+    ode_solve_args sa = *a;
+    sa.n = mc;
+    sa.memory = ODE_MEM_DEVICE;
+    sa.stream = s;
+    sa.u0 = (const double*)din[b][0];
+    sa.p = (const double*)din[b][1];
+    sa.dt0 = (const double*)din[b][2];
+    ode_solve_out so;
+    so.us = (double*)dout[b][0];
+    so.u_final = (double*)dout[b][1];
+    so.t_final = (double*)dout[b][2];
+    so.retcode = (int8_t*)dout[b][3];
+    so.naccept = (int32_t*)dout[b][4];
+    so.nreject = (int32_t*)dout[b][5];
+    so.dt_first = (double*)dout[b][6];
+    cudaError_t e = cudaStreamWaitEvent(s, ready[b], 0);
+    if (e != cudaSuccess) {
+      release();
+      return cuda_fail(h, e, "wait chunk inputs");
+    }
+    ode_solve_stats cst;
+    const int r = solve_impl(h, &sa, &so, &cst, nullptr);  /* returns when the chunk's kernel is done */
+    if (r != ODE_OK && r != ODE_ETRAJ) {
+      release();
+      return r;
+    }
+    early = early || r == ODE_ETRAJ;
+    total.kernel_ms += cst.kernel_ms;
+    total.attempts += cst.attempts;
+    total.saves += cst.saves;
+    total.launches += cst.launches;
+    total.schedule_used = cst.schedule_used;
+    total.graph_replayed += cst.graph_replayed;
+    total.jit = cst.jit;
+    /* the next chunk's inputs go first, so that its kernel need not wait for this chunk's outputs */
+    if (c + 1 < nchunks) rc = upload(c + 1);
+    for (int k = 0; k < 7 && rc == ODE_OK; ++k) {
+      if (!dout[b][k]) continue;
+      const size_t el = outs[k].elem;
+      e = cudaMemcpy2DAsync((char*)outs[k].host_out + i0 * el, n * el, dout[b][k], mc * el, mc * el, outs[k].rows,
+                            cudaMemcpyDeviceToHost, cs);
+      if (e != cudaSuccess) rc = cuda_fail(h, e, "copy chunk outputs");
+    }
+  }
+  const cudaError_t e = cudaStreamSynchronize(cs);
+  release();
+  if (rc != ODE_OK) return rc;
+  if (e != cudaSuccess) return cuda_fail(h, e, "chunk copies");
+  if (st) {
+    *st = total;
+    st->graph_replayed = total.graph_replayed == nchunks ? 1 : 0;
+    st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
+  }
+  return early ? fail(h, ODE_ETRAJ, "some trajectories stopped early (dt<dtmin or maxiters); see retcode") : ODE_OK;
+}
+
 }  // namespace
 
 extern "C" {
 
 int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_solve_stats* st) {
+  if (h && a && o && a->memory == ODE_MEM_HOST && a->n >= 2 * kChunk && !is_fixed(a->alg) &&
+      a->alg >= ODE_ALG_RK4 && a->alg <= ODE_ALG_EULER && a->dim >= 1 && a->nparams >= 0 &&
+      (a->nparams == 0 || a->p) && a->u0 && (a->nsave == 0 || a->saveat))
+    return solve_chunked(h, a, o, st);
   return solve_impl(h, a, o, st, nullptr);
 }
 

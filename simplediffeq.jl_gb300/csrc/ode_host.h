@@ -43,7 +43,10 @@ struct GraphEntry {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int launches = 0;
+  unsigned long long last_use = 0;
 };
+
+constexpr int kGraphCache = 6;  /* captured solves kept per handle (least recently used evicted) */
 
 constexpr int kCostBins = 1024;  /* bins of the learned schedule's counting sort */
 
@@ -53,6 +56,7 @@ struct ode_handle {
   int device = 0;
   int nsm = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  /* host<->device copies of the chunked host-buffer path */
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::string err;
   std::map<std::string, gbode::DevBuf> bufs;
@@ -65,7 +69,8 @@ struct ode_handle {
   std::vector<gbode::UserOutput> outputs;
   std::vector<gbode::UserSde> sdes;
   std::map<std::string, CUfunction> sde_kernels;
-  gbode::GraphEntry graph;
+  std::vector<gbode::GraphEntry> graphs;
+  unsigned long long graph_tick = 0;
   gbode::Model* model = nullptr;
 };
 

@@ -1057,7 +1057,7 @@ __device__ __forceinline__ void run_adaptive_persistent(const KParams& P) {
  * warp iteration pays for a full interpolation on a few lanes).  Here an
  * accepted step only appends a job per saveat point to a per-warp ring in
  * shared memory (a snapshot of what the interpolation reads: the state before
- * the step, the stage values, the parameters, t, dt and theta); whenever 32
+ * the step, the stage values, for Verner the parameters, t and dt); whenever 32
  * jobs are waiting the whole warp interpolates 32 points at once, one per
  * lane.  Each point is computed by the same M::dense call on the same values,
  * so the results are bit-identical to the other drivers. */
@@ -1079,7 +1079,7 @@ struct StageLayout {
   typedef typename PR::T T;
   /* the parameters ride along only when the dense output evaluates f (Verner's extra stages) */
   enum { NREC = D * (PR::KAHAN ? 2 : 1) + M::NK * D + (M::DENSE_F ? F::NP : 0) };
-  enum { JOB = 4 * (int)sizeof(T) + 8 + NREC * (int)sizeof(R) + 4 };
+  enum { JOB = 3 * (int)sizeof(T) + 8 + NREC * (int)sizeof(R) + 4 };
   enum { CAP = (kStageBytesPerWarp / JOB) & ~7 };
 };
 
@@ -1093,10 +1093,10 @@ __device__ __forceinline__ void run_adaptive_staged(const KParams& P) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   unsigned char* qb = qmem[threadIdx.x >> 5];
-  T* tv = (T*)qb;                                            /* told, tnew, dtold, theta: [4][CAP] */
-  long long* iv = (long long*)(qb + 4 * CAP * sizeof(T));    /* trajectory: [CAP] */
-  R* rv = (R*)(qb + 4 * CAP * sizeof(T) + 8 * CAP);          /* record values: [NREC][CAP] */
-  int* jv = (int*)(qb + 4 * CAP * sizeof(T) + 8 * CAP + SL::NREC * CAP * sizeof(R)); /* saveat index */
+  T* tv = (T*)qb;                                            /* told, tnew, dtold: [3][CAP] */
+  long long* iv = (long long*)(qb + 3 * CAP * sizeof(T));    /* trajectory: [CAP] */
+  R* rv = (R*)(qb + 3 * CAP * sizeof(T) + 8 * CAP);          /* record values: [NREC][CAP] */
+  int* jv = (int*)(qb + 3 * CAP * sizeof(T) + 8 * CAP + SL::NREC * CAP * sizeof(R)); /* saveat index */
   int qhead = 0, qcount = 0; /* warp-uniform */
 
   Lane<PR, D, F, NK> l;
@@ -1124,7 +1124,11 @@ __device__ __forceinline__ void run_adaptive_staged(const KParams& P) {
         for (int q = 0; q < F::NP; ++q) f2.p[q] = rv[(POFF + q) * CAP + slot];
       }
       double v[D];
-      M::dense(f2, uh, uc, tv[slot], tv[CAP + slot], tv[2 * CAP + slot], tv[3 * CAP + slot], kk, v);
+      /* the abscissa is computed here, by all lanes of the round at once, rather
+       * than by the few lanes that crossed a save point in their step */
+      const T told = tv[slot], dtold = tv[2 * CAP + slot];
+      const T theta = ((T)P.saveat[jv[slot]] - told) * recip(dtold);
+      M::dense(f2, uh, uc, told, tv[CAP + slot], dtold, theta, kk, v);
       store_point<PR, D>(P, iv[slot], jv[slot], v);
     }
     __syncwarp();
@@ -1181,16 +1185,13 @@ __device__ __forceinline__ void run_adaptive_staged(const KParams& P) {
       space = CAP - qcount;
     }
     if (njobs) {
-      const T inv_dt = recip(st.dtold);
       for (int q = 0; q < njobs; ++q) {
         const long long j = l.cur + q;
-        const T theta = ((T)P.saveat[j] - st.told) * inv_dt;
         if (excl + q < space) {
           const int slot = (qhead + qcount + excl + q) % CAP;
           tv[slot] = st.told;
           tv[CAP + slot] = l.t;
           tv[2 * CAP + slot] = st.dtold;
-          tv[3 * CAP + slot] = theta;
           iv[slot] = l.idx;
           jv[slot] = (int)j;
 #pragma unroll
@@ -1208,6 +1209,7 @@ __device__ __forceinline__ void run_adaptive_staged(const KParams& P) {
           }
         } else {
           /* the ring is full: interpolate here */
+          const T theta = ((T)P.saveat[j] - st.told) * recip(st.dtold);
           double v[D];
           M::dense(l.f, l.uh, l.uc, st.told, l.t, st.dtold, theta, l.k, v);
           store_point<PR, D>(P, l.idx, j, v);

@@ -249,3 +249,38 @@ def test_every_step_output_verner_fp32_kahan(pkg, po):
                    save_everystep=True, abstol=1e-7, reltol=1e-7, nthreads=8)
     assert np.array_equal(sol.offsets, ref["offsets"])
     assert np.array_equal(sol.ts_rows, ref["ts_rows"]) and np.array_equal(sol.us_rows, ref["us_rows"])
+
+
+def test_chunked_host_path_equals_device_path(pkg):
+    """Host buffers and at least 2 x 262,144 trajectories: the solve runs in
+    chunks whose output copies overlap the next chunk's kernel.  Every output
+    equals the unchunked device-buffer solve's."""
+    import torch
+    from conftest import lorenz_inputs
+    n = 540000
+    u0, p = lorenz_inputs(n, seed=71)
+    sv = np.linspace(0, 2, 11)
+    e = pkg.EnsembleProblem(pkg.ODEProblem("lorenz", u0[:, 0], (0.0, 2.0), p[:, 0]), u0s=u0, ps=p)
+    kw = dict(dt=0.1, abstol=1e-8, reltol=1e-6, saveat=sv, schedule="persistent")
+    a = pkg.solve(e, pkg.GPUSimpleATsit5(), trajectories=n, **kw)
+    assert a.stats.launches >= 3  # three chunks
+    L = pkg._lib
+    h = pkg._handle(0)
+    args = pkg.make_args(pkg.GPUSimpleATsit5(), 0, u0, p, (0.0, 2.0), 0.1, 1e-8, 1e-6, sv, False, "fp64",
+                         "persistent", 0, memory=L.MEM_DEVICE)
+    du0, dp = torch.tensor(u0, device="cuda"), torch.tensor(p, device="cuda")
+    args.u0, args.p = du0.data_ptr(), dp.data_ptr()
+    outs = {"us": torch.empty((11, 3, n), dtype=torch.float64, device="cuda"),
+            "u_final": torch.empty((3, n), dtype=torch.float64, device="cuda"),
+            "naccept": torch.empty(n, dtype=torch.int32, device="cuda"),
+            "retcode": torch.empty(n, dtype=torch.int8, device="cuda")}
+    o = L.SolveOut()
+    for k, v in outs.items():
+        setattr(o, k, v.data_ptr())
+    st = L.SolveStats()
+    h.check(h.solve_raw(args, o, st), allow=(L.ETRAJ,))
+    assert st.launches == 1
+    assert np.array_equal(a.us, outs["us"].cpu().numpy())
+    assert np.array_equal(a.u_final, outs["u_final"].cpu().numpy())
+    assert np.array_equal(a.naccept, outs["naccept"].cpu().numpy())
+    assert np.array_equal(a.retcode, outs["retcode"].cpu().numpy())
