@@ -881,6 +881,13 @@ __device__ __forceinline__ int adaptive_try(const KParams& P, Lane<PR, D, F, NK>
   const double dtmin = M::DTMIN_1F7 ? (double)1.0e-7f : 1.0e-14;
   if ((double)l.dt < dtmin) { lane_finish(P, l, RET_DTMIN, tot); return TRY_STOPPED; }
   if (P.maxiters > 0 && l.att >= P.maxiters) { lane_finish(P, l, RET_MAXITERS, tot); return TRY_STOPPED; }
+  /* The end-of-span bookkeeping of an accepted step depends only on t and dt,
+   * both known now: computed before the stages (the same operations, so the
+   * same values), it overlaps them instead of lengthening every attempt's
+   * dependency chain after the error estimate. */
+  const T tf = (T)P.tf;
+  const T rest = tf - l.t - l.dt;
+  const T tnext = ((double)rest < dtmin) ? tf : l.t + l.dt;
   R e[D];
   M::attempt(l.f, l.uh, l.uc, l.t, l.dt, l.k, nh, nc, e, true);
   l.att += 1;
@@ -929,13 +936,11 @@ __device__ __forceinline__ int adaptive_try(const KParams& P, Lane<PR, D, F, NK>
   float q = is_zero ? QMAXI : __fdiv_rn(q11, l.qoldp);
   q = fm_max(QMAXI, fm_min(QMINI, __fdiv_rn(q, GAM)));
   l.qoldp = ctrl_pow(jmax(Ef, QOLDINIT), B2);
-  const T tf = (T)P.tf;
   const T dtold = l.dt;
   const T dtn = l.dt * (T)__fdiv_rn(1.0f, q);
-  const T rest = tf - l.t - dtold;
   l.dt = absmin(dtn, rest);
   const T told = l.t;
-  l.t = ((double)rest < dtmin) ? tf : l.t + dtold;
+  l.t = tnext;
   if (l.nacc == 0) l.dt_first = (double)dtold;
   l.nacc += 1;
   acc_out.told = told;
