@@ -133,7 +133,11 @@ typedef struct {
   const double* u0;     /* [dim][n] */
   const double* p;      /* [nparams][n] */
   const double* dt0;    /* optional [n] per-trajectory initial dt (adaptive), or NULL */
-  void* stream;         /* cudaStream_t, or NULL for the handle's stream */
+  void* stream;         /* cudaStream_t, or NULL for the handle's stream.  With device buffers, a
+                           stream and stats == NULL, ode_ensemble_solve is asynchronous: it
+                           returns once the work is enqueued (per-trajectory retcodes tell of
+                           early stops; ODE_ETRAJ is not reported) and later calls on the same
+                           stream are ordered after it */
   int32_t output;       /* ODE_OUTPUT_* (0: the state) */
 } ode_solve_args;
 

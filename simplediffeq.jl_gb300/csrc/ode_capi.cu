@@ -878,6 +878,8 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
   }
   CK(cudaEventRecord(h->ev1, s), "event");
 
+  /* asynchronous call: device buffers, the caller's stream, no statistics asked */
+  if (!host && a->stream && !st) return ODE_OK;
   /* outputs back to the host */
   if (host) {
     for (OutMap& m : outs)

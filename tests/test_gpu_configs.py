@@ -284,3 +284,34 @@ def test_chunked_host_path_equals_device_path(pkg):
     assert np.array_equal(a.u_final, outs["u_final"].cpu().numpy())
     assert np.array_equal(a.naccept, outs["naccept"].cpu().numpy())
     assert np.array_equal(a.retcode, outs["retcode"].cpu().numpy())
+
+
+def test_asynchronous_device_solve_on_a_caller_stream(pkg):
+    """Device buffers + the caller's stream + no stats: the call returns once
+    the solve is enqueued; after a stream synchronize the results equal a
+    synchronous solve's."""
+    import torch
+    from conftest import lorenz_inputs
+    L = pkg._lib
+    h = pkg._handle(0)
+    n = 20000
+    u0, p = lorenz_inputs(n, seed=81)
+    sv = np.linspace(0, 5, 26)
+    stream = torch.cuda.Stream()
+    du0, dp = torch.tensor(u0, device="cuda"), torch.tensor(p, device="cuda")
+    res = []
+    for asynchronous in (True, False):
+        a = pkg.make_args(pkg.GPUSimpleATsit5(), 0, u0, p, (0.0, 5.0), 0.1, 1e-8, 1e-6, sv, False, "fp64",
+                          "persistent", 0, memory=L.MEM_DEVICE)
+        a.u0, a.p = du0.data_ptr(), dp.data_ptr()
+        a.stream = stream.cuda_stream if asynchronous else None
+        us = torch.empty((26, 3, n), dtype=torch.float64, device="cuda")
+        uf = torch.empty((3, n), dtype=torch.float64, device="cuda")
+        o = L.SolveOut()
+        o.us, o.u_final = us.data_ptr(), uf.data_ptr()
+        rc = h.solve_raw(a, o, None if asynchronous else L.SolveStats())
+        assert rc == L.OK
+        stream.synchronize()
+        torch.cuda.synchronize()
+        res.append((us.cpu(), uf.cpu()))
+    assert torch.equal(res[0][0], res[1][0]) and torch.equal(res[0][1], res[1][1])
