@@ -194,8 +194,8 @@ def julia_range(start, step, stop, T="fp64"):
         ln = round(lf) + 1
         stop2 = _t(T, start + _t(T, (ln - 1) * step))
         ln -= int(start < stop < stop2) + int(start > stop > stop2)
-    fs, fh = Fraction(start), Fraction(step)
-    return np.array([_to_T(fs + i * fh, T) for i in range(ln)])
+    # literal StepRangeLen: start + (i*step), each rounded once in Float64 (Float32 ranges too), then to T
+    return np.array([_to_T(Fraction(float(start) + float(i) * float(step)), T) for i in range(ln)])
 
 
 # --------------------------------------------------------------------------- solve

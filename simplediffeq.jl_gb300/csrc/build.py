@@ -25,7 +25,7 @@ LIB = os.path.join(PKG, "lib")
 NVCC = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
 CUDA_HOME = os.path.dirname(os.path.dirname(os.path.realpath(NVCC)))
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC", "-I", HERE]
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", HERE]
 
 # Kernels compiled ahead of time: (alg, kind, rhs, dim, precision, rhs C++ type).
 # Everything else is compiled on first use with NVRTC from the same headers.

@@ -7,11 +7,12 @@
  * looks for small-integer ratios start = a/d, step = b/d, stop = c/d with
  * Base.rat (a continued fraction limited to 2^24 for Float64, 2^11 for
  * Float32); if found, the length comes from integer arithmetic and element i
- * is the correctly rounded value of (a + (i-1) b)/d.  Otherwise it takes
- * start and step literally, length round((stop-start)/step)+1 adjusted for
- * overshoot, and element i is the correctly rounded value of
- * start + (i-1)*step.  Both are restated here in double (or float) arithmetic
- * with exact integer and fused-multiply-add helpers.
+ * is (a + (i-1) b)/d, which Julia evaluates in double-double (restated here
+ * as the correctly rounded quotient).  Otherwise it takes start and step
+ * literally, length round((stop-start)/step)+1 adjusted for overshoot, and
+ * element i is what StepRangeLen's getindex computes with a zero low part
+ * in start and step: start + ((i-1)*step), each operation rounded once (for
+ * Float32 in Float64, then rounded to Float32).
  */
 #pragma once
 #include <cmath>
@@ -73,17 +74,13 @@ static T ratio(int64_t num, int64_t den) {
   return (T)f;
 }
 
-/* start + i*step rounded once (double-double evaluation of the exact value) */
+/* start + (i*step), each rounded once in double (getindex of the literal
+ * StepRangeLen: the product i*step.hi rounds, the sum with start is exact in
+ * two parts and rounds once when the parts are added) */
 template <class T>
 static T literal_elem(T start, T step, int64_t i) {
-  double s = (double)step, a = (double)start, fi = (double)i;
-  double p = fi * s;
-  double pe = std::fma(fi, s, -p);   /* exact product = p + pe */
-  double sum = a + p;
-  double bb = sum - a;
-  double err = (a - (sum - bb)) + (p - bb); /* exact a + p = sum + err */
-  double r = sum + (err + pe);
-  return (T)r;
+  const double p = (double)i * (double)step;
+  return (T)((double)start + p);
 }
 
 /* Number of elements and (optionally) the elements. */

@@ -104,3 +104,23 @@ def test_ctypes_structs_match_the_c_layout(pkg, tmp_path):
     subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     assert got == expect
+
+
+def test_fixed_grid_property_random_ranges(pkg, po):
+    """Property check of the library's Julia-range restatement against the
+    oracle's independent one on random (t0, dt, tf), including steps that do
+    not divide the span and spans of one point."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+
+    @hyp.settings(max_examples=300, deadline=None)
+    @hyp.given(st.floats(-100, 100), st.floats(1e-3, 10), st.floats(0, 200))
+    def check(t0, dt, span):
+        tf = t0 + span
+        if span / dt > 1e5:
+            return
+        a = pkg.fixed_grid(t0, dt, tf, "fp64")
+        b = po.julia_range(t0, dt, tf, "fp64")
+        assert len(a) == len(b) and np.array_equal(a, b)
+
+    check()
