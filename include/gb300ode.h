@@ -55,7 +55,8 @@ enum {
   ODE_ENVRTC = -5,   /* run-time compilation of a kernel failed (log in ode_last_error) */
   ODE_ETRAJ = -6,    /* the solve completed but some trajectory ended with retcode DTMIN or MAXITERS */
   ODE_ENOMODEL = -7, /* learned schedule requested without a fitted model */
-  ODE_ESMALL = -8    /* output buffers too small: the size needed is reported (ode_ensemble_solve_everystep) */
+  ODE_ESMALL = -8,   /* output buffers too small: the size needed is reported (ode_ensemble_solve_everystep) */
+  ODE_ECHECK = -9    /* bounds-check mode found an out-of-range index or a trajectory not solved exactly once */
 };
 
 /* algorithms: the GPUSimple* solver types */
@@ -163,6 +164,14 @@ typedef struct {
   int32_t graph_replayed; /* 1 if a captured CUDA graph was replayed */
   int32_t jit;            /* 1 if the solver kernel was compiled at run time */
 } ode_solve_stats;
+
+/* Bounds-check mode (debugging; compute-sanitizer stands in for nothing
+ * here): with enable = 1 every later solve on this handle runs kernels
+ * compiled at run time with an index check before every access to a caller
+ * array and a per-trajectory start counter; a solve that saw an out-of-range
+ * index, or a trajectory started other than exactly once, returns ODE_ECHECK
+ * (the message says which).  Slower; results are unchanged. */
+int ode_set_bounds_check(ode_handle* h, int enable);
 
 /* Library version (ODE_ABI_VERSION). */
 int ode_abi_version(void);

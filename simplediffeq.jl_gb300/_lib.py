@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libgb300ode.so")
 PROBE_PATH = os.path.join(HERE, "lib", "libgb300ode_probe.so")
 
-OK, EINVAL, ECUDA, ENOMEM, ENOTSUP, ENVRTC, ETRAJ, ENOMODEL, ESMALL = 0, -1, -2, -3, -4, -5, -6, -7, -8
+OK, EINVAL, ECUDA, ENOMEM, ENOTSUP, ENVRTC, ETRAJ, ENOMODEL, ESMALL, ECHECK = 0, -1, -2, -3, -4, -5, -6, -7, -8, -9
 ALG = {"RK4": 0, "Tsit5": 1, "ATsit5": 2, "Vern7": 3, "AVern7": 4, "Vern9": 5, "AVern9": 6, "Euler": 7}
 RHS = {"lorenz": 0, "vanderpol": 1, "r3bp": 2, "kuramoto": 3, "linear": 4}
 PREC = {"fp64": 0, "fp32": 1, "fp32_kahan": 2}
@@ -26,7 +26,7 @@ RET_DEFAULT, RET_DTMIN, RET_MAXITERS, RET_NAN = 0, 1, 2, 3
 EXPORTS = ["ode_abi_version", "ode_create", "ode_destroy", "ode_last_error", "ode_ensemble_solve",
            "ode_fixed_grid", "ode_rhs_compile", "ode_output_compile", "ode_learn_default_opts", "ode_learn_fit",
            "ode_learn_predict", "ode_learn_gradcheck", "ode_ensemble_solve_noalloc", "ode_autotune",
-           "ode_ensemble_solve_everystep", "ode_sde_solve", "ode_sde_compile"]
+           "ode_ensemble_solve_everystep", "ode_sde_solve", "ode_sde_compile", "ode_set_bounds_check"]
 SDE = {"gbm": 0, "ou": 1, "lorenz": 2}
 
 
@@ -198,6 +198,9 @@ class Handle:
     def solve_raw(self, args, out, stats=None):
         return self.lib.ode_ensemble_solve(self.h, ctypes.byref(args), ctypes.byref(out),
                                            ctypes.byref(stats) if stats is not None else None)
+
+    def set_bounds_check(self, enable=True):
+        self.check(self.lib.ode_set_bounds_check(self.h, int(bool(enable))))
 
     def solve_everystep(self, args, out, stats=None):
         return self.lib.ode_ensemble_solve_everystep(self.h, ctypes.byref(args), ctypes.byref(out),

@@ -290,8 +290,8 @@ int output_width(ode_handle* h, const ode_solve_args* a) {
 
 std::string kernel_key(ode_handle* h, const ode_solve_args* a, int sched) {
   char b[160];
-  snprintf(b, sizeof b, "%s|%s|%d|%d|%s|%d", alg_name(a->alg), entry_kind(a->alg, sched, a->nsave), a->rhs, a->dim,
-           prec_name(a->precision), a->output >= ODE_OUTPUT_USER ? a->output : 0);
+  snprintf(b, sizeof b, "%s|%s|%d|%d|%s|%d%s", alg_name(a->alg), entry_kind(a->alg, sched, a->nsave), a->rhs, a->dim,
+           prec_name(a->precision), a->output >= ODE_OUTPUT_USER ? a->output : 0, h->bounds_check ? "|chk" : "");
   return b;
 }
 
@@ -385,7 +385,9 @@ int load_cubin(ode_handle* h, const std::vector<char>& cubin, int block, CUfunct
 int compile_jit(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn, std::string* log_out) {
   std::vector<char> cubin;
   std::string err;
-  const int rc = nvrtc_cubin(jit_source(h, a, sched), {}, &cubin, log_out, &err);
+  std::vector<std::string> opts;
+  if (h->bounds_check) opts.push_back("-DGBODE_BOUNDS_CHECK");
+  const int rc = nvrtc_cubin(jit_source(h, a, sched), opts, &cubin, log_out, &err);
   if (rc != ODE_OK) return fail(h, rc, err);
   return load_cubin(h, cubin, 128, fn);
 }
@@ -394,7 +396,7 @@ int compile_jit(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* f
 int get_kernel(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn, int* jit) {
   const std::string key = kernel_key(h, a, sched);
   auto tt = h->tuned.find(key);
-  if (tt != h->tuned.end()) {
+  if (!h->bounds_check && tt != h->tuned.end()) {
     *fn = tt->second;
     *jit = 1;
     return ODE_OK;
@@ -407,7 +409,7 @@ int get_kernel(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn
   }
   const char* kind = entry_kind(a->alg, sched, a->nsave);
   for (const AotEntry& e : kAotEntries) {
-    if (a->output < ODE_OUTPUT_USER && e.alg == a->alg && e.rhs == a->rhs && e.dim == a->dim &&
+    if (!h->bounds_check && a->output < ODE_OUTPUT_USER && e.alg == a->alg && e.rhs == a->rhs && e.dim == a->dim &&
         e.precision == a->precision && std::strcmp(e.kind, kind) == 0) {
       cudaFunction_t f;
       cudaError_t ce = cudaGetFuncBySymbol(&f, e.fn);
@@ -490,6 +492,12 @@ int launch_params(ode_handle* h, CUfunction fn, unsigned grid, unsigned block, v
 extern "C" {
 
 int ode_abi_version(void) { return ODE_ABI_VERSION; }
+
+int ode_set_bounds_check(ode_handle* h, int enable) {
+  if (!h) return ODE_EINVAL;
+  h->bounds_check = enable != 0;
+  return ODE_OK;
+}
 
 int ode_create(ode_handle** out, int device) {
   if (!out) return ODE_EINVAL;
@@ -629,6 +637,7 @@ struct EveryStep {
 };
 
 int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_solve_stats* st, const EveryStep* ev) {
+  NvtxRange nvtx("gbode solve");
   const auto wall0 = std::chrono::steady_clock::now();
   if (!h) return ODE_EINVAL;
   if (!a || !o) return fail(h, ODE_EINVAL, "null argument");
@@ -768,6 +777,13 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
   if (!stats) return rc;
   kp.stats = stats;
   kp.counter = stats + 3;
+  unsigned* chk = nullptr;
+  if (h->bounds_check) {
+    /* [0] violation bits, [16..16+n) per-trajectory start counts */
+    if (!(chk = (unsigned*)buf(h, "check", ((size_t)n + 16) * sizeof(unsigned), &rc))) return rc;
+    kp.check_flags = chk;
+    kp.visited = chk + 16;
+  }
 
   /* schedule */
   int launches = 0;
@@ -806,6 +822,7 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
    * graph and replayed while the launch parameters stay the same. */
   auto enqueue = [&](int* nl) -> int {
     CK(cudaMemsetAsync(stats, 0, 4 * sizeof(unsigned long long), s), "memset stats");
+    if (chk) CK(cudaMemsetAsync(chk, 0, ((size_t)n + 16) * sizeof(unsigned), s), "memset check");
     if (sched == ODE_SCHED_LEARNED && n > 0) {
       int r = model_predict_device(h, a, kp, latt, ldt, s, nl);
       if (r == ODE_OK) r = order_by_cost(h, latt, n, order, bins, s, nl);
@@ -879,7 +896,7 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
   CK(cudaEventRecord(h->ev1, s), "event");
 
   /* asynchronous call: device buffers, the caller's stream, no statistics asked */
-  if (!host && a->stream && !st) return ODE_OK;
+  if (!host && a->stream && !st && !chk) return ODE_OK;
   /* outputs back to the host */
   if (host) {
     for (OutMap& m : outs)
@@ -887,7 +904,24 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
   }
   unsigned long long hs[4] = {0, 0, 0, 0};
   CK(cudaMemcpyAsync(hs, stats, sizeof hs, cudaMemcpyDeviceToHost, s), "copy stats");
+  std::vector<unsigned> hchk;
+  if (chk) {
+    hchk.resize((size_t)n + 16);
+    CK(cudaMemcpyAsync(hchk.data(), chk, hchk.size() * sizeof(unsigned), cudaMemcpyDeviceToHost, s), "copy check");
+  }
   CK(cudaStreamSynchronize(s), "solve");
+  if (chk) {
+    int64_t bad = -1;
+    for (int64_t i = 0; i < n && bad < 0; ++i)
+      if (hchk[16 + (size_t)i] != 1) bad = i;
+    if (hchk[0] || bad >= 0) {
+      char m[256];
+      snprintf(m, sizeof m, "bounds check: violation bits 0x%x (1 trajectory, 2 save point, 4 every-step row, "
+               "8 staging ring, 16 order); trajectory %lld started %u times",
+               hchk[0], (long long)bad, bad >= 0 ? hchk[16 + (size_t)bad] : 1u);
+      return fail(h, ODE_ECHECK, m);
+    }
+  }
   float ms = 0.f;
   cudaEventElapsedTime(&ms, h->ev0, h->ev1);
   if (st) {
@@ -918,6 +952,7 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
 constexpr int64_t kChunk = 262144;
 
 int solve_chunked(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_solve_stats* st) {
+  NvtxRange nvtx("gbode chunked solve");
   const auto wall0 = std::chrono::steady_clock::now();
   CK(cudaSetDevice(h->device), "cudaSetDevice");
   const int64_t n = a->n;
@@ -1151,6 +1186,8 @@ int ode_ensemble_solve_everystep(ode_handle* h, const ode_solve_args* a, ode_eve
  * saveat staging ring, never in arithmetic, so results do not change. */
 int ode_autotune(ode_handle* h, const ode_solve_args* a, int64_t sample, ode_tune_report* rep) {
   if (!h) return ODE_EINVAL;
+  NvtxRange nvtx("gbode autotune");
+  if (h->bounds_check) return fail(h, ODE_ENOTSUP, "autotuning is off in bounds-check mode");
   if (!a) return fail(h, ODE_EINVAL, "null arguments");
   if (is_fixed(a->alg)) return fail(h, ODE_EINVAL, "autotuning applies to the adaptive algorithms");
   if (a->n < 1 || (a->memory != ODE_MEM_HOST && a->memory != ODE_MEM_DEVICE))

@@ -8,6 +8,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/gb300ode.h"
 #include "ode_kparams.h"
 
@@ -72,9 +74,18 @@ struct ode_handle {
   std::vector<gbode::GraphEntry> graphs;
   unsigned long long graph_tick = 0;
   gbode::Model* model = nullptr;
+  bool bounds_check = false;  /* ode_set_bounds_check */
 };
 
 namespace gbode {
+
+/* NVTX range for the lifetime of a scope (visible in Nsight Systems / ncu --nvtx) */
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 /* error helpers: record a message on the handle and return the code */
 int fail(ode_handle* h, int code, const std::string& msg);

@@ -35,6 +35,8 @@ struct KParams {
   const int* order;        /* persistent: position -> trajectory, or 0 for identity */
   unsigned long long* counter;   /* persistent: next position to hand out (zeroed before launch) */
   unsigned long long* stats;     /* [2] attempts and saves summed over trajectories, or 0 */
+  unsigned* check_flags;   /* bounds-check builds: violation bits (CHK_*), or 0 */
+  unsigned* visited;       /* bounds-check builds: [n] starts of each trajectory, or 0 */
 };
 
 }  // namespace gbode

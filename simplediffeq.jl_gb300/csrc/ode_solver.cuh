@@ -38,6 +38,19 @@
 
 namespace gbode {
 
+/* Bounds-check build (-DGBODE_BOUNDS_CHECK, compiled at run time when a
+ * handle asks for it): every index into a caller array is checked against
+ * its extent before the access; a violation sets a bit in P.check_flags and
+ * the access is skipped (or clamped to a valid index).  Each trajectory start
+ * is counted in P.visited, so the host can verify that the schedule handed
+ * every trajectory out exactly once.  Without the flag the checks vanish. */
+enum { CHK_TRAJ = 1, CHK_SAVE = 2, CHK_STEP = 4, CHK_RING = 8, CHK_ORDER = 16 };
+#ifdef GBODE_BOUNDS_CHECK
+#define GBODE_CHECK(P, cond, bit) ((cond) ? true : (atomicOr((P).check_flags, (unsigned)(bit)), false))
+#else
+#define GBODE_CHECK(P, cond, bit) true
+#endif
+
 /* ------------------------------------------------------------------ math */
 __device__ __forceinline__ double fmaR(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ float fmaR(float a, float b, float c) { return __fmaf_rn(a, b, c); }
@@ -727,6 +740,7 @@ struct Lane {
 template <class PR, int D>
 __device__ __forceinline__ void store_point(const KParams& P, long long idx, long long j, const double (&v)[D]) {
   if (!P.us) return;
+  if (!GBODE_CHECK(P, idx >= 0 && idx < P.n && j >= 0 && j < (P.nsave > 0 ? P.nsave : P.ngrid), CHK_SAVE)) return;
 #ifdef GBODE_USER_OUTPUT
   /* a user output function (ode_output_compile), defined before this header by
    * the run-time compiled translation unit together with GBODE_OUTPUT_WIDTH and
@@ -772,6 +786,7 @@ template <class PR, int D, class L>
 __device__ __forceinline__ void store_step(const KParams& P, const L& l, long long k) {
   if (!P.ev_t) return;
   const long long r = P.ev_off[l.idx] + k;
+  if (!GBODE_CHECK(P, r >= P.ev_off[l.idx] && r < P.ev_off[l.idx + 1], CHK_STEP)) return;
   double v[D];
   state_value<PR, D>(l, v);
   P.ev_t[r] = (double)l.t;
@@ -782,6 +797,10 @@ __device__ __forceinline__ void store_step(const KParams& P, const L& l, long lo
 /* Load trajectory idx: parameters, u0, t0, dt; first saveat point if it is t0. */
 template <class PR, int D, class F, int NK>
 __device__ __forceinline__ void lane_load(const KParams& P, long long idx, Lane<PR, D, F, NK>& l) {
+  if (!GBODE_CHECK(P, idx >= 0 && idx < P.n, CHK_TRAJ)) idx = 0;
+#ifdef GBODE_BOUNDS_CHECK
+  atomicAdd(&P.visited[idx], 1u);
+#endif
   typedef typename PR::R R;
   typedef typename PR::T T;
   l.idx = idx;
@@ -849,8 +868,13 @@ __device__ __forceinline__ void lane_finish(const KParams& P, Lane<PR, D, F, NK>
   if (P.nreject) P.nreject[idx] = l.nrej;
   if (P.dt_first) P.dt_first[idx] = l.dt_first;
   if (P.us) {
+    /* save points never reached: NaN, in the layout of the output kind */
     const double qnan = __longlong_as_double(0x7ff8000000000000LL);
+#ifdef GBODE_USER_OUTPUT
+    const int width = P.output == 1 ? 1 : (P.output >= 1000 ? GBODE_OUTPUT_WIDTH : D);
+#else
     const int width = P.output == 1 ? 1 : D;
+#endif
     for (long long j = l.cur; j < P.nsave; ++j)
       for (int d = 0; d < width; ++d) P.us[(j * width + d) * P.n + idx] = qnan;
   }
@@ -1038,7 +1062,8 @@ __device__ __forceinline__ void run_adaptive_persistent(const KParams& P) {
       if (want) {
         const unsigned long long w = base + (unsigned long long)__popc(need & ((1u << lane) - 1u));
         if (w < (unsigned long long)P.n) {
-          const long long idx = P.order ? (long long)P.order[w] : (long long)w;
+          long long idx = P.order ? (long long)P.order[w] : (long long)w;
+          if (!GBODE_CHECK(P, idx >= 0 && idx < P.n, CHK_ORDER)) idx = 0;
           active = !adaptive_start<M>(P, idx, l, tot);
         } else {
           exhausted = true;
@@ -1152,7 +1177,8 @@ __device__ __forceinline__ void run_adaptive_staged(const KParams& P) {
       if (want) {
         const unsigned long long w = base + (unsigned long long)__popc(need & ((1u << lane) - 1u));
         if (w < (unsigned long long)P.n) {
-          const long long idx = P.order ? (long long)P.order[w] : (long long)w;
+          long long idx = P.order ? (long long)P.order[w] : (long long)w;
+          if (!GBODE_CHECK(P, idx >= 0 && idx < P.n, CHK_ORDER)) idx = 0;
           active = !adaptive_start<M>(P, idx, l, tot);
         } else {
           exhausted = true;
@@ -1224,6 +1250,7 @@ __device__ __forceinline__ void run_adaptive_staged(const KParams& P) {
       l.ninterp += njobs;
     }
     qcount += total < space ? total : space;
+    (void)GBODE_CHECK(P, qcount >= 0 && qcount <= CAP, CHK_RING);
     if (r == TRY_ACCEPTED) {
       adaptive_commit<M>(l, nh, nc);
       store_step<PR, D>(P, l, l.nacc);

@@ -1,0 +1,75 @@
+"""Bounds-check mode (ode_set_bounds_check): the kernels recompiled with an
+index check before every access to a caller array and a per-trajectory start
+counter.  Every schedule and path reports no violation, every trajectory is
+started exactly once (the persistent work counter hands each out once), and
+the results equal those of the unchecked kernels."""
+import numpy as np
+import pytest
+
+from conftest import lorenz_inputs
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def checked(pkg):
+    h = pkg._lib.Handle(0)
+    h.set_bounds_check(True)
+    yield h
+    h.close()
+
+
+def _solve(pkg, h, alg, sched, u0, p, tspan, sv, every=False, output="state"):
+    L = pkg._lib
+    n = u0.shape[1]
+    oid = pkg._output_id(h, output, 3, 3)
+    a = pkg.make_args(alg, 0, u0, p, tspan, 0.1 if alg.adaptive else 0.01, 1e-8, 1e-6, sv, every, "fp64", sched, 0,
+                      output=oid)
+    width = output.width if isinstance(output, pkg.UserOutput) else 3
+    npts = len(sv) if sv is not None else (len(pkg.fixed_grid(tspan[0], 0.01, tspan[1])) if every else 0)
+    outs = {"u_final": np.empty((3, n)), "naccept": np.empty(n, dtype=np.int32),
+            "retcode": np.empty(n, dtype=np.int8)}
+    if npts:
+        outs["us"] = np.empty((npts, width, n))
+    o = L.SolveOut()
+    for k, v in outs.items():
+        setattr(o, k, v.ctypes.data)
+    rc = h.solve_raw(a, o, L.SolveStats())
+    return rc, outs
+
+
+@pytest.mark.parametrize("alg,sched", [("ATsit5", "plain"), ("ATsit5", "persistent"), ("AVern7", "persistent"),
+                                       ("AVern9", "persistent"), ("Tsit5", "plain"), ("RK4", "plain"),
+                                       ("Euler", "plain")])
+def test_no_violation_and_same_results(pkg, checked, alg, sched):
+    L = pkg._lib
+    u0, p = lorenz_inputs(3000, seed=101)
+    algo = getattr(pkg, "GPUSimple" + alg)()
+    fixed = alg in ("Tsit5", "RK4", "Euler")
+    sv = None if alg in ("RK4", "Euler") else np.linspace(0, 2, 17)
+    every = alg in ("RK4", "Euler")
+    rc, a = _solve(pkg, checked, algo, sched, u0, p, (0.0, 2.0), sv, every)
+    assert rc in (L.OK, L.ETRAJ), checked.error()
+    rc2, b = _solve(pkg, pkg._handle(0), algo, sched, u0, p, (0.0, 2.0), sv, every)
+    for k in a:
+        assert np.array_equal(a[k], b[k], equal_nan=True), k
+    assert not fixed or (a["naccept"] == 200).all()
+
+
+def test_no_violation_every_step_and_user_output(pkg, checked):
+    L = pkg._lib
+    u0, p = lorenz_inputs(2000, seed=102)
+    out = pkg.UserOutput("out[0] = u[0] * u[1];", width=1)
+    sv = np.array([0.0, 1.0, 3.0])  # the last point is never reached: NaN rows in width 1
+    rc, a = _solve(pkg, checked, pkg.GPUSimpleATsit5(), "persistent", u0, p, (0.0, 2.0), sv, output=out)
+    assert rc == L.OK, checked.error()
+    assert np.isnan(a["us"][2]).all()
+    args = pkg.make_args(pkg.GPUSimpleATsit5(), 0, u0, p, (0.0, 2.0), 0.1, 1e-8, 1e-6, None, False, "fp64",
+                         "persistent", 0)
+    off = np.empty(2001, dtype=np.int64)
+    o = L.EverystepOut()
+    o.offsets = off.ctypes.data
+    assert checked.solve_everystep(args, o) == L.ESMALL
+    ts, us = np.empty(o.total), np.empty((o.total, 3))
+    o.ts, o.us, o.capacity = ts.ctypes.data, us.ctypes.data, o.total
+    assert checked.solve_everystep(args, o) == L.OK, checked.error()

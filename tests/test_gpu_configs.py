@@ -315,3 +315,20 @@ def test_asynchronous_device_solve_on_a_caller_stream(pkg):
         torch.cuda.synchronize()
         res.append((us.cpu(), uf.cpu()))
     assert torch.equal(res[0][0], res[1][0]) and torch.equal(res[0][1], res[1][1])
+
+
+def test_user_output_unreached_points_are_nan_in_its_width(pkg):
+    """Save points after tf are never reached: their rows are NaN in the
+    output function's own width (2 here, not the state's 3), and every reached
+    row equals the function of the full-state solve."""
+    from conftest import lorenz_inputs
+    u0, p = lorenz_inputs(500, seed=91)
+    e = pkg.EnsembleProblem(pkg.ODEProblem("lorenz", u0[:, 0], (0.0, 1.0), p[:, 0]), u0s=u0, ps=p)
+    out = pkg.UserOutput("out[0] = u[0] + u[1];\n out[1] = u[2];", width=2)
+    sv = np.array([0.0, 0.5, 1.0, 1.5, 2.0])
+    for sched in ("plain", "persistent"):
+        a = pkg.solve(e, pkg.GPUSimpleATsit5(), trajectories=500, dt=0.1, saveat=sv, schedule=sched, output=out)
+        b = pkg.solve(e, pkg.GPUSimpleATsit5(), trajectories=500, dt=0.1, saveat=sv, schedule=sched)
+        assert a.us.shape == (5, 2, 500)
+        assert np.isnan(a.us[3:]).all()
+        assert np.array_equal(a.us[:3, 0], b.us[:3, 0] + b.us[:3, 1]) and np.array_equal(a.us[:3, 1], b.us[:3, 2])
