@@ -321,6 +321,15 @@ typedef struct {
 
 int ode_autotune(ode_handle* h, const ode_solve_args* a, int64_t sample, ode_tune_report* rep);
 
+/* Autotuning cache: ode_tune_save writes the launch shapes this handle has
+ * chosen (built-in right-hand sides and outputs only) to a text file tagged
+ * with the GPU's name and SM count; ode_tune_load reads such a file and, if
+ * it was written on the same kind of GPU, makes later solves use those shapes
+ * without tuning again (the kernels are compiled on first use).  A file from
+ * another GPU is ignored (ODE_ENOTSUP). */
+int ode_tune_save(ode_handle* h, const char* path);
+int ode_tune_load(ode_handle* h, const char* path);
+
 /* ---- learned schedule ---------------------------------------------------
  * A 2-hidden-layer ReLU MLP (bf16 weights, fp32 accumulation) maps each
  * trajectory's (p, u0) to (log attempts, log dt of the first accepted step).

@@ -26,7 +26,8 @@ RET_DEFAULT, RET_DTMIN, RET_MAXITERS, RET_NAN = 0, 1, 2, 3
 EXPORTS = ["ode_abi_version", "ode_create", "ode_destroy", "ode_last_error", "ode_ensemble_solve",
            "ode_fixed_grid", "ode_rhs_compile", "ode_output_compile", "ode_learn_default_opts", "ode_learn_fit",
            "ode_learn_predict", "ode_learn_gradcheck", "ode_ensemble_solve_noalloc", "ode_autotune",
-           "ode_ensemble_solve_everystep", "ode_sde_solve", "ode_sde_compile", "ode_set_bounds_check"]
+           "ode_ensemble_solve_everystep", "ode_sde_solve", "ode_sde_compile", "ode_set_bounds_check",
+           "ode_tune_save", "ode_tune_load"]
 SDE = {"gbm": 0, "ou": 1, "lorenz": 2}
 
 
@@ -146,6 +147,9 @@ def load():
     lib.ode_learn_gradcheck.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     lib.ode_autotune.argtypes = [ctypes.c_void_p, ctypes.POINTER(SolveArgs), ctypes.c_int64, ctypes.POINTER(TuneReport)]
+    lib.ode_tune_save.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+    lib.ode_tune_load.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
+    lib.ode_set_bounds_check.argtypes = [ctypes.c_void_p, ctypes.c_int]
     lib.ode_ensemble_solve_noalloc.argtypes = [ctypes.POINTER(SolveArgs), ctypes.POINTER(SolveOut), ctypes.c_char_p,
                                                ctypes.c_size_t]
     _lib = lib
@@ -198,6 +202,12 @@ class Handle:
     def solve_raw(self, args, out, stats=None):
         return self.lib.ode_ensemble_solve(self.h, ctypes.byref(args), ctypes.byref(out),
                                            ctypes.byref(stats) if stats is not None else None)
+
+    def tune_save(self, path):
+        self.check(self.lib.ode_tune_save(self.h, str(path).encode()))
+
+    def tune_load(self, path):
+        return self.lib.ode_tune_load(self.h, str(path).encode())
 
     def set_bounds_check(self, enable=True):
         self.check(self.lib.ode_set_bounds_check(self.h, int(bool(enable))))

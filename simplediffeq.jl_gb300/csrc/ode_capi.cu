@@ -401,6 +401,22 @@ int get_kernel(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn
     *jit = 1;
     return ODE_OK;
   }
+  auto ch = h->tune_choice.find(key);
+  if (!h->bounds_check && ch != h->tune_choice.end() && ch->second.size() == 3 && ch->second[0] > 0) {
+    /* a launch shape from ode_tune_load: compile that variant once */
+    const std::vector<int>& c = ch->second;
+    std::vector<std::string> o = {"-DGBODE_BLOCK=" + std::to_string(c[0]), "-DGBODE_STAGE_BYTES=" + std::to_string(c[2])};
+    if (c[1]) o.push_back("--maxrregcount=" + std::to_string(c[1]));
+    std::vector<char> cubin;
+    std::string lg, err;
+    int rc = nvrtc_cubin(jit_source(h, a, sched), o, &cubin, &lg, &err);
+    if (rc != ODE_OK) return fail(h, rc, err);
+    rc = load_cubin(h, cubin, c[0], fn);
+    if (rc != ODE_OK) return rc;
+    h->tuned[key] = *fn;
+    *jit = 1;
+    return ODE_OK;
+  }
   auto it = h->kcache.find(key);
   if (it != h->kcache.end()) {
     *fn = it->second;
@@ -496,6 +512,80 @@ int ode_abi_version(void) { return ODE_ABI_VERSION; }
 int ode_set_bounds_check(ode_handle* h, int enable) {
   if (!h) return ODE_EINVAL;
   h->bounds_check = enable != 0;
+  return ODE_OK;
+}
+
+/* GPU tag of a tuning file: name and SM count */
+static std::string gpu_tag(ode_handle* h) {
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, h->device) != cudaSuccess) {
+    cudaGetLastError();
+    return "unknown";
+  }
+  std::string name = prop.name;
+  for (char& c : name)
+    if (c == ' ' || c == '\t') c = '_';
+  return name + "/" + std::to_string(prop.multiProcessorCount);
+}
+
+/* kernel keys are alg|kind|rhs|dim|prec|output[|chk]; only built-in ids travel */
+static bool portable_key(const std::string& key) {
+  std::vector<std::string> f;
+  size_t a = 0;
+  for (size_t b; (b = key.find('|', a)) != std::string::npos; a = b + 1) f.push_back(key.substr(a, b - a));
+  f.push_back(key.substr(a));
+  return f.size() == 6 && std::atoi(f[2].c_str()) < ODE_RHS_USER && std::atoi(f[5].c_str()) < ODE_OUTPUT_USER;
+}
+
+int ode_tune_save(ode_handle* h, const char* path) {
+  if (!h) return ODE_EINVAL;
+  if (!path) return fail(h, ODE_EINVAL, "null path");
+  FILE* f = std::fopen(path, "w");
+  if (!f) return fail(h, ODE_EINVAL, std::string("cannot write ") + path);
+  std::fprintf(f, "gb300ode-tune 1 %s\n", gpu_tag(h).c_str());
+  for (const auto& kv : h->tune_choice)
+    if (portable_key(kv.first) && kv.second.size() == 3)
+      std::fprintf(f, "%s %d %d %d\n", kv.first.c_str(), kv.second[0], kv.second[1], kv.second[2]);
+  const bool ok = std::fclose(f) == 0;
+  return ok ? ODE_OK : fail(h, ODE_EINVAL, std::string("cannot write ") + path);
+}
+
+int ode_tune_load(ode_handle* h, const char* path) {
+  if (!h) return ODE_EINVAL;
+  if (!path) return fail(h, ODE_EINVAL, "null path");
+  FILE* f = std::fopen(path, "r");
+  if (!f) return fail(h, ODE_EINVAL, std::string("cannot read ") + path);
+  char magic[32] = {0}, tag[256] = {0};
+  int version = 0;
+  if (std::fscanf(f, "%31s %d %255s", magic, &version, tag) != 3 || std::strcmp(magic, "gb300ode-tune") != 0 ||
+      version != 1) {
+    std::fclose(f);
+    return fail(h, ODE_EINVAL, "not a tuning file");
+  }
+  if (gpu_tag(h) != tag) {
+    std::fclose(f);
+    return fail(h, ODE_ENOTSUP, std::string("tuning file written on another GPU (") + tag + ")");
+  }
+  std::map<std::string, std::vector<int>> read;
+  char key[160];
+  int b = 0, r = 0, st = 0;
+  int rc = ODE_OK;
+  while (true) {
+    const int got = std::fscanf(f, "%159s %d %d %d", key, &b, &r, &st);
+    if (got == EOF) break;
+    if (got != 4 || b < 0 || b > 1024 || b % 32 || r < 0 || r > 255 || st < 0 || st > 49152 ||
+        !portable_key(key)) {
+      rc = fail(h, ODE_EINVAL, "malformed tuning entry");
+      break;
+    }
+    read[key] = {b, r, st};
+  }
+  std::fclose(f);
+  if (rc != ODE_OK) return rc;
+  for (auto& kv : read) {
+    h->tune_choice[kv.first] = kv.second;
+    h->tuned.erase(kv.first);
+  }
   return ODE_OK;
 }
 
@@ -843,7 +933,7 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
     key += extra;
     if (sched == ODE_SCHED_LEARNED) key += model_key(h->model);
   }
-  const bool use_graph = s != 0 && !std::getenv("GBODE_NO_GRAPH");
+  const bool use_graph = s != 0;  /* the legacy default stream cannot be captured */
   int replayed = 0;
   CK(cudaEventRecord(h->ev0, s), "event");
   GraphEntry* cached = nullptr;
@@ -1316,6 +1406,8 @@ int ode_autotune(ode_handle* h, const ode_solve_args* a, int64_t sample, ode_tun
     }
   }
   if (best >= 0) h->tuned[key] = best_fn;
+  h->tune_choice[key] = best >= 0 ? std::vector<int>{vars[best].block, vars[best].regs, vars[best].stage}
+                                   : std::vector<int>{0, 0, 0};  /* 0: the default kernel won */
   if (rep) {
     rep->variants = tried;
     rep->block = best >= 0 ? vars[best].block : 128;

@@ -65,6 +65,9 @@ struct ode_handle {
   std::map<std::string, CUfunction> kcache;
   std::map<std::string, int> kjit;  /* 1 if the cached function was compiled at run time */
   std::map<std::string, CUfunction> tuned;  /* autotuned variant per kernel key */
+  /* launch shape chosen per kernel key (block, register cap, ring bytes), by
+   * ode_autotune or read by ode_tune_load; compiled on first use */
+  std::map<std::string, std::vector<int>> tune_choice;
   std::map<CUfunction, int> fblock;         /* threads per block of run-time compiled functions */
   std::vector<CUmodule> modules;
   std::vector<gbode::UserRhs> users;

@@ -124,3 +124,9 @@ def test_fixed_grid_property_random_ranges(pkg, po):
         assert len(a) == len(b) and np.array_equal(a, b)
 
     check()
+
+
+def test_tuning_cache_rejects_bad_files_without_a_gpu(pkg, tmp_path):
+    lib = pkg._lib.load()
+    assert lib.ode_tune_load(None, b"x") == pkg._lib.EINVAL
+    assert lib.ode_tune_save(None, b"x") == pkg._lib.EINVAL

@@ -332,3 +332,43 @@ def test_user_output_unreached_points_are_nan_in_its_width(pkg):
         assert a.us.shape == (5, 2, 500)
         assert np.isnan(a.us[3:]).all()
         assert np.array_equal(a.us[:3, 0], b.us[:3, 0] + b.us[:3, 1]) and np.array_equal(a.us[:3, 1], b.us[:3, 2])
+
+
+def test_tuning_cache_round_trip(pkg, tmp_path):
+    """ode_autotune's choice saved to a file and loaded by a fresh handle: the
+    fresh handle solves with the tuned variant (run-time compiled) without
+    tuning, and the results are unchanged; malformed files are refused."""
+    from conftest import lorenz_inputs
+    L = pkg._lib
+    n = 20000
+    u0, p = lorenz_inputs(n, seed=111)
+    sv = np.linspace(0, 5, 11)
+    args = pkg.make_args(pkg.GPUSimpleATsit5(), 0, u0, p, (0.0, 5.0), 0.1, 1e-8, 1e-6, sv, False, "fp64",
+                         "persistent", 0)
+    h1 = L.Handle(0)
+    rep = h1.autotune(args, sample=8192)
+    path = tmp_path / "tune.txt"
+    h1.tune_save(path)
+    text = path.read_text().splitlines()
+    assert text[0].startswith("gb300ode-tune 1 ") and len(text) == 2
+    h2 = L.Handle(0)
+    assert h2.tune_load(path) == L.OK
+    outs = []
+    for h in (h1, h2):
+        us, uf = np.empty((11, 3, n)), np.empty((3, n))
+        o = L.SolveOut()
+        o.us, o.u_final = us.ctypes.data, uf.ctypes.data
+        st = L.SolveStats()
+        h.check(h.solve_raw(args, o, st), allow=(L.ETRAJ,))
+        outs.append((us, uf, st.jit))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+    if rep.block and rep.best_ms < rep.default_ms:
+        assert outs[1][2] == 1  # the loaded shape was compiled at run time
+    bad = tmp_path / "bad.txt"
+    bad.write_text("gb300ode-tune 1 %s\natsit5|staged|0|3|fp64|0 33 0 12288\n" % text[0].split()[2])
+    assert h2.tune_load(bad) == L.EINVAL
+    other = tmp_path / "other.txt"
+    other.write_text("gb300ode-tune 1 Some_Other_GPU/99\n")
+    assert h2.tune_load(other) == L.ENOTSUP
+    h1.close()
+    h2.close()
