@@ -433,6 +433,7 @@ int get_kernel(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn
       *fn = (CUfunction)f;
       h->kcache[key] = *fn;
       h->kjit[key] = 0;
+      h->fblock[*fn] = e.block;
       *jit = 0;
       return ODE_OK;
     }
