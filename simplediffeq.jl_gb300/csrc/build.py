@@ -62,14 +62,17 @@ GROUPS = {
                ("avern9", "persistent", "r3bp", 4, "fp32k")],
     "kuramoto": [("atsit5", "plain", "kuramoto", 12, "fp64"),
                  ("atsit5", "persistent", "kuramoto", 12, "fp64")],
+    "kuramoto_staged": [("atsit5", "staged", "kuramoto", 12, "fp64")],
 }
 
 
 # Launch shape of a group's kernels (threads per block, staging-ring bytes per
 # warp), where it is not the default 128 / 12 KB: the staged kernels take the
 # shape the autotuner picks on the benchmark workloads (a ring that holds a
-# round plus a step's worth of new jobs, at no cost in occupancy).
-SHAPES = {"lorenz_staged": (64, 24576), "vdp_staged": (64, 24576)}
+# round plus a step's worth of new jobs, at no cost in occupancy); Kuramoto-12's
+# 804-byte jobs take one-warp blocks with a ring of exactly one round (32 jobs),
+# eight warps per SM.
+SHAPES = {"lorenz_staged": (64, 24576), "vdp_staged": (64, 24576), "kuramoto_staged": (32, 26112)}
 
 
 def kname(alg, kind, rhs, dim, prec):

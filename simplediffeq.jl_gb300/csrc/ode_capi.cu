@@ -1351,9 +1351,13 @@ int ode_autotune(ode_handle* h, const ode_solve_args* a, int64_t sample, ode_tun
   const bool staged = std::strcmp(entry_kind(ta.alg, ta.schedule, ta.nsave), "staged") == 0;
   const int job = stage_job_bytes(&ta);
   std::vector<Variant> vars;
+  /* large jobs (Kuramoto-12: 804 bytes) also try the smallest ring that holds
+   * one round, which leaves room for the most warps per SM */
+  const int fit = (32 * job + 511) / 512 * 512;
   for (int block : {128, 64, 32}) {
     std::vector<int> rings;
     if (staged) {
+      if (fit > 12288 && fit / 32 * block <= 49152) rings.push_back(fit);
       for (int ring : {12288, 16384, 24576, 36864, 49152})
         if (ring / 32 * block <= 49152 && (ring / job & ~7) >= 32) rings.push_back(ring);
     }

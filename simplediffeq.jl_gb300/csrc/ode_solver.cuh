@@ -226,14 +226,15 @@ template <> struct CB<float> {
  * a sum of products in) */
 template <int D, class R>
 __device__ __forceinline__ void lc_acc(R (&s)[D]) {}
-template <int D, class R, class... Rest>
-__device__ __forceinline__ void lc_acc(R (&s)[D], R c, const R (&k)[D], const Rest&... rest) {
+template <int D, class R, class K, class... Rest>
+__device__ __forceinline__ void lc_acc(R (&s)[D], R c, const K& k, const Rest&... rest) {
 #pragma unroll
   for (int d = 0; d < D; ++d) s[d] = fmaR(c, k[d], s[d]);
   lc_acc(s, rest...);
 }
-template <int D, class R, class... Rest>
-__device__ __forceinline__ void lc(R (&s)[D], R c, const R (&k)[D], const Rest&... rest) {
+/* k: any row indexable by d (a register array, or a RingRow of staged stage values) */
+template <int D, class R, class K, class... Rest>
+__device__ __forceinline__ void lc(R (&s)[D], R c, const K& k, const Rest&... rest) {
 #pragma unroll
   for (int d = 0; d < D; ++d) s[d] = c * k[d];
   lc_acc(s, rest...);
@@ -398,8 +399,9 @@ struct MTsit5 {
     }
   }
 
+  template <class KK>
   __device__ static __forceinline__ void dense(const F& f, const R (&uh)[D], const R (&uc)[D], T told, T tnew,
-                                               T dtold, T theta, R (&k)[NK][D], double (&out)[D]) {
+                                               T dtold, T theta, const KK& k, double (&out)[D]) {
     const R th = (R)theta;
     const R th2 = th * th;
     R ex, b1, b2, b3, b4, b5, b6, b7;
@@ -470,8 +472,9 @@ struct MVern7 {
 #undef C7T
   }
 
+  template <class KK>
   __device__ static __forceinline__ void dense(const F& f, const R (&uh)[D], const R (&uc)[D], T told, T tnew,
-                                               T dtold, T theta, R (&k)[NK][D], double (&out)[D]) {
+                                               T dtold, T theta, const KK& k, double (&out)[D]) {
 #define X7(x) CB<R>::v7x(vern7x_##x)
 #define X7T(x) CB<T>::v7x(vern7x_##x)
 #define R7(x) CB<R>::v7r(vern7r_##x)
@@ -592,21 +595,22 @@ struct MVern9Impl {
 #undef C9T
   }
 
+  template <class KK>
   __device__ static __forceinline__ void dense(const F& f, const R (&uh)[D], const R (&uc)[D], T told, T tnew,
-                                               T dtold, T theta, R (&k)[NK][D], double (&out)[D]) {
+                                               T dtold, T theta, const KK& k, double (&out)[D]) {
 #define X9(x) CB<R>::v9x(vern9x_##x)
 #define X9T(x) CB<T>::v9x(vern9x_##x)
 #define R9(x) CB<R>::v9r(vern9r_##x)
     /* K1..K9: the nine stages the dense formulas call k1..k9 */
-    const R (&K1)[D] = k[0];
-    const R (&K2)[D] = k[ADAPTIVE ? 7 : 1];
-    const R (&K3)[D] = k[ADAPTIVE ? 8 : 2];
-    const R (&K4)[D] = k[ADAPTIVE ? 9 : 3];
-    const R (&K5)[D] = k[ADAPTIVE ? 10 : 4];
-    const R (&K6)[D] = k[ADAPTIVE ? 11 : 5];
-    const R (&K7)[D] = k[ADAPTIVE ? 12 : 6];
-    const R (&K8)[D] = k[ADAPTIVE ? 13 : 7];
-    const R (&K9)[D] = k[ADAPTIVE ? 14 : 8];
+    const auto& K1 = k[0];
+    const auto& K2 = k[ADAPTIVE ? 7 : 1];
+    const auto& K3 = k[ADAPTIVE ? 8 : 2];
+    const auto& K4 = k[ADAPTIVE ? 9 : 3];
+    const auto& K5 = k[ADAPTIVE ? 10 : 4];
+    const auto& K6 = k[ADAPTIVE ? 11 : 5];
+    const auto& K7 = k[ADAPTIVE ? 12 : 6];
+    const auto& K8 = k[ADAPTIVE ? 13 : 7];
+    const auto& K9 = k[ADAPTIVE ? 14 : 8];
     const T tb = ADAPTIVE ? told : tnew;
     const R h = (R)dtold;
     R x[10][D], s[D], tmp[D];
@@ -1113,6 +1117,25 @@ struct StageLayout {
   enum { CAP = (kStageBytesPerWarp / JOB) & ~7 };
 };
 
+/* The stage values of one staged job as the dense formulas index them,
+ * k[q][d], read where they are used from the ring's [row][CAP] layout (rows
+ * STRIDE elements apart) instead of into registers first: a round then holds
+ * one accumulator per component rather than every stage value of its job,
+ * which for large states (Kuramoto-12: 84 stage values) is the difference
+ * between spilling the lane's own state and not. */
+template <class R, int STRIDE>
+struct RingRow {
+  const R* p;
+  __device__ __forceinline__ R operator[](int d) const { return p[d * STRIDE]; }
+};
+template <class R, int D, int STRIDE>
+struct RingStages {
+  const R* p;
+  __device__ __forceinline__ RingRow<R, STRIDE> operator[](int q) const {
+    return RingRow<R, STRIDE>{p + q * D * STRIDE};
+  }
+};
+
 template <class M, class PR, int D, class F>
 __device__ __forceinline__ void run_adaptive_staged(const KParams& P) {
   typedef typename PR::R R;
@@ -1138,17 +1161,14 @@ __device__ __forceinline__ void run_adaptive_staged(const KParams& P) {
     __syncwarp();
     if (lane < m) {
       const int slot = (qhead + lane) % CAP;
-      R uh[D], uc[D], kk[NK][D];
+      R uh[D], uc[D];
       F f2;
 #pragma unroll
       for (int d = 0; d < D; ++d) {
         uh[d] = rv[d * CAP + slot];
         uc[d] = PR::KAHAN ? rv[(D + d) * CAP + slot] : (R)0;
       }
-#pragma unroll
-      for (int q = 0; q < NK; ++q)
-#pragma unroll
-        for (int d = 0; d < D; ++d) kk[q][d] = rv[(KOFF + q * D + d) * CAP + slot];
+      const RingStages<R, D, CAP> kk{rv + KOFF * CAP + slot};
       if (M::DENSE_F) {
 #pragma unroll
         for (int q = 0; q < F::NP; ++q) f2.p[q] = rv[(POFF + q) * CAP + slot];
