@@ -324,13 +324,21 @@ struct RhsR3BP {
   }
 };
 
+/* The phases' sine/cosine loop is kept rolled: unrolled, the seven right-hand
+ * side evaluations of a Tsit5 step put 7 x 12 sine/cosine bodies in the step
+ * loop, more code than the instruction cache holds once the warps of an SM
+ * are at different points of their steps (measured on the persistent
+ * kernel: about ten warps waiting for instruction fetch per instruction
+ * issued, and 1.56x the time of a rolled loop).  Indexed by the loop
+ * counter, the phases and the sines and cosines live in local memory (L1),
+ * whose traffic costs far less than the FP64 work it sits between. */
 template <class R, class T, int DD>
 struct RhsKuramoto {
   enum { D = DD, NP = DD + 1 };
   R p[DD + 1];
   __device__ __forceinline__ void operator()(const R (&u)[DD], T t, R (&du)[DD]) const {
     R sn[DD], cs[DD], S = 0, C = 0;
-#pragma unroll
+#pragma unroll 1
     for (int j = 0; j < DD; ++j) {
       sincosR(u[j], &sn[j], &cs[j]);
       S = S + sn[j];
@@ -763,7 +771,7 @@ __device__ __forceinline__ void store_point(const KParams& P, long long idx, lon
 #endif
   if (P.output == 1) {
     double C = 0.0, S = 0.0;
-#pragma unroll
+#pragma unroll 1
     for (int d = 0; d < D; ++d) {
       double sn, cs;
       sincos_cw(v[d], &sn, &cs);
