@@ -604,6 +604,7 @@ int ode_create(ode_handle** out, int device) {
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->chunk_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&h->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&h->ev1);
   if (e != cudaSuccess) {
@@ -622,6 +623,7 @@ void ode_destroy(ode_handle* h) {
   if (!h) return;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->chunk_stream) cudaStreamSynchronize(h->chunk_stream);
   for (GraphEntry& g : h->graphs) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
     if (g.graph) cudaGraphDestroy(g.graph);
@@ -634,6 +636,8 @@ void ode_destroy(ode_handle* h) {
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->stream) cudaStreamDestroy(h->stream);
   if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+  if (h->chunk_stream) cudaStreamDestroy(h->chunk_stream);
+  if (h->chunk_stats) cudaFreeHost(h->chunk_stats);
   delete h;
 }
 
@@ -727,7 +731,19 @@ struct EveryStep {
   double* u;
 };
 
-int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_solve_stats* st, const EveryStep* ev) {
+/* One chunk of the host-buffer pipeline, enqueued without waiting: its
+ * scratch buffers carry the slot's tag (two chunks run at once), its timing
+ * events and a pinned array for its statistics words come from the caller,
+ * which reads them after synchronizing. */
+struct ChunkSlot {
+  const char* tag;
+  cudaEvent_t ev0, ev1;
+  unsigned long long* host_stats; /* 4 words: attempts, saves, early stops, work counter */
+  int launches, replayed, jit, sched;
+};
+
+int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_solve_stats* st, const EveryStep* ev,
+               ChunkSlot* slot = nullptr) {
   NvtxRange nvtx("gbode solve");
   const auto wall0 = std::chrono::steady_clock::now();
   if (!h) return ODE_EINVAL;
@@ -762,6 +778,9 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
   cudaStream_t s = a->stream ? (cudaStream_t)a->stream : h->stream;
   const int64_t n = a->n;
   const int D = a->dim, NP = a->nparams;
+  /* scratch buffer names, per chunk slot when two chunks are in flight */
+  auto nm = [&](const char* base) { return slot ? std::string(base) + slot->tag : std::string(base); };
+  cudaEvent_t ev0 = slot ? slot->ev0 : h->ev0, ev1 = slot ? slot->ev1 : h->ev1;
 
   int sched = fixed ? ODE_SCHED_PLAIN : a->schedule;
   if (sched == ODE_SCHED_LEARNED && !model_ready(h->model, a)) {
@@ -827,13 +846,13 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
     kp.dt0 = a->dt0;
   }
   if (a->nsave > 0) {
-    double* ds = (double*)buf(h, "saveat", (size_t)a->nsave * sizeof(double), &rc);
+    double* ds = (double*)buf(h, nm("saveat"), (size_t)a->nsave * sizeof(double), &rc);
     if (!ds) return rc;
     CK(cudaMemcpyAsync(ds, a->saveat, (size_t)a->nsave * sizeof(double), cudaMemcpyHostToDevice, s), "copy saveat");
     kp.saveat = ds;
   }
   if (fixed && ngrid > 0) {
-    double* dg = (double*)buf(h, "grid", (size_t)ngrid * sizeof(double), &rc);
+    double* dg = (double*)buf(h, nm("grid"), (size_t)ngrid * sizeof(double), &rc);
     if (!dg) return rc;
     CK(cudaMemcpyAsync(dg, grid.data(), (size_t)ngrid * sizeof(double), cudaMemcpyHostToDevice, s), "copy grid");
     kp.grid = dg;
@@ -864,7 +883,7 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
     kp.ev_t = ev->t;
     kp.ev_u = ev->u;
   }
-  unsigned long long* stats = (unsigned long long*)buf(h, "stats", 4 * sizeof(unsigned long long), &rc);
+  unsigned long long* stats = (unsigned long long*)buf(h, nm("stats"), 4 * sizeof(unsigned long long), &rc);
   if (!stats) return rc;
   kp.stats = stats;
   kp.counter = stats + 3;
@@ -899,11 +918,11 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
   double* dseed = nullptr;
   const bool seeding = sched == ODE_SCHED_LEARNED && !a->dt0 && model_seed_dt0(h->model);
   if (sched == ODE_SCHED_LEARNED) {
-    if (!(latt = (float*)buf(h, "pred_att", (size_t)n * 4, &rc))) return rc;
-    if (!(ldt = (float*)buf(h, "pred_dt", (size_t)n * 4, &rc))) return rc;
-    if (!(order = (int*)buf(h, "order", (size_t)n * 4 + 16, &rc))) return rc;
-    if (!(bins = (unsigned*)buf(h, "bins", kCostBins * sizeof(unsigned), &rc))) return rc;
-    if (seeding && !(dseed = (double*)buf(h, "dt0_seed", nd, &rc))) return rc;
+    if (!(latt = (float*)buf(h, nm("pred_att"), (size_t)n * 4, &rc))) return rc;
+    if (!(ldt = (float*)buf(h, nm("pred_dt"), (size_t)n * 4, &rc))) return rc;
+    if (!(order = (int*)buf(h, nm("order"), (size_t)n * 4 + 16, &rc))) return rc;
+    if (!(bins = (unsigned*)buf(h, nm("bins"), kCostBins * sizeof(unsigned), &rc))) return rc;
+    if (seeding && !(dseed = (double*)buf(h, nm("dt0_seed"), nd, &rc))) return rc;
     kp.order = order;
     if (seeding) kp.dt0 = dseed;
   }
@@ -936,7 +955,7 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
   }
   const bool use_graph = s != 0;  /* the legacy default stream cannot be captured */
   int replayed = 0;
-  CK(cudaEventRecord(h->ev0, s), "event");
+  CK(cudaEventRecord(ev0, s), "event");
   GraphEntry* cached = nullptr;
   for (GraphEntry& g : h->graphs)
     if (g.exec && g.key == key) cached = &g;
@@ -984,7 +1003,19 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
     rc = enqueue(&launches);
     if (rc != ODE_OK) return rc;
   }
-  CK(cudaEventRecord(h->ev1, s), "event");
+  if (slot) {
+    /* chunk of the host pipeline: statistics to pinned memory before the end
+     * event, which the caller's copies and final synchronization wait on */
+    CK(cudaMemcpyAsync(slot->host_stats, stats, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s),
+       "copy stats");
+    CK(cudaEventRecord(ev1, s), "event");
+    slot->launches = launches;
+    slot->replayed = replayed;
+    slot->jit = jit;
+    slot->sched = sched;
+    return ODE_OK;
+  }
+  CK(cudaEventRecord(ev1, s), "event");
 
   /* asynchronous call: device buffers, the caller's stream, no statistics asked */
   if (!host && a->stream && !st && !chk) return ODE_OK;
@@ -1014,7 +1045,7 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
     }
   }
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  cudaEventElapsedTime(&ms, ev0, ev1);
   if (st) {
     st->kernel_ms = ms;
     st->attempts = (int64_t)hs[0];
@@ -1084,13 +1115,37 @@ int solve_chunked(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_
         return rc;
     }
   }
-  cudaEvent_t ready[2] = {nullptr, nullptr};
-  for (int b = 0; b < 2; ++b) CK(cudaEventCreateWithFlags(&ready[b], cudaEventDisableTiming), "event");
+  if (h->chunk_stats_cap < nchunks) {
+    if (h->chunk_stats) cudaFreeHost(h->chunk_stats);
+    h->chunk_stats = nullptr;
+    h->chunk_stats_cap = 0;
+    CK(cudaMallocHost((void**)&h->chunk_stats, (size_t)nchunks * 4 * sizeof(unsigned long long)), "pinned stats");
+    h->chunk_stats_cap = nchunks;
+  }
+  /* events: inputs of a slot uploaded; start and end of every chunk's solve */
+  std::vector<cudaEvent_t> evs;
   auto release = [&]() {
-    for (int b = 0; b < 2; ++b)
-      if (ready[b]) cudaEventDestroy(ready[b]);
+    for (cudaEvent_t e : evs)
+      if (e) cudaEventDestroy(e);
   };
-  /* chunk c's inputs to slot c % 2, then an event the compute stream waits on */
+  auto make_event = [&](unsigned flags, cudaEvent_t* e) -> int {
+    const cudaError_t r = cudaEventCreateWithFlags(e, flags);
+    if (r != cudaSuccess) return cuda_fail(h, r, "event");
+    evs.push_back(*e);
+    return ODE_OK;
+  };
+  cudaEvent_t ready[2];
+  std::vector<cudaEvent_t> ev_start((size_t)nchunks), ev_end((size_t)nchunks);
+  for (int b = 0; b < 2 && rc == ODE_OK; ++b) rc = make_event(cudaEventDisableTiming, &ready[b]);
+  for (int64_t c = 0; c < nchunks && rc == ODE_OK; ++c) {
+    rc = make_event(cudaEventDefault, &ev_start[(size_t)c]);
+    if (rc == ODE_OK) rc = make_event(cudaEventDefault, &ev_end[(size_t)c]);
+  }
+  if (rc != ODE_OK) {
+    release();
+    return rc;
+  }
+  /* chunk c's inputs to slot c % 2 (copy stream), then the slot's ready event */
   auto upload = [&](int64_t c) -> int {
     const int b = (int)(c & 1);
     const int64_t i0 = c * m, mc = std::min(m, n - i0);
@@ -1104,21 +1159,38 @@ int solve_chunked(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_
     CK(cudaEventRecord(ready[b], cs), "event");
     return ODE_OK;
   };
+  /* chunk c's outputs from slot c % 2 to the host, after its solve (copy stream) */
+  auto download = [&](int64_t c) -> int {
+    const int b = (int)(c & 1);
+    const int64_t i0 = c * m, mc = std::min(m, n - i0);
+    CK(cudaStreamWaitEvent(cs, ev_end[(size_t)c], 0), "wait chunk solve");
+    for (int k = 0; k < 7; ++k) {
+      if (!dout[b][k]) continue;
+      const size_t el = outs[k].elem;
+      CK(cudaMemcpy2DAsync((char*)outs[k].host_out + i0 * el, n * el, dout[b][k], mc * el, mc * el, outs[k].rows,
+                           cudaMemcpyDeviceToHost, cs),
+         "copy chunk outputs");
+    }
+    return ODE_OK;
+  };
+  /* Even chunks solve on the caller's stream, odd ones on the handle's second
+   * compute stream, so that a chunk's kernel starts on the SMs that the
+   * previous chunk's finished warps leave, during that chunk's tail.  On the
+   * copy stream: wait for chunk c-1's solve, copy its outputs out, then copy
+   * chunk c+1's inputs into the slot chunk c-1 used; chunk c+1's solve waits
+   * for those copies (its slot is free then) and overlaps chunk c. */
   ode_solve_stats total;
   std::memset(&total, 0, sizeof total);
-  bool early = false;
+  int replayed = 0;
   rc = upload(0);
-  if (rc != ODE_OK) {
-    release();
-    return rc;
-  }
   for (int64_t c = 0; c < nchunks && rc == ODE_OK; ++c) {
     const int b = (int)(c & 1);
+    cudaStream_t sc = b ? h->chunk_stream : s;
     const int64_t i0 = c * m, mc = std::min(m, n - i0);
     ode_solve_args sa = *a;
     sa.n = mc;
     sa.memory = ODE_MEM_DEVICE;
-    sa.stream = s;
+    sa.stream = sc;
     sa.u0 = (const double*)din[b][0];
     sa.p = (const double*)din[b][1];
     sa.dt0 = (const double*)din[b][2];
@@ -1130,45 +1202,56 @@ int solve_chunked(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_
     so.naccept = (int32_t*)dout[b][4];
     so.nreject = (int32_t*)dout[b][5];
     so.dt_first = (double*)dout[b][6];
-    cudaError_t e = cudaStreamWaitEvent(s, ready[b], 0);
+    const cudaError_t e = cudaStreamWaitEvent(sc, ready[b], 0);
     if (e != cudaSuccess) {
-      release();
-      return cuda_fail(h, e, "wait chunk inputs");
+      rc = cuda_fail(h, e, "wait chunk inputs");
+      break;
     }
-    ode_solve_stats cst;
-    const int r = solve_impl(h, &sa, &so, &cst, nullptr);  /* returns when the chunk's kernel is done */
-    if (r != ODE_OK && r != ODE_ETRAJ) {
-      release();
-      return r;
-    }
-    early = early || r == ODE_ETRAJ;
-    total.kernel_ms += cst.kernel_ms;
-    total.attempts += cst.attempts;
-    total.saves += cst.saves;
-    total.launches += cst.launches;
-    total.schedule_used = cst.schedule_used;
-    total.graph_replayed += cst.graph_replayed;
-    total.jit = cst.jit;
-    /* the next chunk's inputs go first, so that its kernel need not wait for this chunk's outputs */
-    if (c + 1 < nchunks) rc = upload(c + 1);
-    for (int k = 0; k < 7 && rc == ODE_OK; ++k) {
-      if (!dout[b][k]) continue;
-      const size_t el = outs[k].elem;
-      e = cudaMemcpy2DAsync((char*)outs[k].host_out + i0 * el, n * el, dout[b][k], mc * el, mc * el, outs[k].rows,
-                            cudaMemcpyDeviceToHost, cs);
-      if (e != cudaSuccess) rc = cuda_fail(h, e, "copy chunk outputs");
-    }
+    ChunkSlot slot = {b ? "#1" : "#0", ev_start[(size_t)c], ev_end[(size_t)c], h->chunk_stats + 4 * c, 0, 0, 0, 0};
+    rc = solve_impl(h, &sa, &so, nullptr, nullptr, &slot);
+    if (rc != ODE_OK) break;
+    total.launches += slot.launches;
+    total.schedule_used = slot.sched;
+    total.jit = slot.jit;
+    replayed += slot.replayed;
+    if (c >= 1) rc = download(c - 1);
+    if (rc == ODE_OK && c + 1 < nchunks) rc = upload(c + 1);
   }
-  const cudaError_t e = cudaStreamSynchronize(cs);
+  if (rc == ODE_OK) rc = download(nchunks - 1);
+  /* everything enqueued is waited for, also after a failure, before the slots are reused */
+  const cudaError_t e1 = cudaStreamSynchronize(cs);
+  const cudaError_t e2 = cudaStreamSynchronize(s);
+  const cudaError_t e3 = cudaStreamSynchronize(h->chunk_stream);
+  if (rc != ODE_OK) {
+    release();
+    return rc;
+  }
+  const cudaError_t e = e1 != cudaSuccess ? e1 : e2 != cudaSuccess ? e2 : e3;
+  if (e != cudaSuccess) {
+    release();
+    return cuda_fail(h, e, "chunked solve");
+  }
+  float span = 0.f;
+  cudaEventElapsedTime(&span, ev_start[0], ev_end[(size_t)nchunks - 1]);
   release();
-  if (rc != ODE_OK) return rc;
-  if (e != cudaSuccess) return cuda_fail(h, e, "chunk copies");
+  unsigned long long early = 0;
+  for (int64_t c = 0; c < nchunks; ++c) {
+    total.attempts += (int64_t)h->chunk_stats[4 * c];
+    total.saves += (int64_t)h->chunk_stats[4 * c + 1];
+    early += h->chunk_stats[4 * c + 2];
+  }
   if (st) {
     *st = total;
-    st->graph_replayed = total.graph_replayed == nchunks ? 1 : 0;
+    st->kernel_ms = span;  /* first chunk's start to last chunk's end: the chunks' solves overlap */
+    st->graph_replayed = replayed == nchunks ? 1 : 0;
     st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
   }
-  return early ? fail(h, ODE_ETRAJ, "some trajectories stopped early (dt<dtmin or maxiters); see retcode") : ODE_OK;
+  if (early) {
+    char msg[128];
+    snprintf(msg, sizeof msg, "%llu trajectories stopped early (dt<dtmin or maxiters); see retcode", early);
+    return fail(h, ODE_ETRAJ, msg);
+  }
+  return ODE_OK;
 }
 
 }  // namespace
@@ -1176,7 +1259,7 @@ int solve_chunked(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_
 extern "C" {
 
 int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_solve_stats* st) {
-  if (h && a && o && a->memory == ODE_MEM_HOST && a->n >= 2 * kChunk && !is_fixed(a->alg) &&
+  if (h && a && o && a->memory == ODE_MEM_HOST && a->n >= 2 * kChunk && !is_fixed(a->alg) && !h->bounds_check &&
       a->alg >= ODE_ALG_RK4 && a->alg <= ODE_ALG_EULER && a->dim >= 1 && a->nparams >= 0 &&
       (a->nparams == 0 || a->p) && a->u0 && (a->nsave == 0 || a->saveat))
     return solve_chunked(h, a, o, st);

@@ -59,6 +59,9 @@ struct ode_handle {
   int nsm = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t copy_stream = nullptr;  /* host<->device copies of the chunked host-buffer path */
+  cudaStream_t chunk_stream = nullptr; /* second compute stream of the chunked path (odd chunks) */
+  unsigned long long* chunk_stats = nullptr;  /* pinned: 4 statistics words per chunk */
+  int64_t chunk_stats_cap = 0;                /* chunks that chunk_stats holds */
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::string err;
   std::map<std::string, gbode::DevBuf> bufs;
