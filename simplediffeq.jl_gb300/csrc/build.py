@@ -109,13 +109,14 @@ def gen_sources():
             lines.append("GBODE_ENTRY(%s, %s, %s, %s, %s)\n" % (kname(alg, kind, rhs, dim, prec), kind,
                                                                METHOD[alg], PREC[prec][1], t))
             decl.append('extern "C" __global__ void %s(gbode::KParams);\n' % kname(alg, kind, rhs, dim, prec))
-            entries.append('  {%d, "%s", %d, %d, %d, (const void*)%s, %d},\n' % (
-                ALG[alg], kind, RHS[rhs], dim, PREC[prec][0], kname(alg, kind, rhs, dim, prec), block))
+            entries.append('  {%d, "%s", %d, %d, %d, (const void*)%s, %d, %d},\n' % (
+                ALG[alg], kind, RHS[rhs], dim, PREC[prec][0], kname(alg, kind, rhs, dim, prec), block, ring))
         path = os.path.join(BUILD, "kern_%s.cu" % g)
         write_if_changed(path, "".join(lines))
         tus.append(path)
     reg = ["/* generated by build.py: kernels compiled ahead of time */\n",
-           "struct AotEntry { int alg; const char* kind; int rhs; int dim; int precision; const void* fn; int block; };\n"]
+           "struct AotEntry { int alg; const char* kind; int rhs; int dim; int precision; const void* fn; int block; "
+           "int stage; };\n"]
     reg += decl
     reg.append("static const AotEntry kAotEntries[] = {\n")
     reg += entries

@@ -371,7 +371,7 @@ int nvrtc_cubin(const std::string& src, const std::vector<std::string>& extra_op
   return ODE_OK;
 }
 
-int load_cubin(ode_handle* h, const std::vector<char>& cubin, int block, CUfunction* fn) {
+int load_cubin(ode_handle* h, const std::vector<char>& cubin, int block, int stage, CUfunction* fn) {
   CUmodule mod;
   CUresult cr = g_drv.cuModuleLoadData(&mod, cubin.data());
   if (cr != CUDA_SUCCESS) return cu_fail(h, cr, "cuModuleLoadData");
@@ -379,6 +379,7 @@ int load_cubin(ode_handle* h, const std::vector<char>& cubin, int block, CUfunct
   cr = g_drv.cuModuleGetFunction(fn, mod, "gbode_jit");
   if (cr != CUDA_SUCCESS) return cu_fail(h, cr, "cuModuleGetFunction");
   h->fblock[*fn] = block;
+  h->fstage[*fn] = stage;
   return ODE_OK;
 }
 
@@ -389,7 +390,7 @@ int compile_jit(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* f
   if (h->bounds_check) opts.push_back("-DGBODE_BOUNDS_CHECK");
   const int rc = nvrtc_cubin(jit_source(h, a, sched), opts, &cubin, log_out, &err);
   if (rc != ODE_OK) return fail(h, rc, err);
-  return load_cubin(h, cubin, 128, fn);
+  return load_cubin(h, cubin, 128, 12288, fn);
 }
 
 /* Find (or build) the kernel for this solve. */
@@ -411,7 +412,7 @@ int get_kernel(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn
     std::string lg, err;
     int rc = nvrtc_cubin(jit_source(h, a, sched), o, &cubin, &lg, &err);
     if (rc != ODE_OK) return fail(h, rc, err);
-    rc = load_cubin(h, cubin, c[0], fn);
+    rc = load_cubin(h, cubin, c[0], c[2], fn);
     if (rc != ODE_OK) return rc;
     h->tuned[key] = *fn;
     *jit = 1;
@@ -434,6 +435,7 @@ int get_kernel(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn
       h->kcache[key] = *fn;
       h->kjit[key] = 0;
       h->fblock[*fn] = e.block;
+      h->fstage[*fn] = e.stage;
       *jit = 0;
       return ODE_OK;
     }
@@ -444,6 +446,11 @@ int get_kernel(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn
   h->kjit[key] = 1;
   *jit = 1;
   return ODE_OK;
+}
+
+int stage_of(ode_handle* h, CUfunction fn) {
+  auto it = h->fstage.find(fn);
+  return it == h->fstage.end() ? 12288 : it->second;
 }
 
 int block_of(ode_handle* h, CUfunction fn) {
@@ -494,7 +501,7 @@ int jit_function(ode_handle* h, const std::string& src, int block, CUfunction* f
   std::string err;
   const int rc = nvrtc_cubin(src, {}, &cubin, log, &err);
   if (rc != ODE_OK) return fail(h, rc, err);
-  return load_cubin(h, cubin, block, fn);
+  return load_cubin(h, cubin, block, 0, fn);
 }
 
 int launch_params(ode_handle* h, CUfunction fn, unsigned grid, unsigned block, void* params, cudaStream_t s) {
@@ -1409,7 +1416,13 @@ int ode_autotune(ode_handle* h, const ode_solve_args* a, int64_t sample, ode_tun
   to.us = dus;
   to.u_final = duf;
   const std::string key = kernel_key(h, &ta, ta.schedule);
+  /* the baseline is the kernel an untuned handle would run */
   h->tuned.erase(key);
+  h->tune_choice.erase(key);
+  CUfunction fn0;
+  int jit0 = 0;
+  rc = get_kernel(h, &ta, ta.schedule, &fn0, &jit0);
+  if (rc != ODE_OK) return rc;
   auto time_solve = [&](double* ms) -> int {
     double best = 1e300;
     for (int r = 0; r < 3; ++r) {
@@ -1478,7 +1491,7 @@ int ode_autotune(ode_handle* h, const ode_solve_args* a, int64_t sample, ode_tun
   for (int v = 0; v < nv; ++v) {
     if (!ok[v]) continue;
     CUfunction fn;
-    rc = load_cubin(h, cubins[v], vars[v].block, &fn);
+    rc = load_cubin(h, cubins[v], vars[v].block, vars[v].stage, &fn);
     if (rc != ODE_OK) return rc;
     h->tuned[key] = fn;
     double ms = 0;
@@ -1498,9 +1511,9 @@ int ode_autotune(ode_handle* h, const ode_solve_args* a, int64_t sample, ode_tun
                                    : std::vector<int>{0, 0, 0};  /* 0: the default kernel won */
   if (rep) {
     rep->variants = tried;
-    rep->block = best >= 0 ? vars[best].block : 128;
+    rep->block = best >= 0 ? vars[best].block : block_of(h, fn0);
     rep->max_registers = best >= 0 ? vars[best].regs : 0;
-    rep->stage_bytes = best >= 0 ? vars[best].stage : 12288;
+    rep->stage_bytes = best >= 0 ? vars[best].stage : stage_of(h, fn0);
     rep->default_ms = base_ms;
     rep->best_ms = best_ms;
     rep->sample = m;

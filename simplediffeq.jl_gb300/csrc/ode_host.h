@@ -72,6 +72,7 @@ struct ode_handle {
    * ode_autotune or read by ode_tune_load; compiled on first use */
   std::map<std::string, std::vector<int>> tune_choice;
   std::map<CUfunction, int> fblock;         /* threads per block of run-time compiled functions */
+  std::map<CUfunction, int> fstage;         /* staging-ring bytes per warp they were compiled with */
   std::vector<CUmodule> modules;
   std::vector<gbode::UserRhs> users;
   std::vector<gbode::UserOutput> outputs;
