@@ -1284,8 +1284,10 @@ double log_dev(double x) {
   return std::fma(de, 0x1.62e42fefa38p-1, std::fma(de, 0x1.ef35793c7673p-45, lm));
 }
 
-void normal_pair(uint64_t seed, int64_t k, int j, int64_t idx, double* z0, double* z1) {
-  const uint32_t c[4] = {(uint32_t)k, (uint32_t)j, (uint32_t)idx, (uint32_t)((uint64_t)idx >> 32)};
+/* normals z_{2P}, z_{2P+1} of trajectory idx's stream: Philox counter
+ * (P low, P high, idx low, idx high), key = seed, then Box-Muller */
+void normal_pair(uint64_t seed, int64_t P, int64_t idx, double* z0, double* z1) {
+  const uint32_t c[4] = {(uint32_t)P, (uint32_t)((uint64_t)P >> 32), (uint32_t)idx, (uint32_t)((uint64_t)idx >> 32)};
   const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
   uint32_t r[4];
   philox(c, key, r);
@@ -1336,11 +1338,25 @@ void solve_em(const oracle_sde_args* a, int64_t i) {
   if (a->us)
     for (int d = 0; d < D; ++d) a->us[d * a->n + i] = u[d];
   const double sqdt = std::sqrt(a->dt);
+  double carry = 0.0;
   for (int64_t k = 0; k < a->nsteps; ++k) {
     const double t = std::fma((double)k, a->dt, a->t0);
     (void)t;  /* the built-in SDEs are autonomous */
     sde_fg(a, dev, u, p, f, g);
-    for (int j = 0; j < (D + 1) / 2; ++j) normal_pair(a->seed, k, j, i, &xi[2 * j], &xi[2 * j + 1]);
+    /* step k takes z_{kD} .. z_{kD+D-1}; a pair that straddles two steps is
+     * drawn once (its second normal kept for the next step) */
+    for (int d = 0; d < D; ++d) {
+      const int64_t gi = k * D + d;
+      if (d == 0 && (gi & 1)) {
+        xi[0] = carry;
+        continue;
+      }
+      if (gi & 1) continue;  /* filled with its pair */
+      double z1;
+      normal_pair(a->seed, gi / 2, i, &xi[d], &z1);
+      if (d + 1 < D) xi[d + 1] = z1;
+      else carry = z1;
+    }
     for (int d = 0; d < D; ++d) {
       const double sg = sqdt * g[d];
       u[d] = dev ? std::fma(sg, xi[d], std::fma(f[d], a->dt, u[d])) : (u[d] + f[d] * a->dt) + sg * xi[d];
@@ -1379,8 +1395,8 @@ extern "C" int oracle_sde_solve(const oracle_sde_args* a) {
 
 extern "C" void oracle_philox(const uint32_t* c, const uint32_t* k, uint32_t* out) { philox(c, k, out); }
 extern "C" double oracle_log(double x) { return log_dev(x); }
-extern "C" void oracle_normal_pair(uint64_t seed, int64_t k, int j, int64_t idx, double* z0, double* z1) {
-  normal_pair(seed, k, j, idx, z0, z1);
+extern "C" void oracle_normal_pair(uint64_t seed, int64_t pair, int64_t idx, double* z0, double* z1) {
+  normal_pair(seed, pair, idx, z0, z1);
 }
 
 extern "C" float oracle_ctrl_pow(float x, float b) { return oracle_pow::ctrl_pow(x, b); }

@@ -91,7 +91,7 @@ void oracle_philox(const uint32_t* c, const uint32_t* k, uint32_t* out);
 /* the device canon's double logarithm */
 double oracle_log(double x);
 /* components 2j, 2j+1 of the step-k normal vector of trajectory idx */
-void oracle_normal_pair(uint64_t seed, int64_t k, int j, int64_t idx, double* z0, double* z1);
+void oracle_normal_pair(uint64_t seed, int64_t pair, int64_t idx, double* z0, double* z1);
 float oracle_ctrl_pow(float x, float b);
 /* the device canon's double sine and cosine (Cody-Waite reduction, Taylor polynomials) */
 void oracle_sincos(double x, double* s, double* c);

@@ -79,7 +79,7 @@ def lib():
         _lib.oracle_philox.restype = None
         _lib.oracle_log.argtypes = [ctypes.c_double]
         _lib.oracle_log.restype = ctypes.c_double
-        _lib.oracle_normal_pair.argtypes = [ctypes.c_uint64, ctypes.c_int64, ctypes.c_int, ctypes.c_int64,
+        _lib.oracle_normal_pair.argtypes = [ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64,
                                             ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         _lib.oracle_normal_pair.restype = None
         _lib.oracle_mlp_forward_backward.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int64] + [ctypes.c_void_p] * 5
@@ -296,7 +296,9 @@ def log_dev(x):
     return lib().oracle_log(float(x))
 
 
-def normal_pair(seed, k, j, idx):
+def normal_pair(seed, pair, idx):
+    """Normals z_{2 pair} and z_{2 pair + 1} of trajectory idx's stream (step k
+    of a dim-D SDE takes z_{kD} .. z_{kD+D-1})."""
     z0, z1 = ctypes.c_double(), ctypes.c_double()
-    lib().oracle_normal_pair(int(seed), int(k), int(j), int(idx), ctypes.byref(z0), ctypes.byref(z1))
+    lib().oracle_normal_pair(int(seed), int(pair), int(idx), ctypes.byref(z0), ctypes.byref(z1))
     return z0.value, z1.value

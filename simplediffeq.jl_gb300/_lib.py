@@ -288,3 +288,19 @@ def probe_rates(device=0, iters=2000):
         raise GB300ODEError(ECUDA, "probe failed (%d)" % rc)
     names = ["dfma", "dadd", "ffma", "cvt_f64_f32_f64", "ddiv", "dsqrt_add", "dmax_add", "fdiv"]
     return {k: (float(r[i]), float(ms[i])) for i, k in enumerate(names)}
+
+
+def probe_fp64_issue(device=0, clock_mhz=2070.0):
+    """FP64 FMA warp instructions retired per second per SM at full occupancy
+    (32 and 8 active lanes), for one warp per SM with 1 and 8 dependency
+    chains, and for one warp per SM sub-partition; plus the cycles of one
+    dependent FMA in a lone warp (libgb300ode_probe.so)."""
+    lib = ctypes.CDLL(PROBE_PATH)
+    lib.probe_fp64_issue.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_void_p]
+    r = np.zeros(6)
+    rc = lib.probe_fp64_issue(int(device), float(clock_mhz), r.ctypes.data)
+    if rc != 0:
+        raise GB300ODEError(ECUDA, "probe failed (%d)" % rc)
+    names = ["full_32_lanes", "full_8_lanes", "one_warp_1_chain", "one_warp_8_chains", "one_warp_per_smsp",
+             "lone_fma_cycles"]
+    return {k: float(r[i]) for i, k in enumerate(names)}

@@ -7,15 +7,19 @@
  *
  * The reference draws xi_k with Julia's randn; this solver draws them from a
  * counter-based generator so that every trajectory's noise is reproducible
- * from (seed, trajectory, step) alone, on any thread and on the CPU:
+ * from (seed, trajectory) alone, on any thread and on the CPU.  Trajectory i
+ * has the stream of standard normals z_0, z_1, z_2, ..., of which step k
+ * takes z_{kD}, ..., z_{kD+D-1} (no normal is drawn and dropped, also for odd
+ * D):
  *   - Philox4x32-10 (J. K. Salmon, M. A. Moraes, R. O. Dror, D. E. Shaw,
  *     "Parallel random numbers: as easy as 1, 2, 3", SC'11), counter
- *     (step k, pair j, trajectory low word, trajectory high word), key = seed;
- *   - each Philox output gives two 53-bit uniforms u1 in (0, 1], u2 in [0, 1)
- *     and the Box-Muller pair (G. E. P. Box, M. E. Muller, 1958)
- *     r = sqrt(-2 log u1), (r cos 2 pi u2, r sin 2 pi u2) for components 2j, 2j+1,
- *     with this file's log_dev and ode_solver.cuh's sincos_cw, so that the
- *     oracle reproduces every normal bit for bit.
+ *     (pair P low word, pair P high word, trajectory low word, trajectory
+ *     high word), key = seed, gives z_{2P} and z_{2P+1}:
+ *   - two 53-bit uniforms u1 in (0, 1], u2 in [0, 1) and the Box-Muller pair
+ *     (G. E. P. Box, M. E. Muller, 1958) r = sqrt(-2 log u1),
+ *     (r cos 2 pi u2, r sin 2 pi u2), with this file's log_dev and
+ *     ode_solver.cuh's sincos_cw, so that the oracle reproduces every normal
+ *     bit for bit.
  * Update rounding (device canon): u = fma(sqdt*g, xi, fma(f, dt, u)). */
 #pragma once
 #include "ode_solver.cuh"
@@ -85,10 +89,11 @@ __device__ __forceinline__ double log_dev(double x) {
   return __fma_rn(de, 0x1.62e42fefa38p-1, __fma_rn(de, 0x1.ef35793c7673p-45, lm));
 }
 
-/* Components 2j and 2j+1 of the step-k normal vector of trajectory idx. */
-__device__ __forceinline__ void normal_pair(unsigned long long seed, long long k, int j, long long idx, double* z0,
+/* Normals z_{2P} and z_{2P+1} of trajectory idx's stream. */
+__device__ __forceinline__ void normal_pair(unsigned long long seed, long long P, long long idx, double* z0,
                                             double* z1) {
-  const U4 r = philox4x32_10(U4{(unsigned)k, (unsigned)j, (unsigned)idx, (unsigned)((unsigned long long)idx >> 32)},
+  const U4 r = philox4x32_10(U4{(unsigned)P, (unsigned)((unsigned long long)P >> 32), (unsigned)idx,
+                                (unsigned)((unsigned long long)idx >> 32)},
                              (unsigned)seed, (unsigned)(seed >> 32));
   const unsigned long long a = ((unsigned long long)(r.x >> 5) << 26) | (r.y >> 6);
   const unsigned long long c = ((unsigned long long)(r.z >> 5) << 26) | (r.w >> 6);
@@ -148,6 +153,24 @@ struct SdeLorenz {
   }
 };
 
+/* xi[0..D) = z_{kD}, ..., z_{kD+D-1}.  For odd D a pair straddles two steps:
+ * an even step draws (D+1)/2 pairs and keeps the last normal in `carry` for
+ * the next step, which starts with it and draws (D-1)/2 pairs. */
+template <int D>
+__device__ __forceinline__ void step_normals(unsigned long long seed, long long k, long long idx, double (&xi)[D + 1],
+                                             double& carry) {
+  const long long g0 = k * D;
+  if ((D & 1) && (g0 & 1)) {
+    xi[0] = carry;
+#pragma unroll
+    for (int j = 0; j < (D - 1) / 2; ++j) normal_pair(seed, (g0 + 1) / 2 + j, idx, &xi[1 + 2 * j], &xi[2 + 2 * j]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < (D + 1) / 2; ++j) normal_pair(seed, g0 / 2 + j, idx, &xi[2 * j], &xi[2 * j + 1]);
+    if (D & 1) carry = xi[D];
+  }
+}
+
 /* ------------------------------------------------------------------ the Euler-Maruyama loop */
 template <class S>
 __device__ __forceinline__ void run_em(const SParams& P) {
@@ -164,13 +187,13 @@ __device__ __forceinline__ void run_em(const SParams& P) {
 #pragma unroll
     for (int d = 0; d < D; ++d) P.us[(long long)d * P.n + i] = u[d];
   const double dt = P.dt, sqdt = __dsqrt_rn(P.dt);
+  double carry = 0.0;
   for (long long k = 0; k < P.nsteps; ++k) {
     const double t = __fma_rn((double)k, dt, P.t0);
     double f[D], g[D], xi[D + 1];
     sde.drift(u, t, f);
     sde.diffusion(u, t, g);
-#pragma unroll
-    for (int j = 0; j < (D + 1) / 2; ++j) normal_pair(P.seed, k, j, i, &xi[2 * j], &xi[2 * j + 1]);
+    step_normals<D>(P.seed, k, i, xi, carry);
 #pragma unroll
     for (int d = 0; d < D; ++d) u[d] = __fma_rn(sqdt * g[d], xi[d], __fma_rn(f[d], dt, u[d]));
     if (P.save_everystep && P.us)

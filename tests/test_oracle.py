@@ -286,13 +286,30 @@ def test_device_canon_log_accuracy(po):
 
 def test_counter_based_normals(po):
     """Box-Muller pairs from Philox: standard normal moments, uncorrelated
-    components, and a stream that depends only on (seed, step, pair, trajectory)."""
-    z = np.array([po.normal_pair(7, k, j, i) for k in range(100) for j in range(2) for i in range(250)])
+    components, and a stream that depends only on (seed, pair, trajectory)."""
+    z = np.array([po.normal_pair(7, P, i) for P in range(200) for i in range(250)])
     for col in (z[:, 0], z[:, 1]):
         assert abs(col.mean()) < 0.02 and abs(col.var() - 1) < 0.03
         assert abs(((col - col.mean()) ** 4).mean() / col.var() ** 2 - 3) < 0.15
     assert abs(np.corrcoef(z[:, 0], z[:, 1])[0, 1]) < 0.02
-    assert po.normal_pair(7, 3, 1, 9) == po.normal_pair(7, 3, 1, 9) != po.normal_pair(8, 3, 1, 9)
+    assert po.normal_pair(7, 3, 9) == po.normal_pair(7, 3, 9) != po.normal_pair(8, 3, 9)
+    assert po.normal_pair(7, 3, 9) != po.normal_pair(7, 3 + (1 << 32), 9)  # the pair index's high word counts
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3, 5])
+def test_simple_em_consumes_the_normal_stream_in_order(po, dim):
+    """Step k of a dim-D SDE takes normals z_{kD} .. z_{kD+D-1} of its
+    trajectory's stream; for odd D a pair straddles two steps and is drawn once.
+    With dW-only Ornstein-Uhlenbeck noise (theta = 0, sigma = 1, dt = 1) each
+    increment is the normal itself."""
+    n, steps = 3, 6
+    o = po.sde_solve("ou", np.zeros((dim, n)), np.tile([[0.0], [0.0], [1.0]], (1, n)), (0.0, float(steps)), 1.0,
+                     seed=11, save_everystep=True)
+    inc = np.diff(o["us"], axis=0)  # (steps, dim, n)
+    for i in range(n):
+        stream = [z for P in range((steps * dim + 1) // 2) for z in po.normal_pair(11, P, i)]
+        want = np.array(stream[:steps * dim]).reshape(steps, dim)
+        assert np.allclose(inc[:, :, i], want, rtol=0, atol=1e-12)
 
 
 def test_simple_em_weak_moments(po):
