@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define ODE_ABI_VERSION 2
+#define ODE_ABI_VERSION 3
 
 /* status codes */
 enum {
@@ -244,20 +244,24 @@ int ode_output_compile(ode_handle* h, const char* body, int dim, int nparams, in
                        size_t loglen);
 
 /* ---- SimpleEM: Euler-Maruyama SDE ensembles ---------------------------------
- * DiffEqBase.solve(prob::SDEProblem, SimpleEM(); dt), src/euler_maruyama.jl:48-98
- * (out-of-place, diagonal noise), for a whole ensemble:
+ * DiffEqBase.solve(prob::SDEProblem, SimpleEM(); dt), src/euler_maruyama.jl:48-142,
+ * for a whole ensemble:
  *   n = Int((tf - t0)/dt) + 1 points t_k = t0 + k*dt,
- *   u_{k+1} = u_k + f(u_k, p, t_k)*dt + sqrt(dt)*g(u_k, p, t_k) .* xi_k.
- * The reference draws xi_k with Julia's randn; here xi_k comes from a
- * counter-based generator (Philox4x32-10 keyed by `seed`, counter = step,
- * component pair, trajectory; Box-Muller with the library's own log and
- * sin/cos), so results depend only on (seed, trajectory index, step) and are
- * reproducible on the CPU.  Non-diagonal noise (a noise_rate_prototype
- * matrix) is not supported. */
+ *   diagonal noise:      u_{k+1} = u_k + f(u_k, p, t_k)*dt + sqrt(dt)*g(u_k, p, t_k) .* xi_k,
+ *   non-diagonal noise:  u_{k+1} = u_k + f(u_k, p, t_k)*dt + sqrt(dt)*(G(u_k, p, t_k) * xi_k),
+ * G a dim x noise_dim matrix (the reference's noise_rate_prototype) and xi_k
+ * noise_dim normals.  The reference draws xi_k with Julia's randn; here each
+ * trajectory has one stream of normals from a counter-based generator
+ * (Philox4x32-10 keyed by `seed`, counter = pair index, trajectory;
+ * Box-Muller with the library's own log and sin/cos) that its steps consume in
+ * order, so results depend only on (seed, trajectory index) and are
+ * reproducible on the CPU. */
 enum {
   ODE_SDE_GBM = 0,     /* geometric Brownian motion: f = mu u, g = sigma u (any dim), p = (mu, sigma) */
   ODE_SDE_OU = 1,      /* Ornstein-Uhlenbeck: f = theta (mu - u), g = sigma (any dim), p = (theta, mu, sigma) */
   ODE_SDE_LORENZ = 2,  /* Lorenz drift, additive noise: dim 3, p = (sigma, rho, beta, noise) */
+  ODE_SDE_MULT = 3,    /* non-diagonal multiplicative noise: f = mu u, G[d][m] = c[d][m] u[d] (noise_dim >= 1),
+                          p = (mu, c row-major dim x noise_dim); the reference's test SDE, test/simpleem_tests.jl */
   ODE_SDE_USER = 1000
 };
 
@@ -272,6 +276,7 @@ typedef struct {
   const double* u0;       /* [dim][n] */
   const double* p;        /* [nparams][n] */
   void* stream;           /* cudaStream_t, or NULL */
+  int32_t noise_dim;      /* 0: diagonal noise; M >= 1: dim x M noise matrix (ODE_SDE_MULT, user SDEs compiled so) */
 } ode_sde_args;
 
 typedef struct {
@@ -287,6 +292,11 @@ int ode_sde_solve(ode_handle* h, const ode_sde_args* a, ode_sde_out* o, ode_solv
  * (diagonal noise: g has dim components). */
 int ode_sde_compile(ode_handle* h, const char* drift, const char* diffusion, int dim, int nparams, int* sde_id,
                     char* log, size_t loglen);
+/* The same for non-diagonal noise: `diffusion` writes the dim x noise_dim
+ * matrix row-major, g[d * noise_dim + m] (noise_dim 0: diagonal, as above).
+ * Solve it with ode_sde_args.noise_dim = noise_dim. */
+int ode_sde_compile_noise(ode_handle* h, const char* drift, const char* diffusion, int dim, int noise_dim,
+                          int nparams, int* sde_id, char* log, size_t loglen);
 
 /* ---- autotuner ----------------------------------------------------------
  * Times launch-shape variants of the solver kernel (threads per block,

@@ -1302,11 +1302,20 @@ void normal_pair(uint64_t seed, int64_t P, int64_t idx, double* z0, double* z1) 
   *z1 = rad * sn;
 }
 
-/* drift and diffusion of the built-in SDEs; the Lorenz drift in the REF/DEV
- * forms of rhs_eval */
+constexpr int MAXM = 16;  /* noise dimensions of a non-diagonal SDE */
+
+/* drift and diffusion of the built-in SDEs (g: dim values for diagonal noise,
+ * the row-major dim x noise_dim matrix otherwise); the Lorenz drift in the
+ * REF/DEV forms of rhs_eval */
 void sde_fg(const oracle_sde_args* a, bool dev, const double* u, const double* p, double* f, double* g) {
-  const int D = a->dim;
+  const int D = a->dim, M = a->noise_dim;
   switch (a->sde) {
+    case ORACLE_SDE_MULT:
+      for (int d = 0; d < D; ++d) {
+        f[d] = p[0] * u[d];
+        for (int m = 0; m < M; ++m) g[d * M + m] = p[1 + d * M + m] * u[d];
+      }
+      break;
     case ORACLE_SDE_GBM:
       for (int d = 0; d < D; ++d) { f[d] = p[0] * u[d]; g[d] = p[1] * u[d]; }
       break;
@@ -1326,13 +1335,34 @@ void sde_fg(const oracle_sde_args* a, bool dev, const double* u, const double* p
   }
 }
 
-/* src/euler_maruyama.jl:66-91 for trajectory i: t_k = t0 + k dt (scalar
- * muladd), u += f dt + sqrt(dt) g .* xi; REF rounds (u + f dt) + (sqdt g) xi
- * with a separate multiply and add each, DEV fuses both. */
+/* xi[0..N) = z_{kN} .. z_{kN+N-1} of trajectory i's normal stream; a pair
+ * that straddles two steps is drawn once, its second normal kept in carry */
+void step_normals(uint64_t seed, int64_t k, int N, int64_t i, double* xi, double* carry) {
+  for (int d = 0; d < N; ++d) {
+    const int64_t gi = k * N + d;
+    if (d == 0 && (gi & 1)) {
+      xi[0] = *carry;
+      continue;
+    }
+    if (gi & 1) continue;  /* filled with its pair */
+    double z1;
+    normal_pair(seed, gi / 2, i, &xi[d], &z1);
+    if (d + 1 < N) xi[d + 1] = z1;
+    else *carry = z1;
+  }
+}
+
+/* src/euler_maruyama.jl:66-91 (diagonal) and :126-134 (non-diagonal) for
+ * trajectory i: t_k = t0 + k dt (scalar muladd).  Diagonal noise:
+ * u += f dt + sqrt(dt) g .* xi, REF rounding (u + f dt) + (sqdt g) xi with a
+ * separate multiply and add each, DEV fma(sqdt g, xi, fma(f, dt, u)).
+ * Non-diagonal noise (M normals a step): s = G xi (left to right; DEV with
+ * fmas), u += f dt + sqrt(dt) s, REF (u + f dt) + sqdt s, DEV
+ * fma(sqdt, s, fma(f, dt, u)). */
 void solve_em(const oracle_sde_args* a, int64_t i) {
-  const int D = a->dim;
+  const int D = a->dim, M = a->noise_dim;
   const bool dev = a->rounding == ORACLE_ROUND_DEVICE;
-  double u[MAXD], p[MAXP], f[MAXD], g[MAXD], xi[MAXD + 1];
+  double u[MAXD], p[MAXP], f[MAXD], g[MAXD * MAXM], xi[MAXM + MAXD + 1];
   for (int q = 0; q < a->nparams; ++q) p[q] = a->p[q * a->n + i];
   for (int d = 0; d < D; ++d) u[d] = a->u0[d * a->n + i];
   if (a->us)
@@ -1343,23 +1373,17 @@ void solve_em(const oracle_sde_args* a, int64_t i) {
     const double t = std::fma((double)k, a->dt, a->t0);
     (void)t;  /* the built-in SDEs are autonomous */
     sde_fg(a, dev, u, p, f, g);
-    /* step k takes z_{kD} .. z_{kD+D-1}; a pair that straddles two steps is
-     * drawn once (its second normal kept for the next step) */
+    /* step k takes the next D (diagonal) or M normals of the stream */
+    step_normals(a->seed, k, M > 0 ? M : D, i, xi, &carry);
     for (int d = 0; d < D; ++d) {
-      const int64_t gi = k * D + d;
-      if (d == 0 && (gi & 1)) {
-        xi[0] = carry;
-        continue;
+      if (M > 0) {
+        double s = g[d * M] * xi[0];
+        for (int m = 1; m < M; ++m) s = dev ? std::fma(g[d * M + m], xi[m], s) : s + g[d * M + m] * xi[m];
+        u[d] = dev ? std::fma(sqdt, s, std::fma(f[d], a->dt, u[d])) : (u[d] + f[d] * a->dt) + sqdt * s;
+      } else {
+        const double sg = sqdt * g[d];
+        u[d] = dev ? std::fma(sg, xi[d], std::fma(f[d], a->dt, u[d])) : (u[d] + f[d] * a->dt) + sg * xi[d];
       }
-      if (gi & 1) continue;  /* filled with its pair */
-      double z1;
-      normal_pair(a->seed, gi / 2, i, &xi[d], &z1);
-      if (d + 1 < D) xi[d + 1] = z1;
-      else carry = z1;
-    }
-    for (int d = 0; d < D; ++d) {
-      const double sg = sqdt * g[d];
-      u[d] = dev ? std::fma(sg, xi[d], std::fma(f[d], a->dt, u[d])) : (u[d] + f[d] * a->dt) + sg * xi[d];
     }
     if (a->us)
       for (int d = 0; d < D; ++d) a->us[((k + 1) * D + d) * a->n + i] = u[d];
@@ -1376,7 +1400,9 @@ extern "C" int oracle_sde_solve(const oracle_sde_args* a) {
   if (a->sde == ORACLE_SDE_GBM && a->nparams != 2) return -1;
   if (a->sde == ORACLE_SDE_OU && a->nparams != 3) return -1;
   if (a->sde == ORACLE_SDE_LORENZ && (a->dim != 3 || a->nparams != 4)) return -1;
-  if (a->sde < 0 || a->sde > ORACLE_SDE_LORENZ) return -1;
+  if (a->sde < 0 || a->sde > ORACLE_SDE_MULT) return -1;
+  if (a->noise_dim < 0 || a->noise_dim > MAXM || (a->noise_dim > 0) != (a->sde == ORACLE_SDE_MULT)) return -1;
+  if (a->sde == ORACLE_SDE_MULT && a->nparams != 1 + a->dim * a->noise_dim) return -1;
   int nt = a->nthreads > 0 ? a->nthreads : 1;
   if ((int64_t)nt > a->n) nt = (int)std::max<int64_t>(1, a->n);
   auto run = [&](int64_t i0, int64_t i1) {

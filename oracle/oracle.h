@@ -69,9 +69,12 @@ typedef struct {
 
 int oracle_solve(const oracle_args* a, oracle_out* o);
 
-/* SimpleEM (src/euler_maruyama.jl:48-98), diagonal noise, with the counter-based
- * normals of the device canon (Philox4x32-10 + Box-Muller). */
-enum oracle_sde { ORACLE_SDE_GBM = 0, ORACLE_SDE_OU = 1, ORACLE_SDE_LORENZ = 2 };
+/* SimpleEM (src/euler_maruyama.jl:48-142), diagonal and non-diagonal noise,
+ * with the counter-based normals of the device canon (Philox4x32-10 +
+ * Box-Muller).  ORACLE_SDE_MULT is the non-diagonal multiplicative noise of the
+ * reference's test (test/simpleem_tests.jl): f = mu u, G[d][m] = c[d][m] u[d],
+ * p = (mu, c row-major dim x noise_dim). */
+enum oracle_sde { ORACLE_SDE_GBM = 0, ORACLE_SDE_OU = 1, ORACLE_SDE_LORENZ = 2, ORACLE_SDE_MULT = 3 };
 typedef struct {
   int sde, rounding;
   int64_t n;
@@ -84,13 +87,14 @@ typedef struct {
   double* us;        /* [nsteps+1][dim][n] or NULL */
   double* u_final;   /* [dim][n] or NULL */
   int nthreads;
+  int noise_dim;     /* 0: diagonal noise; M > 0: dim x M noise matrix, M normals a step */
 } oracle_sde_args;
 int oracle_sde_solve(const oracle_sde_args* a);
 /* Philox4x32-10 of counter c[4] under key k[2] into out[4] */
 void oracle_philox(const uint32_t* c, const uint32_t* k, uint32_t* out);
 /* the device canon's double logarithm */
 double oracle_log(double x);
-/* components 2j, 2j+1 of the step-k normal vector of trajectory idx */
+/* normals z_{2 pair}, z_{2 pair + 1} of trajectory idx's stream */
 void oracle_normal_pair(uint64_t seed, int64_t pair, int64_t idx, double* z0, double* z1);
 float oracle_ctrl_pow(float x, float b);
 /* the device canon's double sine and cosine (Cody-Waite reduction, Taylor polynomials) */

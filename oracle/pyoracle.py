@@ -50,10 +50,10 @@ class _SdeArgs(ctypes.Structure):
                 ("nparams", ctypes.c_int), ("t0", ctypes.c_double), ("dt", ctypes.c_double),
                 ("nsteps", ctypes.c_int64), ("seed", ctypes.c_uint64), ("u0", ctypes.c_void_p),
                 ("p", ctypes.c_void_p), ("us", ctypes.c_void_p), ("u_final", ctypes.c_void_p),
-                ("nthreads", ctypes.c_int)]
+                ("nthreads", ctypes.c_int), ("noise_dim", ctypes.c_int)]
 
 
-SDE = {"gbm": 0, "ou": 1, "lorenz": 2}
+SDE = {"gbm": 0, "ou": 1, "lorenz": 2, "mult": 3}
 
 _lib = None
 
@@ -265,9 +265,10 @@ def sde_grid_steps(t0, tf, dt):
     return int(q)
 
 
-def sde_solve(sde, u0, p, tspan, dt, seed, rounding="device", save_everystep=True, nthreads=1):
-    """SimpleEM (src/euler_maruyama.jl:48-98) for n trajectories with the device
-    canon's counter-based normals.  Returns u_final (dim, n) and, with
+def sde_solve(sde, u0, p, tspan, dt, seed, rounding="device", save_everystep=True, nthreads=1, noise_dim=0):
+    """SimpleEM (src/euler_maruyama.jl:48-142) for n trajectories with the device
+    canon's counter-based normals; noise_dim > 0 for the non-diagonal "mult"
+    SDE (dim x noise_dim noise matrix).  Returns u_final (dim, n) and, with
     save_everystep, us (npoints, dim, n) and the grid t."""
     u0 = np.ascontiguousarray(u0, dtype=np.float64)
     p = np.ascontiguousarray(p, dtype=np.float64)
@@ -276,7 +277,7 @@ def sde_solve(sde, u0, p, tspan, dt, seed, rounding="device", save_everystep=Tru
     us = np.full((nsteps + 1, dim, n), np.nan) if save_everystep else None
     uf = np.zeros((dim, n))
     a = _SdeArgs(SDE[sde], ROUND[rounding], n, dim, p.shape[0], float(tspan[0]), float(dt), nsteps, int(seed),
-                 _ptr(u0), _ptr(p), _ptr(us), _ptr(uf), int(nthreads))
+                 _ptr(u0), _ptr(p), _ptr(us), _ptr(uf), int(nthreads), int(noise_dim))
     if lib().oracle_sde_solve(ctypes.byref(a)) != 0:
         raise ValueError("oracle_sde_solve rejected the arguments")
     # t_k = fma(k, dt, t0): one rounding of the exact value

@@ -144,27 +144,43 @@ class SimpleEM(_Alg):
 
 
 class UserSDE:
-    """A user SDE with diagonal noise: the C++ bodies of
+    """A user SDE: the C++ bodies of
     ``__device__ void drift(double* f, const double* u, const double* p, double t)`` and
     ``__device__ void diffusion(double* g, const double* u, const double* p, double t)``,
-    compiled with NVRTC on first use."""
+    compiled with NVRTC on first use.  With ``noise_dim = M > 0`` the noise is
+    non-diagonal and ``diffusion`` writes the dim x M matrix row-major,
+    ``g[d * M + m]``."""
 
-    def __init__(self, drift, diffusion, dim, nparams):
+    def __init__(self, drift, diffusion, dim, nparams, noise_dim=0):
         self.drift, self.diffusion, self.dim, self.nparams = drift, diffusion, int(dim), int(nparams)
+        self.noise_dim = int(noise_dim)
 
 
 class SDEProblem:
-    """Out-of-place SDE du = f(u, p, t) dt + g(u, p, t) .* dW with diagonal noise.
-    ``sde`` is "gbm" (f = mu u, g = sigma u; p = (mu, sigma)), "ou"
-    (f = theta (mu - u), g = sigma; p = (theta, mu, sigma)), "lorenz"
-    (Lorenz drift, additive noise; p = (sigma, rho, beta, noise)) or a UserSDE."""
+    """Out-of-place SDE du = f(u, p, t) dt + g(u, p, t) dW.  ``sde`` is "gbm"
+    (f = mu u, g = sigma u; p = (mu, sigma)), "ou" (f = theta (mu - u),
+    g = sigma; p = (theta, mu, sigma)), "lorenz" (Lorenz drift, additive noise;
+    p = (sigma, rho, beta, noise)), "mult" (non-diagonal multiplicative noise
+    f = mu u, G[d, m] = c[d, m] u[d]; p = (mu, c row-major)) or a UserSDE.
+    ``noise_rate_prototype`` (a dim x M array, as in the reference) makes the
+    noise non-diagonal with M Wiener processes; without it the noise is
+    diagonal (g .* dW)."""
 
-    def __init__(self, sde, u0, tspan, p=(), inplace=False):
+    def __init__(self, sde, u0, tspan, p=(), inplace=False, noise_rate_prototype=None):
         self.f = sde
         self.u0 = np.atleast_1d(np.asarray(u0, dtype=np.float64))
         self.tspan = (float(tspan[0]), float(tspan[1]))
         self.p = np.atleast_1d(np.asarray(p, dtype=np.float64)) if np.size(p) else np.zeros(0)
         self.inplace = bool(inplace)
+        self.noise_rate_prototype = None if noise_rate_prototype is None else np.asarray(noise_rate_prototype)
+        if self.noise_rate_prototype is not None and (
+                self.noise_rate_prototype.ndim != 2 or self.noise_rate_prototype.shape[0] != self.u0.size):
+            raise ValueError("noise_rate_prototype must be a (dim, M) array")
+
+    @property
+    def noise_dim(self):
+        """M of a non-diagonal problem, 0 for diagonal noise."""
+        return 0 if self.noise_rate_prototype is None else int(self.noise_rate_prototype.shape[1])
 
 
 class EnsembleProblem:
@@ -424,11 +440,15 @@ def _solve_sde(eprob, alg, n, dt, save_everystep, device, single, seed):
     dim, nparams = u0s.shape[0], ps.shape[0]
     if ps.shape[0] == 0:
         ps = np.zeros((0, n))
+    M = base.noise_dim
     if isinstance(base.f, UserSDE):
+        if base.f.noise_dim != M:
+            raise ValueError("the UserSDE was declared with noise_dim %d, the problem's noise_rate_prototype has %d "
+                             "columns" % (base.f.noise_dim, M))
         cache = h.__dict__.setdefault("_sde_ids", {})
-        key = (base.f.drift, base.f.diffusion, base.f.dim, base.f.nparams)
+        key = (base.f.drift, base.f.diffusion, base.f.dim, base.f.nparams, M)
         if key not in cache:
-            cache[key] = h.compile_sde(base.f.drift, base.f.diffusion, base.f.dim, base.f.nparams)
+            cache[key] = h.compile_sde(base.f.drift, base.f.diffusion, base.f.dim, base.f.nparams, M)
         sid = cache[key]
     else:
         sid = _lib.SDE[base.f]
@@ -439,7 +459,7 @@ def _solve_sde(eprob, alg, n, dt, save_everystep, device, single, seed):
         raise ValueError("InexactError: (tf - t0)/dt = %r is not an integer" % q)
     nsteps = int(q)
     a = _lib.SdeArgs()
-    a.sde, a.n, a.dim, a.nparams = sid, n, dim, nparams
+    a.sde, a.n, a.dim, a.nparams, a.noise_dim = sid, n, dim, nparams, M
     a.t0, a.tf, a.dt, a.seed = t0, tf, float(dt), int(seed)
     a.save_everystep, a.memory = int(every), _lib.MEM_HOST
     a.u0, a.p = u0s.ctypes.data, ps.ctypes.data

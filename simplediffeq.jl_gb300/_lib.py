@@ -26,9 +26,9 @@ RET_DEFAULT, RET_DTMIN, RET_MAXITERS, RET_NAN = 0, 1, 2, 3
 EXPORTS = ["ode_abi_version", "ode_create", "ode_destroy", "ode_last_error", "ode_ensemble_solve",
            "ode_fixed_grid", "ode_rhs_compile", "ode_output_compile", "ode_learn_default_opts", "ode_learn_fit",
            "ode_learn_predict", "ode_learn_gradcheck", "ode_ensemble_solve_noalloc", "ode_autotune",
-           "ode_ensemble_solve_everystep", "ode_sde_solve", "ode_sde_compile", "ode_set_bounds_check",
-           "ode_tune_save", "ode_tune_load"]
-SDE = {"gbm": 0, "ou": 1, "lorenz": 2}
+           "ode_ensemble_solve_everystep", "ode_sde_solve", "ode_sde_compile", "ode_sde_compile_noise",
+           "ode_set_bounds_check", "ode_tune_save", "ode_tune_load"]
+SDE = {"gbm": 0, "ou": 1, "lorenz": 2, "mult": 3}
 
 
 class SolveArgs(ctypes.Structure):
@@ -59,7 +59,7 @@ class SdeArgs(ctypes.Structure):
     _fields_ = [("sde", ctypes.c_int32), ("n", ctypes.c_int64), ("dim", ctypes.c_int32), ("nparams", ctypes.c_int32),
                 ("t0", ctypes.c_double), ("tf", ctypes.c_double), ("dt", ctypes.c_double), ("seed", ctypes.c_uint64),
                 ("save_everystep", ctypes.c_int32), ("memory", ctypes.c_int32), ("u0", ctypes.c_void_p),
-                ("p", ctypes.c_void_p), ("stream", ctypes.c_void_p)]
+                ("p", ctypes.c_void_p), ("stream", ctypes.c_void_p), ("noise_dim", ctypes.c_int32)]
 
 
 class SdeOut(ctypes.Structure):
@@ -133,6 +133,9 @@ def load():
                                   ctypes.POINTER(SolveStats)]
     lib.ode_sde_compile.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(ctypes.c_int), ctypes.c_char_p, ctypes.c_size_t]
+    lib.ode_sde_compile_noise.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_char_p,
+                                          ctypes.c_size_t]
     lib.ode_fixed_grid.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                    ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
     lib.ode_rhs_compile.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
@@ -220,11 +223,11 @@ class Handle:
         return self.lib.ode_sde_solve(self.h, ctypes.byref(args), ctypes.byref(out),
                                       ctypes.byref(stats) if stats is not None else None)
 
-    def compile_sde(self, drift, diffusion, dim, nparams):
+    def compile_sde(self, drift, diffusion, dim, nparams, noise_dim=0):
         sid = ctypes.c_int(0)
         log = ctypes.create_string_buffer(8192)
-        rc = self.lib.ode_sde_compile(self.h, drift.encode(), diffusion.encode(), int(dim), int(nparams),
-                                      ctypes.byref(sid), log, 8192)
+        rc = self.lib.ode_sde_compile_noise(self.h, drift.encode(), diffusion.encode(), int(dim), int(noise_dim),
+                                            int(nparams), ctypes.byref(sid), log, 8192)
         if rc != OK:
             raise GB300ODEError(rc, self.error() + "\n" + log.value.decode(errors="replace"))
         return sid.value

@@ -36,6 +36,7 @@ struct UserOutput {
 struct UserSde {
   std::string drift, diffusion;
   int dim = 0, nparams = 0;
+  int noise_dim = 0;  /* 0: diagonal noise */
 };
 
 struct Model;  /* learned-schedule model, defined in learn.cu */

@@ -34,6 +34,16 @@ namespace {
 constexpr int kBlock = 128;
 
 int check_sde(ode_handle* h, const ode_sde_args* a) {
+  if (a->noise_dim < 0 || a->noise_dim > 32) return fail(h, ODE_EINVAL, "noise_dim must be in [0, 32]");
+  if (a->sde == ODE_SDE_MULT) {
+    if (a->dim < 1 || a->dim > 32 || a->noise_dim < 1 || a->dim * a->noise_dim > 64 ||
+        a->nparams != 1 + a->dim * a->noise_dim)
+      return fail(h, ODE_EINVAL, "non-diagonal multiplicative noise needs noise_dim >= 1, dim x noise_dim <= 64, "
+                                 "1 + dim x noise_dim parameters");
+    return ODE_OK;
+  }
+  if (a->noise_dim != 0 && a->sde < ODE_SDE_USER)
+    return fail(h, ODE_EINVAL, "this built-in SDE has diagonal noise (noise_dim 0)");
   switch (a->sde) {
     case ODE_SDE_GBM:
       if (a->dim < 1 || a->dim > 32 || a->nparams != 2) return fail(h, ODE_EINVAL, "GBM needs 1 <= dim <= 32, 2 parameters");
@@ -47,8 +57,8 @@ int check_sde(ode_handle* h, const ode_sde_args* a) {
   }
   if (a->sde >= ODE_SDE_USER && a->sde < ODE_SDE_USER + (int)h->sdes.size()) {
     const UserSde& u = h->sdes[a->sde - ODE_SDE_USER];
-    if (u.dim != a->dim || u.nparams != a->nparams)
-      return fail(h, ODE_EINVAL, "the SDE was compiled for another dim / nparams");
+    if (u.dim != a->dim || u.nparams != a->nparams || u.noise_dim != a->noise_dim)
+      return fail(h, ODE_EINVAL, "the SDE was compiled for another dim / nparams / noise_dim");
     return ODE_OK;
   }
   return fail(h, ODE_EINVAL, "unknown SDE");
@@ -60,7 +70,8 @@ std::string sde_source(ode_handle* h, const ode_sde_args* a) {
   char buf[256];
   if (a->sde >= ODE_SDE_USER) {
     const UserSde& u = h->sdes[a->sde - ODE_SDE_USER];
-    snprintf(buf, sizeof buf, "struct UserSde {\n  enum { D = %d, NP = %d };\n  double p[%d];\n", u.dim, u.nparams,
+    snprintf(buf, sizeof buf, "struct UserSde {\n  enum { D = %d, M = %d, GN = %d, NP = %d };\n  double p[%d];\n",
+             u.dim, u.noise_dim, u.noise_dim > 0 ? u.dim * u.noise_dim : u.dim, u.nparams,
              u.nparams > 0 ? u.nparams : 1);
     src += buf;
     src += "  __device__ static __forceinline__ void user_drift(double* f, const double* u, const double* p, "
@@ -72,12 +83,15 @@ std::string sde_source(ode_handle* h, const ode_sde_args* a) {
     src += "\n  }\n"
            "  __device__ __forceinline__ void drift(const double (&u)[D], double t, double (&f)[D]) const {\n"
            "    user_drift(f, u, p, t);\n  }\n"
-           "  __device__ __forceinline__ void diffusion(const double (&u)[D], double t, double (&g)[D]) const {\n"
+           "  __device__ __forceinline__ void diffusion(const double (&u)[D], double t, double (&g)[GN]) const {\n"
            "    user_diffusion(g, u, p, t);\n  }\n};\n";
     src += "GBODE_SDE_ENTRY(gbode_jit, UserSde)\n";
     return src;
   }
-  if (a->sde == ODE_SDE_GBM) snprintf(buf, sizeof buf, "GBODE_SDE_ENTRY(gbode_jit, gbode::SdeGBM<%d>)\n", a->dim);
+  if (a->sde == ODE_SDE_MULT)  /* a typedef: the macro argument may not hold the template's comma */
+    snprintf(buf, sizeof buf, "typedef gbode::SdeMult<%d, %d> SdeT;\nGBODE_SDE_ENTRY(gbode_jit, SdeT)\n", a->dim,
+             a->noise_dim);
+  else if (a->sde == ODE_SDE_GBM) snprintf(buf, sizeof buf, "GBODE_SDE_ENTRY(gbode_jit, gbode::SdeGBM<%d>)\n", a->dim);
   else if (a->sde == ODE_SDE_OU) snprintf(buf, sizeof buf, "GBODE_SDE_ENTRY(gbode_jit, gbode::SdeOU<%d>)\n", a->dim);
   else snprintf(buf, sizeof buf, "GBODE_SDE_ENTRY(gbode_jit, gbode::SdeLorenz)\n");
   return src + buf;
@@ -85,7 +99,7 @@ std::string sde_source(ode_handle* h, const ode_sde_args* a) {
 
 int sde_kernel(ode_handle* h, const ode_sde_args* a, CUfunction* fn) {
   char key[64];
-  snprintf(key, sizeof key, "%d|%d", a->sde, a->dim);
+  snprintf(key, sizeof key, "%d|%d|%d", a->sde, a->dim, a->noise_dim);
   auto it = h->sde_kernels.find(key);
   if (it != h->sde_kernels.end()) {
     *fn = it->second;
@@ -115,8 +129,14 @@ extern "C" {
 
 int ode_sde_compile(ode_handle* h, const char* drift, const char* diffusion, int dim, int nparams, int* sde_id,
                     char* log, size_t loglen) {
+  return ode_sde_compile_noise(h, drift, diffusion, dim, 0, nparams, sde_id, log, loglen);
+}
+
+int ode_sde_compile_noise(ode_handle* h, const char* drift, const char* diffusion, int dim, int noise_dim,
+                          int nparams, int* sde_id, char* log, size_t loglen) {
   if (!h) return ODE_EINVAL;
-  if (!drift || !diffusion || !sde_id || dim < 1 || dim > 32 || nparams < 0 || nparams > 256)
+  if (!drift || !diffusion || !sde_id || dim < 1 || dim > 32 || nparams < 0 || nparams > 256 || noise_dim < 0 ||
+      noise_dim > 32 || dim * noise_dim > 256)
     return fail(h, ODE_EINVAL, "ode_sde_compile: bad arguments");
   SCK(cudaSetDevice(h->device), "cudaSetDevice");
   UserSde u;
@@ -124,12 +144,14 @@ int ode_sde_compile(ode_handle* h, const char* drift, const char* diffusion, int
   u.diffusion = diffusion;
   u.dim = dim;
   u.nparams = nparams;
+  u.noise_dim = noise_dim;
   h->sdes.push_back(u);
   ode_sde_args a;
   std::memset(&a, 0, sizeof a);
   a.sde = ODE_SDE_USER + (int)h->sdes.size() - 1;
   a.dim = dim;
   a.nparams = nparams;
+  a.noise_dim = noise_dim;
   CUfunction fn;
   std::string lg;
   const int rc = jit_function(h, sde_source(h, &a), kBlock, &fn, &lg);
@@ -142,7 +164,7 @@ int ode_sde_compile(ode_handle* h, const char* drift, const char* diffusion, int
     return rc;
   }
   char key[64];
-  snprintf(key, sizeof key, "%d|%d", a.sde, a.dim);
+  snprintf(key, sizeof key, "%d|%d|%d", a.sde, a.dim, a.noise_dim);
   h->sde_kernels[key] = fn;
   *sde_id = a.sde;
   return ODE_OK;
@@ -179,6 +201,7 @@ int ode_sde_solve(ode_handle* h, const ode_sde_args* a, ode_sde_out* o, ode_solv
   sp.seed = a->seed;
   sp.dim = D;
   sp.nparams = NP;
+  sp.noise_dim = a->noise_dim;
   sp.save_everystep = a->save_everystep ? 1 : 0;
   const bool host = a->memory == ODE_MEM_HOST;
   const size_t nd = (size_t)n * sizeof(double);

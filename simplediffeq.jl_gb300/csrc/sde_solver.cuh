@@ -1,9 +1,11 @@
-/* Device side of the SimpleEM ensemble solver (src/euler_maruyama.jl:48-98):
- * fixed-step Euler-Maruyama for SDEs with diagonal noise, one trajectory per
- * thread.
+/* Device side of the SimpleEM ensemble solver (src/euler_maruyama.jl:48-142):
+ * fixed-step Euler-Maruyama, one trajectory per thread.
  *
  *   n = Int((tf - t0) / dt) + 1 points, t_k = t0 + k*dt (a scalar muladd),
- *   u_{k+1} = u_k + f(u_k, p, t_k)*dt + sqrt(dt)*g(u_k, p, t_k) .* xi_k
+ *   diagonal noise:      u_{k+1} = u_k + f(u_k, p, t_k)*dt + sqrt(dt)*g(u_k, p, t_k) .* xi_k
+ *   non-diagonal noise:  u_{k+1} = u_k + f(u_k, p, t_k)*dt + sqrt(dt)*(G(u_k, p, t_k) * xi_k)
+ * with G a dim x M matrix (the reference's noise_rate_prototype) and xi_k M
+ * normals.
  *
  * The reference draws xi_k with Julia's randn; this solver draws them from a
  * counter-based generator so that every trajectory's noise is reproducible
@@ -20,7 +22,11 @@
  *     (r cos 2 pi u2, r sin 2 pi u2), with this file's log_dev and
  *     ode_solver.cuh's sincos_cw, so that the oracle reproduces every normal
  *     bit for bit.
- * Update rounding (device canon): u = fma(sqdt*g, xi, fma(f, dt, u)). */
+ * Non-diagonal noise takes M normals a step from the same stream.
+ * Update rounding (device canon): diagonal u = fma(sqdt*g, xi, fma(f, dt, u));
+ * non-diagonal s = G[d][0] xi_0, s = fma(G[d][m], xi_m, s) for m = 1..M-1,
+ * u = fma(sqdt, s, fma(f, dt, u)) (the reference's mul!(gtmp2, gtmp, dW) and
+ * uprev + ftmp*dt + sqdt*gtmp2 under @muladd). */
 #pragma once
 #include "ode_solver.cuh"
 
@@ -32,6 +38,7 @@ struct SParams {
   double t0, dt;
   unsigned long long seed;
   int dim, nparams;
+  int noise_dim;         /* 0: diagonal noise; M: dim x M noise matrix */
   int save_everystep;
   const double* u0;      /* [dim][n] */
   const double* p;       /* [nparams][n] */
@@ -110,7 +117,7 @@ __device__ __forceinline__ void normal_pair(unsigned long long seed, long long P
 /* geometric Brownian motion: f = mu u, g = sigma u; p = (mu, sigma) */
 template <int DD>
 struct SdeGBM {
-  enum { D = DD, NP = 2 };
+  enum { D = DD, M = 0, GN = DD, NP = 2 };
   double p[2];
   __device__ __forceinline__ void drift(const double (&u)[DD], double t, double (&f)[DD]) const {
 #pragma unroll
@@ -125,7 +132,7 @@ struct SdeGBM {
 /* Ornstein-Uhlenbeck: f = theta (mu - u), g = sigma; p = (theta, mu, sigma) */
 template <int DD>
 struct SdeOU {
-  enum { D = DD, NP = 3 };
+  enum { D = DD, M = 0, GN = DD, NP = 3 };
   double p[3];
   __device__ __forceinline__ void drift(const double (&u)[DD], double t, double (&f)[DD]) const {
 #pragma unroll
@@ -139,7 +146,7 @@ struct SdeOU {
 
 /* Lorenz drift with additive noise of strength p[3]; p = (sigma, rho, beta, noise) */
 struct SdeLorenz {
-  enum { D = 3, NP = 4 };
+  enum { D = 3, M = 0, GN = 3, NP = 4 };
   double p[4];
   __device__ __forceinline__ void drift(const double (&u)[3], double t, double (&f)[3]) const {
     f[0] = p[0] * (u[1] - u[0]);
@@ -153,23 +160,43 @@ struct SdeLorenz {
   }
 };
 
-/* xi[0..D) = z_{kD}, ..., z_{kD+D-1}.  For odd D a pair straddles two steps:
- * an even step draws (D+1)/2 pairs and keeps the last normal in `carry` for
- * the next step, which starts with it and draws (D-1)/2 pairs. */
-template <int D>
-__device__ __forceinline__ void step_normals(unsigned long long seed, long long k, long long idx, double (&xi)[D + 1],
+/* xi[0..N) = z_{kN}, ..., z_{kN+N-1} (N = dim for diagonal noise, M
+ * otherwise).  For odd N a pair straddles two steps: an even step draws
+ * (N+1)/2 pairs and keeps the last normal in `carry` for the next step, which
+ * starts with it and draws (N-1)/2 pairs. */
+template <int N>
+__device__ __forceinline__ void step_normals(unsigned long long seed, long long k, long long idx, double (&xi)[N + 1],
                                              double& carry) {
-  const long long g0 = k * D;
-  if ((D & 1) && (g0 & 1)) {
+  const long long g0 = k * N;
+  if ((N & 1) && (g0 & 1)) {
     xi[0] = carry;
 #pragma unroll
-    for (int j = 0; j < (D - 1) / 2; ++j) normal_pair(seed, (g0 + 1) / 2 + j, idx, &xi[1 + 2 * j], &xi[2 + 2 * j]);
+    for (int j = 0; j < (N - 1) / 2; ++j) normal_pair(seed, (g0 + 1) / 2 + j, idx, &xi[1 + 2 * j], &xi[2 + 2 * j]);
   } else {
 #pragma unroll
-    for (int j = 0; j < (D + 1) / 2; ++j) normal_pair(seed, g0 / 2 + j, idx, &xi[2 * j], &xi[2 * j + 1]);
-    if (D & 1) carry = xi[D];
+    for (int j = 0; j < (N + 1) / 2; ++j) normal_pair(seed, g0 / 2 + j, idx, &xi[2 * j], &xi[2 * j + 1]);
+    if (N & 1) carry = xi[N];
   }
 }
+
+/* Non-diagonal multiplicative noise, the reference's test SDE
+ * (test/simpleem_tests.jl): f = mu u, G[d][m] = c[d][m] u[d];
+ * p = (mu, c row-major DD x MM) */
+template <int DD, int MM>
+struct SdeMult {
+  enum { D = DD, M = MM, GN = DD * MM, NP = 1 + DD * MM };
+  double p[NP];
+  __device__ __forceinline__ void drift(const double (&u)[DD], double t, double (&f)[DD]) const {
+#pragma unroll
+    for (int d = 0; d < DD; ++d) f[d] = p[0] * u[d];
+  }
+  __device__ __forceinline__ void diffusion(const double (&u)[DD], double t, double (&g)[GN]) const {
+#pragma unroll
+    for (int d = 0; d < DD; ++d)
+#pragma unroll
+      for (int m = 0; m < MM; ++m) g[d * MM + m] = p[1 + d * MM + m] * u[d];
+  }
+};
 
 /* ------------------------------------------------------------------ the Euler-Maruyama loop */
 template <class S>
@@ -187,15 +214,26 @@ __device__ __forceinline__ void run_em(const SParams& P) {
 #pragma unroll
     for (int d = 0; d < D; ++d) P.us[(long long)d * P.n + i] = u[d];
   const double dt = P.dt, sqdt = __dsqrt_rn(P.dt);
+  enum { N = S::M > 0 ? S::M : D };  /* normals a step */
   double carry = 0.0;
   for (long long k = 0; k < P.nsteps; ++k) {
     const double t = __fma_rn((double)k, dt, P.t0);
-    double f[D], g[D], xi[D + 1];
+    double f[D], g[S::GN], xi[N + 1];
     sde.drift(u, t, f);
     sde.diffusion(u, t, g);
-    step_normals<D>(P.seed, k, i, xi, carry);
+    step_normals<N>(P.seed, k, i, xi, carry);
+    if constexpr (S::M > 0) {
 #pragma unroll
-    for (int d = 0; d < D; ++d) u[d] = __fma_rn(sqdt * g[d], xi[d], __fma_rn(f[d], dt, u[d]));
+      for (int d = 0; d < D; ++d) {
+        double s = g[d * N] * xi[0];
+#pragma unroll
+        for (int m = 1; m < N; ++m) s = __fma_rn(g[d * N + m], xi[m], s);
+        u[d] = __fma_rn(sqdt, s, __fma_rn(f[d], dt, u[d]));
+      }
+    } else {
+#pragma unroll
+      for (int d = 0; d < D; ++d) u[d] = __fma_rn(sqdt * g[d], xi[d], __fma_rn(f[d], dt, u[d]));
+    }
     if (P.save_everystep && P.us)
 #pragma unroll
       for (int d = 0; d < D; ++d) P.us[((k + 1) * D + d) * P.n + i] = u[d];

@@ -32,7 +32,7 @@ def test_library_exports_every_declared_symbol(pkg):
     for name in declared_functions():
         assert name in exported, name
         assert getattr(lib, name) is not None
-    assert lib.ode_abi_version() == 2
+    assert lib.ode_abi_version() == 3
 
 
 def test_library_needs_no_driver_at_load_time(pkg):
@@ -82,7 +82,8 @@ def test_null_handle_and_bad_arguments(pkg):
 
 STRUCTS = [("SolveArgs", "ode_solve_args"), ("SolveOut", "ode_solve_out"), ("SolveStats", "ode_solve_stats"),
            ("LearnOpts", "ode_learn_opts"), ("LearnReport", "ode_learn_report"), ("TuneVariant", "ode_tune_variant"),
-           ("TuneReport", "ode_tune_report")]
+           ("TuneReport", "ode_tune_report"), ("SdeArgs", "ode_sde_args"), ("SdeOut", "ode_sde_out"),
+           ("EverystepOut", "ode_everystep_out")]
 
 
 def test_ctypes_structs_match_the_c_layout(pkg, tmp_path):

@@ -1,4 +1,4 @@
-"""GPU SimpleEM (src/euler_maruyama.jl:48-98) against the oracle: every
+"""GPU SimpleEM (src/euler_maruyama.jl:48-142) against the oracle: every
 trajectory's path bit-identical to the CPU restatement with the same
 counter-based normals (Philox4x32-10 + Box-Muller), for the built-in SDEs
 compiled ahead of time and at run time, a user SDE compiled with NVRTC, host
@@ -68,4 +68,68 @@ def test_simple_em_device_buffers_and_bad_grid(pkg, po):
     ref = po.sde_solve("gbm", u0, p, (0.0, 1.0), 0.01, seed=99, save_everystep=False)
     assert np.array_equal(uf.cpu().numpy(), ref["u_final"])
     a.dt = 0.3  # (tf - t0)/dt not an integer: the reference's Int(...) throws
+    assert h.sde_solve(a, o) == L.EINVAL
+
+
+def sde_nd(pkg, kind, u0, p, M, tspan, dt, seed, every=True):
+    proto = np.zeros((u0.shape[0], M))
+    ep = pkg.EnsembleProblem(pkg.SDEProblem(kind, u0[:, 0], tspan, p[:, 0], noise_rate_prototype=proto),
+                             u0s=u0, ps=p)
+    return pkg.solve(ep, pkg.SimpleEM(), trajectories=u0.shape[1], dt=dt, seed=seed, save_everystep=every)
+
+
+@pytest.mark.parametrize("dim,M", [(2, 4), (3, 3), (1, 1), (4, 5)])
+def test_simple_em_non_diagonal_bitexact(pkg, po, dim, M):
+    """Non-diagonal noise (src/euler_maruyama.jl:126-134), the reference's test
+    SDE generalised (test/simpleem_tests.jl: f = 1.01u, G = c .* u, 2 x 4):
+    bit-identical to the oracle, for even and odd noise dimensions (odd M
+    shares a Box-Muller pair between steps)."""
+    rng = np.random.default_rng(10 * dim + M)
+    n = 2500
+    u0 = rng.uniform(0.5, 2.0, (dim, n))
+    c = rng.uniform(0.05, 1.8, (dim * M, n))
+    p = np.vstack([np.full((1, n), 1.01), c])
+    sol = sde_nd(pkg, "mult", u0, p, M, (0.0, 1.0), 0.25 if (dim, M) == (2, 4) else 0.01, seed=21)
+    ref = po.sde_solve("mult", u0, p, (0.0, 1.0), 0.25 if (dim, M) == (2, 4) else 0.01, seed=21, nthreads=8,
+                       noise_dim=M)
+    assert sol.us.shape == ref["us"].shape
+    assert np.array_equal(sol.us, ref["us"]) and np.array_equal(sol.u_final, ref["u_final"])
+
+
+def test_user_sde_non_diagonal_equals_builtin(pkg):
+    rng = np.random.default_rng(8)
+    n, M = 2000, 3
+    u0 = rng.uniform(0.5, 2.0, (2, n))
+    p = np.vstack([np.full((1, n), 0.3), rng.uniform(0.1, 1.0, (2 * M, n))])
+    user = pkg.UserSDE("for (int d = 0; d < 2; ++d) f[d] = p[0] * u[d];",
+                       "for (int d = 0; d < 2; ++d) for (int m = 0; m < 3; ++m) g[d * 3 + m] = p[1 + d * 3 + m] * u[d];",
+                       dim=2, nparams=1 + 2 * M, noise_dim=M)
+    a = sde_nd(pkg, user, u0, p, M, (0.0, 1.0), 0.01, seed=6)
+    b = sde_nd(pkg, "mult", u0, p, M, (0.0, 1.0), 0.01, seed=6)
+    assert np.array_equal(a.us, b.us)
+    with pytest.raises(ValueError):
+        sde_nd(pkg, user, u0, p, M + 1, (0.0, 1.0), 0.01, seed=6)  # declared noise_dim differs
+
+
+def test_non_diagonal_argument_checks(pkg):
+    L = pkg._lib
+    h = pkg._handle(0)
+    n = 10
+    u0 = np.ones((2, n))
+    p = np.ones((9, n))
+    a = L.SdeArgs()
+    a.sde, a.n, a.dim, a.nparams, a.noise_dim = L.SDE["mult"], n, 2, 9, 4
+    a.t0, a.tf, a.dt, a.seed = 0.0, 1.0, 0.25, 1
+    a.memory = L.MEM_HOST
+    a.u0, a.p = u0.ctypes.data, p.ctypes.data
+    uf = np.zeros((2, n))
+    o = L.SdeOut()
+    o.u_final = uf.ctypes.data
+    h.check(h.sde_solve(a, o))
+    assert np.all(np.isfinite(uf))
+    a.nparams = 8  # needs 1 + dim x noise_dim
+    assert h.sde_solve(a, o) == L.EINVAL
+    a.nparams, a.noise_dim = 9, 0  # the multiplicative SDE is non-diagonal only
+    assert h.sde_solve(a, o) == L.EINVAL
+    a.sde, a.nparams, a.noise_dim = L.SDE["gbm"], 2, 2  # a diagonal built-in takes no noise matrix
     assert h.sde_solve(a, o) == L.EINVAL

@@ -333,6 +333,36 @@ def test_simple_em_weak_moments(po):
     assert o["t"][-1] == 10.0
 
 
+def test_simple_em_non_diagonal_noise(po):
+    """Non-diagonal noise (src/euler_maruyama.jl:126-134): the reference's test
+    SDE (test/simpleem_tests.jl) f = 1.01u, G = [0.3 0.6 0.9 0.12; 1.2 0.2 0.3 1.8] .* u,
+    a 2 x 4 noise matrix, u0 = ones(2), dt = 0.25 on (0, 1): five points per
+    trajectory, EM's exact mean (1 + 1.01 dt)^4 (the noise has mean zero), and
+    with one noise dimension the same path as diagonal GBM up to rounding."""
+    n = 40000
+    c = np.array([[0.3, 0.6, 0.9, 0.12], [1.2, 0.2, 0.3, 1.8]])
+    p = np.tile(np.concatenate([[1.01], c.ravel()])[:, None], (1, n))
+    o = po.sde_solve("mult", np.ones((2, n)), p, (0.0, 1.0), 0.25, seed=5, noise_dim=4, nthreads=8)
+    assert o["us"].shape == (5, 2, n) and len(o["t"]) == 5
+    # per component the EM factor is prod_k (1 + 1.01 dt + sqrt(dt) c_d . xi_k): mean (1 + 1.01 dt)^4
+    var1 = (1 + 1.01 * 0.25) ** 2 + 0.25 * (c ** 2).sum(axis=1)
+    sd = np.sqrt(var1 ** 4 - (1 + 1.01 * 0.25) ** 8) / np.sqrt(n)
+    assert np.all(np.abs(o["u_final"].mean(axis=1) - (1 + 1.01 * 0.25) ** 4) < 5 * sd)
+    # the two components share the four normals of a step: their increments correlate as c0 . c1 says
+    inc = np.diff(o["us"][:2], axis=0)[0]
+    rho = (c[0] @ c[1]) / np.sqrt((c[0] @ c[0]) * (c[1] @ c[1]))
+    assert abs(np.corrcoef(inc[0], inc[1])[0, 1] - rho) < 0.02
+    # one noise dimension: the diagonal GBM path, up to the rounding of sqdt (g xi) against (sqdt g) xi
+    m = 2000
+    a = po.sde_solve("mult", np.ones((1, m)), np.tile([[0.1], [0.2]], (1, m)), (0.0, 1.0), 0.01, seed=9,
+                     noise_dim=1, save_everystep=False)
+    b = po.sde_solve("gbm", np.ones((1, m)), np.tile([[0.1], [0.2]], (1, m)), (0.0, 1.0), 0.01, seed=9,
+                     save_everystep=False)
+    assert np.allclose(a["u_final"], b["u_final"], rtol=1e-13, atol=0)
+    with pytest.raises(ValueError):
+        po.sde_solve("mult", np.ones((2, 4)), np.ones((9, 4)), (0.0, 1.0), 0.25, seed=1, noise_dim=3)
+
+
 def test_simple_em_rounding_modes_and_grid(po):
     u0 = np.array([[1.0], [1.0], [1.0]])
     p = np.array([[10.0], [28.0], [8 / 3], [0.1]])
