@@ -194,6 +194,12 @@ int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o,
  * `out` (may be NULL) and the full length to *len. */
 int ode_fixed_grid(double t0, double dt, double tf, int precision, double* out, int64_t cap, int64_t* len);
 
+/* Select a built-in right-hand side (ODE_RHS_LORENZ .. ODE_RHS_LINEAR) for a
+ * state of `dim` components: on success *rhs_out receives the id to put in
+ * ode_solve_args.rhs and *nparams_out (may be NULL) the number of parameters
+ * it takes; ODE_EINVAL if that right-hand side has no form of that dimension. */
+int ode_rhs_builtin(ode_handle* h, int rhs_id, int dim, int* rhs_out, int* nparams_out);
+
 /* Compile a user right-hand side with NVRTC.  `body` is the body of
  *   template <class R> __device__ void rhs(R* du, const R* u, const R* p, R t)
  * for a state of `dim` components and `nparams` parameters; R is double or

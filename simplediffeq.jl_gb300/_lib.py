@@ -27,7 +27,7 @@ EXPORTS = ["ode_abi_version", "ode_create", "ode_destroy", "ode_last_error", "od
            "ode_fixed_grid", "ode_rhs_compile", "ode_output_compile", "ode_learn_default_opts", "ode_learn_fit",
            "ode_learn_predict", "ode_learn_gradcheck", "ode_ensemble_solve_noalloc", "ode_autotune",
            "ode_ensemble_solve_everystep", "ode_sde_solve", "ode_sde_compile", "ode_sde_compile_noise",
-           "ode_set_bounds_check", "ode_tune_save", "ode_tune_load"]
+           "ode_set_bounds_check", "ode_tune_save", "ode_tune_load", "ode_rhs_builtin"]
 SDE = {"gbm": 0, "ou": 1, "lorenz": 2, "mult": 3}
 
 
@@ -138,6 +138,8 @@ def load():
                                           ctypes.c_size_t]
     lib.ode_fixed_grid.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                    ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
+    lib.ode_rhs_builtin.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                    ctypes.POINTER(ctypes.c_int)]
     lib.ode_rhs_compile.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(ctypes.c_int), ctypes.c_char_p, ctypes.c_size_t]
     lib.ode_output_compile.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -222,6 +224,13 @@ class Handle:
     def sde_solve(self, args, out, stats=None):
         return self.lib.ode_sde_solve(self.h, ctypes.byref(args), ctypes.byref(out),
                                       ctypes.byref(stats) if stats is not None else None)
+
+    def rhs_builtin(self, name, dim):
+        """(rhs id, number of parameters) of a built-in right-hand side of dimension dim."""
+        rid, np_ = ctypes.c_int(-1), ctypes.c_int(-1)
+        self.check(self.lib.ode_rhs_builtin(self.h, RHS[name] if isinstance(name, str) else int(name), int(dim),
+                                            ctypes.byref(rid), ctypes.byref(np_)))
+        return rid.value, np_.value
 
     def compile_sde(self, drift, diffusion, dim, nparams, noise_dim=0):
         sid = ctypes.c_int(0)

@@ -1265,6 +1265,30 @@ int solve_chunked(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_
 
 extern "C" {
 
+int ode_rhs_builtin(ode_handle* h, int rhs_id, int dim, int* rhs_out, int* nparams_out) {
+  if (!h) return ODE_EINVAL;
+  if (!rhs_out) return fail(h, ODE_EINVAL, "null rhs_out");
+  int np = -1;
+  switch (rhs_id) {
+    case ODE_RHS_LORENZ: np = 3; break;
+    case ODE_RHS_VANDERPOL: np = 1; break;
+    case ODE_RHS_R3BP: np = 1; break;
+    case ODE_RHS_KURAMOTO: np = dim + 1; break;
+    case ODE_RHS_LINEAR: np = dim * dim; break;
+    default: return fail(h, ODE_EINVAL, "not a built-in right-hand side id");
+  }
+  ode_solve_args a;
+  std::memset(&a, 0, sizeof a);
+  a.rhs = rhs_id;
+  a.dim = dim;
+  a.nparams = np;
+  const int rc = check_rhs(h, &a);  /* the dimension rules the solver applies */
+  if (rc != ODE_OK) return rc;
+  *rhs_out = rhs_id;
+  if (nparams_out) *nparams_out = np;
+  return ODE_OK;
+}
+
 int ode_ensemble_solve(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_solve_stats* st) {
   if (h && a && o && a->memory == ODE_MEM_HOST && a->n >= 2 * kChunk && !is_fixed(a->alg) && !h->bounds_check &&
       a->alg >= ODE_ALG_RK4 && a->alg <= ODE_ALG_EULER && a->dim >= 1 && a->nparams >= 0 &&

@@ -131,3 +131,9 @@ def test_tuning_cache_rejects_bad_files_without_a_gpu(pkg, tmp_path):
     lib = pkg._lib.load()
     assert lib.ode_tune_load(None, b"x") == pkg._lib.EINVAL
     assert lib.ode_tune_save(None, b"x") == pkg._lib.EINVAL
+
+
+def test_rhs_builtin_without_handle(pkg):
+    lib = pkg._lib.load()
+    rid = ctypes.c_int(-1)
+    assert lib.ode_rhs_builtin(None, 0, 3, ctypes.byref(rid), None) == pkg._lib.EINVAL

@@ -68,3 +68,17 @@ def test_single_trajectory_every_step(pkg, po):
     one = pkg.solve(pkg.ODEProblem("lorenz", u0[:, 0], (0.0, 1.0), p[:, 0]), pkg.GPUSimpleATsit5(), dt=0.1,
                     save_everystep=True)
     assert np.array_equal(one.t, ref["ts_rows"]) and len(one.u) == len(ref["ts_rows"])
+
+
+def test_rhs_builtin_selects_by_dimension(pkg):
+    """ode_rhs_builtin: the id and parameter count of a built-in right-hand
+    side for a dimension, EINVAL where it has no form of that dimension."""
+    h = pkg._handle(0)
+    assert h.rhs_builtin("lorenz", 3) == (0, 3)
+    assert h.rhs_builtin("kuramoto", 12) == (3, 13)
+    assert h.rhs_builtin("linear", 4) == (4, 16)
+    for name, dim in (("lorenz", 2), ("vanderpol", 3), ("r3bp", 2), ("linear", 9), ("kuramoto", 0)):
+        with pytest.raises(pkg.GB300ODEError):
+            h.rhs_builtin(name, dim)
+    with pytest.raises(pkg.GB300ODEError):
+        h.rhs_builtin(999, 3)
