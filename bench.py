@@ -131,9 +131,9 @@ CONFIGS = {
                                  "(drift sigma=10, rho~U[0,30], beta=8/3; additive noise 0.5 per component), "
                                  "u0~U[-1,1]^3+(0,0,20), tspan (0,1), dt 1e-3, final state; Philox4x32-10 normals",
             sde="lorenz", n=1048576, tspan=(0.0, 1.0), dt=1e-3, inputs=inputs_sde_lorenz, dtype="f64",
-            # per step: drift 8, 1.5 Box-Muller pairs x 69 (3 normals a step from a stream of pairs; a pair:
-            # log 31, sqrt, 2 pi u2, sin/cos 33, 2 products), update 3 x 5, grid time 2
-            flops_step=8 + 1.5 * 69 + 15 + 2),
+            # per step: drift 8, 1.5 Box-Muller pairs x 61 (3 normals a step from a stream of pairs; a pair:
+            # table-driven log 23, sqrt, 2 pi u2, sin/cos 33, 2 products), update 3 x 5, grid time 2
+            flops_step=8 + 1.5 * 61 + 15 + 2),
 }
 
 

@@ -40,6 +40,7 @@
 #include "oracle.h"
 #include "ctrl_pow.h"
 #include "../simplediffeq.jl_gb300/csrc/tableaus.h"
+#include "../simplediffeq.jl_gb300/csrc/log_table.h"
 
 #include <algorithm>
 #include <cmath>
@@ -1260,28 +1261,24 @@ void philox(const uint32_t* cin, const uint32_t* kin, uint32_t* out) {
   out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
-/* log of a positive normal double, device canon: x = m 2^e with m in
- * [sqrt(1/2), sqrt(2)), log m = 2 atanh(s) = 2 (s + s^3/3 + ... + s^23/23),
- * s = (m-1)/(m+1), plus e (LN2_HI + LN2_LO) with LN2_HI of 42 bits. */
+/* log of a positive normal double, device canon (table-driven, Tang 1990):
+ * x = 2^e m, m in [1, 2), row j = top 7 fraction bits of log_table.h;
+ * log x = e' ln2 + T_j + log1p(r), r = fma(m, 1/F_j, -1), e' = e + [j >= 53],
+ * log1p(r) = r + r^2 q(r) with the Taylor coefficients -1/2 .. -1/8. */
 double log_dev(double x) {
   uint64_t b;
   std::memcpy(&b, &x, 8);
-  int e = (int)((b >> 52) & 0x7ff) - 1023;
+  const int j = (int)((b >> 45) & 127);
+  const int e = (int)((b >> 52) & 0x7ff) - 1023 + (j >= GBODE_LOGTAB_SHIFT_FROM ? 1 : 0);
   const uint64_t mb = (b & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL;
   double m;
   std::memcpy(&m, &mb, 8);
-  if (m > 0x1.6a09e667f3bcdp+0) {
-    m = m * 0.5;
-    e += 1;
-  }
-  const double s = (m - 1.0) / (m + 1.0);
-  const double z = s * s;
-  double q = 1.0 / 23.0;
-  for (int k = 10; k >= 1; --k) q = std::fma(q, z, 1.0 / (double)(2 * k + 1));
-  const double t2 = s + s;
-  const double lm = std::fma(t2 * z, q, t2);
+  const double r = std::fma(m, kLogTab[j][0], -1.0);
+  double q = -1.0 / 8.0;
+  for (int k = 7; k >= 2; --k) q = std::fma(q, r, (k & 1 ? 1.0 : -1.0) / (double)k);
+  const double l1p = std::fma(r * r, q, r);
   const double de = (double)e;
-  return std::fma(de, 0x1.62e42fefa38p-1, std::fma(de, 0x1.ef35793c7673p-45, lm));
+  return std::fma(de, 0x1.62e42fefa38p-1, kLogTab[j][1]) + (std::fma(de, 0x1.ef35793c7673p-45, kLogTab[j][2]) + l1p);
 }
 
 /* normals z_{2P}, z_{2P+1} of trajectory idx's stream: Philox counter

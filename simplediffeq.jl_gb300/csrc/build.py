@@ -91,7 +91,8 @@ def gen_sources():
     # 1. embedded headers
     parts = ["/* generated by build.py: device headers for NVRTC */\n"]
     for fname, var in (("ode_solver.cuh", "kSrc_ode_solver_cuh"), ("ode_kparams.h", "kSrc_ode_kparams_h"),
-                       ("tableaus.h", "kSrc_tableaus_h"), ("sde_solver.cuh", "kSrc_sde_solver_cuh")):
+                       ("tableaus.h", "kSrc_tableaus_h"), ("sde_solver.cuh", "kSrc_sde_solver_cuh"),
+                       ("log_table.h", "kSrc_log_table_h")):
         text = open(os.path.join(HERE, fname)).read()
         assert ")GBSRC\"" not in text
         parts.append('static const char* %s = R"GBSRC(%s)GBSRC";\n' % (var, text))
@@ -150,7 +151,7 @@ def build(verbose=False, jobs=None):
     tus = gen_sources()
     os.makedirs(LIB, exist_ok=True)
     headers = [os.path.join(HERE, f) for f in ("ode_solver.cuh", "ode_kparams.h", "tableaus.h", "ode_host.h",
-                                               "jlrange.h", "sde_solver.cuh")] + [
+                                               "jlrange.h", "sde_solver.cuh", "log_table.h")] + [
         os.path.join(PKG, "..", "include", "gb300ode.h")]
     host_tus = [os.path.join(HERE, f) for f in ("ode_capi.cu", "learn.cu", "noalloc.cu", "sde_capi.cu")]
     gen = [os.path.join(BUILD, "aot_registry.inc"), os.path.join(BUILD, "embedded_src.inc")]

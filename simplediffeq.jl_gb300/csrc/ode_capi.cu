@@ -342,9 +342,9 @@ int nvrtc_cubin(const std::string& src, const std::vector<std::string>& extra_op
     return ODE_ENVRTC;
   }
   nvrtcProgram prog;
-  const char* hdrs[] = {kSrc_ode_solver_cuh, kSrc_ode_kparams_h, kSrc_tableaus_h, kSrc_sde_solver_cuh};
-  const char* names[] = {"ode_solver.cuh", "ode_kparams.h", "tableaus.h", "sde_solver.cuh"};
-  nvrtcResult r = g_nvrtc.create(&prog, src.c_str(), "gbode_jit.cu", 4, hdrs, names);
+  const char* hdrs[] = {kSrc_ode_solver_cuh, kSrc_ode_kparams_h, kSrc_tableaus_h, kSrc_sde_solver_cuh, kSrc_log_table_h};
+  const char* names[] = {"ode_solver.cuh", "ode_kparams.h", "tableaus.h", "sde_solver.cuh", "log_table.h"};
+  nvrtcResult r = g_nvrtc.create(&prog, src.c_str(), "gbode_jit.cu", 5, hdrs, names);
   if (r != NVRTC_SUCCESS) {
     *err = std::string("nvrtcCreateProgram: ") + g_nvrtc.errstr(r);
     return ODE_ENVRTC;

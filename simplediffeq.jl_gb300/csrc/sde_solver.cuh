@@ -30,6 +30,9 @@
 #pragma once
 #include "ode_solver.cuh"
 
+#define GBODE_LOGTAB_SPACE __device__ const
+#include "log_table.h"
+
 namespace gbode {
 
 struct SParams {
@@ -63,37 +66,32 @@ __device__ __forceinline__ U4 philox4x32_10(U4 c, unsigned k0, unsigned k1) {
   return c;
 }
 
-/* Natural logarithm of a positive normal double: x = m * 2^e with m in
- * [sqrt(1/2), sqrt(2)), log m = 2 atanh(s), s = (m - 1)/(m + 1), from the odd
- * series 2(s + s^3/3 + ... + s^23/23) (|s| <= 0.1716, truncation below 1e-19
- * relative), and e*ln 2 added in two parts (ln 2 = LN2_HI + LN2_LO, LN2_HI of
- * 42 significant bits so that e*LN2_HI is exact).  Every step is one IEEE
- * double operation. */
+/* Natural logarithm of a positive normal double, table-driven (P. T. P.
+ * Tang, ACM TOMS 16(4), 1990): x = 2^e m with m in [1, 2); the top 7 bits of
+ * m's fraction pick row j of log_table.h (gen_logtab.py), and
+ *   log x = e' ln 2 + T_j + log1p(r),  r = fma(m, 1/F_j, -1),  |r| < 2^-7,
+ * e' = e + 1 for j >= 53, whose T_j carries the -ln 2 (no cancellation of two
+ * terms of size ln 2 just below 1); log1p(r) = r + r^2 q(r) with q the Taylor
+ * coefficients -1/2, 1/3, ..., -1/8 (truncation below 2^-66), and e' ln 2 in
+ * two parts (LN2_HI of 42 significant bits, so e' LN2_HI is exact).  Every
+ * step is one IEEE double operation; no division. */
 __device__ __forceinline__ double log_dev(double x) {
-  long long b = __double_as_longlong(x);
-  int e = (int)((b >> 52) & 0x7ff) - 1023;
-  double m = __longlong_as_double((b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
-  if (m > 0x1.6a09e667f3bcdp+0) {  /* sqrt(2) */
-    m = m * 0.5;
-    e += 1;
-  }
-  const double s = (m - 1.0) / (m + 1.0);
-  const double z = s * s;
-  double q = 0x1.642c8590b2164p-5;     /* 1/23 */
-  q = __fma_rn(q, z, 0x1.8618618618618p-5);   /* 1/21 */
-  q = __fma_rn(q, z, 0x1.af286bca1af28p-5);   /* 1/19 */
-  q = __fma_rn(q, z, 0x1.e1e1e1e1e1e1ep-5);   /* 1/17 */
-  q = __fma_rn(q, z, 0x1.1111111111111p-4);   /* 1/15 */
-  q = __fma_rn(q, z, 0x1.3b13b13b13b14p-4);   /* 1/13 */
-  q = __fma_rn(q, z, 0x1.745d1745d1746p-4);   /* 1/11 */
-  q = __fma_rn(q, z, 0x1.c71c71c71c71cp-4);   /* 1/9 */
-  q = __fma_rn(q, z, 0x1.2492492492492p-3);   /* 1/7 */
-  q = __fma_rn(q, z, 0x1.999999999999ap-3);   /* 1/5 */
-  q = __fma_rn(q, z, 0x1.5555555555555p-2);   /* 1/3 */
-  const double t2 = s + s;
-  const double lm = __fma_rn(t2 * z, q, t2);
+  const long long b = __double_as_longlong(x);
+  const int j = (int)((b >> 45) & 127);
+  const int e = (int)((b >> 52) & 0x7ff) - 1023 + (j >= GBODE_LOGTAB_SHIFT_FROM ? 1 : 0);
+  const double m = __longlong_as_double((b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
+  const double inv = __ldg(&kLogTab[j][0]), thi = __ldg(&kLogTab[j][1]), tlo = __ldg(&kLogTab[j][2]);
+  const double r = __fma_rn(m, inv, -1.0);
+  double q = -0.125;
+  q = __fma_rn(q, r, 0x1.2492492492492p-3);   /* 1/7 */
+  q = __fma_rn(q, r, -0x1.5555555555555p-3);  /* -1/6 */
+  q = __fma_rn(q, r, 0x1.999999999999ap-3);   /* 1/5 */
+  q = __fma_rn(q, r, -0.25);
+  q = __fma_rn(q, r, 0x1.5555555555555p-2);   /* 1/3 */
+  q = __fma_rn(q, r, -0.5);
+  const double l1p = __fma_rn(r * r, q, r);
   const double de = (double)e;
-  return __fma_rn(de, 0x1.62e42fefa38p-1, __fma_rn(de, 0x1.ef35793c7673p-45, lm));
+  return __fma_rn(de, 0x1.62e42fefa38p-1, thi) + (__fma_rn(de, 0x1.ef35793c7673p-45, tlo) + l1p);
 }
 
 /* Normals z_{2P} and z_{2P+1} of trajectory idx's stream. */
