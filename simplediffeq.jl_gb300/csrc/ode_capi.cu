@@ -1238,8 +1238,12 @@ int solve_chunked(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_
     release();
     return cuda_fail(h, e, "chunked solve");
   }
+  /* from the first chunk's start to the latest end (a short last chunk can end before the one before it) */
   float span = 0.f;
-  cudaEventElapsedTime(&span, ev_start[0], ev_end[(size_t)nchunks - 1]);
+  for (int64_t c = 0; c < nchunks; ++c) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ev_start[0], ev_end[(size_t)c]) == cudaSuccess) span = std::max(span, ms);
+  }
   release();
   unsigned long long early = 0;
   for (int64_t c = 0; c < nchunks; ++c) {
