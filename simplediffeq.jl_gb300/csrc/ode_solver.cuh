@@ -480,14 +480,18 @@ struct MVern7 {
 #undef C7T
   }
 
+  enum { NX = 6 };  /* extra stages of the dense output */
+
+  /* The six extra stages of the dense output (they depend on the step, not
+   * on theta); dense = dense_stages + dense_eval, so that several save
+   * points of one step can share them. */
   template <class KK>
-  __device__ static __forceinline__ void dense(const F& f, const R (&uh)[D], const R (&uc)[D], T told, T tnew,
-                                               T dtold, T theta, const KK& k, double (&out)[D]) {
+  __device__ static __forceinline__ void dense_stages(const F& f, const R (&uh)[D], const R (&uc)[D], T told,
+                                                      T tnew, T dtold, const KK& k, R (&x)[NX][D]) {
 #define X7(x) CB<R>::v7x(vern7x_##x)
 #define X7T(x) CB<T>::v7x(vern7x_##x)
-#define R7(x) CB<R>::v7r(vern7r_##x)
     const R h = (R)dtold;
-    R x[6][D], s[D], tmp[D];
+    R s[D], tmp[D];
     lc(s, X7(a1101), k[0], X7(a1104), k[3], X7(a1105), k[4], X7(a1106), k[5], X7(a1107), k[6], X7(a1108), k[7],
        X7(a1109), k[8]);
     axpy(tmp, uh, h, s); f(tmp, stime(tnew, X7T(c11), dtold), x[0]);
@@ -506,7 +510,17 @@ struct MVern7 {
     lc(s, X7(a1601), k[0], X7(a1604), k[3], X7(a1605), k[4], X7(a1606), k[5], X7(a1607), k[6], X7(a1608), k[7],
        X7(a1609), k[8], X7(a1611), x[0], X7(a1612), x[1], X7(a1613), x[2]);
     axpy(tmp, uh, h, s); f(tmp, stime(tnew, X7T(c16), dtold), x[5]);
+#undef X7
+#undef X7T
+  }
 
+  /* The dense output at theta from the step's stages and extra stages. */
+  template <class KK, class XX>
+  __device__ static __forceinline__ void dense_eval(const R (&uh)[D], const R (&uc)[D], T dtold, T theta,
+                                                    const KK& k, const XX& x, double (&out)[D]) {
+#define R7(x) CB<R>::v7r(vern7r_##x)
+    const R h = (R)dtold;
+    R s[D];
     const R th = (R)theta;
     const R th2 = th * th;
     R b[13], ex;
@@ -522,9 +536,15 @@ struct MVern7 {
     lc(s, b[0], k[0], b[1], k[3], b[2], k[4], b[3], k[5], b[4], k[6], b[5], k[7], b[6], k[8], b[7], x[0],
        b[8], x[1], b[9], x[2], b[10], x[3], b[11], x[4], b[12], x[5]);
     finish_dense<PR, D>(uh, uc, h, s, out);
-#undef X7
-#undef X7T
 #undef R7
+  }
+
+  template <class KK>
+  __device__ static __forceinline__ void dense(const F& f, const R (&uh)[D], const R (&uc)[D], T told, T tnew,
+                                               T dtold, T theta, const KK& k, double (&out)[D]) {
+    R x[NX][D];
+    dense_stages(f, uh, uc, told, tnew, dtold, k, x);
+    dense_eval(uh, uc, dtold, theta, k, x, out);
   }
 };
 
@@ -603,12 +623,15 @@ struct MVern9Impl {
 #undef C9T
   }
 
+  enum { NX = 10 };  /* extra stages of the dense output */
+
+  /* The ten extra stages of the dense output (they depend on the step, not on
+   * theta); dense = dense_stages + dense_eval. */
   template <class KK>
-  __device__ static __forceinline__ void dense(const F& f, const R (&uh)[D], const R (&uc)[D], T told, T tnew,
-                                               T dtold, T theta, const KK& k, double (&out)[D]) {
+  __device__ static __forceinline__ void dense_stages(const F& f, const R (&uh)[D], const R (&uc)[D], T told,
+                                                      T tnew, T dtold, const KK& k, R (&x)[NX][D]) {
 #define X9(x) CB<R>::v9x(vern9x_##x)
 #define X9T(x) CB<T>::v9x(vern9x_##x)
-#define R9(x) CB<R>::v9r(vern9r_##x)
     /* K1..K9: the nine stages the dense formulas call k1..k9 */
     const auto& K1 = k[0];
     const auto& K2 = k[ADAPTIVE ? 7 : 1];
@@ -621,7 +644,7 @@ struct MVern9Impl {
     const auto& K9 = k[ADAPTIVE ? 14 : 8];
     const T tb = ADAPTIVE ? told : tnew;
     const R h = (R)dtold;
-    R x[10][D], s[D], tmp[D];
+    R s[D], tmp[D];
     lc(s, X9(a1701), K1, X9(a1708), K2, X9(a1709), K3, X9(a1710), K4, X9(a1711), K5, X9(a1712), K6, X9(a1713), K7,
        X9(a1714), K8, X9(a1715), K9);
     axpy(tmp, uh, h, s); f(tmp, stime(tb, X9T(c17), dtold), x[0]);
@@ -657,7 +680,26 @@ struct MVern9Impl {
        X9(a2614), K8, X9(a2615), K9, X9(a2617), x[0], X9(a2618), x[1], X9(a2619), x[2], X9(a2620), x[3],
        X9(a2621), x[4]);
     axpy(tmp, uh, h, s); f(tmp, stime(tb, X9T(c26), dtold), x[9]);
+#undef X9
+#undef X9T
+  }
 
+  /* The dense output at theta from the step's stages and extra stages. */
+  template <class KK, class XX>
+  __device__ static __forceinline__ void dense_eval(const R (&uh)[D], const R (&uc)[D], T dtold, T theta,
+                                                    const KK& k, const XX& x, double (&out)[D]) {
+#define R9(x) CB<R>::v9r(vern9r_##x)
+    const auto& K1 = k[0];
+    const auto& K2 = k[ADAPTIVE ? 7 : 1];
+    const auto& K3 = k[ADAPTIVE ? 8 : 2];
+    const auto& K4 = k[ADAPTIVE ? 9 : 3];
+    const auto& K5 = k[ADAPTIVE ? 10 : 4];
+    const auto& K6 = k[ADAPTIVE ? 11 : 5];
+    const auto& K7 = k[ADAPTIVE ? 12 : 6];
+    const auto& K8 = k[ADAPTIVE ? 13 : 7];
+    const auto& K9 = k[ADAPTIVE ? 14 : 8];
+    const R h = (R)dtold;
+    R s[D];
     const R th = (R)theta;
     const R th2 = th * th;
     R b[19], ex;
@@ -676,9 +718,15 @@ struct MVern9Impl {
        b[10], x[1], b[11], x[2], b[12], x[3], b[13], x[4], b[14], x[5], b[15], x[6], b[16], x[7], b[17], x[8],
        b[18], x[9]);
     finish_dense<PR, D>(uh, uc, h, s, out);
-#undef X9
-#undef X9T
 #undef R9
+  }
+
+  template <class KK>
+  __device__ static __forceinline__ void dense(const F& f, const R (&uh)[D], const R (&uc)[D], T told, T tnew,
+                                               T dtold, T theta, const KK& k, double (&out)[D]) {
+    R x[NX][D];
+    dense_stages(f, uh, uc, told, tnew, dtold, k, x);
+    dense_eval(uh, uc, dtold, theta, k, x, out);
   }
 };
 template <class PR, int D, class F> struct MAVern9 : MVern9Impl<PR, D, F, true> {};
@@ -1293,10 +1341,241 @@ __device__ __forceinline__ void run_adaptive_staged(const KParams& P) {
   flush_totals(P, tot);
 }
 
+/* ------------------------------------------------------------------ staged dense output, two queues */
+/* For the methods whose dense output first evaluates extra stages (Verner 7
+ * and 9, M::NX of them), those stages depend on the step and not on the save
+ * point, and a step often holds two or three save points.  This driver keeps
+ * two per-warp queues in shared memory: step records (what the extra stages
+ * and the interpolation read, and room for the extra stages) and save points
+ * (a record slot and a saveat index).  The warp computes the extra stages of
+ * 32 records at a time, one per lane, then interpolates 32 save points at a
+ * time from their records, so each step's extra stages are computed once
+ * however many save points it holds.  The operations and their operands are
+ * those of M::dense: results are bit-identical to the other drivers. */
+template <class M, class PR, int D, class F>
+struct StageLayout2 {
+  typedef typename PR::R R;
+  typedef typename PR::T T;
+  enum { KOFF = D * (PR::KAHAN ? 2 : 1), POFF = KOFF + M::NK * D, XOFF = POFF + F::NP, NREC = XOFF + M::NX * D };
+  /* bytes of a record (3 times, trajectory, point count, values) and of a point (record slot, saveat index) */
+  enum { REC = 3 * (int)sizeof(T) + 8 + 4 + NREC * (int)sizeof(R), PT = 8 };
+  /* room for twice as many points as records */
+  enum { CR = (kStageBytesPerWarp / (REC + 2 * PT)) & ~7, CP = 2 * CR };
+};
+
+template <class M, class PR, int D, class F>
+__device__ __forceinline__ void run_adaptive_staged2(const KParams& P) {
+  typedef typename PR::R R;
+  typedef typename PR::T T;
+  typedef StageLayout2<M, PR, D, F> SL;
+  enum { CR = SL::CR, CP = SL::CP, NK = M::NK, NX = M::NX, KOFF = SL::KOFF, POFF = SL::POFF, XOFF = SL::XOFF,
+         NREC = SL::NREC };
+  __shared__ __align__(16) unsigned char qmem[kWarpsPerBlock][kStageBytesPerWarp];
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  unsigned char* qb = qmem[threadIdx.x >> 5];
+  T* tv = (T*)qb;                                                      /* told, tnew, dtold: [3][CR] */
+  long long* iv = (long long*)(qb + 3 * CR * sizeof(T));               /* trajectory: [CR] */
+  R* rv = (R*)(qb + 3 * CR * sizeof(T) + 8 * CR);                      /* record values: [NREC][CR] */
+  int* nv = (int*)(qb + 3 * CR * sizeof(T) + 8 * CR + NREC * CR * sizeof(R)); /* save points of a record: [CR] */
+  int* pv = nv + CR;                                                   /* record slot, saveat index: [2][CP] */
+  /* warp-uniform queue state: records [rh, rh + rc), of which the first rs
+   * have their extra stages; points [ph, ph + pc), of which the first pr
+   * belong to such records; hd points of the head record done */
+  int rh = 0, rc = 0, rs = 0, ph = 0, pc = 0, pr = 0, hd = 0;
+
+  /* extra stages of the m oldest records without them, one per lane */
+  auto stage_round = [&](int m) {
+    __syncwarp();
+    int np = 0;
+    if (lane < m) {
+      const int slot = (rh + rs + lane) % CR;
+      R uh[D], uc[D];
+      F f2;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        uh[d] = rv[d * CR + slot];
+        uc[d] = PR::KAHAN ? rv[(D + d) * CR + slot] : (R)0;
+      }
+#pragma unroll
+      for (int q = 0; q < F::NP; ++q) f2.p[q] = rv[(POFF + q) * CR + slot];
+      const RingStages<R, D, CR> kk{rv + KOFF * CR + slot};
+      R x[NX][D];
+      M::dense_stages(f2, uh, uc, tv[slot], tv[CR + slot], tv[2 * CR + slot], kk, x);
+#pragma unroll
+      for (int q = 0; q < NX; ++q)
+#pragma unroll
+        for (int d = 0; d < D; ++d) rv[(XOFF + q * D + d) * CR + slot] = x[q][d];
+      np = nv[slot];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) np += __shfl_xor_sync(FULL, np, o);
+    __syncwarp();
+    rs += m;
+    pr += np;
+  };
+
+  /* interpolate the m oldest points (their records have the extra stages), one per lane */
+  auto point_round = [&](int m) {
+    __syncwarp();
+    if (lane < m) {
+      const int ps = (ph + lane) % CP;
+      int slot = pv[ps];
+      const int j = pv[CP + ps];
+      if (!GBODE_CHECK(P, slot >= 0 && slot < CR, CHK_RING)) slot = 0;
+      R uh[D], uc[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        uh[d] = rv[d * CR + slot];
+        uc[d] = PR::KAHAN ? rv[(D + d) * CR + slot] : (R)0;
+      }
+      const T told = tv[slot], dtold = tv[2 * CR + slot];
+      const T theta = ((T)P.saveat[j] - told) * recip(dtold);
+      const RingStages<R, D, CR> kk{rv + KOFF * CR + slot};
+      const RingStages<R, D, CR> xx{rv + XOFF * CR + slot};
+      double v[D];
+      M::dense_eval(uh, uc, dtold, theta, kk, xx, v);
+      store_point<PR, D>(P, iv[slot], j, v);
+    }
+    __syncwarp();
+    ph = (ph + m) % CP;
+    pc -= m;
+    pr -= m;
+    hd += m;
+    /* records whose points are all done leave the queue, oldest first */
+    while (rs > 0 && hd >= nv[rh]) {
+      hd -= nv[rh];
+      rh = (rh + 1) % CR;
+      --rc;
+      --rs;
+    }
+  };
+
+  Lane<PR, D, F, NK> l;
+  Totals tot = {0, 0, 0};
+  bool active = false, exhausted = false;
+  for (;;) {
+    const bool want = !active && !exhausted;
+    const unsigned need = __ballot_sync(FULL, want);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(P.counter, (unsigned long long)__popc(need));
+      base = __shfl_sync(FULL, base, leader);
+      if (want) {
+        const unsigned long long w = base + (unsigned long long)__popc(need & ((1u << lane) - 1u));
+        if (w < (unsigned long long)P.n) {
+          long long idx = P.order ? (long long)P.order[w] : (long long)w;
+          if (!GBODE_CHECK(P, idx >= 0 && idx < P.n, CHK_ORDER)) idx = 0;
+          active = !adaptive_start<M>(P, idx, l, tot);
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (!__any_sync(FULL, active)) {
+      if (!__any_sync(FULL, !exhausted)) break;
+      continue;
+    }
+    R nh[D], nc[D];
+    Accepted<T> st;
+    int r = TRY_REJECTED, njobs = 0;
+    if (active) {
+      r = adaptive_try<M>(P, l, tot, nh, nc, st);
+      if (r == TRY_STOPPED) active = false;
+      if (r == TRY_ACCEPTED)
+        while (l.cur + njobs < P.nsave && (T)P.saveat[l.cur + njobs] <= l.t) ++njobs;
+    }
+    /* a record per lane with save points, and its points: ranks over the warp */
+    const unsigned hb = __ballot_sync(FULL, njobs > 0);
+    const int nrec = __popc(hb), rrank = __popc(hb & ((1u << lane) - 1u));
+    int incl = njobs;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(FULL, incl, 31);
+    const int excl = incl - njobs;
+    if (nrec > 0) {
+      /* make room: extra stages for the records waiting for them, then every
+       * ready point, until this iteration's records and points fit */
+      while ((rc + nrec > CR || pc + total > CP) && rc > 0) {
+        if (rc - rs > 0) stage_round(rc - rs < 32 ? rc - rs : 32);
+        while (pr > 0) point_round(pr < 32 ? pr : 32);
+      }
+      if (total <= CP) {
+        if (njobs) {
+          const int slot = (rh + rc + rrank) % CR;
+          tv[slot] = st.told;
+          tv[CR + slot] = l.t;
+          tv[2 * CR + slot] = st.dtold;
+          iv[slot] = l.idx;
+          nv[slot] = njobs;
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            rv[d * CR + slot] = l.uh[d];
+            if (PR::KAHAN) rv[(D + d) * CR + slot] = l.uc[d];
+          }
+#pragma unroll
+          for (int k = 0; k < NK; ++k)
+#pragma unroll
+            for (int d = 0; d < D; ++d) rv[(KOFF + k * D + d) * CR + slot] = l.k[k][d];
+#pragma unroll
+          for (int k = 0; k < F::NP; ++k) rv[(POFF + k) * CR + slot] = l.f.p[k];
+          for (int q = 0; q < njobs; ++q) {
+            const int ps = (ph + pc + excl + q) % CP;
+            pv[ps] = slot;
+            pv[CP + ps] = l.cur + q;
+          }
+        }
+        rc += nrec;
+        pc += total;
+      } else if (njobs) {
+        /* more save points in one iteration than the point queue holds: interpolate here */
+        for (int q = 0; q < njobs; ++q) {
+          const long long j = l.cur + q;
+          const T theta = ((T)P.saveat[j] - st.told) * recip(st.dtold);
+          double v[D];
+          M::dense(l.f, l.uh, l.uc, st.told, l.t, st.dtold, theta, l.k, v);
+          store_point<PR, D>(P, l.idx, j, v);
+        }
+      }
+      if (njobs) {
+        l.cur += njobs;
+        l.ninterp += njobs;
+      }
+    }
+    (void)GBODE_CHECK(P, rc >= 0 && rc <= CR && pc >= 0 && pc <= CP && rs <= rc && pr <= pc, CHK_RING);
+    if (r == TRY_ACCEPTED) {
+      adaptive_commit<M>(l, nh, nc);
+      store_step<PR, D>(P, l, l.nacc);
+      if (!(l.t < (T)P.tf)) {
+        lane_finish(P, l, RET_DEFAULT, tot);
+        active = false;
+      }
+    }
+    while (rc - rs >= 32) stage_round(32);
+    while (pr >= 32) point_round(32);
+  }
+  while (rc - rs > 0) stage_round(rc - rs < 32 ? rc - rs : 32);
+  while (pr > 0) point_round(pr < 32 ? pr : 32);
+  flush_totals(P, tot);
+}
+
 /* Staged when a full round of jobs fits the ring, the unstaged persistent
  * driver otherwise (large states: Verner 9 with dim 4, Kuramoto-12). */
 template <class M, class PR, int D, class F>
 __device__ __forceinline__ void run_adaptive_staged_or_persistent(const KParams& P) {
+  if constexpr (M::DENSE_F) {
+    /* dense output with extra stages: the two-queue form shares them between a step's save points */
+    if constexpr (StageLayout2<M, PR, D, F>::CR >= 32) {
+      if (P.nsave > 0) {
+        run_adaptive_staged2<M, PR, D, F>(P);
+        return;
+      }
+    }
+  }
   if constexpr (StageLayout<M, PR, D, F>::CAP >= 32) {
     if (P.nsave > 0) {
       run_adaptive_staged<M, PR, D, F>(P);
