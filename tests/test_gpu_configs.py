@@ -372,3 +372,24 @@ def test_tuning_cache_round_trip(pkg, tmp_path):
     assert h2.tune_load(other) == L.ENOTSUP
     h1.close()
     h2.close()
+
+
+@pytest.mark.parametrize("nsave", [151, 401, 2001])
+def test_two_queue_staging_dense_saveat_bitexact(pkg, po, nsave):
+    """The Verner two-queue staged kernel when steps hold several save points
+    (about 62 steps per trajectory here): with 151 points (2.4 a step) the
+    point queue fills and the warp makes room with partial rounds; with 401
+    and 2001 points (6 and 32 a step) one iteration can bring more save points
+    than the queue holds and the lanes interpolate those in place.  Every
+    path gives the oracle's values."""
+    rng = np.random.default_rng(nsave)
+    n = 1024
+    mu = np.exp(rng.uniform(np.log(0.1), np.log(10), n))[None, :]
+    u0 = rng.uniform(-2, 2, (2, n))
+    sv = np.linspace(0, 20, nsave)
+    sol = gpu(pkg, pkg.GPUSimpleAVern7(), "vanderpol", u0, mu, (0.0, 20.0), 0.1, abstol=1e-5, reltol=1e-4,
+              saveat=sv, schedule="persistent")
+    ref = po.solve("AVern7", "vanderpol", u0, mu, (0, 20), 0.1, rounding="device", abstol=1e-5, reltol=1e-4,
+                   saveat=sv, nthreads=8)
+    assert_bitexact(sol, ref)
+    assert sol.stats.saves == n * nsave
