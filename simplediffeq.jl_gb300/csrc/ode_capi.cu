@@ -281,6 +281,45 @@ int stage_job_bytes(const ode_solve_args* a) {
   return 3 * t + 8 + nrec * r + 4;
 }
 
+/* Bytes per step record of the two-queue staged kernel of the Verner methods,
+ * with room for two save points: the host-side copy of StageLayout2<...>::REC
+ * + 2 * PT in ode_solver.cuh (3 times, trajectory, point count, state, stage
+ * values, parameters and the extra dense-output stages; 8 bytes a point).
+ * 0 for the methods without extra dense-output stages. */
+int stage_record_bytes(const ode_solve_args* a) {
+  const int nx = a->alg == ODE_ALG_AVERN9 ? 10 : a->alg == ODE_ALG_AVERN7 ? 6 : 0;
+  if (!nx) return 0;
+  const int nk = a->alg == ODE_ALG_AVERN9 ? 16 : 10;
+  const int r = a->precision == ODE_FP64 ? 8 : 4, t = a->precision == ODE_FP32 ? 4 : 8;
+  const int nrec = a->dim * (a->precision == ODE_FP32_KAHAN ? 2 : 1) + nk * a->dim + a->nparams + nx * a->dim;
+  return 3 * t + 8 + 4 + nrec * r + 2 * 8;
+}
+
+/* Bytes a ring spends per queued unit: a step record for the Verner methods,
+ * a save-point job otherwise. */
+int stage_unit_bytes(const ode_solve_args* a) {
+  const int rec = stage_record_bytes(a);
+  return rec ? rec : stage_job_bytes(a);
+}
+
+/* Launch shape of an untuned run-time compiled kernel: 128 threads and 12 KB
+ * staging rings, unless those rings cannot hold a round of 32 (a staged kernel
+ * with large records): then one-warp blocks with the smallest ring that can,
+ * up to 48 KB (measured on AVern9, restricted three-body problem, 65,536
+ * trajectories, 100 save points: 161.7 ms unstaged, 116.4 ms staged in
+ * one-warp blocks with 29 KB rings, 121.3 with 36 KB, 128.8 with 48 KB). */
+void default_shape(const ode_solve_args* a, int sched, int* block, int* stage) {
+  *block = 128;
+  *stage = 12288;
+  if (std::strcmp(entry_kind(a->alg, sched, a->nsave), "staged") != 0) return;
+  const int unit = stage_unit_bytes(a);
+  if (((12288 / unit) & ~7) >= 32) return;
+  const int fit = (32 * unit + 511) / 512 * 512;
+  if (fit > 49152) return;  /* no ring holds a round: the kernel runs unstaged */
+  *block = 32;
+  *stage = fit;
+}
+
 /* values stored per saveat point and trajectory */
 int output_width(ode_handle* h, const ode_solve_args* a) {
   if (a->output == ODE_OUTPUT_KURAMOTO_R) return 1;
@@ -386,11 +425,14 @@ int load_cubin(ode_handle* h, const std::vector<char>& cubin, int block, int sta
 int compile_jit(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn, std::string* log_out) {
   std::vector<char> cubin;
   std::string err;
-  std::vector<std::string> opts;
+  int block = 128, stage = 12288;
+  default_shape(a, sched, &block, &stage);
+  std::vector<std::string> opts = {"-DGBODE_BLOCK=" + std::to_string(block),
+                                   "-DGBODE_STAGE_BYTES=" + std::to_string(stage)};
   if (h->bounds_check) opts.push_back("-DGBODE_BOUNDS_CHECK");
   const int rc = nvrtc_cubin(jit_source(h, a, sched), opts, &cubin, log_out, &err);
   if (rc != ODE_OK) return fail(h, rc, err);
-  return load_cubin(h, cubin, 128, 12288, fn);
+  return load_cubin(h, cubin, block, stage, fn);
 }
 
 /* Find (or build) the kernel for this solve. */
@@ -1478,7 +1520,7 @@ int ode_autotune(ode_handle* h, const ode_solve_args* a, int64_t sample, ode_tun
     int block, regs, stage;
   };
   const bool staged = std::strcmp(entry_kind(ta.alg, ta.schedule, ta.nsave), "staged") == 0;
-  const int job = stage_job_bytes(&ta);
+  const int job = stage_unit_bytes(&ta);
   std::vector<Variant> vars;
   /* large jobs (Kuramoto-12: 804 bytes) also try the smallest ring that holds
    * one round, which leaves room for the most warps per SM */
