@@ -244,7 +244,7 @@ int check_rhs(ode_handle* h, const ode_solve_args* a) {
   return fail(h, ODE_EINVAL, "unknown right-hand side id");
 }
 
-std::string rhs_type_expr(ode_handle* h, const ode_solve_args* a) {
+std::string rhs_type_expr(ode_handle* /*h*/, const ode_solve_args* a) {
   const char *R, *T;
   rt_types(a->precision, &R, &T);
   char b[256];
