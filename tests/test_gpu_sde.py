@@ -133,3 +133,14 @@ def test_non_diagonal_argument_checks(pkg):
     assert h.sde_solve(a, o) == L.EINVAL
     a.sde, a.nparams, a.noise_dim = L.SDE["gbm"], 2, 2  # a diagonal built-in takes no noise matrix
     assert h.sde_solve(a, o) == L.EINVAL
+
+
+def test_readme_non_diagonal_example(pkg):
+    """The README's SimpleEM example (the reference test's non-diagonal SDE)."""
+    c = [0.3, 0.6, 0.9, 0.12, 1.2, 0.2, 0.3, 1.8]
+    n = 5000
+    sde = pkg.SDEProblem("mult", [1.0, 1.0], (0.0, 1.0), [1.01] + c, noise_rate_prototype=np.zeros((2, 4)))
+    ens = pkg.EnsembleProblem(sde, u0s=np.ones((2, n)), ps=np.tile(np.array([1.01] + c)[:, None], (1, n)))
+    paths = pkg.solve(ens, pkg.SimpleEM(), trajectories=n, dt=0.01, seed=1)
+    assert paths.us.shape == (101, 2, n)
+    assert np.all(np.isfinite(paths.us)) and np.array_equal(paths.us[0], np.ones((2, n)))
