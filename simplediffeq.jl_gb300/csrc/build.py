@@ -50,6 +50,7 @@ GROUPS = {
     # the ensemble workloads: fixed Tsit5 / adaptive ATsit5 on Lorenz, AVern7 on
     # Van der Pol, AVern9 on the restricted three-body problem, ATsit5 on Kuramoto-12
     "lorenz": [("tsit5", "fixed", "lorenz", 3, "fp64"),
+               ("tsit5", "fixedsplit", "lorenz", 3, "fp64"),
                ("atsit5", "plain", "lorenz", 3, "fp64"),
                ("atsit5", "persistent", "lorenz", 3, "fp64")],
     "lorenz_staged": [("atsit5", "staged", "lorenz", 3, "fp64")],

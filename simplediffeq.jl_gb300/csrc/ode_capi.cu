@@ -269,6 +269,25 @@ const char* entry_kind(int alg, int sched, int64_t nsave) {
   return nsave > 0 ? "staged" : "persistent";
 }
 
+/* Fixed-step Tsit5 on an ensemble of fewer warps than half the GPU's SM
+ * sub-partitions (FP64, final states or every-step output, state output):
+ * the kernel that spreads a trajectory's components over the warps of a
+ * block (run_fixed_split), one block of 32 * dim threads per 32 trajectories.
+ * Only for right-hand sides whose components are separate expressions (each
+ * warp computes its own); one with shared work, like Kuramoto's sums of
+ * sines, would repeat that work in every warp. */
+bool use_fixed_split(const ode_handle* h, const ode_solve_args* a) {
+  const bool separable = a->rhs == ODE_RHS_LORENZ || a->rhs == ODE_RHS_VANDERPOL || a->rhs == ODE_RHS_LINEAR;
+  return a->alg == ODE_ALG_TSIT5 && separable && a->nsave == 0 && a->output == ODE_OUTPUT_STATE &&
+         a->precision == ODE_FP64 && !h->bounds_check && a->dim >= 2 && a->dim <= 8 &&
+         (a->n + 31) / 32 <= (int64_t)h->nsm * 2;
+}
+
+/* entry_kind, with the component-split fixed-step kernel where it applies */
+const char* kernel_kind(const ode_handle* h, const ode_solve_args* a, int sched) {
+  return use_fixed_split(h, a) ? "fixedsplit" : entry_kind(a->alg, sched, a->nsave);
+}
+
 /* Bytes of one saveat job in the staged kernel's ring: the host-side copy of
  * StageLayout<M, PR, D, F>::JOB in ode_solver.cuh (3 times of type T, the
  * trajectory index, the saveat index, and D (x2 with Kahan) state values,
@@ -329,7 +348,7 @@ int output_width(ode_handle* h, const ode_solve_args* a) {
 
 std::string kernel_key(ode_handle* h, const ode_solve_args* a, int sched) {
   char b[160];
-  snprintf(b, sizeof b, "%s|%s|%d|%d|%s|%d%s", alg_name(a->alg), entry_kind(a->alg, sched, a->nsave), a->rhs, a->dim,
+  snprintf(b, sizeof b, "%s|%s|%d|%d|%s|%d%s", alg_name(a->alg), kernel_kind(h, a, sched), a->rhs, a->dim,
            prec_name(a->precision), a->output >= ODE_OUTPUT_USER ? a->output : 0, h->bounds_check ? "|chk" : "");
   return b;
 }
@@ -367,7 +386,7 @@ std::string jit_source(ode_handle* h, const ode_solve_args* a, int sched) {
            "    user_rhs<R>(du, u, p, (R)t);\n  }\n};\n";
   }
   src += "typedef " + rhs_type_expr(h, a) + " RHS_T;\n";
-  src += std::string("GBODE_ENTRY(gbode_jit, ") + entry_kind(a->alg, sched, a->nsave) + ", " + method_type(a->alg) +
+  src += std::string("GBODE_ENTRY(gbode_jit, ") + kernel_kind(h, a, sched) + ", " + method_type(a->alg) +
          ", " + prec_type(a->precision) + ", RHS_T)\n";
   return src;
 }
@@ -466,7 +485,7 @@ int get_kernel(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn
     *jit = h->kjit[key];
     return ODE_OK;
   }
-  const char* kind = entry_kind(a->alg, sched, a->nsave);
+  const char* kind = kernel_kind(h, a, sched);
   for (const AotEntry& e : kAotEntries) {
     if (!h->bounds_check && a->output < ODE_OUTPUT_USER && e.alg == a->alg && e.rhs == a->rhs && e.dim == a->dim &&
         e.precision == a->precision && std::strcmp(e.kind, kind) == 0) {
@@ -948,7 +967,10 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
   int launches = 0;
   unsigned gridx;
   int block = block_of(h, fn);
-  if (sched == ODE_SCHED_PLAIN) {
+  if (use_fixed_split(h, a)) {
+    block = 32 * D;  /* D warps per 32 trajectories */
+    gridx = (unsigned)((n + 31) / 32);
+  } else if (sched == ODE_SCHED_PLAIN) {
     block = plain_block(n, h->nsm, block);
     gridx = (unsigned)((n + block - 1) / block);
   } else {

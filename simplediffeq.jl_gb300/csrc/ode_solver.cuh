@@ -1585,6 +1585,136 @@ __device__ __forceinline__ void run_adaptive_staged_or_persistent(const KParams&
   run_adaptive_persistent<M, PR, D, F>(P);
 }
 
+/* ------------------------------------------------------------------ fixed-step Tsit5, components over warps */
+/* Small fixed-step ensembles.  Every SM sub-partition issues one FP64 warp
+ * instruction per 64 cycles whatever the number of active lanes, so an
+ * ensemble of fewer warps than the GPU has sub-partitions leaves most of them
+ * idle (8,192 trajectories are 256 warps for 608 sub-partitions).  Here a
+ * block of D warps solves 32 trajectories: lane l of warp c holds component c
+ * of trajectory 32 * blockIdx.x + l and computes that component's stage
+ * combinations and right-hand side; the stage inputs are exchanged through
+ * shared memory (double-buffered, one barrier per exchange).  The right-hand
+ * side functor is inlined with the component fixed at compile time, so the
+ * other components' arithmetic is dead code.  Per component these are the
+ * operations of MTsit5::attempt (without the error estimate) and run_fixed,
+ * in the same order: results are bit-identical.  Final states and
+ * save_everystep output only (no saveat dense output). */
+template <class PR, int D, class F>
+struct FixedSplitTsit5 {
+  typedef typename PR::R R;
+  typedef typename PR::T T;
+
+  /* all D components of the stage input of the 32 trajectories: each warp
+   * writes its own, then reads all of them.  The warps run different
+   * instantiations of run<C>, so they meet at the barrier from different
+   * instructions: the non-aligned barrier.sync over the block's 32 * D
+   * threads (every lane of every warp arrives, the same number of times). */
+  __device__ static __forceinline__ void exchange(R (*xb)[D][32], int& b, int c, int lane, R mine, R (&full)[D]) {
+    xb[b][c][lane] = mine;
+    asm volatile("barrier.sync 1, %0;" ::"r"(32 * D) : "memory");
+#pragma unroll
+    for (int d = 0; d < D; ++d) full[d] = xb[b][d][lane];
+    b ^= 1;
+  }
+
+  template <int C>
+  __device__ static __forceinline__ R rhs(const F& f, const R (&u)[D], T t) {
+    R du[D];
+    f(u, t, du);
+    return du[C];
+  }
+
+  template <int C>
+  __device__ static __forceinline__ void run(const KParams& P, R (*xb)[D][32]) {
+#define C5(x) CB<R>::t5(tsit5_##x)
+#define C5T(x) CB<T>::t5(tsit5_##x)
+    const int lane = threadIdx.x & 31;
+    const long long i = (long long)blockIdx.x * 32 + lane;
+    const bool valid = i < P.n;
+    const long long idx = valid ? i : 0;  /* lanes past n compute on trajectory 0 and store nothing */
+    F f;
+#pragma unroll
+    for (int j = 0; j < F::NP; ++j) f.p[j] = (R)P.p[(long long)j * P.n + idx];
+    R uh[1] = {(R)P.u0[(long long)C * P.n + idx]}, uc[1] = {(R)0};
+    T t = (T)P.t0;
+    const T dt = (T)P.dt;
+    const bool every = P.nsave == 0 && P.save_everystep && P.us;
+    auto value = [&]() { return PR::KAHAN ? (double)uh[0] - (double)uc[0] : (double)uh[0]; };
+    if (every && valid) P.us[(long long)C * P.n + i] = value();
+    int b = 0;
+    R full[D], k[7][1];
+    exchange(xb, b, C, lane, uh[0], full);
+    k[0][0] = rhs<C>(f, full, t);
+    const R h0 = (R)dt;
+    for (long long g = 1; g < P.ngrid; ++g) {
+      t = (T)P.grid[g - 1];
+      const R h = h0;
+      const R a = (R)(dt * C5T(a21));
+      R tmp[1], sv[1], nh[1], nc[1];
+      tmp[0] = fmaR(a, k[0][0], uh[0]);
+      exchange(xb, b, C, lane, tmp[0], full);
+      k[1][0] = rhs<C>(f, full, stime(t, C5T(c1), dt));
+      lc(sv, C5(a31), k[0], C5(a32), k[1]);
+      axpy(tmp, uh, h, sv);
+      exchange(xb, b, C, lane, tmp[0], full);
+      k[2][0] = rhs<C>(f, full, stime(t, C5T(c2), dt));
+      lc(sv, C5(a41), k[0], C5(a42), k[1], C5(a43), k[2]);
+      axpy(tmp, uh, h, sv);
+      exchange(xb, b, C, lane, tmp[0], full);
+      k[3][0] = rhs<C>(f, full, stime(t, C5T(c3), dt));
+      lc(sv, C5(a51), k[0], C5(a52), k[1], C5(a53), k[2], C5(a54), k[3]);
+      axpy(tmp, uh, h, sv);
+      exchange(xb, b, C, lane, tmp[0], full);
+      k[4][0] = rhs<C>(f, full, stime(t, C5T(c4), dt));
+      lc(sv, C5(a61), k[0], C5(a62), k[1], C5(a63), k[2], C5(a64), k[3], C5(a65), k[4]);
+      axpy(tmp, uh, h, sv);
+      exchange(xb, b, C, lane, tmp[0], full);
+      k[5][0] = rhs<C>(f, full, t + dt);
+      lc(sv, C5(a71), k[0], C5(a72), k[1], C5(a73), k[2], C5(a74), k[3], C5(a75), k[4], C5(a76), k[5]);
+      state_update<PR, 1>(uh, uc, h, sv, nh, nc);
+      exchange(xb, b, C, lane, nh[0], full);
+      k[6][0] = rhs<C>(f, full, t + dt);
+      t = t + dt;
+      uh[0] = nh[0];
+      uc[0] = nc[0];
+      if (every && valid) P.us[(g * D + C) * P.n + i] = value();
+      k[0][0] = k[6][0];
+    }
+#undef C5
+#undef C5T
+    const int nacc = P.ngrid > 0 ? (int)(P.ngrid - 1) : 0;
+    if (valid && P.u_final) P.u_final[(long long)C * P.n + i] = value();
+    if (C == 0) {
+      Totals tot = {0, 0, 0};
+      if (valid) {
+        if (P.t_final) P.t_final[i] = (double)t;
+        if (P.retcode) P.retcode[i] = (signed char)RET_DEFAULT;
+        if (P.naccept) P.naccept[i] = nacc;
+        if (P.nreject) P.nreject[i] = 0;
+        if (P.dt_first) P.dt_first[i] = nacc > 0 ? (double)dt : __longlong_as_double(0x7ff8000000000000LL);
+        tot.att = (unsigned long long)nacc;
+      }
+      flush_totals(P, tot);
+    }
+  }
+
+  /* the warp's component as a compile-time constant */
+  template <int C>
+  __device__ static __forceinline__ void dispatch(const KParams& P, R (*xb)[D][32], int w) {
+    if constexpr (C < D) {
+      if (w == C) run<C>(P, xb);
+      else dispatch<C + 1>(P, xb, w);
+    }
+  }
+};
+
+template <class PR, int D, class F>
+__device__ __forceinline__ void run_fixed_split(const KParams& P) {
+  typedef typename PR::R R;
+  __shared__ R xb[2][D][32];
+  FixedSplitTsit5<PR, D, F>::template dispatch<0>(P, xb, (int)(threadIdx.x >> 5));
+}
+
 /* Fixed-step methods: thread i, the grid of Julia's t0:dt:tf shared by all. */
 template <class M, class PR, int D, class F>
 __device__ __forceinline__ void run_fixed(const KParams& P) {
@@ -1700,6 +1830,11 @@ __device__ __forceinline__ void run_onestep(const KParams& P) {
 #define GBODE_ENTRY_fixed(NAME, M, PR, RHS)                                                  \
   extern "C" __global__ void __launch_bounds__(GBODE_BLOCK) NAME(gbode::KParams P) {                \
     gbode::run_fixed<M<PR, RHS::D, RHS>, PR, RHS::D, RHS>(P);                               \
+  }
+/* fixed-step Tsit5 with a trajectory's components over the warps of a block (32 * D threads) */
+#define GBODE_ENTRY_fixedsplit(NAME, M, PR, RHS)                                             \
+  extern "C" __global__ void __launch_bounds__(32 * RHS::D) NAME(gbode::KParams P) {              \
+    gbode::run_fixed_split<PR, RHS::D, RHS>(P);                                             \
   }
 #define GBODE_ENTRY_onestep(NAME, M, PR, RHS)                                                \
   extern "C" __global__ void __launch_bounds__(GBODE_BLOCK) NAME(gbode::KParams P) {                \

@@ -204,3 +204,27 @@ def test_nan_state_finishes_like_the_reference(pkg, po):
     assert (sol.retcode[:5] == 3).all() and (sol.retcode[5:] == 0).all()
     assert (sol.t_final[:5] == 1.0).all() and np.isnan(sol.u_final[:, :5]).all()
     assert_bitexact(sol, ref)
+
+
+@pytest.mark.parametrize("rhs,dim,n", [("lorenz", 3, 1000), ("vanderpol", 2, 4001), ("linear", 5, 777),
+                                       ("lorenz", 3, 40000)])
+def test_tsit5_fixed_component_split_bitexact(pkg, po, rhs, dim, n):
+    """Fixed-step Tsit5 on small FP64 ensembles runs with a trajectory's
+    components over the warps of a block (up to 304 warps' worth of
+    trajectories; 40,000 takes the one-thread-per-trajectory kernel): every
+    grid point of every trajectory equals the oracle, including ensembles
+    that do not fill their last block."""
+    rng = np.random.default_rng(dim * 1000 + n)
+    if rhs == "lorenz":
+        u0 = rng.uniform(-1, 1, (3, n)) + np.array([[0], [0], [20]])
+        p = np.stack([np.full(n, 10.0), rng.uniform(0, 28, n), np.full(n, 8 / 3)])
+    elif rhs == "vanderpol":
+        u0 = rng.uniform(-2, 2, (2, n))
+        p = np.exp(rng.uniform(np.log(0.1), np.log(3), n))[None, :]
+    else:
+        u0 = rng.uniform(-1, 1, (dim, n))
+        p = rng.normal(0, 0.5, (dim * dim, n))
+    sol = gpu(pkg, pkg.GPUSimpleTsit5(), rhs, u0, p, (0.0, 1.0), 0.01, save_everystep=True)
+    ref = po.solve("Tsit5", rhs, u0, p, (0, 1), 0.01, rounding="device", save_everystep=True, nthreads=8)
+    assert sol.us.shape == (101, dim, n)
+    assert_bitexact(sol, ref)
