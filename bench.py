@@ -18,8 +18,14 @@ roofline   FP64 pipe: algorithmic FLOPs per launch (263 per step attempt, 101 pe
            saveat point) over the kernel's event time, against the FP64 FMA
            peak this run measures with the probe library;
 cpu_baseline  the oracle's SimpleATsit5 (CPU restatement, reference rounding)
-           on all host cores over a bounded sample of the same workload.
-With --impl reference only the CPU restatement runs (rank 0).
+           on all host cores over a bounded sample of the same workload;
+persistent_unsorted  the learned schedule's kernel in identity order (what
+           the trained network's ordering adds), amortized  the learned
+           schedule's one-off cost (training solve + fit) against plain;
+parity_vs_ref  the GPU's results on the first 4,096 trajectories against the
+           oracle in the reference's rounding.
+With --impl reference only the CPU restatement runs (rank 0), over the whole
+1,048,576-trajectory workload every step.
 
 --config N measures another ensemble workload of the same solver family
 (1: fixed-step Tsit5; 3: AVern7 Van der Pol; 4: AVern9 restricted three-body
@@ -229,20 +235,15 @@ def cpu_baseline(cfg, seconds=CPU_SECONDS, threads=None):
 
 
 def run_reference(args, rank):
+    """The CPU restatement of SimpleATsit5 (reference rounding) on every host
+    core, over the whole workload each step (all 1,048,576 trajectories)."""
     if rank != 0:
         return
     import __graft_entry__ as g
     po = g.oracle()
     threads = os.cpu_count()
-    u0_all, p_all = inputs(N_TRAJ)
+    u0, p = inputs(N_TRAJ)
     sv = np.linspace(*TSPAN, NSAVE)
-
-    def solve_first(m):
-        po.solve("SimpleATsit5", "lorenz", np.ascontiguousarray(u0_all[:, :m]), np.ascontiguousarray(p_all[:, :m]),
-                 TSPAN, DT0, rounding="ref", abstol=ABSTOL, reltol=RELTOL, saveat=sv, nthreads=threads)
-    # each step: about 2 s of CPU work (the first trajectories of the workload)
-    _, _, n_sample = sized_sample(solve_first, N_TRAJ, 2.0)
-    u0, p = np.ascontiguousarray(u0_all[:, :n_sample]), np.ascontiguousarray(p_all[:, :n_sample])
 
     def run():
         po.solve("SimpleATsit5", "lorenz", u0, p, TSPAN, DT0, rounding="ref", abstol=ABSTOL, reltol=RELTOL,
@@ -253,17 +254,63 @@ def run_reference(args, rank):
     for _ in range(args.steps):
         run()
     el = time.perf_counter() - t
-    v = n_sample * args.steps / el
+    v = N_TRAJ * args.steps / el
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_trajectories": n_sample},
+        "config": {"workload": WORKLOAD, "trajectories_per_step": N_TRAJ},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "first %d trajectories per step; Julia SimpleDiffEq.jl cannot run on this box, "
-                                   "the C++ restatement of SimpleATsit5 stands in" % n_sample},
+                         "sample": "all %d trajectories of the workload per step; Julia SimpleDiffEq.jl cannot run "
+                                   "on this box, the C++ restatement of SimpleATsit5 stands in" % N_TRAJ},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
+
+
+def parity_vs_ref(cfg, u0, p, sv, res, m=4096):
+    """The GPU's results on the first m trajectories against the oracle's
+    restatement of the reference's own rounding (unfused SVector arithmetic,
+    libm pow): fraction of final states and of saveat series within 10x the
+    error scale abstol + reltol*max|u| of each trajectory, the largest
+    deviation in that unit, and the accepted-step count differences.  Fixed
+    step: the largest normwise relative deviation of the final state."""
+    import __graft_entry__ as g
+    po = g.oracle()
+    m = min(m, u0.shape[1])
+    ref = po.solve(cfg["alg"], cfg["rhs"], np.ascontiguousarray(u0[:, :m]), np.ascontiguousarray(p[:, :m]),
+                   cfg["tspan"], cfg["dt"], rounding="ref", abstol=cfg["abstol"], reltol=cfg["reltol"], saveat=sv,
+                   nthreads=os.cpu_count(), output=cfg["output"])
+    uf = res["u_final"][:, :m]
+    if cfg["alg"] in ("Tsit5", "Vern7", "Vern9", "RK4"):
+        rel = np.abs(uf - ref["u_final"]).max(0) / np.maximum(np.abs(ref["u_final"]).max(0), 1e-300)
+        return {"trajectories": m, "max_rel_err_final": float(rel.max()), "bar": "1e-12 relative"}
+    scale = cfg["abstol"] + cfg["reltol"] * np.abs(ref["u_final"]).max(0)
+    e = np.abs(uf - ref["u_final"]).max(0) / scale
+    dn = np.abs(res["naccept"][:m].astype(np.int64) - ref["naccept"])
+    out = {"trajectories": m, "final_frac_within_10x": float(np.mean(e <= 10)), "final_max_in_error_scale": float(e.max()),
+           "naccept_max_abs_diff": int(dn.max()), "naccept_frac_within_1": float(np.mean(dn <= 1)),
+           "error_scale": "abstol + reltol*max|u_final| per trajectory (saveat: max|us|)"}
+    if sv is not None and res.get("us") is not None:
+        us = res["us"][:, :, :m]
+        us_scale = cfg["abstol"] + cfg["reltol"] * np.nanmax(np.abs(ref["us"]), axis=(0, 1))
+        eu = np.nanmax(np.abs(us - ref["us"]), axis=(0, 1)) / us_scale
+        out.update(saveat_frac_within_10x=float(np.mean(eu <= 10)), saveat_max_in_error_scale=float(eu.max()))
+    return out
+
+
+def probe_rates(device=0, iters=2000):
+    """Measured lane-operation rates of the arithmetic pipes (bench_probe.cu,
+    built by __graft_entry__.build() into _build/libbench_probe.so)."""
+    import ctypes
+    lib = ctypes.CDLL(os.path.join(ROOT, "_build", "libbench_probe.so"))
+    lib.probe_op_rates.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+    r = np.zeros(8)
+    ms = np.zeros(8)
+    rc = lib.probe_op_rates(int(device), int(iters), r.ctypes.data, ms.ctypes.data, 8)
+    if rc != 0:
+        raise RuntimeError("probe failed (%d)" % rc)
+    names = ["dfma", "dadd", "ffma", "cvt_f64_f32_f64", "ddiv", "dsqrt_add", "dmax_add", "fdiv"]
+    return {k: (float(r[i]), float(ms[i])) for i, k in enumerate(names)}
 
 
 def load_traffic():
@@ -360,7 +407,7 @@ def run_sde(args, cfg, rank, world, local):
         if dist:
             dist.destroy_process_group()
         return
-    rates = L.probe_rates(local, 2000)
+    rates = probe_rates(local, 2000)
     peak = rates["dfma"][0] * 2 / 1e12
     achieved = n * nsteps * cfg["flops_step"] / (step_ms * 1e-3) / 1e12
     line = {
@@ -374,7 +421,7 @@ def run_sde(args, cfg, rank, world, local):
         "trajectory_steps_per_s": n * world * nsteps / (step_ms * 1e-3),
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                      "traffic": None,
-                     "peak_source": "FP64 FMA lane rate measured by this run's probe (libgb300ode_probe.so)"},
+                     "peak_source": "FP64 FMA lane rate measured by this run's probe (bench_probe.cu)"},
         "e2e": {"value": n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": u0.nbytes + p.nbytes,
                 "d2h_bytes_per_step": huf.numel() * 8},
         "gpu_launches": launches,
@@ -452,9 +499,10 @@ def main():
         outs["us"] = torch.empty((nsave, width, n), dtype=torch.float64, device=dev)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
 
-    def args_for(schedule, memory, u0p, pp, uu=u0, ppp=p):
+    def args_for(schedule, memory, u0p, pp, uu=u0, ppp=p, controller="fp32"):
         a = pkg.make_args(alg, L.RHS[cfg["rhs"]], uu, ppp, cfg["tspan"], cfg["dt"], cfg["abstol"], cfg["reltol"],
-                          sv, False, cfg["precision"], schedule, 0, memory=memory, output=cfg["output"])
+                          sv, False, cfg["precision"], schedule, 0, memory=memory, output=cfg["output"],
+                          controller=controller)
         a.u0, a.p = u0p, pp
         return a
 
@@ -474,7 +522,8 @@ def main():
         try:
             rep = h.learn_fit(ta)
             fit_report = {"loss_first": rep.loss_first, "loss_last": rep.loss_last, "r2_log_attempts": rep.r2_attempts,
-                          "train_solve_ms": rep.train_solve_ms, "train_fit_ms": rep.train_fit_ms}
+                          "train_solve_ms": rep.train_solve_ms, "train_fit_ms": rep.train_fit_ms,
+                          "train_kernel_ms": rep.train_kernel_ms, "train_cluster_ctas": rep.train_ctas}
         except L.GB300ODEError as e:
             fit_report = {"unavailable": str(e)}
             schedule = "persistent"
@@ -493,15 +542,15 @@ def main():
         except L.GB300ODEError as e:
             tune = {"unavailable": str(e)}
 
-    def device_step(sched):
-        a = args_for(sched, L.MEM_DEVICE, du0.data_ptr(), dp.data_ptr())
+    def device_step(sched, controller="fp32"):
+        a = args_for(sched, L.MEM_DEVICE, du0.data_ptr(), dp.data_ptr(), controller=controller)
         st = L.SolveStats()
         h.check(h.solve_raw(a, out_dev(), st), allow=(L.ETRAJ,))
         return st
 
-    def timed(sched, steps, warmup):
+    def timed(sched, steps, warmup, controller="fp32"):
         for _ in range(warmup):
-            device_step(sched)
+            device_step(sched, controller)
         kms, att, sav, launches = [], 0, 0, 0
         if dist:
             dist.barrier()
@@ -509,7 +558,7 @@ def main():
         for _ in range(steps):
             flush.zero_()
             torch.cuda.synchronize()
-            st = device_step(sched)
+            st = device_step(sched, controller)
             kms.append(st.kernel_ms)
             att, sav, launches = att + st.attempts, sav + st.saves, launches + st.launches
         torch.cuda.synchronize()
@@ -522,7 +571,16 @@ def main():
     clocks = clk.summary()
     step_ms = max_over_ranks(sum(kms) / len(kms), dist, dev)
     uf_measured = outs["u_final"].cpu().numpy()
+    m_par = min(n, 4096)
+    res_sample = {"u_final": uf_measured[:, :m_par], "naccept": outs["naccept"][:m_par].cpu().numpy(),
+                  "us": outs["us"][:, :, :m_par].cpu().numpy() if nsave else None}
     value = n * world / (step_ms * 1e-3)
+
+    # the same persistent staged kernel in identity order: what the trained network's ordering adds
+    unsorted_ms = None
+    if schedule == "learned":
+        uk, _, _, _ = timed("persistent", max(1, min(args.steps, 3)), 1)
+        unsorted_ms = sum(uk) / len(uk)
 
     # plain one-thread-per-trajectory kernel on the same inputs, same timing rules
     if schedule != "plain":
@@ -531,6 +589,17 @@ def main():
     else:
         plain_ms = step_ms
     uf_plain = outs["u_final"].cpu().numpy()
+
+    # the same schedule with the FP64 step-size controller (kernel compiled at run time, untuned): its cost,
+    # and its parity with the reference's rounding below
+    ctl64 = None
+    if not fixed and cfg["precision"] == "fp64" and rank == 0:
+        ck, _, _, _ = timed(schedule, max(1, min(args.steps, 3)), 1, controller="fp64")
+        ctl64 = {"ms_per_step": sum(ck) / len(ck), "value": n / (sum(ck) / len(ck) * 1e-3),
+                 "cost_vs_fp32_controller": (sum(ck) / len(ck)) / step_ms}
+        ctl64_sample = {"u_final": outs["u_final"][:, :m_par].cpu().numpy(),
+                        "naccept": outs["naccept"][:m_par].cpu().numpy(),
+                        "us": outs["us"][:, :, :m_par].cpu().numpy() if nsave else None}
     scale = cfg["abstol"] + cfg["reltol"] * np.abs(uf_plain).max(0)
     dev_err = np.abs(uf_measured - uf_plain).max(0) / scale
     dev_err = dev_err[np.isfinite(dev_err)] if np.isfinite(dev_err).any() else np.zeros(1)
@@ -559,7 +628,7 @@ def main():
             dist.destroy_process_group()
         return
     # pipe peak, measured live: FP64 FMA (or FP32 FMA for the single-precision mode)
-    rates = L.probe_rates(local, 2000)
+    rates = probe_rates(local, 2000)
     fp32 = cfg["precision"] != "fp64"
     peak = (rates["ffma"][0] if fp32 else rates["dfma"][0]) * 2 / 1e12
     flops = (att / args.steps) * cfg["flops_attempt"] + (sav / args.steps) * cfg["flops_save"]
@@ -585,14 +654,33 @@ def main():
         "rhs_evals_per_s": (att / args.steps) * cfg["rhs_per_attempt"] / (step_ms * 1e-3),
         "roofline": {"bound": "fp32" if fp32 else "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": tr,
-                     "peak_source": "%s FMA lane rate measured by this run's probe (libgb300ode_probe.so); "
+                     "peak_source": "%s FMA lane rate measured by this run's probe (bench_probe.cu); "
                                     "MEASURED_PEAKS.json carries no FP64/FP32-pipe figure" % ("FP32" if fp32 else "FP64")},
         "e2e": {"value": n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clocks,
     }
+    if unsorted_ms is not None:
+        line["persistent_unsorted"] = {"value": n * world / (unsorted_ms * 1e-3), "ms_per_step": unsorted_ms}
+        line["speedup_vs_unsorted"] = unsorted_ms / step_ms
     if fit_report is not None:
         line["learned_fit"] = fit_report
+        if "train_fit_ms" in fit_report:
+            # the learned schedule's one-off cost (training solve + fit) against what each solve saves
+            once = fit_report["train_solve_ms"] + fit_report["train_fit_ms"]
+            line["amortized"] = {
+                "fit_cost_ms": once, "first_solve_ms_incl_fit": once + step_ms,
+                "speedup_vs_plain_first_solve": plain_ms / (once + step_ms),
+                "break_even_solves_vs_plain": once / (plain_ms - step_ms) if plain_ms > step_ms else None,
+                "break_even_solves_vs_unsorted": (once / (unsorted_ms - step_ms)
+                                                  if unsorted_ms and unsorted_ms > step_ms else None),
+                "fit_over_solve": fit_report["train_fit_ms"] / step_ms}
+    if args.config != 4:
+        line["parity_vs_ref"] = parity_vs_ref(cfg, u0, p, sv, res_sample)
+    if ctl64 is not None:
+        if args.config != 4:
+            ctl64["parity_vs_ref"] = parity_vs_ref(cfg, u0, p, sv, ctl64_sample)
+        line["fp64_controller"] = ctl64
     if tune is not None:
         line["autotune"] = tune
     if args.config == 4:

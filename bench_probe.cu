@@ -1,10 +1,12 @@
-/* Throughput probes for the arithmetic pipes the solver kernels use.
+/* Throughput probes for the arithmetic pipes the solver kernels use: the
+ * benchmark's roofline denominators (an FP64-bound solver is measured against
+ * the FP64 pipe peak, which the measured-peaks file does not carry).
  *
- * libgb300ode_probe.so is a measurement aid for the benchmark (the roofline
- * denominator of an FP64-bound solver is the FP64 pipe peak, which the
- * driver-provided peaks file does not carry).  Each probe runs a grid of
- * 8 independent dependency chains per thread, two full waves of resident
- * blocks per SM, and times it with CUDA events after a warm-up launch.
+ * Measurement aid of bench.py, built by __graft_entry__.build() into
+ * _build/libbench_probe.so; not part of the solver library.  Each probe runs
+ * a grid of 8 independent dependency chains per thread, two full waves of
+ * resident blocks per SM, and times it with CUDA events after a warm-up
+ * launch.
  */
 #include <cuda_runtime.h>
 
@@ -76,79 +78,9 @@ float time_op(double* out, int blocks, int iters) {
   return ms;
 }
 
-/* FP64 issue structure: CH independent chains of dependent FMAs per thread,
- * only the first `active` lanes of each warp computing. */
-template <int CH>
-__global__ void issue_kernel(double* out, int iters, double a, double b, int active) {
-  double d[CH];
-#pragma unroll
-  for (int j = 0; j < CH; ++j) d[j] = 1.0 + 1e-3 * (threadIdx.x + j);
-  if ((int)(threadIdx.x & 31) < active) {
-    for (int i = 0; i < iters; ++i) {
-#pragma unroll
-      for (int u = 0; u < 8; ++u)
-#pragma unroll
-        for (int j = 0; j < CH; ++j) d[j] = __fma_rn(d[j], a, b);
-    }
-  }
-  double s = 0;
-#pragma unroll
-  for (int j = 0; j < CH; ++j) s += d[j];
-  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
-}
-
-template <int CH>
-float time_issue(double* out, int blocks, int threads, int iters, int active) {
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  issue_kernel<CH><<<blocks, threads>>>(out, iters / 4 + 1, 0.999999, 1e-6, active);
-  cudaEventRecord(e0);
-  issue_kernel<CH><<<blocks, threads>>>(out, iters, 0.999999, 1e-6, active);
-  cudaEventRecord(e1);
-  cudaEventSynchronize(e1);
-  float ms = 0;
-  cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  return ms;
-}
-
 }  // namespace
 
 extern "C" {
-
-/* FP64 FMA warp instructions retired per second per SM in five
- * configurations (r[0..4]):
- *   0: 64 warps per SM, 8 chains per thread, 32 active lanes
- *   1: the same with 8 active lanes per warp (masked lanes)
- *   2: 1 warp per SM, 1 chain
- *   3: 1 warp per SM, 8 chains
- *   4: 4 warps per SM (one per sub-partition), 1 chain
- * and the time of one dependent FMA in a lone warp in cycles at clock_mhz
- * (r[5]).  Returns 0 on success. */
-int probe_fp64_issue(int device, double clock_mhz, double* r) {
-  if (cudaSetDevice(device) != cudaSuccess) return -2;
-  int nsm = 0;
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
-  double* out = nullptr;
-  if (cudaMalloc(&out, (size_t)nsm * 8 * 256 * sizeof(double)) != cudaSuccess) return -3;
-  const float t0 = time_issue<8>(out, nsm * 8, 256, 1000, 32);
-  const float t1 = time_issue<8>(out, nsm * 8, 256, 1000, 8);
-  const float t2 = time_issue<1>(out, nsm, 32, 10000, 32);
-  const float t3 = time_issue<8>(out, nsm, 32, 2000, 32);
-  const float t4 = time_issue<1>(out, nsm, 128, 10000, 32);
-  cudaFree(out);
-  /* warp instructions per SM: warps per SM x iterations x 8 x chains */
-  r[0] = 64.0 * 1000 * 8 * 8 / (t0 * 1e-3);
-  r[1] = 64.0 * 1000 * 8 * 8 / (t1 * 1e-3);
-  r[2] = 1.0 * 10000 * 8 / (t2 * 1e-3);
-  r[3] = 1.0 * 2000 * 8 * 8 / (t3 * 1e-3);
-  r[4] = 4.0 * 10000 * 8 / (t4 * 1e-3);
-  r[5] = (t2 * 1e-3) / (10000.0 * 8) * clock_mhz * 1e6;
-  return cudaGetLastError() == cudaSuccess ? 0 : -1;
-}
-
 
 /* Lane operations per second for each probe (index = OP_*), and the device
  * time of each timed launch in ms.  `iters` sets the loop length (each

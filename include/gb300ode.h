@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define ODE_ABI_VERSION 3
+#define ODE_ABI_VERSION 4
 
 /* status codes */
 enum {
@@ -104,6 +104,26 @@ enum {
   ODE_OUTPUT_USER = 1000     /* ids >= ODE_OUTPUT_USER come from ode_output_compile: us[npoints][width][n] */
 };
 
+/* layout of the saveat / every-step output us */
+enum {
+  ODE_LAYOUT_SOA = 0,  /* us[npoints][width][n]: one row of n trajectories per point and value */
+  ODE_LAYOUT_TRAJ = 1  /* us[n][npoints][width]: each trajectory's series contiguous, the layout of the
+                          reference's per-trajectory sol.u (a Vector of SVectors).  A trajectory's
+                          consecutive points fill whole memory sectors, where the [n]-inner layout
+                          puts one 8-byte value of each sector per trajectory (neighbours in a
+                          sector are solved at different times under the persistent schedules) */
+};
+
+/* arithmetic of the adaptive step-size controller (ode_solve_args.controller) */
+enum {
+  ODE_CTRL_FP32 = 0, /* the factor q = EEst^beta1 / qold^beta2, its clamps and reciprocal in single
+                        precision (deterministic power function): the fastest; step sizes follow the
+                        reference's to about 2^-24 relative */
+  ODE_CTRL_FP64 = 1  /* the same factors in double precision (table-driven log and exp, a few ulps):
+                        step sizes follow the reference's to about 2^-50 relative, so accepted-step
+                        sequences match the reference's rounding far more often; FP64 precision only */
+};
+
 /* per-trajectory return codes */
 enum {
   ODE_RET_DEFAULT = 0,  /* finished at tf (ReturnCode.Default in the reference) */
@@ -140,12 +160,15 @@ typedef struct {
                            early stops; ODE_ETRAJ is not reported) and later calls on the same
                            stream are ordered after it */
   int32_t output;       /* ODE_OUTPUT_* (0: the state) */
+  int32_t layout;       /* ODE_LAYOUT_* of us (0: [npoints][width][n]) */
+  int32_t controller;   /* ODE_CTRL_* step-size controller arithmetic (adaptive FP64 solves) */
 } ode_solve_args;
 
 typedef struct {
   double* us;           /* [npoints][dim][n] (ODE_OUTPUT_STATE) or [npoints][1][n]
-                           (ODE_OUTPUT_KURAMOTO_R): npoints = nsave, or the grid length
-                           when save_everystep applies; NULL to skip */
+                           (ODE_OUTPUT_KURAMOTO_R), or [n][npoints][width] with ODE_LAYOUT_TRAJ:
+                           npoints = nsave, or the grid length when save_everystep applies;
+                           NULL to skip */
   double* u_final;      /* [dim][n] state at the end, or NULL */
   double* t_final;      /* [n], or NULL */
   int8_t* retcode;      /* [n] ODE_RET_*, or NULL */
@@ -163,7 +186,19 @@ typedef struct {
   int32_t schedule_used;  /* ODE_SCHED_* actually run */
   int32_t graph_replayed; /* 1 if a captured CUDA graph was replayed */
   int32_t jit;            /* 1 if the solver kernel was compiled at run time */
+  int32_t kernel;         /* ODE_KERNEL_* that ran */
 } ode_solve_stats;
+
+/* solver kernels (ode_solve_stats.kernel) */
+enum {
+  ODE_KERNEL_PLAIN = 0,      /* adaptive, one thread per trajectory */
+  ODE_KERNEL_PERSISTENT = 1, /* adaptive, resident warps refilled from a work counter */
+  ODE_KERNEL_STAGED = 2,     /* persistent with saveat interpolation batched per warp in shared memory */
+  ODE_KERNEL_FIXED = 3,      /* fixed step, one thread per trajectory */
+  ODE_KERNEL_FIXEDSPLIT = 4, /* fixed-step Tsit5 with a trajectory's components over the warps of a block
+                                (FP64 ensembles of at most 2 x SMs warps, separable right-hand side) */
+  ODE_KERNEL_ONESTEP = 5     /* RK4 / Euler, one thread per trajectory */
+};
 
 /* Bounds-check mode (debugging; compute-sanitizer stands in for nothing
  * here): with enable = 1 every later solve on this handle runs kernels
@@ -354,9 +389,9 @@ int ode_tune_load(ode_handle* h, const char* path);
  * cost (longest first) and, if asked, to seed each trajectory's initial dt. */
 typedef struct {
   int32_t hidden;      /* hidden width (default 64) */
-  int32_t epochs;      /* passes over the training set (default 200) */
+  int32_t epochs;      /* passes over the training set (default 30) */
   int32_t batch;       /* minibatch size (default 1024) */
-  float lr;            /* Adam learning rate (default 3e-3) */
+  float lr;            /* Adam learning rate (default 5e-3) */
   uint64_t seed;       /* initialisation and shuffling seed */
   int32_t seed_dt0;    /* 1: seed each trajectory's initial dt with the prediction in
                           ODE_SCHED_LEARNED (default 0: ordering only, results
@@ -367,7 +402,10 @@ typedef struct {
 typedef struct {
   float loss_first, loss_last;  /* training loss of the first and last epoch */
   float r2_attempts;            /* R^2 of log attempts on the training set */
-  double train_solve_ms, train_fit_ms;
+  double train_solve_ms;        /* wall time of the training ensemble's solve (step counts recorded) */
+  double train_fit_ms;          /* wall time of the fit: targets, standardisation, upload, training kernel */
+  double train_kernel_ms;       /* device time of the training kernel (CUDA events), all epochs */
+  int32_t train_ctas;           /* CTAs of the thread-block cluster that trained (16 or 8) */
 } ode_learn_report;
 
 /* Fill `o` with defaults. */
@@ -390,7 +428,9 @@ int ode_learn_gradcheck(ode_handle* h, int nin, int nh, int64_t batch, const flo
  * allocate GPU memory, such as applications that own the whole device memory
  * budget (pools sized at start-up) or real-time loops that cannot afford
  * cudaMalloc/cudaFree synchronising the device.  The caller passes device
- * buffers for every input and output (memory = ODE_MEM_DEVICE); the solver's
+ * buffers of the current device for every input and output (memory =
+ * ODE_MEM_DEVICE; managed memory is accepted too); `saveat` may be host or
+ * device memory (it is copied into the scratch array); the solver's
  * own scratch (work counter, statistics, saveat times) lives in a fixed
  * 33,024-byte array inside the library's device image, which every GPU that
  * loads the library keeps until the process exits.

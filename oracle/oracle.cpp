@@ -41,6 +41,7 @@
 #include "ctrl_pow.h"
 #include "../simplediffeq.jl_gb300/csrc/tableaus.h"
 #include "../simplediffeq.jl_gb300/csrc/log_table.h"
+#include "../simplediffeq.jl_gb300/csrc/exp_table.h"
 
 #include <algorithm>
 #include <cmath>
@@ -771,6 +772,14 @@ static void put_step(const oracle_args* a, oracle_out* o, int64_t i, int64_t k, 
   for (int d = 0; d < a->dim; ++d) o->ev_u[r * a->dim + d] = v[d];
 }
 
+double log_dev(double x);
+double exp_dev(double x);
+
+/* logarithms of the controller constants for the FP64 controller (rounded to double):
+ * ln(1/qmax) = ln 0.1, ln(1/qmin) = ln 5, ln gamma = ln 0.9, ln qoldinit = ln 1e-4 */
+static const double LN_QMAXI = -0x1.26bb1bbb55516p+1, LN_QMINI = 0x1.9c041f7ed8d33p+0,
+                    LN_GAMMA = -0x1.af8e8210a415dp-4, LN_QOLDINIT = -0x1.26bb1bbb55516p+3;
+
 template <class P, class M>
 static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
   typedef typename P::R R;
@@ -791,6 +800,8 @@ static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
               GAM = (float)(9.0 / 10.0), QOLDINIT = (float)1.0e-4;
   R qold = qoldinit;
   float qoldp = oracle_pow::ctrl_pow(QOLDINIT, B2);
+  /* FP64 controller of the device canon (a->ctrl64): beta2 * log(qold) */
+  double lqold = (2.0 / 25.0) * LN_QOLDINIT;
   const double dtmin = M::DTMIN_1F7 ? (double)1.0e-7f : 1.0e-14;
 
   int64_t cur = 0;
@@ -873,18 +884,37 @@ static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
         }
       } else {
         const float Ef = (float)EEst;
-        const float q11 = oracle_pow::ctrl_pow(Ef, B1);
+        /* FP64 controller: the reference's factors in double, on logarithms
+         * (log_dev, exp_dev), in the kernels' order of operations */
+        const double E = (double)EEst;
+        const double lE = !a->ctrl64 ? 0.0
+                          : (E != E) ? E
+                                     : log_dev(std::fmin(std::fmax(E, 0x1p-1022), 0x1.fffffffffffffp+1023));
+        const float q11 = a->ctrl64 ? 0.0f : oracle_pow::ctrl_pow(Ef, B1);
         if (EEst > (R)1) {
-          const float fac = jmin(QMINI, q11 / GAM);
-          dt = dt * (T)(1.0f / fac);
+          if (a->ctrl64) {
+            const double lf = jmin(LN_QMINI, std::fma(7.0 / 50.0, lE, -LN_GAMMA));
+            dt = dt * (T)exp_dev(-lf);
+          } else {
+            const float fac = jmin(QMINI, q11 / GAM);
+            dt = dt * (T)(1.0f / fac);
+          }
           ++nrej;
         } else {
-          float q = (EEst == (R)0) ? QMAXI : q11 / qoldp;
-          q = fmax_(QMAXI, fmin_(QMINI, q / GAM));
-          const float qoldf = jmax(Ef, QOLDINIT);
-          qoldp = oracle_pow::ctrl_pow(qoldf, B2);
+          T dtn;
+          if (a->ctrl64) {
+            const double lq0 = (EEst == (R)0) ? LN_QMAXI : std::fma(7.0 / 50.0, lE, -lqold);
+            const double lq = fmax_(LN_QMAXI, fmin_(LN_QMINI, lq0 - LN_GAMMA));
+            lqold = (2.0 / 25.0) * jmax(lE, LN_QOLDINIT);
+            dtn = dt * (T)exp_dev(-lq);
+          } else {
+            float q = (EEst == (R)0) ? QMAXI : q11 / qoldp;
+            q = fmax_(QMAXI, fmin_(QMINI, q / GAM));
+            const float qoldf = jmax(Ef, QOLDINIT);
+            qoldp = oracle_pow::ctrl_pow(qoldf, B2);
+            dtn = dt * (T)(1.0f / q);
+          }
           const T dtold = dt;
-          const T dtn = dt * (T)(1.0f / q);
           dt = jmin((T)std::fabs(dtn), (T)std::fabs(tf - t - dtold));
           const T told = t;
           if ((double)(tf - t - dtold) < dtmin) t = tf;
@@ -1281,6 +1311,31 @@ double log_dev(double x) {
   return std::fma(de, 0x1.62e42fefa38p-1, kLogTab[j][1]) + (std::fma(de, 0x1.ef35793c7673p-45, kLogTab[j][2]) + l1p);
 }
 
+/* exp of a double with |x| < 700, device canon (table-driven, Tang 1989):
+ * n = round(x 32/ln2) via the 1.5*2^52 shifter, r = x - n ln2/32 (two parts),
+ * exp(r) - 1 = r + r^2 q(r) with the Taylor coefficients 1/2 .. 1/720,
+ * 2^(j/32) = lead + trail from exp_table.h, scaled by 2^m. */
+double exp_dev(double x) {
+  const double t = std::fma(x, GBODE_EXP_INV_L, 0x1.8p52);
+  int64_t tb;
+  std::memcpy(&tb, &t, 8);
+  const int n = (int)(tb - 0x4338000000000000LL);
+  const double nd = t - 0x1.8p52;
+  const double r = std::fma(-nd, GBODE_EXP_L_TRAIL, std::fma(-nd, GBODE_EXP_L_LEAD, x));
+  double q = std::fma(r, 1.0 / 720.0, 1.0 / 120.0);
+  q = std::fma(q, r, 1.0 / 24.0);
+  q = std::fma(q, r, 1.0 / 6.0);
+  q = std::fma(q, r, 0.5);
+  const double p = std::fma(r * r, q, r);
+  const int j = n & 31, m = n >> 5;
+  const double lead = kExpTab[j][0], trail = kExpTab[j][1];
+  const double v = lead + std::fma(lead, p, std::fma(trail, p, trail));
+  const int64_t sb = (int64_t)(m + 1023) << 52;
+  double sc;
+  std::memcpy(&sc, &sb, 8);
+  return v * sc;
+}
+
 /* normals z_{2P}, z_{2P+1} of trajectory idx's stream: Philox counter
  * (P low, P high, idx low, idx high), key = seed, then Box-Muller */
 void normal_pair(uint64_t seed, int64_t P, int64_t idx, double* z0, double* z1) {
@@ -1418,6 +1473,7 @@ extern "C" int oracle_sde_solve(const oracle_sde_args* a) {
 
 extern "C" void oracle_philox(const uint32_t* c, const uint32_t* k, uint32_t* out) { philox(c, k, out); }
 extern "C" double oracle_log(double x) { return log_dev(x); }
+extern "C" double oracle_exp(double x) { return exp_dev(x); }
 extern "C" void oracle_normal_pair(uint64_t seed, int64_t pair, int64_t idx, double* z0, double* z1) {
   normal_pair(seed, pair, idx, z0, z1);
 }
@@ -1475,5 +1531,76 @@ extern "C" int oracle_mlp_forward_backward(int nin, int nh, int64_t batch, const
   }
   for (int i = 0; i < np; ++i) grad[i] = (float)g[i];
   *loss = (float)L;
+  return 0;
+}
+
+/* The same forward and backward pass in the rounding of the device training
+ * kernel (simplediffeq.jl_gb300/csrc/learn.cu): every matrix product takes
+ * bfloat16 operands -- parameters, features, activations, output deltas --
+ * and accumulates in fp32 (here: in double, rounded to float once, which the
+ * fp32 tensor-core accumulation approaches within a few float ulps); the ReLU
+ * masks come from the fp32 pre-activations; the output deltas are
+ * 2 (out - y) / batch in float, rounded to bfloat16; the layer-2 deltas are
+ * W3[0][j] d0 + W3[1][j] d1 (exact products, one rounding). */
+static inline float bf16_rn(float v) {
+  uint32_t u;
+  std::memcpy(&u, &v, 4);
+  if ((u & 0x7f800000u) == 0x7f800000u) return v;
+  u = (u + 0x7fffu + ((u >> 16) & 1u)) & 0xffff0000u;
+  std::memcpy(&v, &u, 4);
+  return v;
+}
+
+extern "C" int oracle_mlp_forward_backward_dev(int nin, int nh, int64_t batch, const float* prm_in, const float* x,
+                                               const float* y, float* grad, float* loss) {
+  if (nin < 1 || nh < 1 || batch < 1) return -1;
+  const int w1 = 0, b1 = nh * nin, w2 = b1 + nh, b2 = w2 + nh * nh, w3 = b2 + nh, b3 = w3 + 2 * nh;
+  const int np = b3 + 2;
+  std::vector<float> prm(np);
+  for (int i = 0; i < np; ++i) prm[i] = bf16_rn(prm_in[i]);
+  std::vector<double> g(np, 0.0);
+  std::vector<float> xb(nin), z1(nh), h1b(nh), z2(nh), h2b(nh), d2b(nh), d1b(nh);
+  const float inv_b = 1.f / (float)batch;
+  float L = 0.f;
+  for (int64_t s = 0; s < batch; ++s) {
+    for (int f = 0; f < nin; ++f) xb[f] = bf16_rn(x[s * nin + f]);
+    for (int j = 0; j < nh; ++j) {
+      double acc = prm[b1 + j];
+      for (int f = 0; f < nin; ++f) acc += (double)prm[w1 + j * nin + f] * xb[f];
+      z1[j] = (float)acc;
+      h1b[j] = bf16_rn(z1[j] > 0.f ? z1[j] : 0.f);
+    }
+    for (int j = 0; j < nh; ++j) {
+      double acc = prm[b2 + j];
+      for (int k = 0; k < nh; ++k) acc += (double)prm[w2 + j * nh + k] * h1b[k];
+      z2[j] = (float)acc;
+      h2b[j] = bf16_rn(z2[j] > 0.f ? z2[j] : 0.f);
+    }
+    float db[2];
+    for (int q = 0; q < 2; ++q) {
+      double acc = prm[b3 + q];
+      for (int k = 0; k < nh; ++k) acc += (double)prm[w3 + q * nh + k] * h2b[k];
+      const float e = (float)acc - y[s * 2 + q];
+      L += e * e * inv_b;
+      db[q] = bf16_rn(2.f * e * inv_b);
+      g[b3 + q] += db[q];
+      for (int k = 0; k < nh; ++k) g[w3 + q * nh + k] += (double)db[q] * h2b[k];
+    }
+    for (int j = 0; j < nh; ++j) {
+      const float d = z2[j] > 0.f ? std::fma(prm[w3 + j], db[0], prm[w3 + nh + j] * db[1]) : 0.f;
+      d2b[j] = bf16_rn(d);
+      g[b2 + j] += d2b[j];
+      for (int k = 0; k < nh; ++k) g[w2 + j * nh + k] += (double)d2b[j] * h1b[k];
+    }
+    for (int k = 0; k < nh; ++k) {
+      double acc = 0;
+      for (int j = 0; j < nh; ++j) acc += (double)prm[w2 + j * nh + k] * d2b[j];
+      d1b[k] = bf16_rn(z1[k] > 0.f ? (float)acc : 0.f);
+      g[b1 + k] += d1b[k];
+      for (int f = 0; f < nin; ++f) g[w1 + k * nin + f] += (double)d1b[k] * xb[f];
+    }
+  }
+  for (int i = 0; i < np; ++i) grad[i] = (float)g[i];
+  *loss = L;
   return 0;
 }

@@ -49,6 +49,7 @@ typedef struct {
   const double* dt0;     /* optional per-trajectory initial dt [n] */
   int nthreads;
   int output;            /* 0: state at saveat points; 1: Kuramoto order parameter r(t) of it */
+  int ctrl64;            /* DEVICE rounding: 1 for the FP64 step-size controller (ODE_CTRL_FP64) */
 } oracle_args;
 
 typedef struct {
@@ -101,6 +102,9 @@ float oracle_ctrl_pow(float x, float b);
 void oracle_sincos(double x, double* s, double* c);
 int oracle_mlp_forward_backward(int nin, int nh, int64_t batch, const float* params, const float* x,
                                 const float* y, float* grad, float* loss);
+/* the same in the device training kernel's rounding (bf16 operands, fp32 accumulation) */
+int oracle_mlp_forward_backward_dev(int nin, int nh, int64_t batch, const float* params, const float* x,
+                                    const float* y, float* grad, float* loss);
 
 #ifdef __cplusplus
 }

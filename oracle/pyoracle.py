@@ -35,7 +35,7 @@ class _Args(ctypes.Structure):
                 ("saveat", ctypes.c_void_p), ("nsave", ctypes.c_int64), ("save_everystep", ctypes.c_int),
                 ("grid", ctypes.c_void_p), ("ngrid", ctypes.c_int64), ("maxiters", ctypes.c_int64),
                 ("u0", ctypes.c_void_p), ("p", ctypes.c_void_p), ("dt0", ctypes.c_void_p),
-                ("nthreads", ctypes.c_int), ("output", ctypes.c_int)]
+                ("nthreads", ctypes.c_int), ("output", ctypes.c_int), ("ctrl64", ctypes.c_int)]
 
 
 class _Out(ctypes.Structure):
@@ -79,10 +79,13 @@ def lib():
         _lib.oracle_philox.restype = None
         _lib.oracle_log.argtypes = [ctypes.c_double]
         _lib.oracle_log.restype = ctypes.c_double
+        _lib.oracle_exp.argtypes = [ctypes.c_double]
+        _lib.oracle_exp.restype = ctypes.c_double
         _lib.oracle_normal_pair.argtypes = [ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64,
                                             ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         _lib.oracle_normal_pair.restype = None
         _lib.oracle_mlp_forward_backward.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int64] + [ctypes.c_void_p] * 5
+        _lib.oracle_mlp_forward_backward_dev.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int64] + [ctypes.c_void_p] * 5
     return _lib
 
 
@@ -97,15 +100,18 @@ def sincos(x):
     return s.value, c.value
 
 
-def mlp_forward_backward(nin, nh, params, x, y):
-    """Gradient and loss of the learned-schedule MLP (double-precision reference)."""
+def mlp_forward_backward(nin, nh, params, x, y, rounding="exact"):
+    """Gradient and loss of the learned-schedule MLP: "exact" in double
+    precision, "device" in the device training kernel's rounding (bf16
+    operands of every product, fp32 accumulation)."""
     params = np.ascontiguousarray(params, dtype=np.float32)
     x = np.ascontiguousarray(x, dtype=np.float32)
     y = np.ascontiguousarray(y, dtype=np.float32)
     grad = np.zeros_like(params)
     loss = np.zeros(1, dtype=np.float32)
-    rc = lib().oracle_mlp_forward_backward(nin, nh, x.shape[0], params.ctypes.data, x.ctypes.data, y.ctypes.data,
-                                           grad.ctypes.data, loss.ctypes.data)
+    fn = lib().oracle_mlp_forward_backward_dev if rounding == "device" else lib().oracle_mlp_forward_backward
+    rc = fn(nin, nh, x.shape[0], params.ctypes.data, x.ctypes.data, y.ctypes.data, grad.ctypes.data,
+            loss.ctypes.data)
     assert rc == 0
     return grad, float(loss[0])
 
@@ -204,7 +210,8 @@ def _ptr(a):
 
 
 def solve(alg, rhs, u0, p, tspan, dt, precision="fp64", rounding="ref", abstol=1e-6, reltol=1e-3,
-          saveat=None, save_everystep=False, maxiters=0, dt0=None, nthreads=1, grid=None, output="state"):
+          saveat=None, save_everystep=False, maxiters=0, dt0=None, nthreads=1, grid=None, output="state",
+          controller="fp32"):
     """Solve n trajectories.  u0: (dim, n) float64, p: (nparams, n) float64.
     Returns a dict of numpy arrays (us is (npoints, dim, n))."""
     u0 = np.ascontiguousarray(u0, dtype=np.float64)
@@ -237,7 +244,7 @@ def solve(alg, rhs, u0, p, tspan, dt, precision="fp64", rounding="ref", abstol=1
     args = _Args(ALG[alg], RHS[rhs], PREC[precision], ROUND[rounding], n, dim, nparams, t0, tf, float(dt),
                  float(abstol), float(reltol), _ptr(sv), 0 if sv is None else len(sv), int(bool(save_everystep)),
                  _ptr(grid), 0 if grid is None else len(grid), int(maxiters), _ptr(u0), _ptr(p), _ptr(d0),
-                 int(nthreads), 1 if output == "kuramoto_r" else 0)
+                 int(nthreads), 1 if output == "kuramoto_r" else 0, 1 if controller == "fp64" else 0)
     o = _Out(_ptr(out["us"]), _ptr(out["u_final"]), _ptr(out["t_final"]), _ptr(out["retcode"]),
              _ptr(out["naccept"]), _ptr(out["nreject"]), _ptr(out["dt_first"]), None, None, None)
     rc = lib().oracle_solve(ctypes.byref(args), ctypes.byref(o))
@@ -295,6 +302,11 @@ def philox(counter, key):
 
 def log_dev(x):
     return lib().oracle_log(float(x))
+
+
+def exp_dev(x):
+    """The device canon's double exponential (table-driven, |x| < 700)."""
+    return lib().oracle_exp(float(x))
 
 
 def normal_pair(seed, pair, idx):

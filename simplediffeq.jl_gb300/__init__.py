@@ -224,6 +224,7 @@ class EnsembleSolution:
         self.retcode, self.naccept, self.nreject, self.dt_first = retcode, naccept, nreject, dt_first
         self.stats = stats
         self.offsets, self.ts_rows, self.us_rows = offsets, ts_rows, us_rows
+        self.us_traj = None
 
     def __len__(self):
         return self.u_final.shape[1]
@@ -301,7 +302,7 @@ def _stack(eprob, trajectories):
 
 
 def make_args(alg, f_id, u0s, ps, tspan, dt, abstol, reltol, saveat, save_everystep, precision, schedule,
-              maxiters, memory=_lib.MEM_HOST, dt0=None, output="state"):
+              maxiters, memory=_lib.MEM_HOST, dt0=None, output="state", layout="soa", controller="fp32"):
     a = _lib.SolveArgs()
     a.alg = _lib.ALG[alg.name]
     a.rhs = f_id
@@ -319,12 +320,14 @@ def make_args(alg, f_id, u0s, ps, tspan, dt, abstol, reltol, saveat, save_everys
     a.u0, a.p = u0s.ctypes.data, ps.ctypes.data
     a.dt0 = None if dt0 is None else dt0.ctypes.data
     a.output = output if isinstance(output, int) else _lib.OUTPUT[output]
+    a.layout = _lib.LAYOUT[layout]
+    a.controller = _lib.CTRL[controller]
     return a
 
 
 def solve(prob, alg, trajectories=None, dt=0.1, abstol=1e-6, reltol=1e-3, saveat=None, save_everystep=None,
           precision="fp64", schedule="persistent", maxiters=0, device=0, dt0=None, throw=True, output="state",
-          **kwargs):
+          layout="soa", controller="fp32", **kwargs):
     """Solve an EnsembleProblem (or a single ODEProblem as an ensemble of one).
 
     Unknown keyword arguments are accepted and ignored, as the reference's
@@ -333,7 +336,11 @@ def solve(prob, alg, trajectories=None, dt=0.1, abstol=1e-6, reltol=1e-3, saveat
     solver returns every accepted step, a different number per trajectory
     (ragged output, as the reference's default for one trajectory); for the
     fixed-step algorithms it saves every grid point.  GPUSimpleRK4 and
-    GPUSimpleEuler ignore ``saveat`` as the reference does."""
+    GPUSimpleEuler ignore ``saveat`` as the reference does.  ``layout="traj"``
+    has the library write each trajectory's saved series contiguously
+    (ODE_LAYOUT_TRAJ); ``sol.us`` is then a (npoints, width, n) view of that
+    (n, npoints, width) array, ``sol.us_traj``.  ``controller="fp64"`` runs the
+    adaptive step-size controller in double precision (ODE_CTRL_FP64)."""
     single = isinstance(prob, (ODEProblem, SDEProblem))
     eprob = EnsembleProblem(prob) if single else prob
     if isinstance(eprob.prob, SDEProblem) or isinstance(alg, SimpleEM):
@@ -365,7 +372,7 @@ def solve(prob, alg, trajectories=None, dt=0.1, abstol=1e-6, reltol=1e-3, saveat
     dim = u0s.shape[0]
     args = make_args(alg, fid, u0s, ps, base.tspan, dt, abstol, reltol, sv, save_everystep, precision, schedule,
                      maxiters, dt0=None if dt0 is None else np.ascontiguousarray(dt0, dtype=np.float64),
-                     output=_output_id(h, output, dim, ps.shape[0]))
+                     output=_output_id(h, output, dim, ps.shape[0]), layout=layout, controller=controller)
     width = output.width if isinstance(output, UserOutput) else (1 if output == "kuramoto_r" else dim)
     if sv is not None:
         npts = len(sv)
@@ -380,9 +387,14 @@ def solve(prob, alg, trajectories=None, dt=0.1, abstol=1e-6, reltol=1e-3, saveat
            "dt_first": np.empty(n)}
     if ragged:
         return _solve_everystep(h, args, out, n, dim, throw, single)
-    us = np.empty((npts, width, n)) if npts else None
+    us_traj = None
+    if npts and layout == "traj":
+        us_traj = np.empty((n, npts, width))
+        us = us_traj.transpose(1, 2, 0)
+    else:
+        us = np.empty((npts, width, n)) if npts else None
     o = _lib.SolveOut()
-    o.us = None if us is None else us.ctypes.data
+    o.us = None if us is None else (us_traj if us_traj is not None else us).ctypes.data
     for k, v in out.items():
         setattr(o, k, v.ctypes.data)
     st = _lib.SolveStats()
@@ -390,6 +402,7 @@ def solve(prob, alg, trajectories=None, dt=0.1, abstol=1e-6, reltol=1e-3, saveat
     h.check(rc, allow=(_lib.ETRAJ,))
     sol = EnsembleSolution(tpts, us, out["u_final"], out["t_final"], out["retcode"], out["naccept"],
                            out["nreject"], out["dt_first"], st)
+    sol.us_traj = us_traj
     if rc == _lib.ETRAJ and throw:
         if (out["retcode"] == _lib.RET_DTMIN).any():
             raise DtLessThanMin("dt<dtmin")

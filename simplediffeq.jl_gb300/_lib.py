@@ -11,12 +11,14 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libgb300ode.so")
-PROBE_PATH = os.path.join(HERE, "lib", "libgb300ode_probe.so")
 
 OK, EINVAL, ECUDA, ENOMEM, ENOTSUP, ENVRTC, ETRAJ, ENOMODEL, ESMALL, ECHECK = 0, -1, -2, -3, -4, -5, -6, -7, -8, -9
 ALG = {"RK4": 0, "Tsit5": 1, "ATsit5": 2, "Vern7": 3, "AVern7": 4, "Vern9": 5, "AVern9": 6, "Euler": 7}
 RHS = {"lorenz": 0, "vanderpol": 1, "r3bp": 2, "kuramoto": 3, "linear": 4}
 PREC = {"fp64": 0, "fp32": 1, "fp32_kahan": 2}
+KERNEL = {0: "plain", 1: "persistent", 2: "staged", 3: "fixed", 4: "fixedsplit", 5: "onestep"}
+CTRL = {"fp32": 0, "fp64": 1}
+LAYOUT = {"soa": 0, "traj": 1}
 SCHED = {"plain": 0, "persistent": 1, "learned": 2}
 MEM_HOST, MEM_DEVICE = 0, 1
 OUTPUT = {"state": 0, "kuramoto_r": 1}
@@ -39,7 +41,7 @@ class SolveArgs(ctypes.Structure):
                 ("saveat", ctypes.c_void_p), ("nsave", ctypes.c_int64), ("save_everystep", ctypes.c_int32),
                 ("memory", ctypes.c_int32), ("maxiters", ctypes.c_int64), ("u0", ctypes.c_void_p),
                 ("p", ctypes.c_void_p), ("dt0", ctypes.c_void_p), ("stream", ctypes.c_void_p),
-                ("output", ctypes.c_int32)]
+                ("output", ctypes.c_int32), ("layout", ctypes.c_int32), ("controller", ctypes.c_int32)]
 
 
 class SolveOut(ctypes.Structure):
@@ -69,7 +71,7 @@ class SdeOut(ctypes.Structure):
 class SolveStats(ctypes.Structure):
     _fields_ = [("kernel_ms", ctypes.c_double), ("total_ms", ctypes.c_double), ("attempts", ctypes.c_int64),
                 ("saves", ctypes.c_int64), ("launches", ctypes.c_int32), ("schedule_used", ctypes.c_int32),
-                ("graph_replayed", ctypes.c_int32), ("jit", ctypes.c_int32)]
+                ("graph_replayed", ctypes.c_int32), ("jit", ctypes.c_int32), ("kernel", ctypes.c_int32)]
 
 
 class LearnOpts(ctypes.Structure):
@@ -80,7 +82,8 @@ class LearnOpts(ctypes.Structure):
 
 class LearnReport(ctypes.Structure):
     _fields_ = [("loss_first", ctypes.c_float), ("loss_last", ctypes.c_float), ("r2_attempts", ctypes.c_float),
-                ("train_solve_ms", ctypes.c_double), ("train_fit_ms", ctypes.c_double)]
+                ("train_solve_ms", ctypes.c_double), ("train_fit_ms", ctypes.c_double),
+                ("train_kernel_ms", ctypes.c_double), ("train_ctas", ctypes.c_int32)]
 
 
 TUNE_MAX_VARIANTS = 64
@@ -289,30 +292,3 @@ class Handle:
         return la, ld
 
 
-def probe_rates(device=0, iters=2000):
-    """Measured lane-operation rates of the arithmetic pipes (libgb300ode_probe.so)."""
-    lib = ctypes.CDLL(PROBE_PATH)
-    lib.probe_op_rates.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
-    r = np.zeros(8)
-    ms = np.zeros(8)
-    rc = lib.probe_op_rates(int(device), int(iters), r.ctypes.data, ms.ctypes.data, 8)
-    if rc != 0:
-        raise GB300ODEError(ECUDA, "probe failed (%d)" % rc)
-    names = ["dfma", "dadd", "ffma", "cvt_f64_f32_f64", "ddiv", "dsqrt_add", "dmax_add", "fdiv"]
-    return {k: (float(r[i]), float(ms[i])) for i, k in enumerate(names)}
-
-
-def probe_fp64_issue(device=0, clock_mhz=2070.0):
-    """FP64 FMA warp instructions retired per second per SM at full occupancy
-    (32 and 8 active lanes), for one warp per SM with 1 and 8 dependency
-    chains, and for one warp per SM sub-partition; plus the cycles of one
-    dependent FMA in a lone warp (libgb300ode_probe.so)."""
-    lib = ctypes.CDLL(PROBE_PATH)
-    lib.probe_fp64_issue.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_void_p]
-    r = np.zeros(6)
-    rc = lib.probe_fp64_issue(int(device), float(clock_mhz), r.ctypes.data)
-    if rc != 0:
-        raise GB300ODEError(ECUDA, "probe failed (%d)" % rc)
-    names = ["full_32_lanes", "full_8_lanes", "one_warp_1_chain", "one_warp_8_chains", "one_warp_per_smsp",
-             "lone_fma_cycles"]
-    return {k: float(r[i]) for i, k in enumerate(names)}

@@ -1,5 +1,5 @@
 #!/usr/bin/env python3
-"""Build libgb300ode.so for sm_103a (and the FP64 pipe probe library).
+"""Build libgb300ode.so for sm_103a.
 
 Steps:
   1. embed the device headers as C strings for run-time compilation (NVRTC);
@@ -93,7 +93,7 @@ def gen_sources():
     parts = ["/* generated by build.py: device headers for NVRTC */\n"]
     for fname, var in (("ode_solver.cuh", "kSrc_ode_solver_cuh"), ("ode_kparams.h", "kSrc_ode_kparams_h"),
                        ("tableaus.h", "kSrc_tableaus_h"), ("sde_solver.cuh", "kSrc_sde_solver_cuh"),
-                       ("log_table.h", "kSrc_log_table_h")):
+                       ("log_table.h", "kSrc_log_table_h"), ("exp_table.h", "kSrc_exp_table_h")):
         text = open(os.path.join(HERE, fname)).read()
         assert ")GBSRC\"" not in text
         parts.append('static const char* %s = R"GBSRC(%s)GBSRC";\n' % (var, text))
@@ -152,7 +152,7 @@ def build(verbose=False, jobs=None):
     tus = gen_sources()
     os.makedirs(LIB, exist_ok=True)
     headers = [os.path.join(HERE, f) for f in ("ode_solver.cuh", "ode_kparams.h", "tableaus.h", "ode_host.h",
-                                               "jlrange.h", "sde_solver.cuh", "log_table.h")] + [
+                                               "jlrange.h", "sde_solver.cuh", "log_table.h", "exp_table.h")] + [
         os.path.join(PKG, "..", "include", "gb300ode.h")]
     host_tus = [os.path.join(HERE, f) for f in ("ode_capi.cu", "learn.cu", "noalloc.cu", "sde_capi.cu")]
     gen = [os.path.join(BUILD, "aot_registry.inc"), os.path.join(BUILD, "embedded_src.inc")]
@@ -160,9 +160,6 @@ def build(verbose=False, jobs=None):
     for src in tus + host_tus:
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
         jobs_list.append((src, obj, headers + gen))
-    probe_src = os.path.join(HERE, "probe.cu")
-    probe_obj = os.path.join(BUILD, "probe.cu.o")
-    jobs_list.append((probe_src, probe_obj, []))
     errors = []
     with cf.ThreadPoolExecutor(max_workers=jobs or os.cpu_count()) as ex:
         futs = [ex.submit(compile_one, s, o, d) for s, o, d in jobs_list]
@@ -174,14 +171,10 @@ def build(verbose=False, jobs=None):
                     print(msg, file=sys.stderr)
     if errors:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
-    objs = [o for s, o, d in jobs_list if s != probe_src]
+    objs = [o for s, o, d in jobs_list]
     out = os.path.join(LIB, "libgb300ode.so")
     link = [NVCC] + ARCH + ["-shared", "-o", out] + objs + ["-ldl"]
     r = subprocess.run(link, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
-    pout = os.path.join(LIB, "libgb300ode_probe.so")
-    r = subprocess.run([NVCC] + ARCH + ["-shared", "-o", pout, probe_obj], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
     return out

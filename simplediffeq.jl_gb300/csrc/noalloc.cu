@@ -21,6 +21,10 @@
  * code is only a host-side stand-in, not a device address) and keeps it for
  * later calls on that device.  Make that first call before any stream capture.
  *
+ * Arguments: every input and output array is device memory of the current
+ * device (or managed memory); the saveat times may be host or device memory
+ * (they are copied into the scratch array).
+ *
  * Sharing: every call uses the same array and the array keeps the last call's
  * contents; each call clears the counters it needs at its start.  Calls that
  * overlap on the GPU (other host threads, or other streams before the
@@ -70,14 +74,17 @@ int say_cuda(char* err, size_t errlen, cudaError_t e, const char* what) {
   return e == cudaErrorMemoryAllocation ? ODE_ENOMEM : ODE_ECUDA;
 }
 
-bool on_device(const void* p) {
+/* p is NULL, or memory the current device `dev` can use in a kernel: its own
+ * device memory, or managed memory */
+bool on_device(const void* p, int dev) {
   if (!p) return true;
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+  if (at.type == cudaMemoryTypeManaged) return true;
+  return at.type == cudaMemoryTypeDevice && at.device == dev;
 }
 
 }  // namespace
@@ -92,6 +99,10 @@ extern "C" int ode_ensemble_solve_noalloc(const ode_solve_args* a, ode_solve_out
     return say(err, errlen, ODE_ENOTSUP, "the allocation-free solve stores the state at saveat points only");
   if (a->schedule != ODE_SCHED_PERSISTENT)
     return say(err, errlen, ODE_ENOTSUP, "the allocation-free solve runs the persistent schedule only");
+  if (a->controller != ODE_CTRL_FP32)
+    return say(err, errlen, ODE_ENOTSUP, "the allocation-free solve runs the single-precision step-size controller");
+  if (a->layout != ODE_LAYOUT_SOA && a->layout != ODE_LAYOUT_TRAJ)
+    return say(err, errlen, ODE_EINVAL, "unknown output layout");
   if (a->memory != ODE_MEM_DEVICE)
     return say(err, errlen, ODE_EINVAL, "the allocation-free solve takes device buffers (memory = ODE_MEM_DEVICE)");
   if (a->n < 0 || a->n > 0x7fffffffLL) return say(err, errlen, ODE_EINVAL, "n must be in [0, 2^31)");
@@ -100,15 +111,15 @@ extern "C" int ode_ensemble_solve_noalloc(const ode_solve_args* a, ode_solve_out
   if (!(a->t0 == a->t0) || !(a->tf == a->tf) || !(a->dt == a->dt))
     return say(err, errlen, ODE_EINVAL, "t0, tf and dt must not be NaN");
   if (a->n > 0 && (!a->u0 || !a->p)) return say(err, errlen, ODE_EINVAL, "u0/p missing");
-  const void* dev_ptrs[] = {a->u0, a->p, a->dt0, o->us, o->u_final, o->t_final, o->retcode, o->naccept,
-                            o->nreject, o->dt_first};
-  for (const void* q : dev_ptrs)
-    if (!on_device(q)) return say(err, errlen, ODE_EINVAL, "every array must be a device pointer");
-
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return say_cuda(err, errlen, e, "cudaGetDevice");
   if (dev < 0 || dev >= kMaxDevices) return say(err, errlen, ODE_ENOTSUP, "device index out of range");
+  const void* dev_ptrs[] = {a->u0, a->p, a->dt0, o->us, o->u_final, o->t_final, o->retcode, o->naccept,
+                            o->nreject, o->dt_first};
+  for (const void* q : dev_ptrs)
+    if (!on_device(q, dev))
+      return say(err, errlen, ODE_EINVAL, "every array must be a device pointer of the current device");
   {
     /* once per device: the scratch array's device address and the grid size */
     std::lock_guard<std::mutex> lock(g_setup_mutex);
@@ -145,6 +156,15 @@ extern "C" int ode_ensemble_solve_noalloc(const ode_solve_args* a, ode_solve_out
   kp.maxiters = a->maxiters > 0 ? a->maxiters : kDefaultMaxIters;
   kp.norm_fp64 = a->abstol < 1e-30 ? 1 : 0;  /* the same rule as ode_ensemble_solve */
   kp.us = o->us;
+  if (a->layout == ODE_LAYOUT_TRAJ) {
+    kp.us_sj = 3;
+    kp.us_sw = 1;
+    kp.us_si = 3 * a->nsave;
+  } else {
+    kp.us_sj = 3 * a->n;
+    kp.us_sw = a->n;
+    kp.us_si = 1;
+  }
   kp.u_final = o->u_final;
   kp.t_final = o->t_final;
   kp.retcode = (signed char*)o->retcode;
@@ -159,8 +179,9 @@ extern "C" int ode_ensemble_solve_noalloc(const ode_solve_args* a, ode_solve_out
   e = cudaMemsetAsync(scratch + kStatsOffset, 0, 4 * sizeof(unsigned long long), s);
   if (e != cudaSuccess) return say_cuda(err, errlen, e, "clear scratch");
   if (a->nsave > 0) {
-    e = cudaMemcpyAsync(scratch + kSaveatOffset, a->saveat, (size_t)a->nsave * sizeof(double),
-                        cudaMemcpyHostToDevice, s);
+    /* saveat may be host or device memory: the copy direction follows the pointer */
+    e = cudaMemcpyAsync(scratch + kSaveatOffset, a->saveat, (size_t)a->nsave * sizeof(double), cudaMemcpyDefault,
+                        s);
     if (e != cudaSuccess) return say_cuda(err, errlen, e, "copy saveat");
   }
   if (a->n > 0) {

@@ -279,13 +279,22 @@ const char* entry_kind(int alg, int sched, int64_t nsave) {
 bool use_fixed_split(const ode_handle* h, const ode_solve_args* a) {
   const bool separable = a->rhs == ODE_RHS_LORENZ || a->rhs == ODE_RHS_VANDERPOL || a->rhs == ODE_RHS_LINEAR;
   return a->alg == ODE_ALG_TSIT5 && separable && a->nsave == 0 && a->output == ODE_OUTPUT_STATE &&
-         a->precision == ODE_FP64 && !h->bounds_check && a->dim >= 2 && a->dim <= 8 &&
+         a->precision == ODE_FP64 && a->dim >= 2 && a->dim <= 8 &&
          (a->n + 31) / 32 <= (int64_t)h->nsm * 2;
 }
 
 /* entry_kind, with the component-split fixed-step kernel where it applies */
 const char* kernel_kind(const ode_handle* h, const ode_solve_args* a, int sched) {
   return use_fixed_split(h, a) ? "fixedsplit" : entry_kind(a->alg, sched, a->nsave);
+}
+
+int kernel_kind_id(const char* k) {
+  if (!std::strcmp(k, "persistent")) return ODE_KERNEL_PERSISTENT;
+  if (!std::strcmp(k, "staged")) return ODE_KERNEL_STAGED;
+  if (!std::strcmp(k, "fixed")) return ODE_KERNEL_FIXED;
+  if (!std::strcmp(k, "fixedsplit")) return ODE_KERNEL_FIXEDSPLIT;
+  if (!std::strcmp(k, "onestep")) return ODE_KERNEL_ONESTEP;
+  return ODE_KERNEL_PLAIN;
 }
 
 /* Bytes of one saveat job in the staged kernel's ring: the host-side copy of
@@ -346,10 +355,14 @@ int output_width(ode_handle* h, const ode_solve_args* a) {
   return a->dim;
 }
 
+/* the FP64 step-size controller applies to the adaptive kernels */
+bool ctrl64(const ode_solve_args* a) { return a->controller == ODE_CTRL_FP64 && !is_fixed(a->alg); }
+
 std::string kernel_key(ode_handle* h, const ode_solve_args* a, int sched) {
   char b[160];
-  snprintf(b, sizeof b, "%s|%s|%d|%d|%s|%d%s", alg_name(a->alg), kernel_kind(h, a, sched), a->rhs, a->dim,
-           prec_name(a->precision), a->output >= ODE_OUTPUT_USER ? a->output : 0, h->bounds_check ? "|chk" : "");
+  snprintf(b, sizeof b, "%s|%s|%d|%d|%s|%d%s%s", alg_name(a->alg), kernel_kind(h, a, sched), a->rhs, a->dim,
+           prec_name(a->precision), a->output >= ODE_OUTPUT_USER ? a->output : 0, h->bounds_check ? "|chk" : "",
+           ctrl64(a) ? "|c64" : "");
   return b;
 }
 
@@ -357,6 +370,7 @@ std::string kernel_key(ode_handle* h, const ode_solve_args* a, int sched) {
  * dim, schedule kind). */
 std::string jit_source(ode_handle* h, const ode_solve_args* a, int sched) {
   std::string src;
+  if (ctrl64(a)) src += "#define GBODE_CTRL64 1\n";
   if (a->output >= ODE_OUTPUT_USER) {
     /* the output function goes before the solver header, whose store_point calls it */
     const UserOutput& u = h->outputs[a->output - ODE_OUTPUT_USER];
@@ -400,9 +414,11 @@ int nvrtc_cubin(const std::string& src, const std::vector<std::string>& extra_op
     return ODE_ENVRTC;
   }
   nvrtcProgram prog;
-  const char* hdrs[] = {kSrc_ode_solver_cuh, kSrc_ode_kparams_h, kSrc_tableaus_h, kSrc_sde_solver_cuh, kSrc_log_table_h};
-  const char* names[] = {"ode_solver.cuh", "ode_kparams.h", "tableaus.h", "sde_solver.cuh", "log_table.h"};
-  nvrtcResult r = g_nvrtc.create(&prog, src.c_str(), "gbode_jit.cu", 5, hdrs, names);
+  const char* hdrs[] = {kSrc_ode_solver_cuh, kSrc_ode_kparams_h, kSrc_tableaus_h, kSrc_sde_solver_cuh, kSrc_log_table_h,
+                        kSrc_exp_table_h};
+  const char* names[] = {"ode_solver.cuh", "ode_kparams.h", "tableaus.h", "sde_solver.cuh", "log_table.h",
+                         "exp_table.h"};
+  nvrtcResult r = g_nvrtc.create(&prog, src.c_str(), "gbode_jit.cu", 6, hdrs, names);
   if (r != NVRTC_SUCCESS) {
     *err = std::string("nvrtcCreateProgram: ") + g_nvrtc.errstr(r);
     return ODE_ENVRTC;
@@ -487,7 +503,8 @@ int get_kernel(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn
   }
   const char* kind = kernel_kind(h, a, sched);
   for (const AotEntry& e : kAotEntries) {
-    if (!h->bounds_check && a->output < ODE_OUTPUT_USER && e.alg == a->alg && e.rhs == a->rhs && e.dim == a->dim &&
+    if (!h->bounds_check && !ctrl64(a) && a->output < ODE_OUTPUT_USER && e.alg == a->alg && e.rhs == a->rhs &&
+        e.dim == a->dim &&
         e.precision == a->precision && std::strcmp(e.kind, kind) == 0) {
       cudaFunction_t f;
       cudaError_t ce = cudaGetFuncBySymbol(&f, e.fn);
@@ -807,7 +824,7 @@ struct ChunkSlot {
   const char* tag;
   cudaEvent_t ev0, ev1;
   unsigned long long* host_stats; /* 4 words: attempts, saves, early stops, work counter */
-  int launches, replayed, jit, sched;
+  int launches, replayed, jit, sched, kernel;
 };
 
 int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_solve_stats* st, const EveryStep* ev,
@@ -821,6 +838,11 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
   if (a->precision < ODE_FP64 || a->precision > ODE_FP32_KAHAN) return fail(h, ODE_EINVAL, "unknown precision");
   if (a->schedule < ODE_SCHED_PLAIN || a->schedule > ODE_SCHED_LEARNED) return fail(h, ODE_EINVAL, "unknown schedule");
   if (a->memory != ODE_MEM_HOST && a->memory != ODE_MEM_DEVICE) return fail(h, ODE_EINVAL, "unknown memory kind");
+  if (a->layout != ODE_LAYOUT_SOA && a->layout != ODE_LAYOUT_TRAJ) return fail(h, ODE_EINVAL, "unknown output layout");
+  if (a->controller != ODE_CTRL_FP32 && a->controller != ODE_CTRL_FP64)
+    return fail(h, ODE_EINVAL, "unknown step-size controller");
+  if (a->controller == ODE_CTRL_FP64 && a->precision != ODE_FP64)
+    return fail(h, ODE_ENOTSUP, "the FP64 step-size controller applies to FP64 solves");
   if (a->n < 0 || a->n > 0x7fffffffLL) return fail(h, ODE_EINVAL, "n must be in [0, 2^31)");
   if (a->n > 0 && (!a->u0 || (a->nparams > 0 && !a->p))) return fail(h, ODE_EINVAL, "u0/p missing");
   if (!(a->t0 == a->t0) || !(a->tf == a->tf) || !(a->dt == a->dt))
@@ -887,6 +909,18 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
   kp.maxiters = a->maxiters > 0 ? a->maxiters : kDefaultMaxIters;
   kp.norm_fp64 = a->abstol < 1e-30 ? 1 : 0;
   kp.output = a->output;
+  {
+    const long long W = output_width(h, a);
+    if (a->layout == ODE_LAYOUT_TRAJ) {
+      kp.us_sj = W;
+      kp.us_sw = 1;
+      kp.us_si = (long long)npoints * W;
+    } else {
+      kp.us_sj = W * (long long)n;
+      kp.us_sw = n;
+      kp.us_si = 1;
+    }
+  }
 
   const bool host = a->memory == ODE_MEM_HOST;
   const size_t nd = (size_t)n * sizeof(double);
@@ -1084,6 +1118,7 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
     slot->replayed = replayed;
     slot->jit = jit;
     slot->sched = sched;
+    slot->kernel = kernel_kind_id(kernel_kind(h, a, sched));
     return ODE_OK;
   }
   CK(cudaEventRecord(ev1, s), "event");
@@ -1125,6 +1160,7 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
     st->schedule_used = sched;
     st->graph_replayed = replayed;
     st->jit = jit;
+    st->kernel = kernel_kind_id(kernel_kind(h, a, sched));
     st->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
   }
   if (hs[2] > 0) {
@@ -1171,7 +1207,10 @@ int solve_chunked(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_
     const char* name;
   };
   const Rows ins[] = {{a->u0, nullptr, D, 8, "ck_u0"}, {a->p, nullptr, NP, 8, "ck_p"}, {a->dt0, nullptr, 1, 8, "ck_dt0"}};
-  const Rows outs[] = {{nullptr, o->us, a->nsave * W, 8, "ck_us"}, {nullptr, o->u_final, D, 8, "ck_uf"},
+  /* a chunk of the [n][nsave][W] layout is one contiguous block: one row of nsave*W doubles per trajectory */
+  const bool traj = a->layout == ODE_LAYOUT_TRAJ;
+  const Rows outs[] = {{nullptr, o->us, traj ? 1 : a->nsave * W, traj ? (size_t)(8 * a->nsave * W) : 8, "ck_us"},
+                       {nullptr, o->u_final, D, 8, "ck_uf"},
                        {nullptr, o->t_final, 1, 8, "ck_tf"},       {nullptr, o->retcode, 1, 1, "ck_ret"},
                        {nullptr, o->naccept, 1, 4, "ck_nacc"},     {nullptr, o->nreject, 1, 4, "ck_nrej"},
                        {nullptr, o->dt_first, 1, 8, "ck_dtf"}};
@@ -1283,12 +1322,13 @@ int solve_chunked(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_
       rc = cuda_fail(h, e, "wait chunk inputs");
       break;
     }
-    ChunkSlot slot = {b ? "#1" : "#0", ev_start[(size_t)c], ev_end[(size_t)c], h->chunk_stats + 4 * c, 0, 0, 0, 0};
+    ChunkSlot slot = {b ? "#1" : "#0", ev_start[(size_t)c], ev_end[(size_t)c], h->chunk_stats + 4 * c, 0, 0, 0, 0, 0};
     rc = solve_impl(h, &sa, &so, nullptr, nullptr, &slot);
     if (rc != ODE_OK) break;
     total.launches += slot.launches;
     total.schedule_used = slot.sched;
     total.jit = slot.jit;
+    total.kernel = slot.kernel;
     replayed += slot.replayed;
     if (c >= 1) rc = download(c - 1);
     if (rc == ODE_OK && c + 1 < nchunks) rc = upload(c + 1);
@@ -1380,6 +1420,11 @@ int ode_ensemble_solve_everystep(ode_handle* h, const ode_solve_args* a, ode_eve
   if (a->nsave != 0 || a->output != ODE_OUTPUT_STATE)
     return fail(h, ODE_EINVAL, "every-step output takes no saveat and the state output");
   if (a->memory != ODE_MEM_HOST && a->memory != ODE_MEM_DEVICE) return fail(h, ODE_EINVAL, "unknown memory kind");
+  if (a->layout != ODE_LAYOUT_SOA && a->layout != ODE_LAYOUT_TRAJ) return fail(h, ODE_EINVAL, "unknown output layout");
+  if (a->controller != ODE_CTRL_FP32 && a->controller != ODE_CTRL_FP64)
+    return fail(h, ODE_EINVAL, "unknown step-size controller");
+  if (a->controller == ODE_CTRL_FP64 && a->precision != ODE_FP64)
+    return fail(h, ODE_ENOTSUP, "the FP64 step-size controller applies to FP64 solves");
   if (a->n < 0 || a->n > 0x7fffffffLL) return fail(h, ODE_EINVAL, "n must be in [0, 2^31)");
   CK(cudaSetDevice(h->device), "cudaSetDevice");
   const int64_t n = a->n;

@@ -22,7 +22,9 @@ struct KParams {
   long long maxiters;      /* <= 0: no cap */
   int norm_fp64;           /* 1: error norm in double (abstol below 1e-30) */
   int output;              /* 0: store the state at saveat points; 1: store the Kuramoto order parameter */
-  double* us;              /* [npoints][dim][n] or 0 */
+  double* us;              /* saveat / every-step output, or 0; element (point j, value w, trajectory i)
+                              at us[j * us_sj + w * us_sw + i * us_si] */
+  long long us_sj, us_sw, us_si; /* [npoints][width][n]: (width*n, n, 1); [n][npoints][width]: (width, 1, npoints*width) */
   double* u_final;         /* [dim][n] or 0 */
   double* t_final;         /* [n] or 0 */
   signed char* retcode;    /* [n] or 0 */

@@ -35,6 +35,10 @@
 #pragma once
 #include "ode_kparams.h"
 #include "tableaus.h"
+#define GBODE_LOGTAB_SPACE __device__ const
+#include "log_table.h"
+#define GBODE_EXPTAB_SPACE __device__ const
+#include "exp_table.h"
 
 namespace gbode {
 
@@ -178,6 +182,68 @@ __device__ __forceinline__ float ctrl_pow(float x, float b) {
   if (x == __int_as_float(0x7f800000)) return x;
   return ctrl_exp2(b * ctrl_log2(x));
 }
+
+/* Natural logarithm of a positive normal double, table-driven (P. T. P.
+ * Tang, ACM TOMS 16(4), 1990): x = 2^e m with m in [1, 2); the top 7 bits of
+ * m's fraction pick row j of log_table.h (gen_logtab.py), and
+ *   log x = e' ln 2 + T_j + log1p(r),  r = fma(m, 1/F_j, -1),  |r| < 2^-7,
+ * e' = e + 1 for j >= 53, whose T_j carries the -ln 2 (no cancellation of two
+ * terms of size ln 2 just below 1); log1p(r) = r + r^2 q(r) with q the Taylor
+ * coefficients -1/2, 1/3, ..., -1/8 (truncation below 2^-66), and e' ln 2 in
+ * two parts (LN2_HI of 42 significant bits, so e' LN2_HI is exact).  Every
+ * step is one IEEE double operation; no division. */
+__device__ __forceinline__ double log_dev(double x) {
+  const long long b = __double_as_longlong(x);
+  const int j = (int)((b >> 45) & 127);
+  const int e = (int)((b >> 52) & 0x7ff) - 1023 + (j >= GBODE_LOGTAB_SHIFT_FROM ? 1 : 0);
+  const double m = __longlong_as_double((b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
+  const double inv = __ldg(&kLogTab[j][0]), thi = __ldg(&kLogTab[j][1]), tlo = __ldg(&kLogTab[j][2]);
+  const double r = __fma_rn(m, inv, -1.0);
+  double q = -0.125;
+  q = __fma_rn(q, r, 0x1.2492492492492p-3);   /* 1/7 */
+  q = __fma_rn(q, r, -0x1.5555555555555p-3);  /* -1/6 */
+  q = __fma_rn(q, r, 0x1.999999999999ap-3);   /* 1/5 */
+  q = __fma_rn(q, r, -0.25);
+  q = __fma_rn(q, r, 0x1.5555555555555p-2);   /* 1/3 */
+  q = __fma_rn(q, r, -0.5);
+  const double l1p = __fma_rn(r * r, q, r);
+  const double de = (double)e;
+  return __fma_rn(de, 0x1.62e42fefa38p-1, thi) + (__fma_rn(de, 0x1.ef35793c7673p-45, tlo) + l1p);
+}
+
+/* Exponential of a double x with |x| < 700, table-driven (P. T. P. Tang,
+ * ACM TOMS 15(2), 1989): n = round(x 32/ln 2) (added to 1.5 * 2^52, so that
+ * the sum's low bits hold n), r = x - n ln2/32 with ln2/32 in two parts
+ * (exp_table.h: a lead of 42 significant bits makes n * lead exact),
+ * |r| <= ln2/64 + tiny; exp(r) - 1 = r + r^2 q(r), q the Taylor coefficients
+ * 1/2 .. 1/720 (degree 6, truncation below 2^-59); with j = n mod 32,
+ * m = (n - j)/32 and 2^(j/32) = lead_j + trail_j from the table,
+ *   exp(x) = 2^m (lead_j + (lead_j p + trail_j (1 + p))).
+ * Every step is one IEEE double operation; within 1 ulp (checked against
+ * 60-digit values by the CPU tests). */
+__device__ __forceinline__ double exp_dev(double x) {
+  const double t = __fma_rn(x, GBODE_EXP_INV_L, 0x1.8p52);
+  const int n = (int)(__double_as_longlong(t) - 0x4338000000000000LL);
+  const double nd = t - 0x1.8p52;
+  const double r = __fma_rn(-nd, GBODE_EXP_L_TRAIL, __fma_rn(-nd, GBODE_EXP_L_LEAD, x));
+  double q = __fma_rn(r, 0x1.6c16c16c16c17p-10, 0x1.1111111111111p-7); /* 1/720, 1/120 */
+  q = __fma_rn(q, r, 0x1.5555555555555p-5);                           /* 1/24 */
+  q = __fma_rn(q, r, 0x1.5555555555555p-3);                           /* 1/6 */
+  q = __fma_rn(q, r, 0.5);
+  const double p = __fma_rn(r * r, q, r);
+  const int j = n & 31, m = n >> 5;
+  const double lead = __ldg(&kExpTab[j][0]), trail = __ldg(&kExpTab[j][1]);
+  const double v = lead + __fma_rn(lead, p, __fma_rn(trail, p, trail));
+  return v * __longlong_as_double((long long)(m + 1023) << 52);
+}
+
+/* Logarithms of the controller constants (src/SimpleDiffEq.jl:67-77) for the
+ * FP64 controller, rounded to double: ln(1/qmax) = ln 0.1, ln(1/qmin) = ln 5,
+ * ln gamma = ln 0.9, ln qoldinit = ln 1e-4. */
+#define CTRL64_LN_QMAXI (-0x1.26bb1bbb55516p+1)
+#define CTRL64_LN_QMINI 0x1.9c041f7ed8d33p+0
+#define CTRL64_LN_GAMMA (-0x1.af8e8210a415dp-4)
+#define CTRL64_LN_QOLDINIT (-0x1.26bb1bbb55516p+3)
 
 /* ------------------------------------------------------------------ precisions */
 struct PFP64 { typedef double R; typedef double T; enum { KAHAN = 0 }; };
@@ -788,11 +854,19 @@ struct Lane {
   F f;
   T t, dt;
   float qoldp;
+#ifdef GBODE_CTRL64
+  double lqold; /* beta2 * log(qold) of the FP64 controller */
+#endif
   long long idx, att, cur, ninterp;
   int nacc, nrej;
   double dt_first;
   bool nan_seen;
 };
+
+/* Address of value w of output point j of trajectory idx (either layout). */
+__device__ __forceinline__ double* us_at(const KParams& P, long long j, long long w, long long idx) {
+  return P.us + j * P.us_sj + w * P.us_sw + idx * P.us_si;
+}
 
 /* Write saveat point j of trajectory idx: the state, or (P.output == 1) the
  * Kuramoto order parameter r = |(1/D) sum_k exp(i v_k)| = sqrt(C^2 + S^2) / D
@@ -813,7 +887,7 @@ __device__ __forceinline__ void store_point(const KParams& P, long long idx, lon
     double o[GBODE_OUTPUT_WIDTH];
     gbode_user_output(o, v, pv, t);
 #pragma unroll
-    for (int w = 0; w < GBODE_OUTPUT_WIDTH; ++w) P.us[(j * GBODE_OUTPUT_WIDTH + w) * P.n + idx] = o[w];
+    for (int w = 0; w < GBODE_OUTPUT_WIDTH; ++w) *us_at(P, j, w, idx) = o[w];
     return;
   }
 #endif
@@ -826,11 +900,11 @@ __device__ __forceinline__ void store_point(const KParams& P, long long idx, lon
       C = C + cs;
       S = S + sn;
     }
-    P.us[j * P.n + idx] = __dsqrt_rn(__fma_rn(C, C, S * S)) / (double)D;
+    *us_at(P, j, 0, idx) = __dsqrt_rn(__fma_rn(C, C, S * S)) / (double)D;
     return;
   }
 #pragma unroll
-  for (int d = 0; d < D; ++d) P.us[(j * D + d) * P.n + idx] = v[d];
+  for (int d = 0; d < D; ++d) *us_at(P, j, d, idx) = v[d];
 }
 
 template <class PR, int D, class L>
@@ -874,6 +948,9 @@ __device__ __forceinline__ void lane_load(const KParams& P, long long idx, Lane<
   l.t = (T)P.t0;
   l.dt = (T)(P.dt0 ? P.dt0[idx] : P.dt);
   l.qoldp = ctrl_pow((float)1.0e-4, (float)(2.0 / 25.0));
+#ifdef GBODE_CTRL64
+  l.lqold = (2.0 / 25.0) * CTRL64_LN_QOLDINIT;
+#endif
   l.att = 0;
   l.cur = 0;
   l.ninterp = 0;
@@ -936,7 +1013,7 @@ __device__ __forceinline__ void lane_finish(const KParams& P, Lane<PR, D, F, NK>
     const int width = P.output == 1 ? 1 : D;
 #endif
     for (long long j = l.cur; j < P.nsave; ++j)
-      for (int d = 0; d < width; ++d) P.us[(j * width + d) * P.n + idx] = qnan;
+      for (int d = 0; d < width; ++d) *us_at(P, j, d, idx) = qnan;
   }
   tot.att += (unsigned long long)l.att;
   tot.sav += (unsigned long long)l.ninterp;
@@ -980,6 +1057,7 @@ __device__ __forceinline__ int adaptive_try(const KParams& P, Lane<PR, D, F, NK>
    * this GPU, FP64 division and square root are not); double when abstol is so
    * small that the scale could leave the float range (P.norm_fp64). */
   float Ef;
+  double EEst64 = 0.0; /* the double norm, when computed */
   bool reject, is_zero;
   if (sizeof(R) == sizeof(float) || !P.norm_fp64) {
     const float abstol = (float)P.abstol, reltol = (float)P.reltol;
@@ -1003,11 +1081,45 @@ __device__ __forceinline__ int adaptive_try(const KParams& P, Lane<PR, D, F, NK>
       acc = (d == 0) ? r * r : fmaR(r, r, acc);
     }
     const R EEst = sqrtR(acc / (R)D);
+    EEst64 = (double)EEst;
     Ef = (float)EEst;
     reject = EEst > (R)1;
     is_zero = EEst == (R)0;
   }
   if (Ef != Ef) l.nan_seen = true;
+#ifdef GBODE_CTRL64
+  {
+    /* FP64 controller: the factors of the reference's controller in double,
+     * in the log domain.  le = log(EEst); reject: dt /= min(1/qmin,
+     * EEst^beta1/gamma); accept: q = EEst^beta1 / qold^beta2 (1/qmax when
+     * EEst == 0), dt /= max(1/qmax, min(1/qmin, q/gamma)), qold = max(EEst,
+     * qoldinit) -- with every power, quotient and clamp taken on logarithms
+     * (log_dev, exp_dev: within 2 ulp) and one exp_dev for the factor, so
+     * that dt follows the reference's step sizes to a few ulps instead of the
+     * single-precision controller's 2^-24. */
+    const double E = (sizeof(R) == sizeof(float) || !P.norm_fp64) ? (double)Ef : (double)EEst64;
+    const double le = (E != E) ? E : log_dev(fmin(fmax(E, 0x1p-1022), 0x1.fffffffffffffp+1023));
+    if (reject) {
+      const double lf = jmin(CTRL64_LN_QMINI, __fma_rn(7.0 / 50.0, le, -CTRL64_LN_GAMMA));
+      l.dt = l.dt * (T)exp_dev(-lf);
+      l.nrej += 1;
+      return TRY_REJECTED;
+    }
+    const double lq0 = is_zero ? CTRL64_LN_QMAXI : __fma_rn(7.0 / 50.0, le, -l.lqold);
+    const double lq = fm_max(CTRL64_LN_QMAXI, fm_min(CTRL64_LN_QMINI, lq0 - CTRL64_LN_GAMMA));
+    l.lqold = (2.0 / 25.0) * jmax(le, CTRL64_LN_QOLDINIT);
+    const T dtold = l.dt;
+    const T dtn = l.dt * (T)exp_dev(-lq);
+    l.dt = absmin(dtn, rest);
+    const T told = l.t;
+    l.t = tnext;
+    if (l.nacc == 0) l.dt_first = (double)dtold;
+    l.nacc += 1;
+    acc_out.told = told;
+    acc_out.dtold = dtold;
+    return TRY_ACCEPTED;
+  }
+#endif
   const float B1 = (float)(7.0 / 50.0), B2 = (float)(2.0 / 25.0), GAM = (float)(9.0 / 10.0);
   const float QMAXI = 0.1f, QMINI = 5.0f, QOLDINIT = (float)1.0e-4;
   const float q11 = ctrl_pow(Ef, B1);
@@ -1631,7 +1743,11 @@ struct FixedSplitTsit5 {
     const int lane = threadIdx.x & 31;
     const long long i = (long long)blockIdx.x * 32 + lane;
     const bool valid = i < P.n;
-    const long long idx = valid ? i : 0;  /* lanes past n compute on trajectory 0 and store nothing */
+    long long idx = valid ? i : 0;  /* lanes past n compute on trajectory 0 and store nothing */
+    if (!GBODE_CHECK(P, idx >= 0 && idx < P.n, CHK_TRAJ)) idx = 0;
+#ifdef GBODE_BOUNDS_CHECK
+    if (C == 0 && valid) atomicAdd(&P.visited[idx], 1u);  /* one start per trajectory, counted by warp 0 */
+#endif
     F f;
 #pragma unroll
     for (int j = 0; j < F::NP; ++j) f.p[j] = (R)P.p[(long long)j * P.n + idx];
@@ -1640,7 +1756,7 @@ struct FixedSplitTsit5 {
     const T dt = (T)P.dt;
     const bool every = P.nsave == 0 && P.save_everystep && P.us;
     auto value = [&]() { return PR::KAHAN ? (double)uh[0] - (double)uc[0] : (double)uh[0]; };
-    if (every && valid) P.us[(long long)C * P.n + i] = value();
+    if (every && valid && GBODE_CHECK(P, i < P.n && P.ngrid > 0, CHK_SAVE)) *us_at(P, 0, C, i) = value();
     int b = 0;
     R full[D], k[7][1];
     exchange(xb, b, C, lane, uh[0], full);
@@ -1677,16 +1793,16 @@ struct FixedSplitTsit5 {
       t = t + dt;
       uh[0] = nh[0];
       uc[0] = nc[0];
-      if (every && valid) P.us[(g * D + C) * P.n + i] = value();
+      if (every && valid && GBODE_CHECK(P, i < P.n && g < P.ngrid, CHK_SAVE)) *us_at(P, g, C, i) = value();
       k[0][0] = k[6][0];
     }
 #undef C5
 #undef C5T
     const int nacc = P.ngrid > 0 ? (int)(P.ngrid - 1) : 0;
-    if (valid && P.u_final) P.u_final[(long long)C * P.n + i] = value();
+    if (valid && P.u_final && GBODE_CHECK(P, i < P.n, CHK_TRAJ)) P.u_final[(long long)C * P.n + i] = value();
     if (C == 0) {
       Totals tot = {0, 0, 0};
-      if (valid) {
+      if (valid && GBODE_CHECK(P, i < P.n, CHK_TRAJ)) {
         if (P.t_final) P.t_final[i] = (double)t;
         if (P.retcode) P.retcode[i] = (signed char)RET_DEFAULT;
         if (P.naccept) P.naccept[i] = nacc;

@@ -19,7 +19,7 @@
  *     high word), key = seed, gives z_{2P} and z_{2P+1}:
  *   - two 53-bit uniforms u1 in (0, 1], u2 in [0, 1) and the Box-Muller pair
  *     (G. E. P. Box, M. E. Muller, 1958) r = sqrt(-2 log u1),
- *     (r cos 2 pi u2, r sin 2 pi u2), with this file's log_dev and
+ *     (r cos 2 pi u2, r sin 2 pi u2), with ode_solver.cuh's log_dev and
  *     ode_solver.cuh's sincos_cw, so that the oracle reproduces every normal
  *     bit for bit.
  * Non-diagonal noise takes M normals a step from the same stream.
@@ -30,8 +30,6 @@
 #pragma once
 #include "ode_solver.cuh"
 
-#define GBODE_LOGTAB_SPACE __device__ const
-#include "log_table.h"
 
 namespace gbode {
 
@@ -64,34 +62,6 @@ __device__ __forceinline__ U4 philox4x32_10(U4 c, unsigned k0, unsigned k1) {
     k1 += 0xBB67AE85u;
   }
   return c;
-}
-
-/* Natural logarithm of a positive normal double, table-driven (P. T. P.
- * Tang, ACM TOMS 16(4), 1990): x = 2^e m with m in [1, 2); the top 7 bits of
- * m's fraction pick row j of log_table.h (gen_logtab.py), and
- *   log x = e' ln 2 + T_j + log1p(r),  r = fma(m, 1/F_j, -1),  |r| < 2^-7,
- * e' = e + 1 for j >= 53, whose T_j carries the -ln 2 (no cancellation of two
- * terms of size ln 2 just below 1); log1p(r) = r + r^2 q(r) with q the Taylor
- * coefficients -1/2, 1/3, ..., -1/8 (truncation below 2^-66), and e' ln 2 in
- * two parts (LN2_HI of 42 significant bits, so e' LN2_HI is exact).  Every
- * step is one IEEE double operation; no division. */
-__device__ __forceinline__ double log_dev(double x) {
-  const long long b = __double_as_longlong(x);
-  const int j = (int)((b >> 45) & 127);
-  const int e = (int)((b >> 52) & 0x7ff) - 1023 + (j >= GBODE_LOGTAB_SHIFT_FROM ? 1 : 0);
-  const double m = __longlong_as_double((b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
-  const double inv = __ldg(&kLogTab[j][0]), thi = __ldg(&kLogTab[j][1]), tlo = __ldg(&kLogTab[j][2]);
-  const double r = __fma_rn(m, inv, -1.0);
-  double q = -0.125;
-  q = __fma_rn(q, r, 0x1.2492492492492p-3);   /* 1/7 */
-  q = __fma_rn(q, r, -0x1.5555555555555p-3);  /* -1/6 */
-  q = __fma_rn(q, r, 0x1.999999999999ap-3);   /* 1/5 */
-  q = __fma_rn(q, r, -0.25);
-  q = __fma_rn(q, r, 0x1.5555555555555p-2);   /* 1/3 */
-  q = __fma_rn(q, r, -0.5);
-  const double l1p = __fma_rn(r * r, q, r);
-  const double de = (double)e;
-  return __fma_rn(de, 0x1.62e42fefa38p-1, thi) + (__fma_rn(de, 0x1.ef35793c7673p-45, tlo) + l1p);
 }
 
 /* Normals z_{2P} and z_{2P+1} of trajectory idx's stream. */

@@ -56,6 +56,28 @@ def test_no_violation_and_same_results(pkg, checked, alg, sched):
     assert not fixed or (a["naccept"] == 200).all()
 
 
+@pytest.mark.parametrize("n", [1000, 3000])
+def test_no_violation_component_split_kernel(pkg, checked, n):
+    """Fixed-step Tsit5 with every-step output on a small FP64 ensemble runs the
+    component-split kernel in bounds-check mode too: no violation, every
+    trajectory started once (counted by the block's first warp), results
+    equal to the unchecked kernel's."""
+    L = pkg._lib
+    u0, p = lorenz_inputs(n, seed=103)
+    rc, a = _solve(pkg, checked, pkg.GPUSimpleTsit5(), "plain", u0, p, (0.0, 1.0), None, every=True)
+    assert rc == L.OK, checked.error()
+    rc2, b = _solve(pkg, pkg._handle(0), pkg.GPUSimpleTsit5(), "plain", u0, p, (0.0, 1.0), None, every=True)
+    for k in a:
+        assert np.array_equal(a[k], b[k], equal_nan=True), k
+    a2 = pkg.make_args(pkg.GPUSimpleTsit5(), 0, u0, p, (0.0, 1.0), 0.01, 1e-8, 1e-6, None, True, "fp64", "plain", 0)
+    us = np.empty((101, 3, n))
+    o = L.SolveOut()
+    o.us = us.ctypes.data
+    st = L.SolveStats()
+    assert checked.solve_raw(a2, o, st) == L.OK, checked.error()
+    assert L.KERNEL[st.kernel] == "fixedsplit"
+
+
 def test_no_violation_every_step_and_user_output(pkg, checked):
     L = pkg._lib
     u0, p = lorenz_inputs(2000, seed=102)

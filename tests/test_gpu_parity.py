@@ -210,10 +210,11 @@ def test_nan_state_finishes_like_the_reference(pkg, po):
                                        ("lorenz", 3, 40000)])
 def test_tsit5_fixed_component_split_bitexact(pkg, po, rhs, dim, n):
     """Fixed-step Tsit5 on small FP64 ensembles runs with a trajectory's
-    components over the warps of a block (up to 304 warps' worth of
-    trajectories; 40,000 takes the one-thread-per-trajectory kernel): every
-    grid point of every trajectory equals the oracle, including ensembles
-    that do not fill their last block."""
+    components over the warps of a block (up to 2 warps' worth of
+    trajectories per SM; 40,000 takes the one-thread-per-trajectory kernel on
+    a GPU with fewer than 625 SMs): every grid point of every trajectory
+    equals the oracle, including ensembles that do not fill their last block,
+    and the statistics name the kernel that ran."""
     rng = np.random.default_rng(dim * 1000 + n)
     if rhs == "lorenz":
         u0 = rng.uniform(-1, 1, (3, n)) + np.array([[0], [0], [20]])
@@ -228,3 +229,41 @@ def test_tsit5_fixed_component_split_bitexact(pkg, po, rhs, dim, n):
     ref = po.solve("Tsit5", rhs, u0, p, (0, 1), 0.01, rounding="device", save_everystep=True, nthreads=8)
     assert sol.us.shape == (101, dim, n)
     assert_bitexact(sol, ref)
+    import torch
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    expected = "fixedsplit" if (n + 31) // 32 <= 2 * nsm else "fixed"
+    assert pkg._lib.KERNEL[sol.stats.kernel] == expected
+
+
+@pytest.mark.parametrize("alg,rhs,schedule", [("ATsit5", "lorenz", "plain"), ("ATsit5", "lorenz", "persistent"),
+                                              ("AVern7", "vanderpol", "persistent"), ("AVern9", "r3bp", "persistent")])
+def test_fp64_controller_bitexact(pkg, po, alg, rhs, schedule):
+    """The FP64 step-size controller (ODE_CTRL_FP64, kernels compiled with it
+    at run time): bit-identical to the oracle's device canon with the same
+    controller, saveat included (staged and two-queue rings)."""
+    rng = np.random.default_rng(77)
+    n = 3000
+    if rhs == "lorenz":
+        u0, p = lorenz_inputs(n, seed=78)
+        tspan, kw = (0.0, 10.0), dict(abstol=1e-8, reltol=1e-6)
+    elif rhs == "vanderpol":
+        u0 = rng.uniform(-2, 2, (2, n))
+        p = np.exp(rng.uniform(np.log(0.1), np.log(10.0), n))[None, :]
+        tspan, kw = (0.0, 20.0), dict(abstol=1e-10, reltol=1e-8)
+    else:
+        u0 = np.array([0.994, 0.0, 0.0, -2.00158510637908])[:, None] + rng.normal(0, 1e-4, (4, n))
+        p = np.full((1, n), 0.012277471)
+        tspan, kw = (0.0, 17.0652165601579625588917206249), dict(abstol=1e-10, reltol=1e-10)
+    sv = np.linspace(tspan[0], tspan[1], 37)
+    sol = gpu(pkg, getattr(pkg, "GPUSimple" + alg)(), rhs, u0, p, tspan, 0.1, saveat=sv, schedule=schedule,
+              controller="fp64", throw=False, **kw)
+    ref = po.solve(alg, rhs, u0, p, tspan, 0.1, rounding="device", controller="fp64", saveat=sv, nthreads=8, **kw)
+    assert sol.stats.jit == 1
+    assert_bitexact(sol, ref)
+
+
+def test_fp64_controller_needs_fp64(pkg):
+    u0, p = lorenz_inputs(16, seed=1)
+    with pytest.raises(pkg.GB300ODEError) as e:
+        gpu(pkg, pkg.GPUSimpleATsit5(), "lorenz", u0, p, (0.0, 1.0), 0.1, precision="fp32", controller="fp64")
+    assert e.value.code == pkg._lib.ENOTSUP

@@ -438,3 +438,91 @@ def test_arenstorf_fp64_matched_accuracy_of_both_roundings(po):
     for f in (np.median, np.max):
         assert f(eb) < 1.5 * f(ea) and f(ea) < 1.5 * f(eb)
     assert np.mean(np.abs(a["naccept"] - b["naccept"]) <= 2) >= 0.99
+
+
+ARENSTORF_MU = 0.012277471
+ARENSTORF_U0 = [0.994, 0.0, 0.0, -2.00158510637908252240537862224]
+ARENSTORF_T = 17.0652165601579625588917206249
+
+
+@pytest.mark.parametrize("alg,loose,tight,bound,est_order", [("AVern9", 1e-10, 1e-13, 1e-9, 9),
+                                                            ("ATsit5", 1e-10, 1e-12, 2e-9, 5),
+                                                            ("AVern7", 1e-10, 1e-13, 5e-10, 7)])
+def test_arenstorf_orbit_closes_after_one_period(po, alg, loose, tight, bound, est_order):
+    """A published known answer, independent of the oracle's own fixtures: the
+    Arenstorf orbit of the restricted three-body problem (Hairer, Norsett and
+    Wanner, Solving ODEs I, section II.0: mu = 0.012277471, u0 = (0.994, 0, 0,
+    -2.00158510637908252240537862224)) is periodic with period
+    T = 17.0652165601579625588917206249, so the state at T returns to u0.  In
+    the reference's rounding the solvers close the orbit to the bound, and the
+    accepted-step counts at two tolerances scale as tol^(-1/q) for the order q
+    of the error estimate (Tsit5 5(4): q = 5, Vern7 7(6): 7, Vern9 9(8): 9), as
+    they do only with correct coefficients and stage order."""
+    u0 = np.array(ARENSTORF_U0)[:, None]
+    p = np.array([[ARENSTORF_MU]])
+    r = {}
+    for tol in (loose, tight):
+        r[tol] = po.solve(alg, "r3bp", u0, p, (0.0, ARENSTORF_T), 0.01, rounding="ref", abstol=tol, reltol=tol)
+        assert r[tol]["retcode"][0] == 0
+    err = np.abs(r[tight]["u_final"][:, 0] - u0[:, 0]).max()
+    assert err < bound, err
+    assert err < np.abs(r[loose]["u_final"][:, 0] - u0[:, 0]).max()
+    ratio = r[tight]["naccept"][0] / r[loose]["naccept"][0]
+    expected = (loose / tight) ** (1.0 / est_order)
+    assert abs(ratio / expected - 1) < 0.15, (ratio, expected)
+
+
+def test_device_canon_exp_accuracy(po):
+    """The table-driven exponential of the FP64 step-size controller: within
+    1 ulp over the controller's range and beyond (|x| < 700), against values
+    computed in 40-digit arithmetic."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 40
+    rng = np.random.default_rng(4)
+    x = np.concatenate([rng.uniform(-3, 3, 3000), rng.uniform(-700, 700, 1000), [0.0, -0.0, 1e-300, 0.5, -2.3025]])
+    got = np.array([po.exp_dev(v) for v in x])
+    want = np.array([float(mp.exp(mp.mpf(float(v)))) for v in x])
+    assert po.exp_dev(0.0) == 1.0
+    assert (np.abs(got - want) / np.spacing(want)).max() <= 1
+
+
+def test_exp_table_is_the_generator_output():
+    """csrc/exp_table.h is what csrc/gen_exptab.py writes (60-digit mpmath)."""
+    pytest.importorskip("mpmath")
+    import importlib.util
+    import os
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "simplediffeq.jl_gb300", "csrc")
+    spec = importlib.util.spec_from_file_location("gen_exptab", os.path.join(here, "gen_exptab.py"))
+    gen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen)
+    assert gen.header() == open(os.path.join(here, "exp_table.h")).read()
+
+
+@pytest.mark.parametrize("alg,rhs", [("ATsit5", "lorenz"), ("AVern7", "vanderpol")])
+def test_fp64_controller_follows_reference_step_sizes(po, alg, rhs):
+    """With the FP64 step-size controller (ODE_CTRL_FP64) the device canon's
+    step sequence follows the reference rounding's: on the benchmark
+    ensembles' first 8,192 trajectories (adaptive Lorenz, Van der Pol) every
+    accepted-step count is within +/-1 and every final state within 10x the
+    error scale, where the single-precision controller's factor q carries
+    2^-24 relative rounding into every step size (chaotic Lorenz trajectories
+    then drift beyond the bar: 3 of 131,072 at up to 84x).  The Arenstorf
+    orbit at 1e-12 is excluded: there fused and unfused stage sums alone
+    separate the solutions (see the matched-accuracy test)."""
+    import bench
+    cid = {"lorenz": 2, "vanderpol": 3}[rhs]
+    cfg = bench.CONFIGS[cid]
+    m = 8192
+    u0, p = cfg["inputs"](cfg["n"], 2024)
+    u0, p = np.ascontiguousarray(u0[:, :m]), np.ascontiguousarray(p[:, :m])
+    tol = (cfg["abstol"], cfg["reltol"])
+    kw = dict(abstol=tol[0], reltol=tol[1], nthreads=8)
+    ref = po.solve(alg, rhs, u0, p, cfg["tspan"], cfg["dt"], rounding="ref", **kw)
+    dev = po.solve(alg, rhs, u0, p, cfg["tspan"], cfg["dt"], rounding="device", controller="fp64", **kw)
+    ok = (ref["retcode"] == 0) & (dev["retcode"] == 0)
+    assert ok.mean() > 0.99
+    dn = np.abs(dev["naccept"].astype(np.int64) - ref["naccept"])[ok]
+    assert dn.max() <= 1
+    scale = tol[0] + tol[1] * np.abs(ref["u_final"]).max(0)
+    e = (np.abs(dev["u_final"] - ref["u_final"]).max(0) / scale)[ok]
+    assert np.mean(e <= 10) == 1.0, e.max()

@@ -45,12 +45,19 @@ def test_noalloc_matches_the_allocating_solve_twice(pkg):
     for k, v in out.items():
         setattr(o, k, v.data_ptr())
     err = ctypes.create_string_buffer(256)
+    dsv = torch.from_numpy(sv).to(dev)
     for call in range(2):
         for v in out.values():  # stale values must not survive
             v.fill_(-1 if v.dtype.is_floating_point else 7)
+        if call == 1:
+            a.saveat = dsv.data_ptr()  # saveat may also be a device array
         torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info(0)[0]
         rc = lib.ode_ensemble_solve_noalloc(ctypes.byref(a), ctypes.byref(o), err, 256)
         assert rc == 0, (call, rc, err.value)
+        if call == 1:
+            # after the first call's one-off set-up (kernel loading), a call takes no device memory
+            assert torch.cuda.mem_get_info(0)[0] == free_before
         assert np.array_equal(out["u_final"].cpu().numpy(), ref.u_final), call
         assert np.array_equal(out["us"].cpu().numpy(), ref.us, equal_nan=True), call
         assert np.array_equal(out["t_final"].cpu().numpy(), ref.t_final), call
@@ -78,3 +85,26 @@ def test_noalloc_rejects_what_it_cannot_hold(pkg):
                       "fp64", "persistent", 0, memory=L.MEM_DEVICE)  # host pointers
     assert lib.ode_ensemble_solve_noalloc(ctypes.byref(a), ctypes.byref(o), err, 256) == L.EINVAL
     assert b"device pointer" in err.value
+
+
+def test_noalloc_reports_trajectories_stopped_early(pkg):
+    """An attempt cap of 2 stops every trajectory: ODE_ETRAJ, retcode MAXITERS,
+    as ode_ensemble_solve reports it."""
+    torch = pytest.importorskip("torch")
+    L = pkg._lib
+    lib = L.load()
+    n = 1000
+    u0, p = lorenz_inputs(n, seed=7)
+    dev = torch.device("cuda", 0)
+    du0, dp = torch.from_numpy(u0).to(dev), torch.from_numpy(p).to(dev)
+    ret = torch.full((n,), 9, dtype=torch.int8, device=dev)
+    uf = torch.empty((3, n), dtype=torch.float64, device=dev)
+    a = pkg.make_args(pkg.GPUSimpleATsit5(), L.RHS["lorenz"], u0, p, (0.0, 10.0), KW["dt"], KW["abstol"],
+                      KW["reltol"], None, False, "fp64", "persistent", 2, memory=L.MEM_DEVICE)
+    a.u0, a.p = du0.data_ptr(), dp.data_ptr()
+    o = L.SolveOut()
+    o.retcode, o.u_final = ret.data_ptr(), uf.data_ptr()
+    err = ctypes.create_string_buffer(256)
+    rc = lib.ode_ensemble_solve_noalloc(ctypes.byref(a), ctypes.byref(o), err, 256)
+    assert rc == L.ETRAJ, (rc, err.value)
+    assert (ret.cpu().numpy() == 2).all()
