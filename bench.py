@@ -457,6 +457,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--tune-sample", type=int, default=262144, help="trajectories the autotuner times each variant on")
+    ap.add_argument("--layout", default="traj", choices=["soa", "traj"],
+                    help="saveat output layout: [npoints][dim][n] (soa) or [n][npoints][dim] (traj)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -496,13 +498,14 @@ def main():
             "naccept": torch.empty(n, dtype=torch.int32, device=dev),
             "nreject": torch.empty(n, dtype=torch.int32, device=dev)}
     if nsave:
-        outs["us"] = torch.empty((nsave, width, n), dtype=torch.float64, device=dev)
+        outs["us"] = torch.empty((n, nsave, width) if args.layout == "traj" else (nsave, width, n),
+                                 dtype=torch.float64, device=dev)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
 
     def args_for(schedule, memory, u0p, pp, uu=u0, ppp=p, controller="fp32"):
         a = pkg.make_args(alg, L.RHS[cfg["rhs"]], uu, ppp, cfg["tspan"], cfg["dt"], cfg["abstol"], cfg["reltol"],
                           sv, False, cfg["precision"], schedule, 0, memory=memory, output=cfg["output"],
-                          controller=controller)
+                          controller=controller, layout=args.layout)
         a.u0, a.p = u0p, pp
         return a
 
@@ -572,8 +575,14 @@ def main():
     step_ms = max_over_ranks(sum(kms) / len(kms), dist, dev)
     uf_measured = outs["u_final"].cpu().numpy()
     m_par = min(n, 4096)
+    def us_sample():
+        if not nsave:
+            return None
+        if args.layout == "traj":
+            return outs["us"][:m_par].permute(1, 2, 0).cpu().numpy()
+        return outs["us"][:, :, :m_par].cpu().numpy()
     res_sample = {"u_final": uf_measured[:, :m_par], "naccept": outs["naccept"][:m_par].cpu().numpy(),
-                  "us": outs["us"][:, :, :m_par].cpu().numpy() if nsave else None}
+                  "us": us_sample()}
     value = n * world / (step_ms * 1e-3)
 
     # the same persistent staged kernel in identity order: what the trained network's ordering adds
@@ -599,7 +608,7 @@ def main():
                  "cost_vs_fp32_controller": (sum(ck) / len(ck)) / step_ms}
         ctl64_sample = {"u_final": outs["u_final"][:, :m_par].cpu().numpy(),
                         "naccept": outs["naccept"][:m_par].cpu().numpy(),
-                        "us": outs["us"][:, :, :m_par].cpu().numpy() if nsave else None}
+                        "us": us_sample()}
     scale = cfg["abstol"] + cfg["reltol"] * np.abs(uf_plain).max(0)
     dev_err = np.abs(uf_measured - uf_plain).max(0) / scale
     dev_err = dev_err[np.isfinite(dev_err)] if np.isfinite(dev_err).any() else np.zeros(1)
@@ -635,14 +644,16 @@ def main():
     achieved = flops / (step_ms * 1e-3) / 1e12
     traffic = load_traffic()
     tr = None
-    if args.config == 2 and traffic and "atsit5_lorenz" in traffic:
-        tr = traffic["atsit5_lorenz"]["bytes_per_trajectory"] * n
+    tkey = "atsit5_lorenz" + ("_traj" if args.layout == "traj" else "")
+    if args.config == 2 and traffic and tkey in traffic:
+        tr = traffic[tkey]["bytes_per_trajectory"] * n
     line = {
         "metric": METRIC if args.config == 2 else "ensemble trajectories/s (workload %d)" % args.config,
         "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": cfg["dtype"], "data": "synthetic (seeded; no public dataset involved)",
         "config": {"workload": cfg["workload"], "trajectories_per_gpu": n, "schedule": schedule,
+                   "output_layout": "[n][nsave][dim]" if args.layout == "traj" else "[nsave][dim][n]",
                    "l2": "flushed between steps by a 512 MB device write",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "plain": {"value": n * world / (plain_ms * 1e-3), "ms_per_step": plain_ms},

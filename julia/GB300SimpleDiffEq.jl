@@ -176,6 +176,7 @@ const AdaptiveAlg = Union{GPUSimpleATsit5, GPUSimpleAVern7, GPUSimpleAVern9}
 const RHS_BUILTIN = Dict(:lorenz => 0, :vanderpol => 1, :r3bp => 2, :kuramoto => 3, :linear => 4)
 const PRECISION = Dict(:fp64 => 0, :fp32 => 1, :fp32_kahan => 2)
 const SCHEDULE = Dict(:plain => 0, :persistent => 1, :learned => 2)
+const CONTROLLER = Dict(:fp32 => 0, :fp64 => 1)
 const SDE_BUILTIN = Dict(:gbm => 0, :ou => 1, :lorenz => 2, :mult => 3)
 const ODE_OK, ODE_ETRAJ, ODE_ESMALL = 0, -6, -8
 const RET_DTMIN, RET_MAXITERS = 1, 2
@@ -294,11 +295,14 @@ function soa_inputs(ep::EnsembleProblem, trajectories::Integer)
     probs, u0, p, D, P
 end
 
+# the saved series come back trajectory-major (ODE_LAYOUT_TRAJ): a Julia W x npts x n array, us[:, j, i]
+# the j-th point of trajectory i, as the reference's per-trajectory sol.u
 function solve_args(alg, h, rhs, u0, p, D, P, n, tspan, dt, abstol, reltol, sv, save_everystep, precision,
-                    schedule, maxiters, output)
+                    schedule, maxiters, output; controller::Symbol = :fp32)
     SolveArgs(ALG_ID[typeof(alg)], rhs_id(h, rhs, D, P), PRECISION[precision], SCHEDULE[schedule], n, D, P,
               tspan[1], tspan[2], dt, abstol, reltol, isempty(sv) ? C_NULL : pointer(sv), length(sv),
-              save_everystep, 0, maxiters, pointer(u0), pointer(p), C_NULL, C_NULL, output_id(output))
+              save_everystep, 0, maxiters, pointer(u0), pointer(p), C_NULL, C_NULL, output_id(output), 1,
+              CONTROLLER[controller])
 end
 
 retcode_of(r) = r == RET_MAXITERS ? SciMLBase.ReturnCode.MaxIters : SciMLBase.ReturnCode.Default
@@ -308,18 +312,20 @@ retcode_of(r) = r == RET_MAXITERS ? SciMLBase.ReturnCode.MaxIters : SciMLBase.Re
 """
     solve(ep::EnsembleProblem, alg::GPUSimple*; trajectories, rhs, dt = 0.1, abstol = 1e-6,
           reltol = 1e-3, saveat = nothing, save_everystep = true, precision = :fp64,
-          schedule = :persistent, maxiters = 0, output = :state, device = 0)
+          schedule = :persistent, maxiters = 0, output = :state, controller = :fp32, device = 0)
 
 The whole ensemble in one call of `ode_ensemble_solve` (`ode_ensemble_solve_everystep`
 for the adaptive algorithms' default every-step output).  `rhs`: `:lorenz`,
 `:vanderpol`, `:r3bp`, `:kuramoto`, `:linear`, an id from `compile_rhs`, or the
-CUDA C++ body itself.  Keyword defaults are the reference's; `dt < dtmin`
-raises the reference's `error("dt<dtmin")`.
+CUDA C++ body itself.  `controller = :fp64` runs the step-size controller in
+double precision (ODE_CTRL_FP64).  Keyword defaults are the reference's;
+`dt < dtmin` raises the reference's `error("dt<dtmin")`.
 """
 function SciMLBase.solve(ep::EnsembleProblem, alg::GPUSimpleAlg; trajectories::Integer, rhs,
                          dt = 0.1, abstol = 1.0e-6, reltol = 1.0e-3, saveat = nothing,
                          save_everystep = true, precision::Symbol = :fp64, schedule::Symbol = :persistent,
-                         maxiters::Integer = 0, output = :state, device::Integer = 0, kwargs...)
+                         maxiters::Integer = 0, output = :state, controller::Symbol = :fp32, device::Integer = 0,
+                         kwargs...)
     prob = ep.prob
     @assert !SciMLBase.isinplace(prob)   # as every GPUSimple solve
     h = handle(device)
@@ -338,12 +344,13 @@ function SciMLBase.solve(ep::EnsembleProblem, alg::GPUSimpleAlg; trajectories::I
     fixed_grid = collect(prob.tspan[1]:dt:prob.tspan[2])
     npts = !isempty(sv) ? length(sv) : (save_everystep && !(alg isa AdaptiveAlg) ? length(fixed_grid) : 0)
     W = output === :kuramoto_r ? 1 : D
-    us = Array{Float64}(undef, n, W, max(npts, 1))    # C [npts][W][n]
+    us = Array{Float64}(undef, W, max(npts, 1), n)    # C [n][npts][W] (ODE_LAYOUT_TRAJ)
     uf = Matrix{Float64}(undef, n, D)
     tf = Vector{Float64}(undef, n)
     ret = Vector{Int8}(undef, n)
     args = solve_args(alg, h, rhs, u0, p, D, P, n, prob.tspan, dt, abstol, reltol, sv,
-                      save_everystep && !(alg isa AdaptiveAlg), precision, schedule, maxiters, output)
+                      save_everystep && !(alg isa AdaptiveAlg), precision, schedule, maxiters, output;
+                      controller = controller)
     out = SolveOut(npts == 0 ? C_NULL : pointer(us), pointer(uf), pointer(tf), pointer(ret), C_NULL, C_NULL,
                    C_NULL)
     rc = GC.@preserve sv u0 p us uf tf ret ccall((:ode_ensemble_solve, lib), Cint,
@@ -353,7 +360,7 @@ function SciMLBase.solve(ep::EnsembleProblem, alg::GPUSimpleAlg; trajectories::I
     check(h, rc; allow = (ODE_ETRAJ,))
     ts = npts == 0 ? [prob.tspan[1], prob.tspan[2]] : (isempty(sv) ? fixed_grid : sv)
     sols = map(1:n) do i
-        u = npts == 0 ? [SVector{D}(u0[i, :]), SVector{D}(uf[i, :])] : [SVector{W}(us[i, :, j]) for j in 1:npts]
+        u = npts == 0 ? [SVector{D}(u0[i, :]), SVector{D}(uf[i, :])] : [SVector{W}(view(us, :, j, i)) for j in 1:npts]
         SciMLBase.build_solution(probs[i], alg, ts, u; retcode = retcode_of(ret[i]), calculate_error = false)
     end
     SciMLBase.EnsembleSolution(sols, 0.0, true)
