@@ -149,6 +149,23 @@ static inline void sincos_of(R x, R* s, R* c) {
   }
 }
 
+/* mu / r^(3/2) in the device canon: double r * sqrt(r) and a division; single
+ * precision mu * y^3, y = 1/sqrt(r) from Lomont's bit-level seed (magic
+ * constant 0x5f375a86) and three Newton steps y (3/2 - (r/2) y^2) */
+static inline double r3bp_pull_dev(double mu, double r) { return mu / (r * std::sqrt(r)); }
+static inline float r3bp_pull_dev(float mu, float r) {
+  int32_t ri;
+  std::memcpy(&ri, &r, 4);
+  const int32_t yi = 0x5f375a86 - (ri >> 1);
+  float y;
+  std::memcpy(&y, &yi, 4);
+  const float hx = 0.5f * r;
+  y = y * std::fma(-(hx * y), y, 1.5f);
+  y = y * std::fma(-(hx * y), y, 1.5f);
+  y = y * std::fma(-(hx * y), y, 1.5f);
+  return mu * ((y * y) * y);
+}
+
 /* ---------------------------------------------------------------- problems */
 /* Built-in right-hand sides.  The REF form is the plain Julia expression; the
  * DEV form fuses the products the device functors fuse. */
@@ -186,8 +203,7 @@ static void rhs_eval(int id, int D, const R* u, const R* p, double t, R* du) {
       R a = x + mu, b = x - mu1;
       if (DEV) {
         R r1 = fmaX(a, a, y * y), r2 = fmaX(b, b, y * y);
-        R d1 = r1 * std::sqrt(r1), d2 = r2 * std::sqrt(r2);
-        R g1 = mu1 / d1, g2 = mu / d2;
+        R g1 = r3bp_pull_dev(mu1, r1), g2 = r3bp_pull_dev(mu, r2);
         du[0] = vx;
         du[1] = vy;
         du[2] = fmaX(-g2, b, fmaX(-g1, a, fmaX((R)2, vy, x)));
@@ -1474,6 +1490,8 @@ extern "C" int oracle_sde_solve(const oracle_sde_args* a) {
 extern "C" void oracle_philox(const uint32_t* c, const uint32_t* k, uint32_t* out) { philox(c, k, out); }
 extern "C" double oracle_log(double x) { return log_dev(x); }
 extern "C" double oracle_exp(double x) { return exp_dev(x); }
+/* the single-precision R3BP pull mu / r^(3/2) of the device canon */
+extern "C" float oracle_r3bp_pull_f(float mu, float r) { return r3bp_pull_dev(mu, r); }
 extern "C" void oracle_normal_pair(uint64_t seed, int64_t pair, int64_t idx, double* z0, double* z1) {
   normal_pair(seed, pair, idx, z0, z1);
 }

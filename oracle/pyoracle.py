@@ -81,6 +81,8 @@ def lib():
         _lib.oracle_log.restype = ctypes.c_double
         _lib.oracle_exp.argtypes = [ctypes.c_double]
         _lib.oracle_exp.restype = ctypes.c_double
+        _lib.oracle_r3bp_pull_f.argtypes = [ctypes.c_float, ctypes.c_float]
+        _lib.oracle_r3bp_pull_f.restype = ctypes.c_float
         _lib.oracle_normal_pair.argtypes = [ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64,
                                             ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         _lib.oracle_normal_pair.restype = None
@@ -307,6 +309,11 @@ def log_dev(x):
 def exp_dev(x):
     """The device canon's double exponential (table-driven, |x| < 700)."""
     return lib().oracle_exp(float(x))
+
+
+def r3bp_pull_f(mu, r):
+    """The device canon's single-precision mu / r^(3/2) (Newton-refined reciprocal square root)."""
+    return lib().oracle_r3bp_pull_f(float(mu), float(r))
 
 
 def normal_pair(seed, pair, idx):

@@ -43,14 +43,27 @@ def test_atsit5_lorenz_bitexact(pkg, po, schedule):
     assert sol.stats.attempts == int((ref["naccept"] + ref["nreject"]).sum())
 
 
-def test_atsit5_lorenz_vs_reference_rounding(pkg, po):
-    """Spec tolerance against the reference's own rounding."""
+@pytest.mark.parametrize("controller", ["fp32", "fp64"])
+def test_atsit5_lorenz_vs_reference_rounding(pkg, po, controller):
+    """Spec tolerance against the reference's own rounding, for the final
+    states and for every saveat value: the accepted-step counts within +/-1
+    and at least 99.9% of the trajectories within 10x the error scale with the
+    single-precision controller (chaos amplifies its 2^-24 step-size rounding
+    in a few trajectories: 3 of 131,072 on this workload), all of them with the
+    FP64 controller."""
     u0, p = lorenz_inputs(2000, seed=4)
-    sol = gpu(pkg, pkg.GPUSimpleATsit5(), "lorenz", u0, p, (0.0, 10.0), 0.1, abstol=1e-8, reltol=1e-6)
-    ref = po.solve("ATsit5", "lorenz", u0, p, (0, 10), 0.1, rounding="ref", abstol=1e-8, reltol=1e-6, nthreads=8)
+    sv = np.linspace(0, 10, 100)
+    sol = gpu(pkg, pkg.GPUSimpleATsit5(), "lorenz", u0, p, (0.0, 10.0), 0.1, abstol=1e-8, reltol=1e-6, saveat=sv,
+              controller=controller)
+    ref = po.solve("ATsit5", "lorenz", u0, p, (0, 10), 0.1, rounding="ref", abstol=1e-8, reltol=1e-6, saveat=sv,
+                   nthreads=8)
     scale = 1e-8 + 1e-6 * np.abs(ref["u_final"]).max(0)
     err = np.abs(sol.u_final - ref["u_final"]).max(0) / scale
-    assert np.mean(err <= 10) >= 0.999, "more than 0.1% of trajectories beyond 10x the error scale"
+    us_scale = 1e-8 + 1e-6 * np.abs(ref["us"]).max(axis=(0, 1))
+    us_err = np.abs(sol.us - ref["us"]).max(axis=(0, 1)) / us_scale
+    need = 1.0 if controller == "fp64" else 0.999
+    assert np.mean(err <= 10) >= need, "final states beyond 10x the error scale"
+    assert np.mean(us_err <= 10) >= need, "saveat values beyond 10x the error scale"
     assert np.abs(sol.naccept - ref["naccept"]).max() <= 1
 
 
