@@ -791,6 +791,54 @@ static void put_step(const oracle_args* a, oracle_out* o, int64_t i, int64_t k, 
 double log_dev(double x);
 double exp_dev(double x);
 
+/* Single-precision modes of the device canon: error norm and controller free
+ * of IEEE division and square root (kernels: rcp_nr, log2_nr, exp2_nr in
+ * ode_solver.cuh).  rcp: seed 0x7ef311c7 - bits(d), three Newton steps
+ * y (2 - d y); log2: the atanh series with (m-1)/(m+1) by rcp and the
+ * sqrt(2) fold; exp2: y = n + f by the 1.5 * 2^23 shifter, Taylor degree 7 in
+ * f ln 2, scaled by 2^n through the exponent bits. */
+static inline float bits_f(int32_t i) { float f; std::memcpy(&f, &i, 4); return f; }
+static inline int32_t fbits(float f) { int32_t i; std::memcpy(&i, &f, 4); return i; }
+static inline float rcp_nr(float d) {
+  float y = bits_f(0x7ef311c7 - fbits(d));
+  y = y * std::fma(-d, y, 2.0f);
+  y = y * std::fma(-d, y, 2.0f);
+  y = y * std::fma(-d, y, 2.0f);
+  return y;
+}
+static inline float log2_nr(float x) {
+  const int32_t b = fbits(x);
+  const int e0 = ((b >> 23) & 0xff) - 127;
+  const float m0 = bits_f((b & 0x007fffff) | 0x3f800000);
+  const bool fold = m0 > 1.41421354f;
+  const float m = fold ? 0.5f * m0 : m0;
+  const int e = fold ? e0 + 1 : e0;
+  const float s = (m - 1.0f) * rcp_nr(m + 1.0f);
+  const float s2 = s * s;
+  float poly = std::fma(s2, 0.0909090936f, 0.111111112f);
+  poly = std::fma(s2, poly, 0.142857149f);
+  poly = std::fma(s2, poly, 0.200000003f);
+  poly = std::fma(s2, poly, 0.333333343f);
+  poly = std::fma(s2, poly, 1.0f);
+  return std::fma(s * poly, 2.88539004f, (float)e);
+}
+static inline float exp2_nr(float y) {
+  const float t = y + 12582912.0f;
+  const int n = fbits(t) - 0x4b400000;
+  const float f = y - (t - 12582912.0f);
+  const float z = f * 0.693147182f;
+  float p = std::fma(z, 1.98412701e-04f, 1.38888892e-03f);
+  p = std::fma(z, p, 8.33333377e-03f);
+  p = std::fma(z, p, 4.16666679e-02f);
+  p = std::fma(z, p, 0.166666672f);
+  p = std::fma(z, p, 0.5f);
+  p = std::fma(z, p, 1.0f);
+  p = std::fma(z, p, 1.0f);
+  return p * bits_f((n + 127) << 23);
+}
+static const float L2_QMINI = 2.32192809f, L2_QMAXI = -3.32192809f, L2_GAMMA = -0.152003093f,
+                   L2_QOLDINIT = -13.2877124f;
+
 /* logarithms of the controller constants for the FP64 controller (rounded to double):
  * ln(1/qmax) = ln 0.1, ln(1/qmin) = ln 5, ln gamma = ln 0.9, ln qoldinit = ln 1e-4 */
 static const double LN_QMAXI = -0x1.26bb1bbb55516p+1, LN_QMINI = 0x1.9c041f7ed8d33p+0,
@@ -815,7 +863,8 @@ static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
   const float B1 = (float)(7.0 / 50.0), B2 = (float)(2.0 / 25.0), QMAXI = 0.1f, QMINI = 5.0f,
               GAM = (float)(9.0 / 10.0), QOLDINIT = (float)1.0e-4;
   R qold = qoldinit;
-  float qoldp = oracle_pow::ctrl_pow(QOLDINIT, B2);
+  /* qold^beta2, or in the single-precision modes beta2 * log2(qold) */
+  float qoldp = sizeof(R) == sizeof(float) ? B2 * L2_QOLDINIT : oracle_pow::ctrl_pow(QOLDINIT, B2);
   /* FP64 controller of the device canon (a->ctrl64): beta2 * log(qold) */
   double lqold = (2.0 / 25.0) * LN_QOLDINIT;
   const double dtmin = M::DTMIN_1F7 ? (double)1.0e-7f : 1.0e-14;
@@ -847,7 +896,17 @@ static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
       ++attempts;
       /* error norm: RMS of e ./ (abstol .+ max.(|uprev|, |u|) * reltol); the
        * device canon evaluates it in single precision unless abstol < 1e-30 */
-      if (P::DEV && a->abstol >= 1e-30) {
+      if (P::DEV && sizeof(R) == sizeof(float)) {
+        /* single-precision modes: EEst here holds the mean square a = EEst^2 */
+        const float fa = (float)a->abstol, fr = (float)a->reltol;
+        float acc = 0;
+        for (int d = 0; d < D; ++d) {
+          float m = jmax(std::fabs((float)up.hi[d]), std::fabs((float)un.hi[d]));
+          float r = (float)e[d] * rcp_nr(std::fma(m, fr, fa));
+          acc = (d == 0) ? r * r : std::fma(r, r, acc);
+        }
+        EEst = (R)(acc * (float)(1.0 / D));
+      } else if (P::DEV && a->abstol >= 1e-30) {
         const float fa = (float)a->abstol, fr = (float)a->reltol;
         float acc = 0;
         for (int d = 0; d < D; ++d) {
@@ -906,9 +965,14 @@ static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
         const double lE = !a->ctrl64 ? 0.0
                           : (E != E) ? E
                                      : log_dev(std::fmin(std::fmax(E, 0x1p-1022), 0x1.fffffffffffffp+1023));
-        const float q11 = a->ctrl64 ? 0.0f : oracle_pow::ctrl_pow(Ef, B1);
+        const bool f32 = sizeof(R) == sizeof(float);
+        const float l2E = !f32 ? 0.0f : (Ef != Ef) ? Ef : 0.5f * log2_nr(Ef);
+        const float q11 = (a->ctrl64 || f32) ? 0.0f : oracle_pow::ctrl_pow(Ef, B1);
         if (EEst > (R)1) {
-          if (a->ctrl64) {
+          if (f32) {
+            const float lf = jmin(L2_QMINI, std::fma(B1, l2E, -L2_GAMMA));
+            dt = dt * (T)exp2_nr(-lf);
+          } else if (a->ctrl64) {
             const double lf = jmin(LN_QMINI, std::fma(7.0 / 50.0, lE, -LN_GAMMA));
             dt = dt * (T)exp_dev(-lf);
           } else {
@@ -918,7 +982,12 @@ static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
           ++nrej;
         } else {
           T dtn;
-          if (a->ctrl64) {
+          if (f32) {
+            const float lq0 = (EEst == (R)0) ? L2_QMAXI : std::fma(B1, l2E, -qoldp);
+            const float lq = fmax_(L2_QMAXI, fmin_(L2_QMINI, lq0 - L2_GAMMA));
+            qoldp = B2 * jmax(l2E, L2_QOLDINIT);
+            dtn = dt * (T)exp2_nr(-lq);
+          } else if (a->ctrl64) {
             const double lq0 = (EEst == (R)0) ? LN_QMAXI : std::fma(7.0 / 50.0, lE, -lqold);
             const double lq = fmax_(LN_QMAXI, fmin_(LN_QMINI, lq0 - LN_GAMMA));
             lqold = (2.0 / 25.0) * jmax(lE, LN_QOLDINIT);
@@ -1490,6 +1559,10 @@ extern "C" int oracle_sde_solve(const oracle_sde_args* a) {
 extern "C" void oracle_philox(const uint32_t* c, const uint32_t* k, uint32_t* out) { philox(c, k, out); }
 extern "C" double oracle_log(double x) { return log_dev(x); }
 extern "C" double oracle_exp(double x) { return exp_dev(x); }
+/* the single-precision modes' reciprocal, log2 and exp2 of the device canon */
+extern "C" float oracle_rcp_nr(float x) { return rcp_nr(x); }
+extern "C" float oracle_log2_nr(float x) { return log2_nr(x); }
+extern "C" float oracle_exp2_nr(float x) { return exp2_nr(x); }
 /* the single-precision R3BP pull mu / r^(3/2) of the device canon */
 extern "C" float oracle_r3bp_pull_f(float mu, float r) { return r3bp_pull_dev(mu, r); }
 extern "C" void oracle_normal_pair(uint64_t seed, int64_t pair, int64_t idx, double* z0, double* z1) {

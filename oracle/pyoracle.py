@@ -83,6 +83,9 @@ def lib():
         _lib.oracle_exp.restype = ctypes.c_double
         _lib.oracle_r3bp_pull_f.argtypes = [ctypes.c_float, ctypes.c_float]
         _lib.oracle_r3bp_pull_f.restype = ctypes.c_float
+        for nm in ("oracle_rcp_nr", "oracle_log2_nr", "oracle_exp2_nr"):
+            getattr(_lib, nm).argtypes = [ctypes.c_float]
+            getattr(_lib, nm).restype = ctypes.c_float
         _lib.oracle_normal_pair.argtypes = [ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64,
                                             ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         _lib.oracle_normal_pair.restype = None
@@ -309,6 +312,11 @@ def log_dev(x):
 def exp_dev(x):
     """The device canon's double exponential (table-driven, |x| < 700)."""
     return lib().oracle_exp(float(x))
+
+
+def fp32_ctrl(fn, x):
+    """The single-precision modes' rcp_nr / log2_nr / exp2_nr of the device canon."""
+    return getattr(lib(), "oracle_" + fn)(float(x))
 
 
 def r3bp_pull_f(mu, r):

@@ -32,7 +32,10 @@
  *     reciprocal refined by one Newton step) and the polynomials that start at
  *     theta^2 multiply by one shared theta^2;
  *   - in single precision the restricted three-body pull mu / r^(3/2) is
- *     mu * y^3 with y from rsqrt_nr (no IEEE division or square root).
+ *     mu * y^3 with y from rsqrt_nr (no IEEE division or square root);
+ *   - in the single-precision modes the error norm and the controller use
+ *     rcp_nr, log2_nr and exp2_nr (no IEEE division, square root or branch;
+ *     the PI factors on log2 EEst).
  */
 #pragma once
 #include "ode_kparams.h"
@@ -246,6 +249,61 @@ __device__ __forceinline__ double exp_dev(double x) {
 #define CTRL64_LN_QMINI 0x1.9c041f7ed8d33p+0
 #define CTRL64_LN_GAMMA (-0x1.af8e8210a415dp-4)
 #define CTRL64_LN_QOLDINIT (-0x1.26bb1bbb55516p+3)
+
+/* Error norm and step-size controller of the single-precision modes, free of
+ * IEEE division, square root and branches (a lone lane's long trajectory
+ * waits on their slow-path checks).  rcp_nr: 1/d for a positive normal float
+ * from the bit-level seed 0x7ef311c7 (relative error below 1.3e-1) and three
+ * Newton steps y (2 - d y) (1.6e-2, 2.7e-4, then rounding).  log2_nr: the
+ * atanh series of ctrl_log2 with the quotient (m-1)/(m+1) taken by rcp_nr and
+ * the sqrt(2) fold by selects; finite for every non-NaN input (0 and
+ * subnormals come out near -127, which the controller's clamps absorb).
+ * exp2_nr: y = n + f by the 1.5 * 2^23 shifter, 2^f from the Taylor series of
+ * exp(f ln 2) to degree 7, scaled by 2^n through the exponent bits; for
+ * |y| < 126.  Every step an IEEE single operation or an explicit fma, so
+ * the oracle reproduces them bit for bit. */
+__device__ __forceinline__ float rcp_nr(float d) {
+  float y = __int_as_float(0x7ef311c7 - __float_as_int(d));
+  y = y * __fmaf_rn(-d, y, 2.0f);
+  y = y * __fmaf_rn(-d, y, 2.0f);
+  y = y * __fmaf_rn(-d, y, 2.0f);
+  return y;
+}
+__device__ __forceinline__ float log2_nr(float x) {
+  const int b = __float_as_int(x);
+  const int e0 = ((b >> 23) & 0xff) - 127;
+  const float m0 = __int_as_float((b & 0x007fffff) | 0x3f800000);
+  const bool fold = m0 > 1.41421354f;
+  const float m = fold ? 0.5f * m0 : m0;
+  const int e = fold ? e0 + 1 : e0;
+  const float s = (m - 1.0f) * rcp_nr(m + 1.0f);
+  const float s2 = s * s;
+  float poly = __fmaf_rn(s2, 0.0909090936f, 0.111111112f);
+  poly = __fmaf_rn(s2, poly, 0.142857149f);
+  poly = __fmaf_rn(s2, poly, 0.200000003f);
+  poly = __fmaf_rn(s2, poly, 0.333333343f);
+  poly = __fmaf_rn(s2, poly, 1.0f);
+  return __fmaf_rn(s * poly, 2.88539004f, (float)e);
+}
+__device__ __forceinline__ float exp2_nr(float y) {
+  const float t = y + 12582912.0f;
+  const int n = __float_as_int(t) - 0x4b400000;
+  const float f = y - (t - 12582912.0f);
+  const float z = f * 0.693147182f;
+  float p = __fmaf_rn(z, 1.98412701e-04f, 1.38888892e-03f); /* 1/7!, 1/6! */
+  p = __fmaf_rn(z, p, 8.33333377e-03f);
+  p = __fmaf_rn(z, p, 4.16666679e-02f);
+  p = __fmaf_rn(z, p, 0.166666672f);
+  p = __fmaf_rn(z, p, 0.5f);
+  p = __fmaf_rn(z, p, 1.0f);
+  p = __fmaf_rn(z, p, 1.0f);
+  return p * __int_as_float((n + 127) << 23);
+}
+/* log2 of the controller constants: 1/qmin = 5, 1/qmax = 0.1, gamma = 0.9, qoldinit = 1e-4 */
+#define CTRL32_L2_QMINI 2.32192809f
+#define CTRL32_L2_QMAXI (-3.32192809f)
+#define CTRL32_L2_GAMMA (-0.152003093f)
+#define CTRL32_L2_QOLDINIT (-13.2877124f)
 
 /* ------------------------------------------------------------------ precisions */
 struct PFP64 { typedef double R; typedef double T; enum { KAHAN = 0 }; };
@@ -973,7 +1031,9 @@ __device__ __forceinline__ void lane_load(const KParams& P, long long idx, Lane<
   }
   l.t = (T)P.t0;
   l.dt = (T)(P.dt0 ? P.dt0[idx] : P.dt);
-  l.qoldp = ctrl_pow((float)1.0e-4, (float)(2.0 / 25.0));
+  /* qold^beta2, or in the single-precision modes beta2 * log2(qold) */
+  l.qoldp = sizeof(R) == sizeof(float) ? (float)(2.0 / 25.0) * CTRL32_L2_QOLDINIT
+                                       : ctrl_pow((float)1.0e-4, (float)(2.0 / 25.0));
 #ifdef GBODE_CTRL64
   l.lqold = (2.0 / 25.0) * CTRL64_LN_QOLDINIT;
 #endif
@@ -1085,7 +1145,22 @@ __device__ __forceinline__ int adaptive_try(const KParams& P, Lane<PR, D, F, NK>
   float Ef;
   double EEst64 = 0.0; /* the double norm, when computed */
   bool reject, is_zero;
-  if (sizeof(R) == sizeof(float) || !P.norm_fp64) {
+  if (sizeof(R) == sizeof(float)) {
+    /* single-precision modes: the mean square a = EEst^2 without division or
+     * square root (rcp_nr; the controller below works on log2 EEst =
+     * log2(a) / 2, and a > 1 exactly when EEst > 1) */
+    const float abstol = (float)P.abstol, reltol = (float)P.reltol;
+    float acc = 0.f;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const float m = jmax(fabsf((float)l.uh[d]), fabsf((float)nh[d]));
+      const float r = (float)e[d] * rcp_nr(__fmaf_rn(m, reltol, abstol));
+      acc = (d == 0) ? r * r : __fmaf_rn(r, r, acc);
+    }
+    Ef = acc * (float)(1.0 / D);
+    reject = Ef > 1.0f;
+    is_zero = Ef == 0.0f;
+  } else if (!P.norm_fp64) {
     const float abstol = (float)P.abstol, reltol = (float)P.reltol;
     float acc = 0.f;
 #pragma unroll
@@ -1114,7 +1189,7 @@ __device__ __forceinline__ int adaptive_try(const KParams& P, Lane<PR, D, F, NK>
   }
   if (Ef != Ef) l.nan_seen = true;
 #ifdef GBODE_CTRL64
-  {
+  if (sizeof(R) == sizeof(double)) {
     /* FP64 controller: the factors of the reference's controller in double,
      * in the log domain.  le = log(EEst); reject: dt /= min(1/qmin,
      * EEst^beta1/gamma); accept: q = EEst^beta1 / qold^beta2 (1/qmax when
@@ -1146,6 +1221,32 @@ __device__ __forceinline__ int adaptive_try(const KParams& P, Lane<PR, D, F, NK>
     return TRY_ACCEPTED;
   }
 #endif
+  if (sizeof(R) == sizeof(float)) {
+    /* single-precision modes: the PI factors on log2 EEst, one exp2_nr per
+     * attempt; l.qoldp holds beta2 * log2(qold).  The clamps are those of
+     * the double controller below, in the log domain. */
+    const float B1F = (float)(7.0 / 50.0), B2F = (float)(2.0 / 25.0);
+    const float l2E = (Ef != Ef) ? Ef : 0.5f * log2_nr(Ef);
+    if (reject) {
+      const float lf = jmin(CTRL32_L2_QMINI, __fmaf_rn(B1F, l2E, -CTRL32_L2_GAMMA));
+      l.dt = l.dt * (T)exp2_nr(-lf);
+      l.nrej += 1;
+      return TRY_REJECTED;
+    }
+    const float lq0 = is_zero ? CTRL32_L2_QMAXI : __fmaf_rn(B1F, l2E, -l.qoldp);
+    const float lq = fm_max(CTRL32_L2_QMAXI, fm_min(CTRL32_L2_QMINI, lq0 - CTRL32_L2_GAMMA));
+    l.qoldp = B2F * jmax(l2E, CTRL32_L2_QOLDINIT);
+    const T dtold = l.dt;
+    const T dtn = l.dt * (T)exp2_nr(-lq);
+    l.dt = absmin(dtn, rest);
+    const T told = l.t;
+    l.t = tnext;
+    if (l.nacc == 0) l.dt_first = (double)dtold;
+    l.nacc += 1;
+    acc_out.told = told;
+    acc_out.dtold = dtold;
+    return TRY_ACCEPTED;
+  }
   const float B1 = (float)(7.0 / 50.0), B2 = (float)(2.0 / 25.0), GAM = (float)(9.0 / 10.0);
   const float QMAXI = 0.1f, QMINI = 5.0f, QOLDINIT = (float)1.0e-4;
   const float q11 = ctrl_pow(Ef, B1);

@@ -540,3 +540,26 @@ def test_single_precision_r3bp_pull_accuracy(po):
     want = float(mu) / r.astype(np.float64) ** 1.5
     ulp = np.spacing(want.astype(np.float32)).astype(np.float64)
     assert (np.abs(got.astype(np.float64) - want) / ulp).max() <= 8
+
+
+def test_single_precision_controller_functions(po):
+    """The division-free reciprocal, log2 and exp2 of the single-precision
+    modes' error norm and controller: 1/d within 2 ulp, log2 within 3e-7
+    absolute plus one ulp of the result (an error d in log2 EEst moves the
+    factor EEst^beta by beta d ln 2 relative, so absolute accuracy is what
+    counts), 2^y within 3 ulp on the controller's range; log2 of 0 and of
+    subnormals finite and below -120."""
+    rng = np.random.default_rng(9)
+    d = (10.0 ** rng.uniform(-30, 30, 3000)).astype(np.float32)
+    got = np.array([po.fp32_ctrl("rcp_nr", v) for v in d], dtype=np.float32).astype(np.float64)
+    want = 1.0 / d.astype(np.float64)
+    assert (np.abs(got - want) / np.spacing(want.astype(np.float32))).max() <= 2
+    x = np.concatenate([(10.0 ** rng.uniform(-37, 37, 3000)), rng.uniform(0.5, 2.0, 2000)]).astype(np.float32)
+    got = np.array([po.fp32_ctrl("log2_nr", v) for v in x], dtype=np.float64)
+    want = np.log2(x.astype(np.float64))
+    assert (np.abs(got - want) <= 3e-7 + np.spacing(np.abs(want).astype(np.float32))).all()
+    assert -130 < po.fp32_ctrl("log2_nr", 0.0) < -120 and -150 < po.fp32_ctrl("log2_nr", 1e-40) < -120
+    y = rng.uniform(-20, 20, 3000).astype(np.float32)
+    got = np.array([po.fp32_ctrl("exp2_nr", v) for v in y], dtype=np.float64)
+    want = 2.0 ** y.astype(np.float64)
+    assert (np.abs(got - want) / np.spacing(want.astype(np.float32))).max() <= 3
