@@ -613,6 +613,25 @@ def main():
     dev_err = np.abs(uf_measured - uf_plain).max(0) / scale
     dev_err = dev_err[np.isfinite(dev_err)] if np.isfinite(dev_err).any() else np.zeros(1)
 
+    # the cost model's second use: seeding each trajectory's first dt with its prediction (opt-in, changes the
+    # step sequences): time, attempts and deviation from the plain kernel's results, then back to ordering only
+    seeded = None
+    if schedule == "learned" and rank == 0 and fit_report and "train_fit_ms" in fit_report:
+        try:
+            h.learn_fit(ta, {"seed_dt0": 1})
+            sk, s_att, _, _ = timed("learned", max(1, min(args.steps, 3)), 1)
+            s_steps = max(1, min(args.steps, 3))
+            uf_seeded = outs["u_final"].cpu().numpy()
+            s_err = np.abs(uf_seeded - uf_plain).max(0) / scale
+            s_err = s_err[np.isfinite(s_err)]
+            seeded = {"ms_per_step": sum(sk) / len(sk), "speedup_vs_ordering_only": step_ms / (sum(sk) / len(sk)),
+                      "attempts_per_step": s_att / s_steps, "attempts_ordering_only": att / args.steps,
+                      "vs_plain_frac_within_10x": float(np.mean(s_err <= 10)),
+                      "note": "results change (other step sequences); chaotic trajectories move beyond the "
+                              "error scale in both roundings"}
+        finally:
+            h.learn_fit(ta)
+
     # end to end through the C ABI with pinned host buffers
     hu0 = torch.from_numpy(u0).pin_memory()
     hp = torch.from_numpy(p).pin_memory()
@@ -688,6 +707,8 @@ def main():
                 "fit_over_solve": fit_report["train_fit_ms"] / step_ms}
     if args.config != 4:
         line["parity_vs_ref"] = parity_vs_ref(cfg, u0, p, sv, res_sample)
+    if seeded is not None:
+        line["dt0_seeded"] = seeded
     if ctl64 is not None:
         if args.config != 4:
             ctl64["parity_vs_ref"] = parity_vs_ref(cfg, u0, p, sv, ctl64_sample)
