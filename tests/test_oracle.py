@@ -563,3 +563,20 @@ def test_single_precision_controller_functions(po):
     got = np.array([po.fp32_ctrl("exp2_nr", v) for v in y], dtype=np.float64)
     want = 2.0 ** y.astype(np.float64)
     assert (np.abs(got - want) / np.spacing(want.astype(np.float32))).max() <= 3
+
+
+def test_bench_parity_block_against_reference_rounding(po):
+    """bench.py's parity_vs_ref on a small sample: the oracle's device canon
+    stands in for the GPU (the GPU reproduces it bit for bit), and the block
+    reports the fractions and extremes it promises."""
+    import bench
+    cfg = dict(bench.CONFIGS[2])
+    u0, p = cfg["inputs"](300, 5)
+    sv = np.linspace(*cfg["tspan"], cfg["nsave"])
+    dev = po.solve("ATsit5", "lorenz", u0, p, cfg["tspan"], cfg["dt"], rounding="device", abstol=cfg["abstol"],
+                   reltol=cfg["reltol"], saveat=sv, nthreads=4)
+    out = bench.parity_vs_ref(cfg, u0, p, sv, {"u_final": dev["u_final"], "naccept": dev["naccept"],
+                                                "us": dev["us"]}, m=300)
+    assert out["trajectories"] == 300
+    assert out["final_frac_within_10x"] == 1.0 and out["saveat_frac_within_10x"] == 1.0
+    assert out["naccept_max_abs_diff"] <= 1 and 0 <= out["final_max_in_error_scale"] < 10
