@@ -30,6 +30,29 @@ def fitted(pkg):
 def test_fit_quality(fitted):
     assert fitted.loss_last < 0.5 * fitted.loss_first
     assert fitted.r2_attempts > 0.8
+    assert fitted.train_ctas in (8, 16) and 0 < fitted.train_kernel_ms < fitted.train_fit_ms
+
+
+def test_training_is_deterministic_and_narrow_models_train(pkg):
+    """The training cluster reduces every gradient in a fixed order, so two fits
+    with the same seed give bit-identical predictions; a model narrower than
+    the kernels' 64 units (zero-padded inside the kernel) trains as well."""
+    u0, p = lorenz_inputs(8192, seed=111)
+    h = pkg._handle(0)
+    args = pkg.make_args(pkg.GPUSimpleATsit5(), 0, u0, p, (0.0, 10.0), 0.1, 1e-8, 1e-6, None, False, "fp64",
+                         "plain", 0)
+    preds = []
+    for _ in range(2):
+        h.learn_fit(args, {"epochs": 10})
+        preds.append(h.learn_predict(args, 8192))
+    assert np.array_equal(preds[0][0], preds[1][0]) and np.array_equal(preds[0][1], preds[1][1])
+    u1, p1 = lorenz_inputs(65536, seed=112)
+    args1 = pkg.make_args(pkg.GPUSimpleATsit5(), 0, u1, p1, (0.0, 10.0), 0.1, 1e-8, 1e-6, None, False, "fp64",
+                          "plain", 0)
+    rep = h.learn_fit(args1, {"hidden": 24})
+    assert rep.r2_attempts > 0.8, rep.r2_attempts
+    tr = lorenz_inputs(65536, seed=101)
+    pkg.learn_fit(ens(pkg, *tr), pkg.GPUSimpleATsit5(), 65536, **KW)  # the module's model back for later tests
 
 
 def warp_cost(att, order):
