@@ -95,3 +95,28 @@ def test_no_violation_every_step_and_user_output(pkg, checked):
     ts, us = np.empty(o.total), np.empty((o.total, 3))
     o.ts, o.us, o.capacity = ts.ctypes.data, us.ctypes.data, o.total
     assert checked.solve_everystep(args, o) == L.OK, checked.error()
+
+
+@pytest.mark.parametrize("alg", ["ATsit5", "AVern7"])
+def test_no_violation_trajectory_major_layout_and_fp64_controller(pkg, checked, alg):
+    """The trajectory-major output layout and the FP64 step-size controller in
+    bounds-check mode (staged and two-queue staged kernels): no violation,
+    every trajectory started once, results equal to the unchecked kernels'."""
+    L = pkg._lib
+    n = 3000
+    u0, p = lorenz_inputs(n, seed=104)
+    sv = np.linspace(0, 2, 17)
+    algo = getattr(pkg, "GPUSimple" + alg)()
+    res = []
+    for h in (checked, pkg._handle(0)):
+        a = pkg.make_args(algo, 0, u0, p, (0.0, 2.0), 0.1, 1e-8, 1e-6, sv, False, "fp64", "persistent", 0,
+                          layout="traj", controller="fp64")
+        out = {"us": np.empty((n, len(sv), 3)), "u_final": np.empty((3, n)), "naccept": np.empty(n, dtype=np.int32)}
+        o = L.SolveOut()
+        for k, v in out.items():
+            setattr(o, k, v.ctypes.data)
+        rc = h.solve_raw(a, o, L.SolveStats())
+        assert rc in (L.OK, L.ETRAJ), h.error()
+        res.append(out)
+    for k in res[0]:
+        assert np.array_equal(res[0][k], res[1][k], equal_nan=True), k
