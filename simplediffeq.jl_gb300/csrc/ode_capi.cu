@@ -1188,7 +1188,7 @@ int solve_chunked(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_
   const int64_t n = a->n;
   const int D = a->dim, NP = a->nparams;
   /* at most kMaxChunks chunks (each chunk boundary costs a partly filled GPU
-   * while the chunk's last trajectories finish: 16 chunks of workload 5 cost
+   * while the chunk's last trajectories finish: 16 chunks of the 4,194,304-trajectory Kuramoto-12 ensemble cost
    * 7.5%, 4 chunks 1.4%); the last chunk half the size of the others, so that
    * the output copy nothing overlaps is short */
   const int64_t nchunks = std::min<int64_t>(kMaxChunks, (n + kChunk - 1) / kChunk);

@@ -3,7 +3,7 @@ oracle on the same seeded inputs.
 
 Against the oracle's DEVICE rounding mode the results must be bit-identical
 (same operations in the same order, IEEE-754 on both sides).  Against the
-oracle's REF mode (the reference's own rounding) the benchmark spec's tolerances
+oracle's REF mode (the reference's own rounding) the parity tolerances
 apply: fixed-step FP64 final states within 1e-12 relative, adaptive FP64 final
 states within 10x the solver's error scale with accepted-step counts within
 +/-1.

@@ -117,9 +117,9 @@ def test_julia_ranges(po):
     assert len(g) == 1001 and g[-1] == 100.0
 
 
-def test_rounding_modes_agree_within_northstar_tolerance(po):
+def test_rounding_modes_agree_within_parity_tolerance(po):
     """The device rounding canon (fused multiply-adds, single-precision step-size
-    factor) stays within the benchmark spec's tolerance of the reference's rounding:
+    factor) stays within the parity tolerance of the reference's rounding:
     accepted-step counts within +/-1 and final states within 10x the error
     scale abstol + reltol*|u| (chaotic trajectories amplify rounding, so the
     bar is 99.9% of trajectories)."""
@@ -395,7 +395,7 @@ def test_simple_em_rounding_modes_and_grid(po):
 
 @pytest.mark.parametrize("alg,rhs,tol,tspan", [("AVern7", "vanderpol", 1e-8, (0, 20)),
                                                ("ATsit5", "kuramoto", 1e-6, (0, 50))])
-def test_device_canon_within_northstar_tolerance_of_reference_rounding(po, alg, rhs, tol, tspan):
+def test_device_canon_within_parity_tolerance_of_reference_rounding(po, alg, rhs, tol, tspan):
     """The adaptive workloads: the device canon (which the GPU reproduces bit
     for bit) against the reference's rounding, final states within 10x the
     error scale abstol + reltol*|u| for >= 99.9% of trajectories and accepted
