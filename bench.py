@@ -602,7 +602,7 @@ def main():
     # the same schedule with the FP64 step-size controller (kernel compiled at run time, untuned): its cost,
     # and its parity with the reference's rounding below
     ctl64 = None
-    if not fixed and cfg["precision"] == "fp64" and rank == 0:
+    if not fixed and cfg["precision"] == "fp64":  # every rank: timed() holds barriers
         ck, _, _, _ = timed(schedule, max(1, min(args.steps, 3)), 1, controller="fp64")
         ctl64 = {"ms_per_step": sum(ck) / len(ck), "value": n / (sum(ck) / len(ck) * 1e-3),
                  "cost_vs_fp32_controller": (sum(ck) / len(ck)) / step_ms}
@@ -616,7 +616,7 @@ def main():
     # the cost model's second use: seeding each trajectory's first dt with its prediction (opt-in, changes the
     # step sequences): time, attempts and deviation from the plain kernel's results, then back to ordering only
     seeded = None
-    if schedule == "learned" and rank == 0 and fit_report and "train_fit_ms" in fit_report:
+    if schedule == "learned" and fit_report and "train_fit_ms" in fit_report:
         try:
             h.learn_fit(ta, {"seed_dt0": 1})
             sk, s_att, _, _ = timed("learned", max(1, min(args.steps, 3)), 1)
