@@ -33,6 +33,11 @@ in FP32 with Kahan-compensated state, with its full-FP64 variant on a sample;
 5: ATsit5 Kuramoto-12 with the order parameter reduced in the kernel;
 6: SimpleEM stochastic Lorenz).  The default is the 1M adaptive Lorenz
 workload above (config 2).
+
+workloads  (default run on one GPU without --n) each other workload measured by a
+           child process `bench.py --config N --brief` after the headline
+           line's own measurements, its line condensed into this key;
+           `--workloads none` skips them, `--workloads 3,5` picks some.
 """
 import argparse
 import json
@@ -298,6 +303,45 @@ def parity_vs_ref(cfg, u0, p, sv, res, m=4096):
     return out
 
 
+WORKLOAD_TIMEOUT_S = 420
+
+
+def condense(sub):
+    """A workload's line without what the headline line already says (metric,
+    unit, step counts) and without the autotuner's per-variant table."""
+    drop = {"metric", "unit", "n_gpus", "higher_is_better", "scaling", "vs_baseline", "data"}
+    out = {k: v for k, v in sub.items() if k not in drop}
+    if isinstance(out.get("autotune"), dict):
+        out["autotune"] = {k: v for k, v in out["autotune"].items() if k != "table"}
+    return out
+
+
+def run_workloads(args):
+    """Each other workload measured by a child process (`bench.py --config N
+    --brief`, the same timing rules: warm-up, L2 flush, CUDA events, clock
+    samples) one after another on this GPU; this process's own solves have
+    ended.  A failed or timed-out child is recorded as such."""
+    which = sorted(c for c in CONFIGS if c != 2) if args.workloads == "auto" else \
+        [int(x) for x in args.workloads.split(",") if x.strip()]
+    out = {}
+    for c in which:
+        cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--config", str(c), "--steps", str(min(args.steps, 3)),
+               "--warmup", "3", "--brief", "--workloads", "none",
+               "--cpu-seconds", "3"]
+        t0 = time.perf_counter()
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=WORKLOAD_TIMEOUT_S)
+            lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+            if r.returncode == 0 and lines:
+                out[str(c)] = condense(json.loads(lines[-1]))
+            else:
+                out[str(c)] = {"error": "exit %d: %s" % (r.returncode, (r.stderr or r.stdout)[-400:])}
+        except subprocess.TimeoutExpired:
+            out[str(c)] = {"error": "timed out after %d s" % WORKLOAD_TIMEOUT_S}
+        out[str(c)]["wall_s"] = time.perf_counter() - t0
+    return out
+
+
 def probe_rates(device=0, iters=2000):
     """Measured lane-operation rates of the arithmetic pipes (bench_probe.cu,
     built by __graft_entry__.build() into _build/libbench_probe.so)."""
@@ -434,7 +478,7 @@ def run_sde(args, cfg, rank, world, local):
         def solve_first(m):
             po.sde_solve(cfg["sde"], np.ascontiguousarray(u0[:, :m]), np.ascontiguousarray(p[:, :m]),
                          cfg["tspan"], cfg["dt"], seed=1234, rounding="ref", save_everystep=False, nthreads=threads)
-        solved, el, m = sized_sample(solve_first, n, CPU_SECONDS)
+        solved, el, m = sized_sample(solve_first, n, args.cpu_seconds)
         line["cpu_baseline"] = {"value": solved / el, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": "the first %d trajectories%s, SimpleEM restated in C++ with the same "
                                           "counter-based normals, one std::thread per core"
@@ -459,6 +503,14 @@ def main():
     ap.add_argument("--tune-sample", type=int, default=262144, help="trajectories the autotuner times each variant on")
     ap.add_argument("--layout", default="traj", choices=["soa", "traj"],
                     help="saveat output layout: [npoints][dim][n] (soa) or [n][npoints][dim] (traj)")
+    ap.add_argument("--cpu-seconds", type=float, default=CPU_SECONDS,
+                    help="length of the timed CPU-baseline sample")
+    ap.add_argument("--brief", action="store_true",
+                    help="skip the dt0-seeding leg, and the identity-order and FP64-controller legs of "
+                         "workloads whose solve takes over a second")
+    ap.add_argument("--workloads", default="auto",
+                    help="other workloads measured after the default one on a single GPU: 'auto' (all), "
+                         "'none', or a comma list of config numbers")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -586,8 +638,9 @@ def main():
     value = n * world / (step_ms * 1e-3)
 
     # the same persistent staged kernel in identity order: what the trained network's ordering adds
+    long_solve = args.brief and step_ms > 1000.0
     unsorted_ms = None
-    if schedule == "learned":
+    if schedule == "learned" and not long_solve:
         uk, _, _, _ = timed("persistent", max(1, min(args.steps, 3)), 1)
         unsorted_ms = sum(uk) / len(uk)
 
@@ -602,7 +655,7 @@ def main():
     # the same schedule with the FP64 step-size controller (kernel compiled at run time, untuned): its cost,
     # and its parity with the reference's rounding below
     ctl64 = None
-    if not fixed and cfg["precision"] == "fp64":  # every rank: timed() holds barriers
+    if not fixed and cfg["precision"] == "fp64" and not long_solve:  # every rank: timed() holds barriers
         ck, _, _, _ = timed(schedule, max(1, min(args.steps, 3)), 1, controller="fp64")
         ctl64 = {"ms_per_step": sum(ck) / len(ck), "value": n / (sum(ck) / len(ck) * 1e-3),
                  "cost_vs_fp32_controller": (sum(ck) / len(ck)) / step_ms}
@@ -616,7 +669,7 @@ def main():
     # the cost model's second use: seeding each trajectory's first dt with its prediction (opt-in, changes the
     # step sequences): time, attempts and deviation from the plain kernel's results, then back to ordering only
     seeded = None
-    if schedule == "learned" and fit_report and "train_fit_ms" in fit_report:
+    if schedule == "learned" and fit_report and "train_fit_ms" in fit_report and not args.brief:
         try:
             h.learn_fit(ta, {"seed_dt0": 1})
             sk, s_att, _, _ = timed("learned", max(1, min(args.steps, 3)), 1)
@@ -744,7 +797,9 @@ def main():
                                 "error_vs_fp64_oracle_1e-14": {"max": float(e64.max()),
                                                                "median": float(np.median(e64))}}
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(cfg)
+        line["cpu_baseline"] = cpu_baseline(cfg, args.cpu_seconds)
+    if args.config == 2 and world == 1 and not args.n and args.workloads != "none":
+        line["workloads"] = run_workloads(args)
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
