@@ -506,7 +506,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=CPU_SECONDS,
                     help="length of the timed CPU-baseline sample")
     ap.add_argument("--brief", action="store_true",
-                    help="skip the dt0-seeding leg, and the identity-order and FP64-controller legs of "
+                    help="skip the dt0-seeding leg, and the identity-order and single-precision-controller legs of "
                          "workloads whose solve takes over a second")
     ap.add_argument("--workloads", default="auto",
                     help="other workloads measured after the default one on a single GPU: 'auto' (all), "
@@ -554,7 +554,7 @@ def main():
                                  dtype=torch.float64, device=dev)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
 
-    def args_for(schedule, memory, u0p, pp, uu=u0, ppp=p, controller="fp32"):
+    def args_for(schedule, memory, u0p, pp, uu=u0, ppp=p, controller="ds"):
         a = pkg.make_args(alg, L.RHS[cfg["rhs"]], uu, ppp, cfg["tspan"], cfg["dt"], cfg["abstol"], cfg["reltol"],
                           sv, False, cfg["precision"], schedule, 0, memory=memory, output=cfg["output"],
                           controller=controller, layout=args.layout)
@@ -597,13 +597,13 @@ def main():
         except L.GB300ODEError as e:
             tune = {"unavailable": str(e)}
 
-    def device_step(sched, controller="fp32"):
+    def device_step(sched, controller="ds"):
         a = args_for(sched, L.MEM_DEVICE, du0.data_ptr(), dp.data_ptr(), controller=controller)
         st = L.SolveStats()
         h.check(h.solve_raw(a, out_dev(), st), allow=(L.ETRAJ,))
         return st
 
-    def timed(sched, steps, warmup, controller="fp32"):
+    def timed(sched, steps, warmup, controller="ds"):
         for _ in range(warmup):
             device_step(sched, controller)
         kms, att, sav, launches = [], 0, 0, 0
@@ -652,14 +652,18 @@ def main():
         plain_ms = step_ms
     uf_plain = outs["u_final"].cpu().numpy()
 
-    # the same schedule with the FP64 step-size controller (kernel compiled at run time, untuned): its cost,
-    # and its parity with the reference's rounding below
-    ctl64 = None
+    # the same schedule with the single-precision error norm and controller (kernel compiled at run time and
+    # autotuned like the default's): what the default double-single arithmetic costs, and the parity it buys
+    ctl32 = None
     if not fixed and cfg["precision"] == "fp64" and not long_solve:  # every rank: timed() holds barriers
-        ck, _, _, _ = timed(schedule, max(1, min(args.steps, 3)), 1, controller="fp64")
-        ctl64 = {"ms_per_step": sum(ck) / len(ck), "value": n / (sum(ck) / len(ck) * 1e-3),
-                 "cost_vs_fp32_controller": (sum(ck) / len(ck)) / step_ms}
-        ctl64_sample = {"u_final": outs["u_final"][:, :m_par].cpu().numpy(),
+        if tune is not None and "unavailable" not in tune:
+            # the same launch-shape search as the default's, so the two legs compare arithmetic only
+            h.autotune(args_for(schedule, L.MEM_DEVICE, du0.data_ptr(), dp.data_ptr(), controller="fp32"),
+                       args.tune_sample)
+        ck, _, _, _ = timed(schedule, max(1, min(args.steps, 3)), 1, controller="fp32")
+        ctl32 = {"ms_per_step": sum(ck) / len(ck), "value": n / (sum(ck) / len(ck) * 1e-3),
+                 "default_cost": step_ms / (sum(ck) / len(ck))}
+        ctl32_sample = {"u_final": outs["u_final"][:, :m_par].cpu().numpy(),
                         "naccept": outs["naccept"][:m_par].cpu().numpy(),
                         "us": us_sample()}
     scale = cfg["abstol"] + cfg["reltol"] * np.abs(uf_plain).max(0)
@@ -762,10 +766,10 @@ def main():
         line["parity_vs_ref"] = parity_vs_ref(cfg, u0, p, sv, res_sample)
     if seeded is not None:
         line["dt0_seeded"] = seeded
-    if ctl64 is not None:
+    if ctl32 is not None:
         if args.config != 4:
-            ctl64["parity_vs_ref"] = parity_vs_ref(cfg, u0, p, sv, ctl64_sample)
-        line["fp64_controller"] = ctl64
+            ctl32["parity_vs_ref"] = parity_vs_ref(cfg, u0, p, sv, ctl32_sample)
+        line["fp32_controller"] = ctl32
     if tune is not None:
         line["autotune"] = tune
     if args.config == 4:

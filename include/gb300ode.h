@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define ODE_ABI_VERSION 4
+#define ODE_ABI_VERSION 5
 
 /* status codes */
 enum {
@@ -114,14 +114,22 @@ enum {
                           sector are solved at different times under the persistent schedules) */
 };
 
-/* arithmetic of the adaptive step-size controller (ode_solve_args.controller) */
+/* arithmetic of the error norm and step-size controller of adaptive FP64 solves
+ * (ode_solve_args.controller); single-precision solves always use their own
+ * single-precision norm and controller */
 enum {
-  ODE_CTRL_FP32 = 0, /* the factor q = EEst^beta1 / qold^beta2, its clamps and reciprocal in single
-                        precision (deterministic power function): the fastest; step sizes follow the
-                        reference's to about 2^-24 relative */
-  ODE_CTRL_FP64 = 1  /* the same factors in double precision (table-driven log and exp, a few ulps):
-                        step sizes follow the reference's to about 2^-50 relative, so accepted-step
-                        sequences match the reference's rounding far more often; FP64 precision only */
+  ODE_CTRL_DS = 0,   /* default: the norm EEst and the factor q = EEst^beta1 / qold^beta2 with its
+                        clamps in double-single arithmetic (pairs of floats, about 48 bits, on the
+                        single-precision pipe; table-driven log and exp; doubles split into pairs by
+                        integer operations): step sizes follow the reference's to about 2^-44
+                        relative, and an attempt takes two double operations (dt times the factor)
+                        where the single-precision norm converts each of its terms to single, a
+                        conversion that occupies the double-precision pipe on this GPU */
+  ODE_CTRL_FP64 = 1, /* the factor q in double precision (table-driven log and exp) on a
+                        single-precision norm, whose 2^-24 rounding (times beta1) bounds how closely
+                        step sizes follow the reference's; FP64 precision only */
+  ODE_CTRL_FP32 = 2  /* the norm and the factor q in single precision (deterministic power
+                        function): step sizes follow the reference's to about 2^-24 relative */
 };
 
 /* per-trajectory return codes */

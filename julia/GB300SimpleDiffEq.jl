@@ -26,7 +26,7 @@ using SimpleDiffEq, SciMLBase, StaticArrays
 export compile_rhs, compile_output, compile_sde, learn_fit!, everystep_solve
 
 const lib = get(ENV, "GB300ODE_LIB", "libgb300ode.so")
-const ABI_VERSION = 4
+const ABI_VERSION = 5
 
 # ----------------------------------------------------------------------------- C structs
 
@@ -176,7 +176,7 @@ const AdaptiveAlg = Union{GPUSimpleATsit5, GPUSimpleAVern7, GPUSimpleAVern9}
 const RHS_BUILTIN = Dict(:lorenz => 0, :vanderpol => 1, :r3bp => 2, :kuramoto => 3, :linear => 4)
 const PRECISION = Dict(:fp64 => 0, :fp32 => 1, :fp32_kahan => 2)
 const SCHEDULE = Dict(:plain => 0, :persistent => 1, :learned => 2)
-const CONTROLLER = Dict(:fp32 => 0, :fp64 => 1)
+const CONTROLLER = Dict(:ds => 0, :fp64 => 1, :fp32 => 2)
 const SDE_BUILTIN = Dict(:gbm => 0, :ou => 1, :lorenz => 2, :mult => 3)
 const ODE_OK, ODE_ETRAJ, ODE_ESMALL = 0, -6, -8
 const RET_DTMIN, RET_MAXITERS = 1, 2
@@ -298,7 +298,7 @@ end
 # the saved series come back trajectory-major (ODE_LAYOUT_TRAJ): a Julia W x npts x n array, us[:, j, i]
 # the j-th point of trajectory i, as the reference's per-trajectory sol.u
 function solve_args(alg, h, rhs, u0, p, D, P, n, tspan, dt, abstol, reltol, sv, save_everystep, precision,
-                    schedule, maxiters, output; controller::Symbol = :fp32)
+                    schedule, maxiters, output; controller::Symbol = :ds)
     SolveArgs(ALG_ID[typeof(alg)], rhs_id(h, rhs, D, P), PRECISION[precision], SCHEDULE[schedule], n, D, P,
               tspan[1], tspan[2], dt, abstol, reltol, isempty(sv) ? C_NULL : pointer(sv), length(sv),
               save_everystep, 0, maxiters, pointer(u0), pointer(p), C_NULL, C_NULL, output_id(output), 1,
@@ -312,19 +312,20 @@ retcode_of(r) = r == RET_MAXITERS ? SciMLBase.ReturnCode.MaxIters : SciMLBase.Re
 """
     solve(ep::EnsembleProblem, alg::GPUSimple*; trajectories, rhs, dt = 0.1, abstol = 1e-6,
           reltol = 1e-3, saveat = nothing, save_everystep = true, precision = :fp64,
-          schedule = :persistent, maxiters = 0, output = :state, controller = :fp32, device = 0)
+          schedule = :persistent, maxiters = 0, output = :state, controller = :ds, device = 0)
 
 The whole ensemble in one call of `ode_ensemble_solve` (`ode_ensemble_solve_everystep`
 for the adaptive algorithms' default every-step output).  `rhs`: `:lorenz`,
 `:vanderpol`, `:r3bp`, `:kuramoto`, `:linear`, an id from `compile_rhs`, or the
-CUDA C++ body itself.  `controller = :fp64` runs the step-size controller in
-double precision (ODE_CTRL_FP64).  Keyword defaults are the reference's;
+CUDA C++ body itself.  `controller` picks the error norm and step-size
+controller arithmetic of adaptive FP64 solves: `:ds` (default, double-single,
+ODE_CTRL_DS), `:fp64` (ODE_CTRL_FP64) or `:fp32` (ODE_CTRL_FP32).  Keyword defaults are the reference's;
 `dt < dtmin` raises the reference's `error("dt<dtmin")`.
 """
 function SciMLBase.solve(ep::EnsembleProblem, alg::GPUSimpleAlg; trajectories::Integer, rhs,
                          dt = 0.1, abstol = 1.0e-6, reltol = 1.0e-3, saveat = nothing,
                          save_everystep = true, precision::Symbol = :fp64, schedule::Symbol = :persistent,
-                         maxiters::Integer = 0, output = :state, controller::Symbol = :fp32, device::Integer = 0,
+                         maxiters::Integer = 0, output = :state, controller::Symbol = :ds, device::Integer = 0,
                          kwargs...)
     prob = ep.prob
     @assert !SciMLBase.isinplace(prob)   # as every GPUSimple solve

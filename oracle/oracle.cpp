@@ -42,6 +42,7 @@
 #include "../simplediffeq.jl_gb300/csrc/tableaus.h"
 #include "../simplediffeq.jl_gb300/csrc/log_table.h"
 #include "../simplediffeq.jl_gb300/csrc/exp_table.h"
+#include "../simplediffeq.jl_gb300/csrc/ds_table.h"
 
 #include <algorithm>
 #include <cmath>
@@ -839,6 +840,145 @@ static inline float exp2_nr(float y) {
 static const float L2_QMINI = 2.32192809f, L2_QMAXI = -3.32192809f, L2_GAMMA = -0.152003093f,
                    L2_QOLDINIT = -13.2877124f;
 
+/* Double-single error norm and controller of the FP64 solves (kernels:
+ * ds_* in ode_solver.cuh, tables from ds_table.h).  A pair (h, l) stands for
+ * h + l; the operations are Knuth's two-sum, Dekker's fast two-sum and the
+ * fma product error, each step one IEEE single operation. */
+struct DS { float h, l; };
+static inline DS ds_two_sum(float a, float b) {
+  const float s = a + b, bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+static inline DS ds_fast(float a, float b) {
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+static inline DS ds_add(DS x, DS y) {
+  const DS s = ds_two_sum(x.h, y.h);
+  return ds_fast(s.h, s.l + (x.l + y.l));
+}
+static inline DS ds_neg(DS x) { return {-x.h, -x.l}; }
+static inline DS ds_mul(DS x, DS y) {
+  const float p = x.h * y.h;
+  return ds_fast(p, std::fma(x.h, y.l, std::fma(x.l, y.h, std::fma(x.h, y.h, -p))));
+}
+static inline DS ds_sqr(DS x) {
+  const float p = x.h * x.h;
+  return ds_fast(p, std::fma(x.h + x.h, x.l, std::fma(x.h, x.h, -p)));
+}
+static inline DS ds_div(DS x, DS y) {
+  if (y.h == 0.0f) return {x.h * INFINITY, 0.0f};
+  const float ry = rcp_nr(y.h);
+  const float q1 = x.h * ry;
+  const float p = q1 * y.h, pe = std::fma(q1, y.h, -p);
+  const float rem = (((x.h - p) - pe) + x.l) - q1 * y.l;
+  return ds_fast(q1, rem * ry);
+}
+static inline bool ds_gt(DS x, DS y) { return x.h > y.h || (x.h == y.h && x.l > y.l); }
+static inline DS ds_min(DS x, DS y) { return ds_gt(y, x) ? x : y; }
+static inline DS ds_max(DS x, DS y) { return ds_gt(y, x) ? y : x; }
+/* h: x with the 29 low fraction bits cleared; l: those bits as an integer
+ * rounded to single, times 2^(e-52) (0 outside 2^-74 <= |x| < 2^128) */
+/* an integer 0 <= i < 2^23 as a single: bits of 2^23 + i, minus 2^23 */
+static inline float ds_small_int(int32_t i) { return bits_f(0x4b000000 | i) - 8388608.0f; }
+/* h: x's sign, exponent and top 23 fraction bits repacked as a single
+ * (2^-126 <= |x| < 2^128; +-0 below, +-inf above, NaN for NaN) */
+static inline DS ds_split(double x) {
+  int64_t b;
+  std::memcpy(&b, &x, 8);
+  const int eb = (int)((b >> 52) & 0x7ff);
+  const uint32_t sign = (uint32_t)((uint64_t)b >> 32) & 0x80000000u;
+  const uint32_t frac = (uint32_t)((b >> 29) & 0x7fffff);
+  const uint32_t hb = eb >= 897 && eb <= 1150 ? sign | ((uint32_t)(eb - 896) << 23) | frac
+                      : eb < 897 ? sign
+                      : (eb == 2047 && (b & 0xfffffffffffffLL)) ? 0x7fc00000u | sign
+                                                                : 0x7f800000u | sign;
+  float hf;
+  std::memcpy(&hf, &hb, 4);
+  float l = 0.0f;
+  if (eb >= 949 && eb <= 1150) {
+    const int32_t low = (int32_t)(b & 0x1fffffff);
+    const float lf = std::fma(ds_small_int(low >> 23), 8388608.0f, ds_small_int(low & 0x7fffff));
+    const float mag = lf * bits_f((eb - 948) << 23);
+    l = b < 0 ? -mag : mag;
+  }
+  return {hf, l};
+}
+static inline int64_t dbits_abs(double x) {
+  int64_t b;
+  std::memcpy(&b, &x, 8);
+  return b & 0x7fffffffffffffffLL;
+}
+static inline double ds_absmax(double u, double v) {
+  const int64_t au = dbits_abs(u), av = dbits_abs(v);
+  const int64_t m = au >= av ? au : av;
+  double r;
+  std::memcpy(&r, &m, 8);
+  return r;
+}
+/* ln(h + l), 2^-120 <= h <= 2^126: h = 2^E m, r = fma(m, c_j, -1) (exact),
+ * ln(1+r) = r - r^2/2 + r^3 (1/3 - r/4 + r^2/5 - r^3/6 + r^4/7), E ln2 in
+ * three parts, + l/h */
+static DS ds_log(DS a) {
+  const int32_t b = fbits(a.h);
+  const int j = (b >> 16) & 127;
+  const float m = bits_f((b & 0x007fffff) | 0x3f800000);
+  const float r = std::fma(m, kDsLogTab[j][0], -1.0f);
+  const float p = r * r, pe = std::fma(r, r, -p);
+  float t = std::fma(r, 0x1.24924ap-3f, -0x1.555556p-3f);
+  t = std::fma(r, t, 0x1.99999ap-3f);
+  t = std::fma(r, t, -0.25f);
+  t = std::fma(r, t, 0x1.555556p-2f);
+  const float tail = t * (r * p);
+  const DS l1 = ds_fast(r, -0.5f * p);
+  const DS lp = {l1.h, l1.l + (tail - 0.5f * pe)};
+  const float fE = ds_small_int((b >> 23) & 0xff) - 127.0f;
+  const float eb = fE * GBODE_DS_LN2_B, ebe = std::fma(fE, GBODE_DS_LN2_B, -eb);
+  const DS e0 = ds_fast(fE * GBODE_DS_LN2_A, eb);
+  const DS eln2 = ds_fast(e0.h, e0.l + (ebe + fE * GBODE_DS_LN2_C));
+  const DS s = ds_add(ds_add(eln2, DS{kDsLogTab[j][1], kDsLogTab[j][2]}), lp);
+  return ds_fast(s.h, s.l + a.l * rcp_nr(a.h));
+}
+/* exp(h + l), |x| < 2.7: k = rint(x 64/ln2), r = x - k ln2/64 (three parts),
+ * exp(r) - 1 to degree 5, times 2^((k&63)/64) from the table and 2^(k>>6) */
+static DS ds_exp(DS x) {
+  if (x.h != x.h) return x;
+  const float sh = x.h * GBODE_DS_EXP_INV_L + 12582912.0f;
+  const int k = fbits(sh) - 0x4b400000;
+  const float kf = sh - 12582912.0f;
+  const float r0 = std::fma(-kf, GBODE_DS_EXP_L_A, x.h);
+  const float pb = kf * GBODE_DS_EXP_L_B, pbe = std::fma(kf, GBODE_DS_EXP_L_B, -pb);
+  const DS rr = ds_two_sum(r0, -pb);
+  const DS r = ds_fast(rr.h, rr.l + ((x.l - pbe) - kf * GBODE_DS_EXP_L_C));
+  const float p = r.h * r.h, pe = std::fma(r.h, r.h, -p);
+  float t = std::fma(r.h, 0x1.111112p-7f, 0x1.555556p-5f);
+  t = std::fma(r.h, t, 0x1.555556p-3f);
+  const float tail = t * (r.h * p);
+  const DS e1 = ds_fast(r.h, 0.5f * p);
+  const DS em1 = ds_fast(e1.h, e1.l + ((r.l + 0.5f * pe) + (r.h * r.l + tail)));
+  const int j = k & 63;
+  const float th = kDsExpTab[j][0], tl = kDsExpTab[j][1];
+  const float pp = th * em1.h, ppe = std::fma(th, em1.h, -pp);
+  const DS v0 = ds_fast(th, pp);
+  const DS v = ds_fast(v0.h, v0.l + (tl + (ppe + std::fma(th, em1.l, tl * em1.h))));
+  const float sc = bits_f(((k >> 6) + 127) << 23);
+  return {v.h * sc, v.l * sc};
+}
+/* a single as a double by its bits: exact for normal singles, +-0 for
+ * zeros and subnormals */
+static inline double f2d_bits(float f) {
+  const uint32_t u = (uint32_t)fbits(f);
+  const uint32_t e = (u >> 23) & 0xff;
+  const uint64_t s = (uint64_t)(u & 0x80000000u) << 32;
+  uint64_t r = s;
+  if (e != 0) r = s | ((e == 255 ? 0x7ffULL : (uint64_t)(e + 896)) << 52) | ((uint64_t)(u & 0x7fffff) << 29);
+  double d;
+  std::memcpy(&d, &r, 8);
+  return d;
+}
+/* d (h + l) as fma(d, l, d h) */
+static inline double ds_scale(double d, DS x) { return std::fma(d, f2d_bits(x.l), d * f2d_bits(x.h)); }
+
 /* logarithms of the controller constants for the FP64 controller (rounded to double):
  * ln(1/qmax) = ln 0.1, ln(1/qmin) = ln 5, ln gamma = ln 0.9, ln qoldinit = ln 1e-4 */
 static const double LN_QMAXI = -0x1.26bb1bbb55516p+1, LN_QMINI = 0x1.9c041f7ed8d33p+0,
@@ -865,8 +1005,16 @@ static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
   R qold = qoldinit;
   /* qold^beta2, or in the single-precision modes beta2 * log2(qold) */
   float qoldp = sizeof(R) == sizeof(float) ? B2 * L2_QOLDINIT : oracle_pow::ctrl_pow(QOLDINIT, B2);
-  /* FP64 controller of the device canon (a->ctrl64): beta2 * log(qold) */
+  /* FP64 controller of the device canon (a->ctrl == 1): beta2 * log(qold) */
   double lqold = (2.0 / 25.0) * LN_QOLDINIT;
+  /* double-single norm and controller (a->ctrl == 0, FP64 solves): beta2 * log(qold) */
+  const bool f32 = sizeof(R) == sizeof(float);
+  const bool c64 = !f32 && a->ctrl == 1, cds = !f32 && a->ctrl == 0;
+  const DS DB1 = {GBODE_DS_B1_H, GBODE_DS_B1_L}, DB2 = {GBODE_DS_B2_H, GBODE_DS_B2_L};
+  const DS LQMAXI = {GBODE_DS_LN_QMAXI_H, GBODE_DS_LN_QMAXI_L}, LQMINI = {GBODE_DS_LN_QMINI_H, GBODE_DS_LN_QMINI_L};
+  const DS MLGAMMA = {-GBODE_DS_LN_GAMMA_H, -GBODE_DS_LN_GAMMA_L};
+  const DS LQOLDINIT = {GBODE_DS_LN_QOLDINIT_H, GBODE_DS_LN_QOLDINIT_L};
+  DS lqds = ds_mul(DB2, LQOLDINIT);
   const double dtmin = M::DTMIN_1F7 ? (double)1.0e-7f : 1.0e-14;
 
   int64_t cur = 0;
@@ -896,7 +1044,57 @@ static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
       ++attempts;
       /* error norm: RMS of e ./ (abstol .+ max.(|uprev|, |u|) * reltol); the
        * device canon evaluates it in single precision unless abstol < 1e-30 */
-      if (P::DEV && sizeof(R) == sizeof(float)) {
+      DS le_ds = {0.0f, 0.0f};
+      bool ds_zero = false;
+      if (P::DEV && cds) {
+        /* double-single: the norm's terms split into single pairs (the
+         * double one when abstol < 1e-30), le = ln(EEst); EEst here only
+         * drives the attempt loop (2: reject, 0: accept) */
+        bool reject;
+        if (a->abstol >= 1e-30) {
+          const DS dabs = ds_split(a->abstol), drel = ds_split(a->reltol);
+          DS acc = {0.0f, 0.0f};
+          bool nan_in = false;
+          ds_zero = true;
+          for (int d = 0; d < D; ++d) {
+            const int64_t eb = dbits_abs((double)e[d]);
+            const double mx = ds_absmax((double)up.hi[d], (double)un.hi[d]);
+            ds_zero = ds_zero && eb == 0;
+            nan_in = nan_in || eb > 0x7ff0000000000000LL || dbits_abs(mx) > 0x7ff0000000000000LL;
+            const DS r = ds_div(ds_split((double)e[d]), ds_add(ds_mul(ds_split(mx), drel), dabs));
+            acc = d == 0 ? ds_sqr(r) : ds_add(acc, ds_sqr(r));
+          }
+          const DS av = ds_mul(acc, DS{(float)(1.0 / D), (float)(1.0 / D - (double)(float)(1.0 / D))});
+          if (nan_in) {
+            saw_nan = true;
+            reject = false;
+            le_ds = {NAN, 0.0f};
+          } else {
+            const bool huge = !(av.h <= 0x1p126f);
+            reject = huge || ds_gt(av, DS{1.0f, 0.0f});
+            const DS ac = huge ? DS{0x1p126f, 0.0f} : av.h < 0x1p-120f ? DS{0x1p-120f, 0.0f} : av;
+            const DS lg = ds_log(ac);
+            le_ds = {0.5f * lg.h, 0.5f * lg.l};
+          }
+        } else {
+          double acc = 0;
+          for (int d = 0; d < D; ++d) {
+            const double m = jmax(std::fabs((double)up.hi[d]), std::fabs((double)un.hi[d]));
+            const double r = (double)e[d] / std::fma(m, a->reltol, a->abstol);
+            acc = (d == 0) ? r * r : std::fma(r, r, acc);
+          }
+          const double E64 = std::sqrt(acc / (double)D);
+          ds_zero = E64 == 0.0;
+          reject = E64 > 1.0;
+          if (E64 != E64) {
+            saw_nan = true;
+            le_ds = {(float)E64, 0.0f};
+          } else {
+            le_ds = ds_log(ds_split(std::fmin(std::fmax(E64, 0x1p-60), 0x1p63)));
+          }
+        }
+        EEst = reject ? (R)2 : (R)0;
+      } else if (P::DEV && sizeof(R) == sizeof(float)) {
         /* single-precision modes: EEst here holds the mean square a = EEst^2 */
         const float fa = (float)a->abstol, fr = (float)a->reltol;
         float acc = 0;
@@ -962,17 +1160,19 @@ static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
         /* FP64 controller: the reference's factors in double, on logarithms
          * (log_dev, exp_dev), in the kernels' order of operations */
         const double E = (double)EEst;
-        const double lE = !a->ctrl64 ? 0.0
+        const double lE = !c64 ? 0.0
                           : (E != E) ? E
                                      : log_dev(std::fmin(std::fmax(E, 0x1p-1022), 0x1.fffffffffffffp+1023));
-        const bool f32 = sizeof(R) == sizeof(float);
         const float l2E = !f32 ? 0.0f : (Ef != Ef) ? Ef : 0.5f * log2_nr(Ef);
-        const float q11 = (a->ctrl64 || f32) ? 0.0f : oracle_pow::ctrl_pow(Ef, B1);
+        const float q11 = (c64 || cds || f32) ? 0.0f : oracle_pow::ctrl_pow(Ef, B1);
         if (EEst > (R)1) {
           if (f32) {
             const float lf = jmin(L2_QMINI, std::fma(B1, l2E, -L2_GAMMA));
             dt = dt * (T)exp2_nr(-lf);
-          } else if (a->ctrl64) {
+          } else if (cds) {
+            const DS lf = ds_min(LQMINI, ds_add(ds_mul(DB1, le_ds), MLGAMMA));
+            dt = (T)ds_scale((double)dt, ds_exp(ds_neg(lf)));
+          } else if (c64) {
             const double lf = jmin(LN_QMINI, std::fma(7.0 / 50.0, lE, -LN_GAMMA));
             dt = dt * (T)exp_dev(-lf);
           } else {
@@ -987,7 +1187,12 @@ static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
             const float lq = fmax_(L2_QMAXI, fmin_(L2_QMINI, lq0 - L2_GAMMA));
             qoldp = B2 * jmax(l2E, L2_QOLDINIT);
             dtn = dt * (T)exp2_nr(-lq);
-          } else if (a->ctrl64) {
+          } else if (cds) {
+            const DS lq0 = ds_zero ? LQMAXI : ds_add(ds_mul(DB1, le_ds), ds_neg(lqds));
+            const DS lq = ds_max(LQMAXI, ds_min(LQMINI, ds_add(lq0, MLGAMMA)));
+            lqds = ds_mul(DB2, ds_max(le_ds, LQOLDINIT));
+            dtn = (T)ds_scale((double)dt, ds_exp(ds_neg(lq)));
+          } else if (c64) {
             const double lq0 = (EEst == (R)0) ? LN_QMAXI : std::fma(7.0 / 50.0, lE, -lqold);
             const double lq = fmax_(LN_QMAXI, fmin_(LN_QMINI, lq0 - LN_GAMMA));
             lqold = (2.0 / 25.0) * jmax(lE, LN_QOLDINIT);
@@ -1561,6 +1766,18 @@ extern "C" double oracle_log(double x) { return log_dev(x); }
 extern "C" double oracle_exp(double x) { return exp_dev(x); }
 /* the single-precision modes' reciprocal, log2 and exp2 of the device canon */
 extern "C" float oracle_rcp_nr(float x) { return rcp_nr(x); }
+extern "C" void oracle_ds_log(float h, float l, float* out) {
+  const DS r = ds_log(DS{h, l});
+  out[0] = r.h; out[1] = r.l;
+}
+extern "C" void oracle_ds_exp(float h, float l, float* out) {
+  const DS r = ds_exp(DS{h, l});
+  out[0] = r.h; out[1] = r.l;
+}
+extern "C" void oracle_ds_split(double x, float* out) {
+  const DS r = ds_split(x);
+  out[0] = r.h; out[1] = r.l;
+}
 extern "C" float oracle_log2_nr(float x) { return log2_nr(x); }
 extern "C" float oracle_exp2_nr(float x) { return exp2_nr(x); }
 /* the single-precision R3BP pull mu / r^(3/2) of the device canon */

@@ -49,7 +49,8 @@ typedef struct {
   const double* dt0;     /* optional per-trajectory initial dt [n] */
   int nthreads;
   int output;            /* 0: state at saveat points; 1: Kuramoto order parameter r(t) of it */
-  int ctrl64;            /* DEVICE rounding: 1 for the FP64 step-size controller (ODE_CTRL_FP64) */
+  int ctrl;              /* DEVICE rounding, FP64 adaptive solves: error norm and step-size controller, as
+                            ODE_CTRL_*: 0 double-single, 1 FP64 factors (single norm), 2 single precision */
 } oracle_args;
 
 typedef struct {

@@ -25,6 +25,8 @@ FIXED = {"RK4", "Tsit5", "Vern7", "Vern9", "SimpleTsit5", "Euler"}
 RHS = {"lorenz": 0, "vanderpol": 1, "r3bp": 2, "kuramoto": 3, "linear": 4}
 PREC = {"fp64": 0, "fp32": 1, "fp32_kahan": 2}
 ROUND = {"ref": 0, "device": 1}
+# error norm and step-size controller of the FP64 adaptive solves (DEVICE rounding), as ODE_CTRL_*
+CTRL = {"ds": 0, "fp64": 1, "fp32": 2}
 
 
 class _Args(ctypes.Structure):
@@ -35,7 +37,7 @@ class _Args(ctypes.Structure):
                 ("saveat", ctypes.c_void_p), ("nsave", ctypes.c_int64), ("save_everystep", ctypes.c_int),
                 ("grid", ctypes.c_void_p), ("ngrid", ctypes.c_int64), ("maxiters", ctypes.c_int64),
                 ("u0", ctypes.c_void_p), ("p", ctypes.c_void_p), ("dt0", ctypes.c_void_p),
-                ("nthreads", ctypes.c_int), ("output", ctypes.c_int), ("ctrl64", ctypes.c_int)]
+                ("nthreads", ctypes.c_int), ("output", ctypes.c_int), ("ctrl", ctypes.c_int)]
 
 
 class _Out(ctypes.Structure):
@@ -83,6 +85,11 @@ def lib():
         _lib.oracle_exp.restype = ctypes.c_double
         _lib.oracle_r3bp_pull_f.argtypes = [ctypes.c_float, ctypes.c_float]
         _lib.oracle_r3bp_pull_f.restype = ctypes.c_float
+        for nm in ("oracle_ds_log", "oracle_ds_exp"):
+            getattr(_lib, nm).argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_void_p]
+            getattr(_lib, nm).restype = None
+        _lib.oracle_ds_split.argtypes = [ctypes.c_double, ctypes.c_void_p]
+        _lib.oracle_ds_split.restype = None
         for nm in ("oracle_rcp_nr", "oracle_log2_nr", "oracle_exp2_nr"):
             getattr(_lib, nm).argtypes = [ctypes.c_float]
             getattr(_lib, nm).restype = ctypes.c_float
@@ -216,7 +223,7 @@ def _ptr(a):
 
 def solve(alg, rhs, u0, p, tspan, dt, precision="fp64", rounding="ref", abstol=1e-6, reltol=1e-3,
           saveat=None, save_everystep=False, maxiters=0, dt0=None, nthreads=1, grid=None, output="state",
-          controller="fp32"):
+          controller="ds"):
     """Solve n trajectories.  u0: (dim, n) float64, p: (nparams, n) float64.
     Returns a dict of numpy arrays (us is (npoints, dim, n))."""
     u0 = np.ascontiguousarray(u0, dtype=np.float64)
@@ -249,7 +256,7 @@ def solve(alg, rhs, u0, p, tspan, dt, precision="fp64", rounding="ref", abstol=1
     args = _Args(ALG[alg], RHS[rhs], PREC[precision], ROUND[rounding], n, dim, nparams, t0, tf, float(dt),
                  float(abstol), float(reltol), _ptr(sv), 0 if sv is None else len(sv), int(bool(save_everystep)),
                  _ptr(grid), 0 if grid is None else len(grid), int(maxiters), _ptr(u0), _ptr(p), _ptr(d0),
-                 int(nthreads), 1 if output == "kuramoto_r" else 0, 1 if controller == "fp64" else 0)
+                 int(nthreads), 1 if output == "kuramoto_r" else 0, CTRL[controller])
     o = _Out(_ptr(out["us"]), _ptr(out["u_final"]), _ptr(out["t_final"]), _ptr(out["retcode"]),
              _ptr(out["naccept"]), _ptr(out["nreject"]), _ptr(out["dt_first"]), None, None, None)
     rc = lib().oracle_solve(ctypes.byref(args), ctypes.byref(o))
@@ -317,6 +324,18 @@ def exp_dev(x):
 def fp32_ctrl(fn, x):
     """The single-precision modes' rcp_nr / log2_nr / exp2_nr of the device canon."""
     return getattr(lib(), "oracle_" + fn)(float(x))
+
+
+def ds(fn, h, l=0.0):
+    """The double-single norm's and controller's ds_log / ds_exp of the device
+    canon on the pair (h, l) (singles), or ds_split of the double h; returns
+    the result pair as two float32 values."""
+    out = np.zeros(2, dtype=np.float32)
+    if fn == "split":
+        lib().oracle_ds_split(float(h), out.ctypes.data)
+    else:
+        getattr(lib(), "oracle_ds_" + fn)(float(h), float(l), out.ctypes.data)
+    return out[0], out[1]
 
 
 def r3bp_pull_f(mu, r):

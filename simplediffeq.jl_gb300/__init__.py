@@ -302,7 +302,7 @@ def _stack(eprob, trajectories):
 
 
 def make_args(alg, f_id, u0s, ps, tspan, dt, abstol, reltol, saveat, save_everystep, precision, schedule,
-              maxiters, memory=_lib.MEM_HOST, dt0=None, output="state", layout="soa", controller="fp32"):
+              maxiters, memory=_lib.MEM_HOST, dt0=None, output="state", layout="soa", controller="ds"):
     a = _lib.SolveArgs()
     a.alg = _lib.ALG[alg.name]
     a.rhs = f_id
@@ -327,7 +327,7 @@ def make_args(alg, f_id, u0s, ps, tspan, dt, abstol, reltol, saveat, save_everys
 
 def solve(prob, alg, trajectories=None, dt=0.1, abstol=1e-6, reltol=1e-3, saveat=None, save_everystep=None,
           precision="fp64", schedule="persistent", maxiters=0, device=0, dt0=None, throw=True, output="state",
-          layout="soa", controller="fp32", **kwargs):
+          layout="soa", controller="ds", **kwargs):
     """Solve an EnsembleProblem (or a single ODEProblem as an ensemble of one).
 
     Unknown keyword arguments are accepted and ignored, as the reference's
@@ -339,8 +339,11 @@ def solve(prob, alg, trajectories=None, dt=0.1, abstol=1e-6, reltol=1e-3, saveat
     GPUSimpleEuler ignore ``saveat`` as the reference does.  ``layout="traj"``
     has the library write each trajectory's saved series contiguously
     (ODE_LAYOUT_TRAJ); ``sol.us`` is then a (npoints, width, n) view of that
-    (n, npoints, width) array, ``sol.us_traj``.  ``controller="fp64"`` runs the
-    adaptive step-size controller in double precision (ODE_CTRL_FP64)."""
+    (n, npoints, width) array, ``sol.us_traj``.  ``controller`` picks the error
+    norm and step-size controller arithmetic of adaptive FP64 solves: "ds"
+    (default, double-single: step sizes follow the reference's to about
+    2^-44), "fp64" (double factors on a single-precision norm) or "fp32"
+    (single precision throughout), ODE_CTRL_DS / _FP64 / _FP32."""
     single = isinstance(prob, (ODEProblem, SDEProblem))
     eprob = EnsembleProblem(prob) if single else prob
     if isinstance(eprob.prob, SDEProblem) or isinstance(alg, SimpleEM):

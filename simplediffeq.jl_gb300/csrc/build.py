@@ -93,7 +93,8 @@ def gen_sources():
     parts = ["/* generated by build.py: device headers for NVRTC */\n"]
     for fname, var in (("ode_solver.cuh", "kSrc_ode_solver_cuh"), ("ode_kparams.h", "kSrc_ode_kparams_h"),
                        ("tableaus.h", "kSrc_tableaus_h"), ("sde_solver.cuh", "kSrc_sde_solver_cuh"),
-                       ("log_table.h", "kSrc_log_table_h"), ("exp_table.h", "kSrc_exp_table_h")):
+                       ("log_table.h", "kSrc_log_table_h"), ("exp_table.h", "kSrc_exp_table_h"),
+                       ("ds_table.h", "kSrc_ds_table_h")):
         text = open(os.path.join(HERE, fname)).read()
         assert ")GBSRC\"" not in text
         parts.append('static const char* %s = R"GBSRC(%s)GBSRC";\n' % (var, text))
@@ -104,6 +105,7 @@ def gen_sources():
         block, ring = SHAPES.get(g, (128, 12288))
         lines = ["/* generated by build.py: ahead-of-time kernels, group %s */\n" % g,
                  "#define GBODE_BLOCK %d\n#define GBODE_STAGE_BYTES %d\n" % (block, ring),
+                 "#define GBODE_CTRL_DS 1 /* the default error norm and controller (ODE_CTRL_DS) */\n",
                  '#include "ode_solver.cuh"\n']
         for i, (alg, kind, rhs, dim, prec) in enumerate(items):
             t = "RHS_%s_%d" % (g, i)
@@ -152,7 +154,8 @@ def build(verbose=False, jobs=None):
     tus = gen_sources()
     os.makedirs(LIB, exist_ok=True)
     headers = [os.path.join(HERE, f) for f in ("ode_solver.cuh", "ode_kparams.h", "tableaus.h", "ode_host.h",
-                                               "jlrange.h", "sde_solver.cuh", "log_table.h", "exp_table.h")] + [
+                                               "jlrange.h", "sde_solver.cuh", "log_table.h", "exp_table.h",
+                                               "ds_table.h")] + [
         os.path.join(PKG, "..", "include", "gb300ode.h")]
     host_tus = [os.path.join(HERE, f) for f in ("ode_capi.cu", "learn.cu", "noalloc.cu", "sde_capi.cu")]
     gen = [os.path.join(BUILD, "aot_registry.inc"), os.path.join(BUILD, "embedded_src.inc")]

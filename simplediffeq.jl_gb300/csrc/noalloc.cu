@@ -37,6 +37,7 @@
 #include <mutex>
 
 #include "../../include/gb300ode.h"
+#define GBODE_CTRL_DS 1 /* the library's default error norm and controller */
 #include "ode_solver.cuh"
 
 namespace {
@@ -99,8 +100,9 @@ extern "C" int ode_ensemble_solve_noalloc(const ode_solve_args* a, ode_solve_out
     return say(err, errlen, ODE_ENOTSUP, "the allocation-free solve stores the state at saveat points only");
   if (a->schedule != ODE_SCHED_PERSISTENT)
     return say(err, errlen, ODE_ENOTSUP, "the allocation-free solve runs the persistent schedule only");
-  if (a->controller != ODE_CTRL_FP32)
-    return say(err, errlen, ODE_ENOTSUP, "the allocation-free solve runs the single-precision step-size controller");
+  if (a->controller != ODE_CTRL_DS)
+    return say(err, errlen, ODE_ENOTSUP, "the allocation-free solve runs the default (double-single) error norm "
+                                         "and step-size controller");
   if (a->layout != ODE_LAYOUT_SOA && a->layout != ODE_LAYOUT_TRAJ)
     return say(err, errlen, ODE_EINVAL, "unknown output layout");
   if (a->memory != ODE_MEM_DEVICE)
@@ -155,6 +157,8 @@ extern "C" int ode_ensemble_solve_noalloc(const ode_solve_args* a, ode_solve_out
   kp.nparams = 3;
   kp.maxiters = a->maxiters > 0 ? a->maxiters : kDefaultMaxIters;
   kp.norm_fp64 = a->abstol < 1e-30 ? 1 : 0;  /* the same rule as ode_ensemble_solve */
+  gbode::ds_split_host(a->abstol, kp.tol_ds);
+  gbode::ds_split_host(a->reltol, kp.tol_ds + 2);
   kp.us = o->us;
   if (a->layout == ODE_LAYOUT_TRAJ) {
     kp.us_sj = 3;

@@ -355,14 +355,19 @@ int output_width(ode_handle* h, const ode_solve_args* a) {
   return a->dim;
 }
 
-/* the FP64 step-size controller applies to the adaptive kernels */
-bool ctrl64(const ode_solve_args* a) { return a->controller == ODE_CTRL_FP64 && !is_fixed(a->alg); }
+/* The norm/controller variant a kernel is compiled with: the controller
+ * choice applies to adaptive FP64 kernels, every other kernel is the same
+ * whichever is asked (and is built as the default, ODE_CTRL_DS). */
+int ctrl_variant(const ode_solve_args* a) {
+  if (is_fixed(a->alg) || a->precision != ODE_FP64) return ODE_CTRL_DS;
+  return a->controller;
+}
 
 std::string kernel_key(ode_handle* h, const ode_solve_args* a, int sched) {
   char b[160];
   snprintf(b, sizeof b, "%s|%s|%d|%d|%s|%d%s%s", alg_name(a->alg), kernel_kind(h, a, sched), a->rhs, a->dim,
            prec_name(a->precision), a->output >= ODE_OUTPUT_USER ? a->output : 0, h->bounds_check ? "|chk" : "",
-           ctrl64(a) ? "|c64" : "");
+           ctrl_variant(a) == ODE_CTRL_FP64 ? "|c64" : ctrl_variant(a) == ODE_CTRL_FP32 ? "|c32" : "");
   return b;
 }
 
@@ -370,7 +375,8 @@ std::string kernel_key(ode_handle* h, const ode_solve_args* a, int sched) {
  * dim, schedule kind). */
 std::string jit_source(ode_handle* h, const ode_solve_args* a, int sched) {
   std::string src;
-  if (ctrl64(a)) src += "#define GBODE_CTRL64 1\n";
+  if (ctrl_variant(a) == ODE_CTRL_FP64) src += "#define GBODE_CTRL64 1\n";
+  if (ctrl_variant(a) == ODE_CTRL_DS) src += "#define GBODE_CTRL_DS 1\n";
   if (a->output >= ODE_OUTPUT_USER) {
     /* the output function goes before the solver header, whose store_point calls it */
     const UserOutput& u = h->outputs[a->output - ODE_OUTPUT_USER];
@@ -415,10 +421,10 @@ int nvrtc_cubin(const std::string& src, const std::vector<std::string>& extra_op
   }
   nvrtcProgram prog;
   const char* hdrs[] = {kSrc_ode_solver_cuh, kSrc_ode_kparams_h, kSrc_tableaus_h, kSrc_sde_solver_cuh, kSrc_log_table_h,
-                        kSrc_exp_table_h};
+                        kSrc_exp_table_h, kSrc_ds_table_h};
   const char* names[] = {"ode_solver.cuh", "ode_kparams.h", "tableaus.h", "sde_solver.cuh", "log_table.h",
-                         "exp_table.h"};
-  nvrtcResult r = g_nvrtc.create(&prog, src.c_str(), "gbode_jit.cu", 6, hdrs, names);
+                         "exp_table.h", "ds_table.h"};
+  nvrtcResult r = g_nvrtc.create(&prog, src.c_str(), "gbode_jit.cu", 7, hdrs, names);
   if (r != NVRTC_SUCCESS) {
     *err = std::string("nvrtcCreateProgram: ") + g_nvrtc.errstr(r);
     return ODE_ENVRTC;
@@ -503,7 +509,8 @@ int get_kernel(ode_handle* h, const ode_solve_args* a, int sched, CUfunction* fn
   }
   const char* kind = kernel_kind(h, a, sched);
   for (const AotEntry& e : kAotEntries) {
-    if (!h->bounds_check && !ctrl64(a) && a->output < ODE_OUTPUT_USER && e.alg == a->alg && e.rhs == a->rhs &&
+    if (!h->bounds_check && ctrl_variant(a) == ODE_CTRL_DS && a->output < ODE_OUTPUT_USER && e.alg == a->alg &&
+        e.rhs == a->rhs &&
         e.dim == a->dim &&
         e.precision == a->precision && std::strcmp(e.kind, kind) == 0) {
       cudaFunction_t f;
@@ -839,7 +846,7 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
   if (a->schedule < ODE_SCHED_PLAIN || a->schedule > ODE_SCHED_LEARNED) return fail(h, ODE_EINVAL, "unknown schedule");
   if (a->memory != ODE_MEM_HOST && a->memory != ODE_MEM_DEVICE) return fail(h, ODE_EINVAL, "unknown memory kind");
   if (a->layout != ODE_LAYOUT_SOA && a->layout != ODE_LAYOUT_TRAJ) return fail(h, ODE_EINVAL, "unknown output layout");
-  if (a->controller != ODE_CTRL_FP32 && a->controller != ODE_CTRL_FP64)
+  if (a->controller != ODE_CTRL_DS && a->controller != ODE_CTRL_FP64 && a->controller != ODE_CTRL_FP32)
     return fail(h, ODE_EINVAL, "unknown step-size controller");
   if (a->controller == ODE_CTRL_FP64 && a->precision != ODE_FP64)
     return fail(h, ODE_ENOTSUP, "the FP64 step-size controller applies to FP64 solves");
@@ -908,6 +915,8 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
   kp.nparams = NP;
   kp.maxiters = a->maxiters > 0 ? a->maxiters : kDefaultMaxIters;
   kp.norm_fp64 = a->abstol < 1e-30 ? 1 : 0;
+  ds_split_host(a->abstol, kp.tol_ds);
+  ds_split_host(a->reltol, kp.tol_ds + 2);
   kp.output = a->output;
   {
     const long long W = output_width(h, a);
@@ -1421,7 +1430,7 @@ int ode_ensemble_solve_everystep(ode_handle* h, const ode_solve_args* a, ode_eve
     return fail(h, ODE_EINVAL, "every-step output takes no saveat and the state output");
   if (a->memory != ODE_MEM_HOST && a->memory != ODE_MEM_DEVICE) return fail(h, ODE_EINVAL, "unknown memory kind");
   if (a->layout != ODE_LAYOUT_SOA && a->layout != ODE_LAYOUT_TRAJ) return fail(h, ODE_EINVAL, "unknown output layout");
-  if (a->controller != ODE_CTRL_FP32 && a->controller != ODE_CTRL_FP64)
+  if (a->controller != ODE_CTRL_DS && a->controller != ODE_CTRL_FP64 && a->controller != ODE_CTRL_FP32)
     return fail(h, ODE_EINVAL, "unknown step-size controller");
   if (a->controller == ODE_CTRL_FP64 && a->precision != ODE_FP64)
     return fail(h, ODE_ENOTSUP, "the FP64 step-size controller applies to FP64 solves");

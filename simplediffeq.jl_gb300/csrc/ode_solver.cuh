@@ -140,6 +140,12 @@ __device__ __forceinline__ double recip(double x) {
 }
 __device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
 
+/* Small integers as singles without a conversion instruction (integer-to-
+ * float conversions issue on this GPU's FP64 pipe): the bits of 2^23 + i
+ * for 0 <= i < 2^23, minus 2^23, exact; small_int_f(i + 127) - 127 for an
+ * exponent i >= -127. */
+__device__ __forceinline__ float small_int_f(int i) { return __int_as_float(0x4b000000 | i) - 8388608.0f; }
+
 /* Single-precision x^b for the step-size controller (x >= 0 or NaN).
  * log2 from the atanh series of the reduced mantissa, 2^y from the Taylor
  * series of exp on [-ln2/2, ln2/2]; every step is one IEEE single operation,
@@ -159,7 +165,7 @@ __device__ __forceinline__ float ctrl_log2(float x) {
   poly = __fmaf_rn(s2, poly, 0.333333343f);
   poly = __fmaf_rn(s2, poly, 1.0f);
   float atanh_s = s * poly;
-  return __fmaf_rn(atanh_s, 2.88539004f, (float)e);
+  return __fmaf_rn(atanh_s, 2.88539004f, small_int_f(e + 151) - 151.0f); /* e >= -151 */
 }
 __device__ __forceinline__ float ctrl_exp2(float y) {
   if (y > 128.0f) return __int_as_float(0x7f800000);
@@ -283,7 +289,7 @@ __device__ __forceinline__ float log2_nr(float x) {
   poly = __fmaf_rn(s2, poly, 0.200000003f);
   poly = __fmaf_rn(s2, poly, 0.333333343f);
   poly = __fmaf_rn(s2, poly, 1.0f);
-  return __fmaf_rn(s * poly, 2.88539004f, (float)e);
+  return __fmaf_rn(s * poly, 2.88539004f, small_int_f(e + 127) - 127.0f);
 }
 __device__ __forceinline__ float exp2_nr(float y) {
   const float t = y + 12582912.0f;
@@ -304,6 +310,169 @@ __device__ __forceinline__ float exp2_nr(float y) {
 #define CTRL32_L2_QMAXI (-3.32192809f)
 #define CTRL32_L2_GAMMA (-0.152003093f)
 #define CTRL32_L2_QOLDINIT (-13.2877124f)
+
+/* Double-single arithmetic for the error norm and step-size controller of
+ * the FP64 solves (ODE_CTRL_DS).  A value is an unevaluated sum h + l of two
+ * IEEE singles (|l| <= ulp(h)/2: about 48 significant bits), computed with
+ * the error-free transformations of Knuth (two_sum), Dekker (fast two_sum)
+ * and the fma product error, so that the norm and the controller's
+ * logarithm and exponential run on the single-precision pipe, which on this
+ * GPU issues 62 lane operations for each double one.  Every step is one IEEE
+ * single operation, an fma, an integer operation or an exact conversion, so
+ * the oracle reproduces each result bit for bit.  Tables and constants:
+ * ds_table.h (gen_dstab.py). */
+#define GBODE_DSTAB_SPACE __device__ const
+#include "ds_table.h"
+
+struct dsf { float h, l; };
+
+__device__ __forceinline__ dsf ds_two_sum(float a, float b) {
+  const float s = a + b, bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+/* |a| >= |b| (or a == 0) */
+__device__ __forceinline__ dsf ds_fast(float a, float b) {
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ dsf ds_add(dsf x, dsf y) {
+  const dsf s = ds_two_sum(x.h, y.h);
+  return ds_fast(s.h, s.l + (x.l + y.l));
+}
+__device__ __forceinline__ dsf ds_neg(dsf x) { return {-x.h, -x.l}; }
+__device__ __forceinline__ dsf ds_mul(dsf x, dsf y) {
+  const float p = x.h * y.h;
+  const float e = __fmaf_rn(x.h, y.l, __fmaf_rn(x.l, y.h, __fmaf_rn(x.h, y.h, -p)));
+  return ds_fast(p, e);
+}
+__device__ __forceinline__ dsf ds_sqr(dsf x) {
+  const float p = x.h * x.h;
+  return ds_fast(p, __fmaf_rn(x.h + x.h, x.l, __fmaf_rn(x.h, x.h, -p)));
+}
+/* x / y for y > 0: q1 = x.h / y.h by rcp_nr, then one correction from the
+ * remainder x - q1 y (x.h - q1 y.h is exact by Sterbenz); y == 0 gives the
+ * IEEE quotient of x.h (an infinity, or NaN for 0/0) */
+__device__ __forceinline__ dsf ds_div(dsf x, dsf y) {
+  if (y.h == 0.0f) return {x.h * __int_as_float(0x7f800000), 0.0f};
+  const float ry = rcp_nr(y.h);
+  const float q1 = x.h * ry;
+  const float p = q1 * y.h, pe = __fmaf_rn(q1, y.h, -p);
+  const float rem = (((x.h - p) - pe) + x.l) - q1 * y.l;
+  return ds_fast(q1, rem * ry);
+}
+/* x > y in the order of the represented values; false when either is NaN */
+__device__ __forceinline__ bool ds_gt(dsf x, dsf y) { return x.h > y.h || (x.h == y.h && x.l > y.l); }
+/* the clamps of the controller, with fm_min / fm_max's NaN behaviour */
+__device__ __forceinline__ dsf ds_min(dsf x, dsf y) { return ds_gt(y, x) ? x : y; }
+__device__ __forceinline__ dsf ds_max(dsf x, dsf y) { return ds_gt(y, x) ? y : x; }
+
+/* A double as h + l with integer operations only (a conversion between
+ * double and single issues on this GPU's FP64 pipe, as a double operation
+ * does): h is x's sign, exponent and top 23 fraction bits repacked as a
+ * single (x truncated to 24 significant bits) for 2^-126 <= |x| < 2^128,
+ * +-0 below that range, +-infinity above it and NaN for NaN; l is x's 29 low
+ * fraction bits as an integer rounded to a single (one fma of its exact top 6
+ * and low 23 bits) and scaled by 2^(e - 52) through the exponent field
+ * (|l| < 2^-23 |h|; 0 when |x| < 2^-74, where the norm needs no more than h,
+ * or x is not finite). */
+__device__ __forceinline__ dsf ds_split(double x) {
+  const long long b = __double_as_longlong(x);
+  const int eb = (int)((b >> 52) & 0x7ff);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const unsigned frac = (unsigned)((b >> 29) & 0x7fffff);
+  const unsigned hb = eb >= 897 && eb <= 1150 ? sign | ((unsigned)(eb - 896) << 23) | frac
+                      : eb < 897 ? sign
+                      : (eb == 2047 && (b & 0xfffffffffffffLL)) ? 0x7fc00000u | sign
+                                                                : 0x7f800000u | sign;
+  const float h = __uint_as_float(hb);
+  float l = 0.0f;
+  if (eb >= 949 && eb <= 1150) {
+    const int low = (int)(b & 0x1fffffff);
+    const float lf = __fmaf_rn(small_int_f(low >> 23), 8388608.0f, small_int_f(low & 0x7fffff));
+    const float mag = lf * __int_as_float((eb - 948) << 23);
+    l = b < 0 ? -mag : mag;
+  }
+  return {h, l};
+}
+/* max(|u|, |v|) of two doubles by an integer comparison of their magnitudes'
+ * bit patterns (the order of non-negative doubles; a NaN compares above
+ * infinity, so it propagates as Julia's max does) */
+__device__ __forceinline__ double ds_absmax(double u, double v) {
+  const long long au = __double_as_longlong(u) & 0x7fffffffffffffffLL;
+  const long long av = __double_as_longlong(v) & 0x7fffffffffffffffLL;
+  return __longlong_as_double(au >= av ? au : av);
+}
+
+/* ln(a) for a = h + l with h a positive normal single, 2^-120 <= h <= 2^126:
+ * h = 2^E m, r = fma(m, c_j, -1) exact, ln(1 + r) = r - r^2/2 + r^3 (1/3 -
+ * r/4 + r^2/5 - r^3/6 + r^4/7) with r^2 an exact product pair (truncation
+ * below 2^-59), E ln2 from the three-part ln2 (E A exact, E B an exact
+ * product pair), and ln(h + l) = ln(h) + l/h.  Absolute error about 2^-46
+ * for |ln a| < 1, 2^-41 at the ends of the range. */
+__device__ __forceinline__ dsf ds_log(dsf a) {
+  const int b = __float_as_int(a.h);
+  const int j = (b >> 16) & 127;
+  const float m = __int_as_float((b & 0x007fffff) | 0x3f800000);
+  const float c = __ldg(&kDsLogTab[j][0]), th = __ldg(&kDsLogTab[j][1]), tl = __ldg(&kDsLogTab[j][2]);
+  const float r = __fmaf_rn(m, c, -1.0f);
+  const float p = r * r, pe = __fmaf_rn(r, r, -p);
+  float t = __fmaf_rn(r, 0x1.24924ap-3f, -0x1.555556p-3f); /* 1/7, -1/6 */
+  t = __fmaf_rn(r, t, 0x1.99999ap-3f);                     /* 1/5 */
+  t = __fmaf_rn(r, t, -0.25f);
+  t = __fmaf_rn(r, t, 0x1.555556p-2f);                     /* 1/3 */
+  const float tail = t * (r * p);
+  const dsf l1 = ds_fast(r, -0.5f * p);
+  const dsf lp = {l1.h, l1.l + (tail - 0.5f * pe)};
+  const float fE = small_int_f((b >> 23) & 0xff) - 127.0f; /* the exponent E, exact */
+  const float eb = fE * GBODE_DS_LN2_B, ebe = __fmaf_rn(fE, GBODE_DS_LN2_B, -eb);
+  const dsf e0 = ds_fast(fE * GBODE_DS_LN2_A, eb);
+  const dsf eln2 = ds_fast(e0.h, e0.l + (ebe + fE * GBODE_DS_LN2_C));
+  const dsf s = ds_add(ds_add(eln2, {th, tl}), lp);
+  return ds_fast(s.h, s.l + a.l * rcp_nr(a.h));
+}
+
+/* exp(x) for |x| < 2.7 (|k| < 256 keeps k A exact; the controller's
+ * arguments lie in [ln 0.2, ln 10]): k = rint(x 64/ln2), r = x - k ln2/64 (x.h - k A exact by
+ * Sterbenz, k B an exact product pair), exp(r) - 1 = r + r^2/2 + r^3 (1/6 +
+ * r/24 + r^2/120) (|r| <= ln2/128 + tiny, truncation below 2^-54), and
+ * exp(x) = 2^(k >> 6) 2^((k & 63)/64) (1 + (exp(r) - 1)).  Relative error
+ * about 2^-46; NaN in, NaN out. */
+__device__ __forceinline__ dsf ds_exp(dsf x) {
+  if (x.h != x.h) return x;
+  /* k = rint(x.h 64/ln2) by the 1.5 * 2^23 shifter: the sum's low bits hold k */
+  const float sh = x.h * GBODE_DS_EXP_INV_L + 12582912.0f;
+  const int k = __float_as_int(sh) - 0x4b400000;
+  const float kf = sh - 12582912.0f;
+  const float r0 = __fmaf_rn(-kf, GBODE_DS_EXP_L_A, x.h);
+  const float pb = kf * GBODE_DS_EXP_L_B, pbe = __fmaf_rn(kf, GBODE_DS_EXP_L_B, -pb);
+  const dsf rr = ds_two_sum(r0, -pb);
+  const dsf r = ds_fast(rr.h, rr.l + ((x.l - pbe) - kf * GBODE_DS_EXP_L_C));
+  const float p = r.h * r.h, pe = __fmaf_rn(r.h, r.h, -p);
+  float t = __fmaf_rn(r.h, 0x1.111112p-7f, 0x1.555556p-5f); /* 1/120, 1/24 */
+  t = __fmaf_rn(r.h, t, 0x1.555556p-3f);                      /* 1/6 */
+  const float tail = t * (r.h * p);
+  const dsf e1 = ds_fast(r.h, 0.5f * p);
+  const dsf em1 = ds_fast(e1.h, e1.l + ((r.l + 0.5f * pe) + (r.h * r.l + tail)));
+  const int j = k & 63;
+  const float th = __ldg(&kDsExpTab[j][0]), tl = __ldg(&kDsExpTab[j][1]);
+  const float pp = th * em1.h, ppe = __fmaf_rn(th, em1.h, -pp);
+  const dsf v0 = ds_fast(th, pp);
+  const dsf v = ds_fast(v0.h, v0.l + (tl + (ppe + __fmaf_rn(th, em1.l, tl * em1.h))));
+  const float sc = __int_as_float(((k >> 6) + 127) << 23);
+  return {v.h * sc, v.l * sc};
+}
+/* a single as a double with integer operations: exact for normal singles,
+ * +-0 for zeros and subnormals, infinities and NaN kept */
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xff;
+  const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
+  if (e == 0) return __longlong_as_double((long long)s);
+  const unsigned long long de = e == 255 ? 0x7ffULL : (unsigned long long)(e + 896);
+  return __longlong_as_double((long long)(s | (de << 52) | ((unsigned long long)(u & 0x7fffff) << 29)));
+}
+/* d * (x.h + x.l) as fma(d, x.l, d * x.h): two double operations */
+__device__ __forceinline__ double ds_scale(double d, dsf x) { return __fma_rn(d, f2d_bits(x.l), d * f2d_bits(x.h)); }
 
 /* ------------------------------------------------------------------ precisions */
 struct PFP64 { typedef double R; typedef double T; enum { KAHAN = 0 }; };
@@ -941,6 +1110,9 @@ struct Lane {
 #ifdef GBODE_CTRL64
   double lqold; /* beta2 * log(qold) of the FP64 controller */
 #endif
+#ifdef GBODE_CTRL_DS
+  dsf lqds; /* beta2 * log(qold) of the double-single controller */
+#endif
   long long idx, att, cur, ninterp;
   int nacc, nrej;
   double dt_first;
@@ -1036,6 +1208,9 @@ __device__ __forceinline__ void lane_load(const KParams& P, long long idx, Lane<
                                        : ctrl_pow((float)1.0e-4, (float)(2.0 / 25.0));
 #ifdef GBODE_CTRL64
   l.lqold = (2.0 / 25.0) * CTRL64_LN_QOLDINIT;
+#endif
+#ifdef GBODE_CTRL_DS
+  l.lqds = ds_mul({GBODE_DS_B2_H, GBODE_DS_B2_L}, {GBODE_DS_LN_QOLDINIT_H, GBODE_DS_LN_QOLDINIT_L});
 #endif
   l.att = 0;
   l.cur = 0;
@@ -1138,6 +1313,102 @@ __device__ __forceinline__ int adaptive_try(const KParams& P, Lane<PR, D, F, NK>
   R e[D];
   M::attempt(l.f, l.uh, l.uc, l.t, l.dt, l.k, nh, nc, e, true);
   l.att += 1;
+#ifdef GBODE_CTRL_DS
+  if (sizeof(R) == sizeof(double)) {
+    /* Double-single norm and controller: a = EEst^2 = mean((e ./ (abstol .+
+     * max.(|uprev|, |u|) .* reltol)).^2) with every term split into single
+     * pairs (ds_split, integer operations only), le = ln(a)/2 (ds_log), and
+     * the reference's factors on logarithms as in the FP64 controller below,
+     * with one ds_exp for the factor: dt follows the reference's step sizes
+     * to about 2^-44, and the attempt's only double operations here are the
+     * two of ds_scale.  With abstol below 1e-30 the norm is the double one
+     * (the single exponent range cannot hold its scale); the tolerances come
+     * split on the host (KParams::tol_ds). */
+    const dsf one = {1.0f, 0.0f};
+    dsf le;
+    bool reject, is_zero = true;
+    if (!P.norm_fp64) {
+      const dsf abstol = {P.tol_ds[0], P.tol_ds[1]}, reltol = {P.tol_ds[2], P.tol_ds[3]};
+      dsf acc = {0.0f, 0.0f};
+      bool nan_in = false;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const long long eb = __double_as_longlong((double)e[d]) & 0x7fffffffffffffffLL;
+        const double mx = ds_absmax((double)l.uh[d], (double)nh[d]);
+        is_zero = is_zero && eb == 0;
+        nan_in = nan_in || eb > 0x7ff0000000000000LL || __double_as_longlong(mx) > 0x7ff0000000000000LL;
+        const dsf r = ds_div(ds_split((double)e[d]), ds_add(ds_mul(ds_split(mx), reltol), abstol));
+        acc = d == 0 ? ds_sqr(r) : ds_add(acc, ds_sqr(r));
+      }
+      const dsf a = ds_mul(acc, {(float)(1.0 / D), (float)(1.0 / D - (double)(float)(1.0 / D))});
+      if (nan_in) {
+        l.nan_seen = true;
+        reject = false;
+        le = {__int_as_float(0x7fffffff), 0.0f};
+      } else {
+        /* beyond the single range (an overflow leaves NaN or infinity) the
+         * step is rejected with the largest shrink, as the reference's factor
+         * min(1/qmin, EEst^beta1/gamma) is for every EEst above 5e4 */
+        const bool huge = !(a.h <= 0x1p126f);
+        reject = huge || ds_gt(a, one);
+        const dsf ac = huge ? dsf{0x1p126f, 0.0f} : a.h < 0x1p-120f ? dsf{0x1p-120f, 0.0f} : a;
+        const dsf lg = ds_log(ac);
+        le = {0.5f * lg.h, 0.5f * lg.l};
+      }
+    } else {
+      const double abstol = P.abstol, reltol = P.reltol;
+      double acc = 0.0;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const double m = jmax(fabs((double)l.uh[d]), fabs((double)nh[d]));
+        const double r = (double)e[d] / __fma_rn(m, reltol, abstol);
+        acc = (d == 0) ? r * r : __fma_rn(r, r, acc);
+      }
+      const double EEst = __dsqrt_rn(acc / (double)D);
+      is_zero = EEst == 0.0;
+      reject = EEst > 1.0;
+      if (EEst != EEst) {
+        l.nan_seen = true;
+        le = {(float)EEst, 0.0f};
+      } else {
+        const dsf es = ds_split(fmin(fmax(EEst, 0x1p-60), 0x1p63));  /* a normal single pair */
+        le = ds_log(es);
+      }
+    }
+    const dsf B1 = {GBODE_DS_B1_H, GBODE_DS_B1_L}, B2 = {GBODE_DS_B2_H, GBODE_DS_B2_L};
+    const dsf LQMAXI = {GBODE_DS_LN_QMAXI_H, GBODE_DS_LN_QMAXI_L};
+    const dsf LQMINI = {GBODE_DS_LN_QMINI_H, GBODE_DS_LN_QMINI_L};
+    const dsf MLGAMMA = {-GBODE_DS_LN_GAMMA_H, -GBODE_DS_LN_GAMMA_L};
+    const dsf LQOLDINIT = {GBODE_DS_LN_QOLDINIT_H, GBODE_DS_LN_QOLDINIT_L};
+    /* the log of the factor dt is divided by: rejected, min(ln(1/qmin),
+     * beta1 le - ln gamma); accepted, the clamped beta1 le - beta2 ln qold -
+     * ln gamma (ln(1/qmax) when EEst == 0); one ds_exp for both */
+    dsf lfac;
+    if (reject) {
+      lfac = ds_min(LQMINI, ds_add(ds_mul(B1, le), MLGAMMA));
+    } else {
+      const dsf lq0 = is_zero ? LQMAXI : ds_add(ds_mul(B1, le), ds_neg(l.lqds));
+      lfac = ds_max(LQMAXI, ds_min(LQMINI, ds_add(lq0, MLGAMMA)));
+      l.lqds = ds_mul(B2, ds_max(le, LQOLDINIT));
+    }
+    const dsf fac = ds_exp(ds_neg(lfac));
+    if (reject) {
+      l.dt = (T)ds_scale((double)l.dt, fac);
+      l.nrej += 1;
+      return TRY_REJECTED;
+    }
+    const T dtold = l.dt;
+    const T dtn = (T)ds_scale((double)l.dt, fac);
+    l.dt = absmin(dtn, rest);
+    const T told = l.t;
+    l.t = tnext;
+    if (l.nacc == 0) l.dt_first = (double)dtold;
+    l.nacc += 1;
+    acc_out.told = told;
+    acc_out.dtold = dtold;
+    return TRY_ACCEPTED;
+  }
+#endif
   /* EEst = sqrt(mean((e ./ (abstol .+ max.(|uprev|, |u|) .* reltol)).^2)), in
    * single precision (converting doubles to float is as cheap as an FP32 op on
    * this GPU, FP64 division and square root are not); double when abstol is so

@@ -118,18 +118,24 @@ def test_julia_ranges(po):
 
 
 def test_rounding_modes_agree_within_parity_tolerance(po):
-    """The device rounding canon (fused multiply-adds, single-precision step-size
-    factor) stays within the parity tolerance of the reference's rounding:
-    accepted-step counts within +/-1 and final states within 10x the error
-    scale abstol + reltol*|u| (chaotic trajectories amplify rounding, so the
-    bar is 99.9% of trajectories)."""
+    """The device rounding canon (fused multiply-adds, double-single error norm
+    and step-size factor) against the reference's rounding: identical
+    accepted-step counts and every final state within the error scale abstol
+    + reltol*|u|.  With the optional single-precision norm and controller
+    (ODE_CTRL_FP32) the factor q carries 2^-24 relative rounding into every
+    step size, which chaotic trajectories amplify: there the bar is steps
+    within +/-1 and 10x the error scale for 99.9% of trajectories."""
     u0, p = lorenz_inputs(3000, seed=21)
     kw = dict(abstol=1e-8, reltol=1e-6, nthreads=8)
     a = po.solve("ATsit5", "lorenz", u0, p, (0, 10), 0.1, rounding="ref", **kw)
-    b = po.solve("ATsit5", "lorenz", u0, p, (0, 10), 0.1, rounding="device", **kw)
-    assert np.abs(a["naccept"] - b["naccept"]).max() <= 1
     scale = 1e-8 + 1e-6 * np.abs(a["u_final"]).max(0)
+    b = po.solve("ATsit5", "lorenz", u0, p, (0, 10), 0.1, rounding="device", **kw)
+    assert np.array_equal(a["naccept"], b["naccept"])
     err = np.abs(a["u_final"] - b["u_final"]).max(0) / scale
+    assert err.max() <= 1, err.max()
+    c = po.solve("ATsit5", "lorenz", u0, p, (0, 10), 0.1, rounding="device", controller="fp32", **kw)
+    assert np.abs(a["naccept"] - c["naccept"]).max() <= 1
+    err = np.abs(a["u_final"] - c["u_final"]).max(0) / scale
     assert np.mean(err <= 10) >= 0.999
 
 
@@ -397,9 +403,11 @@ def test_simple_em_rounding_modes_and_grid(po):
                                                ("ATsit5", "kuramoto", 1e-6, (0, 50))])
 def test_device_canon_within_parity_tolerance_of_reference_rounding(po, alg, rhs, tol, tspan):
     """The adaptive workloads: the device canon (which the GPU reproduces bit
-    for bit) against the reference's rounding, final states within 10x the
-    error scale abstol + reltol*|u| for >= 99.9% of trajectories and accepted
-    steps within +/-1."""
+    for bit) against the reference's rounding, every final state within 10x
+    the error scale abstol + reltol*|u| and accepted steps within +/-1 for
+    >= 99.9% of trajectories (Van der Pol's step sequences sit at its
+    stability boundary, where last-bit differences of the fused stage sums
+    flip accept/reject: 9 of 524,288 trajectories differ by 2-3 steps)."""
     sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
     import make_golden
     if rhs == "vanderpol":
@@ -415,7 +423,7 @@ def test_device_canon_within_parity_tolerance_of_reference_rounding(po, alg, rhs
     assert ok.mean() > 0.98
     scale = abstol + tol * np.abs(a["u_final"][:, ok]).max(0)
     err = np.abs(a["u_final"][:, ok] - b["u_final"][:, ok]).max(0) / scale
-    assert np.mean(err <= 10) >= 0.999
+    assert err.max() <= 10, err.max()
     assert np.mean(np.abs(a["naccept"][ok] - b["naccept"][ok]) <= 1) >= 0.999
 
 
@@ -498,17 +506,20 @@ def test_exp_table_is_the_generator_output():
     assert gen.header() == open(os.path.join(here, "exp_table.h")).read()
 
 
+@pytest.mark.parametrize("controller", ["ds", "fp64"])
 @pytest.mark.parametrize("alg,rhs", [("ATsit5", "lorenz"), ("AVern7", "vanderpol")])
-def test_fp64_controller_follows_reference_step_sizes(po, alg, rhs):
-    """With the FP64 step-size controller (ODE_CTRL_FP64) the device canon's
-    step sequence follows the reference rounding's: on the benchmark
-    ensembles' first 8,192 trajectories (adaptive Lorenz, Van der Pol) every
-    accepted-step count is within +/-1 and every final state within 10x the
-    error scale, where the single-precision controller's factor q carries
-    2^-24 relative rounding into every step size (chaotic Lorenz trajectories
-    then drift beyond the bar: 3 of 131,072 at up to 84x).  The Arenstorf
-    orbit at 1e-12 is excluded: there fused and unfused stage sums alone
-    separate the solutions (see the matched-accuracy test)."""
+def test_controllers_follow_reference_step_sizes(po, alg, rhs, controller):
+    """With the double-single norm and controller (the default) or the FP64
+    controller the device canon's step sequence follows the reference
+    rounding's: on the benchmark ensembles' first 8,192 trajectories
+    (adaptive Lorenz, Van der Pol) every accepted-step count is within +/-1
+    (the default: Lorenz identical) and every final state within the error
+    scale (10x for the FP64 controller, whose single-precision norm still
+    rounds to 2^-24), where the single-precision controller's factor q
+    carries 2^-24 relative rounding into every step size (chaotic Lorenz
+    trajectories then drift beyond the bar: 21 of 1,048,576 at up to 559x).
+    The Arenstorf orbit at 1e-12 is excluded: there fused and unfused stage
+    sums alone separate the solutions (see the matched-accuracy test)."""
     import bench
     cid = {"lorenz": 2, "vanderpol": 3}[rhs]
     cfg = bench.CONFIGS[cid]
@@ -518,14 +529,58 @@ def test_fp64_controller_follows_reference_step_sizes(po, alg, rhs):
     tol = (cfg["abstol"], cfg["reltol"])
     kw = dict(abstol=tol[0], reltol=tol[1], nthreads=8)
     ref = po.solve(alg, rhs, u0, p, cfg["tspan"], cfg["dt"], rounding="ref", **kw)
-    dev = po.solve(alg, rhs, u0, p, cfg["tspan"], cfg["dt"], rounding="device", controller="fp64", **kw)
+    dev = po.solve(alg, rhs, u0, p, cfg["tspan"], cfg["dt"], rounding="device", controller=controller, **kw)
     ok = (ref["retcode"] == 0) & (dev["retcode"] == 0)
     assert ok.mean() > 0.99
     dn = np.abs(dev["naccept"].astype(np.int64) - ref["naccept"])[ok]
-    assert dn.max() <= 1
+    assert dn.max() <= (0 if (controller == "ds" and rhs == "lorenz") else 1)
     scale = tol[0] + tol[1] * np.abs(ref["u_final"]).max(0)
     e = (np.abs(dev["u_final"] - ref["u_final"]).max(0) / scale)[ok]
-    assert np.mean(e <= 10) == 1.0, e.max()
+    assert e.max() <= (1 if controller == "ds" else 10), e.max()
+
+
+def test_double_single_functions(po):
+    """The double-single norm's and controller's building blocks against
+    40-digit values: ds_split holds a double to 2^-47 relative (2^-74 <= |x|
+    < 2^128), ds_log is within 2^-45 absolute where |ln a| < 2 and 2^-40 over
+    the whole range 2^-120 .. 2^126, ds_exp within 2^-45 relative on the
+    controller's arguments (|x| < 2.4)."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 40
+    rng = np.random.default_rng(6)
+
+    def val(pair):
+        return mp.mpf(float(pair[0])) + mp.mpf(float(pair[1]))
+
+    def pair(x):
+        h = np.float32(x)
+        return h, np.float32(x - float(h))
+    for x in np.concatenate([rng.uniform(-1e3, 1e3, 500), 10 ** rng.uniform(-22, 38, 1000),
+                             -(10 ** rng.uniform(-20, 20, 200))]):
+        assert abs(val(po.ds("split", x)) - mp.mpf(x)) <= abs(mp.mpf(x)) * mp.mpf(2) ** -47, x
+    assert po.ds("split", 0.0) == (0.0, 0.0) and np.isinf(po.ds("split", 4e38)[0])
+    assert np.isnan(po.ds("split", float("nan"))[0])
+    for e in np.concatenate([rng.uniform(-120, 126, 800), rng.uniform(-2.8, 2.8, 800), [0.0]]):
+        h, l = pair(2.0 ** e)
+        exact = mp.log(val((h, l)))
+        bound = mp.mpf(2) ** (-45 if abs(exact) < 2 else -40)
+        assert abs(val(po.ds("log", h, l)) - exact) <= bound, e
+    for x in np.concatenate([rng.uniform(-2.4, 2.4, 1500), rng.uniform(-1e-3, 1e-3, 200), [0.0]]):
+        h, l = pair(x)
+        exact = mp.exp(val((h, l)))
+        assert abs(val(po.ds("exp", h, l)) - exact) <= exact * mp.mpf(2) ** -45, x
+    assert np.isnan(po.ds("exp", float("nan"))[0])
+
+
+def test_ds_table_is_the_generator_output():
+    """csrc/ds_table.h is what csrc/gen_dstab.py writes (60-digit mpmath)."""
+    pytest.importorskip("mpmath")
+    import importlib.util
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "simplediffeq.jl_gb300", "csrc")
+    spec = importlib.util.spec_from_file_location("gen_dstab", os.path.join(here, "gen_dstab.py"))
+    gen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen)
+    assert gen.header() == open(os.path.join(here, "ds_table.h")).read()
 
 
 def test_single_precision_r3bp_pull_accuracy(po):
