@@ -348,12 +348,12 @@ def probe_rates(device=0, iters=2000):
     import ctypes
     lib = ctypes.CDLL(os.path.join(ROOT, "_build", "libbench_probe.so"))
     lib.probe_op_rates.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
-    r = np.zeros(8)
-    ms = np.zeros(8)
-    rc = lib.probe_op_rates(int(device), int(iters), r.ctypes.data, ms.ctypes.data, 8)
+    r = np.zeros(7)
+    ms = np.zeros(7)
+    rc = lib.probe_op_rates(int(device), int(iters), r.ctypes.data, ms.ctypes.data, 7)
     if rc != 0:
         raise RuntimeError("probe failed (%d)" % rc)
-    names = ["dfma", "dadd", "ffma", "cvt_f64_f32_f64", "ddiv", "dsqrt_add", "dmax_add", "fdiv"]
+    names = ["dfma", "dadd", "ffma", "ddiv", "dsqrt_add", "dmax_add", "fdiv"]
     return {k: (float(r[i]), float(ms[i])) for i, k in enumerate(names)}
 
 

@@ -18,11 +18,10 @@ enum {
   OP_DFMA = 0,    /* d = fma(d, a, b)                 2 flops */
   OP_DADD = 1,    /* d = d + a                        1 flop */
   OP_FFMA = 2,    /* f = fmaf(f, a, b)                2 flops */
-  OP_CVT = 3,     /* d = (double)((float)d * fa)      f64->f32, f32 mul, f32->f64 */
-  OP_DDIV = 4,    /* d = a / d                        IEEE double division */
-  OP_DSQRT = 5,   /* d = sqrt(d) + b                  IEEE double square root + add */
-  OP_DMAX = 6,    /* d = fmax(d, a) - b               double max + add */
-  OP_FDIV = 7,    /* f = fa / f                       IEEE float division */
+  OP_DDIV = 3,    /* d = a / d                        IEEE double division */
+  OP_DSQRT = 4,   /* d = sqrt(d) + b                  IEEE double square root + add */
+  OP_DMAX = 5,    /* d = fmax(d, a) - b               double max + add */
+  OP_FDIV = 6,    /* f = fa / f                       IEEE float division */
   OP_NOPS
 };
 
@@ -44,7 +43,6 @@ __global__ void __launch_bounds__(256) probe_kernel(double* out, int iters, doub
         if (OP == OP_DFMA) d[j] = __fma_rn(d[j], a, b);
         if (OP == OP_DADD) d[j] = __dadd_rn(d[j], a);
         if (OP == OP_FFMA) f[j] = __fmaf_rn(f[j], fa, fb);
-        if (OP == OP_CVT) d[j] = (double)__fmul_rn((float)d[j], fa);
         if (OP == OP_DDIV) d[j] = __ddiv_rn(a, d[j]);
         if (OP == OP_DSQRT) d[j] = __dadd_rn(__dsqrt_rn(d[j]), b);
         if (OP == OP_DMAX) d[j] = __dadd_rn(fmax(d[j], a), b);
@@ -64,7 +62,7 @@ float time_op(double* out, int blocks, int iters) {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   /* a, b chosen so chains neither overflow nor denormalise */
-  const double a = (OP == OP_DFMA || OP == OP_FFMA) ? 0.999999 : (OP == OP_DADD ? 1e-9 : (OP == OP_CVT ? 1.0 : 1.0));
+  const double a = (OP == OP_DFMA || OP == OP_FFMA) ? 0.999999 : (OP == OP_DADD ? 1e-9 : 1.0);
   const double b = (OP == OP_DFMA || OP == OP_FFMA) ? 1e-6 : (OP == OP_DSQRT ? 0.5 : (OP == OP_DMAX ? 0.0 : 0.0));
   probe_kernel<OP><<<blocks, 256>>>(out, iters / 8 + 1, a, b);
   cudaEventRecord(e0);
@@ -99,13 +97,12 @@ int probe_op_rates(int device, int iters, double* ops_per_s, double* ms_out, int
   ms[OP_DFMA] = time_op<OP_DFMA>(out, blocks, iters);
   ms[OP_DADD] = time_op<OP_DADD>(out, blocks, iters);
   ms[OP_FFMA] = time_op<OP_FFMA>(out, blocks, iters * 16);
-  ms[OP_CVT] = time_op<OP_CVT>(out, blocks, iters);
   ms[OP_DDIV] = time_op<OP_DDIV>(out, blocks, iters / 4);
   ms[OP_DSQRT] = time_op<OP_DSQRT>(out, blocks, iters / 4);
   ms[OP_DMAX] = time_op<OP_DMAX>(out, blocks, iters);
   ms[OP_FDIV] = time_op<OP_FDIV>(out, blocks, iters);
   const double lanes = (double)blocks * 256.0 * 32.0;
-  const int it[OP_NOPS] = {iters, iters, iters * 16, iters, iters / 4, iters / 4, iters, iters};
+  const int it[OP_NOPS] = {iters, iters, iters * 16, iters / 4, iters / 4, iters, iters};
   for (int k = 0; k < nops && k < OP_NOPS; ++k) {
     ops_per_s[k] = lanes * it[k] / (ms[k] * 1e-3);
     if (ms_out) ms_out[k] = ms[k];

@@ -1410,9 +1410,10 @@ __device__ __forceinline__ int adaptive_try(const KParams& P, Lane<PR, D, F, NK>
   }
 #endif
   /* EEst = sqrt(mean((e ./ (abstol .+ max.(|uprev|, |u|) .* reltol)).^2)), in
-   * single precision (converting doubles to float is as cheap as an FP32 op on
-   * this GPU, FP64 division and square root are not); double when abstol is so
-   * small that the scale could leave the float range (P.norm_fp64). */
+   * single precision (ODE_CTRL_FP32 and the single-precision modes; each
+   * conversion of a double term costs one FP64-pipe instruction, the FP64
+   * division and square root it avoids about nine each); double when abstol
+   * is so small that the scale could leave the float range (P.norm_fp64). */
   float Ef;
   double EEst64 = 0.0; /* the double norm, when computed */
   bool reject, is_zero;
