@@ -621,13 +621,16 @@ static std::string gpu_tag(ode_handle* h) {
   return name + "/" + std::to_string(prop.multiProcessorCount);
 }
 
-/* kernel keys are alg|kind|rhs|dim|prec|output[|chk]; only built-in ids travel */
+/* kernel keys are alg|kind|rhs|dim|prec|output[|chk][|c64 or |c32]; only built-in ids travel, and
+ * no bounds-check build */
 static bool portable_key(const std::string& key) {
   std::vector<std::string> f;
   size_t a = 0;
   for (size_t b; (b = key.find('|', a)) != std::string::npos; a = b + 1) f.push_back(key.substr(a, b - a));
   f.push_back(key.substr(a));
-  return f.size() == 6 && std::atoi(f[2].c_str()) < ODE_RHS_USER && std::atoi(f[5].c_str()) < ODE_OUTPUT_USER;
+  const bool ctrl_suffix = f.size() == 7 && (f[6] == "c64" || f[6] == "c32");
+  return (f.size() == 6 || ctrl_suffix) && std::atoi(f[2].c_str()) < ODE_RHS_USER &&
+         std::atoi(f[5].c_str()) < ODE_OUTPUT_USER;
 }
 
 int ode_tune_save(ode_handle* h, const char* path) {

@@ -347,10 +347,15 @@ def test_tuning_cache_round_trip(pkg, tmp_path):
                          "persistent", 0)
     h1 = L.Handle(0)
     rep = h1.autotune(args, sample=8192)
+    # a kernel built for another controller has its own key, and its choice travels too
+    args32 = pkg.make_args(pkg.GPUSimpleATsit5(), 0, u0, p, (0.0, 5.0), 0.1, 1e-8, 1e-6, sv, False, "fp64",
+                           "persistent", 0, controller="fp32")
+    h1.autotune(args32, sample=8192)
     path = tmp_path / "tune.txt"
     h1.tune_save(path)
     text = path.read_text().splitlines()
-    assert text[0].startswith("gb300ode-tune 1 ") and len(text) == 2
+    assert text[0].startswith("gb300ode-tune 1 ") and len(text) == 3
+    assert sum(line.split()[0].endswith("|c32") for line in text[1:]) == 1
     h2 = L.Handle(0)
     assert h2.tune_load(path) == L.OK
     outs = []
