@@ -421,10 +421,10 @@ int nvrtc_cubin(const std::string& src, const std::vector<std::string>& extra_op
   }
   nvrtcProgram prog;
   const char* hdrs[] = {kSrc_ode_solver_cuh, kSrc_ode_kparams_h, kSrc_tableaus_h, kSrc_sde_solver_cuh, kSrc_log_table_h,
-                        kSrc_exp_table_h, kSrc_ds_table_h};
+                        kSrc_exp_table_h, kSrc_ds_table_h, kSrc_bitops_h};
   const char* names[] = {"ode_solver.cuh", "ode_kparams.h", "tableaus.h", "sde_solver.cuh", "log_table.h",
-                         "exp_table.h", "ds_table.h"};
-  nvrtcResult r = g_nvrtc.create(&prog, src.c_str(), "gbode_jit.cu", 7, hdrs, names);
+                         "exp_table.h", "ds_table.h", "bitops.h"};
+  nvrtcResult r = g_nvrtc.create(&prog, src.c_str(), "gbode_jit.cu", 8, hdrs, names);
   if (r != NVRTC_SUCCESS) {
     *err = std::string("nvrtcCreateProgram: ") + g_nvrtc.errstr(r);
     return ODE_ENVRTC;

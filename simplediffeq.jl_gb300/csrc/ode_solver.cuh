@@ -39,6 +39,7 @@
  */
 #pragma once
 #include "ode_kparams.h"
+#include "bitops.h"
 #include "tableaus.h"
 #define GBODE_LOGTAB_SPACE __device__ const
 #include "log_table.h"
@@ -129,6 +130,25 @@ __device__ __forceinline__ double absmin(double a, double b) {
   return __longlong_as_double((long long)r);
 }
 __device__ __forceinline__ float absmin(float a, float b) { return jmin(fabsf(a), fabsf(b)); }
+
+/* The time comparisons of the solver loops: (T)s <= t for a saveat time s,
+ * t < (T)tf, and x < dtmin.  The FP64 kernels, bound by their FP64 pipe,
+ * compare doubles with the exact integer forms of bitops.h (a double
+ * comparison issues on the FP64 pipe); the single-precision modes, whose
+ * long trajectories are bound by one lane's dependency chain, keep the IEEE
+ * comparisons and casts, which are shorter on that chain. */
+template <class PR> __device__ __forceinline__ bool t_le(double s, typename PR::T t) {
+  if (sizeof(typename PR::R) == sizeof(double)) return bo_le(s, (double)t);
+  return (typename PR::T)s <= t;
+}
+template <class PR> __device__ __forceinline__ bool t_lt(typename PR::T t, double tf) {
+  if (sizeof(typename PR::R) == sizeof(double)) return bo_lt((double)t, tf);
+  return t < (typename PR::T)tf;
+}
+template <class PR> __device__ __forceinline__ bool d_lt(double x, double y) {
+  if (sizeof(typename PR::R) == sizeof(double)) return bo_lt(x, y);
+  return x < y;
+}
 
 /* 1/x for the dense-output abscissa theta = (t_save - told) / dt: a single
  * precision reciprocal refined by one Newton step in double (relative error
@@ -1301,7 +1321,7 @@ __device__ __forceinline__ int adaptive_try(const KParams& P, Lane<PR, D, F, NK>
   typedef typename PR::R R;
   typedef typename PR::T T;
   const double dtmin = M::DTMIN_1F7 ? (double)1.0e-7f : 1.0e-14;
-  if ((double)l.dt < dtmin) { lane_finish(P, l, RET_DTMIN, tot); return TRY_STOPPED; }
+  if (d_lt<PR>((double)l.dt, dtmin)) { lane_finish(P, l, RET_DTMIN, tot); return TRY_STOPPED; }
   if (P.maxiters > 0 && l.att >= P.maxiters) { lane_finish(P, l, RET_MAXITERS, tot); return TRY_STOPPED; }
   /* The end-of-span bookkeeping of an accepted step depends only on t and dt,
    * both known now: computed before the stages (the same operations, so the
@@ -1309,7 +1329,7 @@ __device__ __forceinline__ int adaptive_try(const KParams& P, Lane<PR, D, F, NK>
    * dependency chain after the error estimate. */
   const T tf = (T)P.tf;
   const T rest = tf - l.t - l.dt;
-  const T tnext = ((double)rest < dtmin) ? tf : l.t + l.dt;
+  const T tnext = d_lt<PR>((double)rest, dtmin) ? tf : l.t + l.dt;
   R e[D];
   M::attempt(l.f, l.uh, l.uc, l.t, l.dt, l.k, nh, nc, e, true);
   l.att += 1;
@@ -1571,8 +1591,8 @@ __device__ __forceinline__ bool adaptive_iter(const KParams& P, Lane<PR, D, F, N
   if (r == TRY_REJECTED) return false;
   const T told = st.told, dtold = st.dtold;
   T inv_dt = (T)0;
-  if (l.cur < P.nsave && (T)P.saveat[l.cur] <= l.t) inv_dt = recip(dtold);
-  while (l.cur < P.nsave && (T)P.saveat[l.cur] <= l.t) {
+  if (l.cur < P.nsave && t_le<PR>(P.saveat[l.cur], l.t)) inv_dt = recip(dtold);
+  while (l.cur < P.nsave && t_le<PR>(P.saveat[l.cur], l.t)) {
     const T theta = ((T)P.saveat[l.cur] - told) * inv_dt;
     double v[D];
     M::dense(l.f, l.uh, l.uc, told, l.t, dtold, theta, l.k, v);
@@ -1582,7 +1602,7 @@ __device__ __forceinline__ bool adaptive_iter(const KParams& P, Lane<PR, D, F, N
   }
   adaptive_commit<M>(l, nh, nc);
   store_step<PR, D>(P, l, l.nacc);
-  if (!(l.t < (T)P.tf)) { lane_finish(P, l, RET_DEFAULT, tot); return true; }
+  if (!t_lt<PR>(l.t, P.tf)) { lane_finish(P, l, RET_DEFAULT, tot); return true; }
   return false;
 }
 
@@ -1783,7 +1803,7 @@ __device__ __forceinline__ void run_adaptive_staged(const KParams& P) {
       r = adaptive_try<M>(P, l, tot, nh, nc, st);
       if (r == TRY_STOPPED) active = false;
       if (r == TRY_ACCEPTED)
-        while (l.cur + njobs < P.nsave && (T)P.saveat[l.cur + njobs] <= l.t) ++njobs;
+        while (l.cur + njobs < P.nsave && t_le<PR>(P.saveat[l.cur + njobs], l.t)) ++njobs;
     }
     /* slots for this iteration's jobs: exclusive prefix sum over the warp */
     int incl = njobs;
@@ -1841,7 +1861,7 @@ __device__ __forceinline__ void run_adaptive_staged(const KParams& P) {
     if (r == TRY_ACCEPTED) {
       adaptive_commit<M>(l, nh, nc);
       store_step<PR, D>(P, l, l.nacc);
-      if (!(l.t < (T)P.tf)) {
+      if (!t_lt<PR>(l.t, P.tf)) {
         lane_finish(P, l, RET_DEFAULT, tot);
         active = false;
       }
@@ -1995,7 +2015,7 @@ __device__ __forceinline__ void run_adaptive_staged2(const KParams& P) {
       r = adaptive_try<M>(P, l, tot, nh, nc, st);
       if (r == TRY_STOPPED) active = false;
       if (r == TRY_ACCEPTED)
-        while (l.cur + njobs < P.nsave && (T)P.saveat[l.cur + njobs] <= l.t) ++njobs;
+        while (l.cur + njobs < P.nsave && t_le<PR>(P.saveat[l.cur + njobs], l.t)) ++njobs;
     }
     /* a record per lane with save points, and its points: ranks over the warp */
     const unsigned hb = __ballot_sync(FULL, njobs > 0);
@@ -2061,7 +2081,7 @@ __device__ __forceinline__ void run_adaptive_staged2(const KParams& P) {
     if (r == TRY_ACCEPTED) {
       adaptive_commit<M>(l, nh, nc);
       store_step<PR, D>(P, l, l.nacc);
-      if (!(l.t < (T)P.tf)) {
+      if (!t_lt<PR>(l.t, P.tf)) {
         lane_finish(P, l, RET_DEFAULT, tot);
         active = false;
       }
@@ -2253,7 +2273,7 @@ __device__ __forceinline__ void run_fixed(const KParams& P) {
     l.t = (T)P.grid[g - 1];
     M::attempt(l.f, l.uh, l.uc, l.t, dt, l.k, nh, nc, e, false);
     l.t = l.t + dt;
-    while (l.cur < P.nsave && (T)P.saveat[l.cur] <= l.t) {
+    while (l.cur < P.nsave && t_le<PR>(P.saveat[l.cur], l.t)) {
       const T theta = ((T)P.saveat[l.cur] - (l.t - dt)) / dt;
       double v[D];
       M::dense(l.f, l.uh, l.uc, l.t - dt, l.t, dt, theta, l.k, v);
