@@ -502,7 +502,7 @@ struct Tsit5 {
   static constexpr bool DTMIN_1F7 = false;
 
   static void attempt(const Alg<P>& A, const State<R>& up, T t, T dt, R (*k)[MAXD], State<R>& u, R* e,
-                      bool want_err) {
+                      int want_err) {
     R tmp[MAXD], s[MAXD];
     const R h = (R)dt;
     const R* uprev = up.hi;
@@ -521,7 +521,7 @@ struct Tsit5 {
     A.f(u.hi, (double)(t + dt), k[6]);
     if (want_err) {
       A.lc(T5_E, 7, k, s);
-      for (int d = 0; d < A.D; ++d) e[d] = h * s[d];
+      for (int d = 0; d < A.D; ++d) e[d] = want_err == 2 ? s[d] : h * s[d];
     }
   }
 
@@ -562,7 +562,7 @@ struct Vern7 {
   static constexpr bool DTMIN_1F7 = false;
 
   static void attempt(const Alg<P>& A, const State<R>& up, T t, T dt, R (*k)[MAXD], State<R>& u, R* e,
-                      bool want_err) {
+                      int want_err) {
     R tmp[MAXD], s[MAXD];
     const R h = (R)dt;
     const R* uprev = up.hi;
@@ -585,7 +585,7 @@ struct Vern7 {
     state_update<P>(A.D, up, h, s, u);
     if (want_err) {
       A.lc(V7_E, 8, k, s);
-      for (int d = 0; d < A.D; ++d) e[d] = h * s[d];
+      for (int d = 0; d < A.D; ++d) e[d] = want_err == 2 ? s[d] : h * s[d];
     }
   }
 
@@ -619,7 +619,7 @@ struct Vern9 {
   static constexpr bool DTMIN_1F7 = true;
 
   static void attempt(const Alg<P>& A, const State<R>& up, T t, T dt, R (*k)[MAXD], State<R>& u, R* e,
-                      bool want_err) {
+                      int want_err) {
     R tmp[MAXD], s[MAXD];
     const R h = (R)dt;
     const R* uprev = up.hi;
@@ -645,7 +645,7 @@ struct Vern9 {
     state_update<P>(A.D, up, h, s, u);
     if (want_err) {
       A.lc(V9_E, 10, k, s);
-      for (int d = 0; d < A.D; ++d) e[d] = h * s[d];
+      for (int d = 0; d < A.D; ++d) e[d] = want_err == 2 ? s[d] : h * s[d];
     }
   }
 
@@ -1040,7 +1040,8 @@ static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
     while (EEst > (R)1) {
       if ((double)dt < dtmin) { ret = RET_DTMIN; goto done; }
       if (a->maxiters > 0 && attempts >= a->maxiters) { ret = RET_MAXITERS; goto done; }
-      M::attempt(A, up, t, dt, k, un, e, true);
+      /* the double-single norm takes the unscaled sum and multiplies by dt itself */
+      M::attempt(A, up, t, dt, k, un, e, (P::DEV && cds) ? 2 : 1);
       ++attempts;
       /* error norm: RMS of e ./ (abstol .+ max.(|uprev|, |u|) * reltol); the
        * device canon evaluates it in single precision unless abstol < 1e-30 */
@@ -1053,15 +1054,16 @@ static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
         bool reject;
         if (a->abstol >= 1e-30) {
           const DS dabs = ds_split(a->abstol), drel = ds_split(a->reltol);
+          const DS hds = ds_split((double)dt);
           DS acc = {0.0f, 0.0f};
-          bool nan_in = false;
+          bool nan_in = dbits_abs((double)dt) > 0x7ff0000000000000LL;
           ds_zero = true;
           for (int d = 0; d < D; ++d) {
             const int64_t eb = dbits_abs((double)e[d]);
             const double mx = ds_absmax((double)up.hi[d], (double)un.hi[d]);
             ds_zero = ds_zero && eb == 0;
             nan_in = nan_in || eb > 0x7ff0000000000000LL || dbits_abs(mx) > 0x7ff0000000000000LL;
-            const DS r = ds_div(ds_split((double)e[d]), ds_add(ds_mul(ds_split(mx), drel), dabs));
+            const DS r = ds_div(ds_mul(ds_split((double)e[d]), hds), ds_add(ds_mul(ds_split(mx), drel), dabs));
             acc = d == 0 ? ds_sqr(r) : ds_add(acc, ds_sqr(r));
           }
           const DS av = ds_mul(acc, DS{(float)(1.0 / D), (float)(1.0 / D - (double)(float)(1.0 / D))});
@@ -1080,7 +1082,7 @@ static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
           double acc = 0;
           for (int d = 0; d < D; ++d) {
             const double m = jmax(std::fabs((double)up.hi[d]), std::fabs((double)un.hi[d]));
-            const double r = (double)e[d] / std::fma(m, a->reltol, a->abstol);
+            const double r = ((double)e[d] * (double)dt) / std::fma(m, a->reltol, a->abstol);
             acc = (d == 0) ? r * r : std::fma(r, r, acc);
           }
           const double E64 = std::sqrt(acc / (double)D);

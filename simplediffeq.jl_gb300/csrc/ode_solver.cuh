@@ -494,6 +494,15 @@ __device__ __forceinline__ double f2d_bits(float f) {
 /* d * (x.h + x.l) as fma(d, x.l, d * x.h): two double operations */
 __device__ __forceinline__ double ds_scale(double d, dsf x) { return __fma_rn(d, f2d_bits(x.l), d * f2d_bits(x.h)); }
 
+/* With the double-single norm the FP64 kernels hand the error estimate over
+ * unscaled: sum(btilde_i k_i), which the norm multiplies by dt in
+ * double-single (one double multiplication per component less an attempt). */
+#ifdef GBODE_CTRL_DS
+template <class R> struct ErrUnscaled { enum { value = sizeof(R) == sizeof(double) }; };
+#else
+template <class R> struct ErrUnscaled { enum { value = 0 }; };
+#endif
+
 /* ------------------------------------------------------------------ precisions */
 struct PFP64 { typedef double R; typedef double T; enum { KAHAN = 0 }; };
 struct PFP32 { typedef float R; typedef float T; enum { KAHAN = 0 }; };
@@ -742,7 +751,7 @@ struct MTsit5 {
       lc(s, C5(btilde1), k[0], C5(btilde2), k[1], C5(btilde3), k[2], C5(btilde4), k[3], C5(btilde5), k[4],
          C5(btilde6), k[5], C5(btilde7), k[6]);
 #pragma unroll
-      for (int d = 0; d < D; ++d) e[d] = h * s[d];
+      for (int d = 0; d < D; ++d) e[d] = ErrUnscaled<R>::value ? s[d] : h * s[d];
     }
   }
 
@@ -813,7 +822,7 @@ struct MVern7 {
       lc(s, C7(btilde1), k[0], C7(btilde4), k[3], C7(btilde5), k[4], C7(btilde6), k[5], C7(btilde7), k[6],
          C7(btilde8), k[7], C7(btilde9), k[8], C7(btilde10), k[9]);
 #pragma unroll
-      for (int d = 0; d < D; ++d) e[d] = h * s[d];
+      for (int d = 0; d < D; ++d) e[d] = ErrUnscaled<R>::value ? s[d] : h * s[d];
     }
 #undef C7
 #undef C7T
@@ -956,7 +965,7 @@ struct MVern9Impl {
       lc(s, C9(btilde1), k[0], C9(btilde8), k[7], C9(btilde9), k[8], C9(btilde10), k[9], C9(btilde11), k[10],
          C9(btilde12), k[11], C9(btilde13), k[12], C9(btilde14), k[13], C9(btilde15), k[14], C9(btilde16), k[15]);
 #pragma unroll
-      for (int d = 0; d < D; ++d) e[d] = h * s[d];
+      for (int d = 0; d < D; ++d) e[d] = ErrUnscaled<R>::value ? s[d] : h * s[d];
     }
 #undef C9
 #undef C9T
@@ -1349,15 +1358,18 @@ __device__ __forceinline__ int adaptive_try(const KParams& P, Lane<PR, D, F, NK>
     bool reject, is_zero = true;
     if (!P.norm_fp64) {
       const dsf abstol = {P.tol_ds[0], P.tol_ds[1]}, reltol = {P.tol_ds[2], P.tol_ds[3]};
+      /* e holds the unscaled sum: e_d = dt e[d], formed before the division
+       * so that the quotient stays in the single range for any tolerance */
+      const dsf hds = ds_split((double)l.dt);
       dsf acc = {0.0f, 0.0f};
-      bool nan_in = false;
+      bool nan_in = bo_isnan((double)l.dt);
 #pragma unroll
       for (int d = 0; d < D; ++d) {
         const long long eb = __double_as_longlong((double)e[d]) & 0x7fffffffffffffffLL;
         const double mx = ds_absmax((double)l.uh[d], (double)nh[d]);
         is_zero = is_zero && eb == 0;
         nan_in = nan_in || eb > 0x7ff0000000000000LL || __double_as_longlong(mx) > 0x7ff0000000000000LL;
-        const dsf r = ds_div(ds_split((double)e[d]), ds_add(ds_mul(ds_split(mx), reltol), abstol));
+        const dsf r = ds_div(ds_mul(ds_split((double)e[d]), hds), ds_add(ds_mul(ds_split(mx), reltol), abstol));
         acc = d == 0 ? ds_sqr(r) : ds_add(acc, ds_sqr(r));
       }
       const dsf a = ds_mul(acc, {(float)(1.0 / D), (float)(1.0 / D - (double)(float)(1.0 / D))});
@@ -1381,7 +1393,7 @@ __device__ __forceinline__ int adaptive_try(const KParams& P, Lane<PR, D, F, NK>
 #pragma unroll
       for (int d = 0; d < D; ++d) {
         const double m = jmax(fabs((double)l.uh[d]), fabs((double)nh[d]));
-        const double r = (double)e[d] / __fma_rn(m, reltol, abstol);
+        const double r = ((double)e[d] * (double)l.dt) / __fma_rn(m, reltol, abstol);
         acc = (d == 0) ? r * r : __fma_rn(r, r, acc);
       }
       const double EEst = __dsqrt_rn(acc / (double)D);

@@ -572,6 +572,22 @@ def test_double_single_functions(po):
     assert np.isnan(po.ds("exp", float("nan"))[0])
 
 
+@pytest.mark.parametrize("abstol,reltol", [(1e-25, 1e-10), (1e-32, 1e-10), (1e-3, 1e-3), (1e-12, 1e-12)])
+def test_double_single_norm_across_tolerances(po, abstol, reltol):
+    """The double-single norm keeps the reference's step sequence from loose to
+    very tight tolerances: abstol 1e-25 (the norm's terms near the single
+    exponent range's edge), 1e-32 (below 1e-30, where the norm is computed
+    in double), 1e-3 and 1e-12 -- identical accepted-step counts and final
+    states within a tenth of the error scale on 200 Lorenz trajectories."""
+    u0, p = lorenz_inputs(200, seed=5)
+    kw = dict(abstol=abstol, reltol=reltol, nthreads=8)
+    a = po.solve("ATsit5", "lorenz", u0, p, (0, 1), 0.1, rounding="ref", **kw)
+    b = po.solve("ATsit5", "lorenz", u0, p, (0, 1), 0.1, rounding="device", **kw)
+    assert np.array_equal(a["naccept"], b["naccept"])
+    scale = abstol + reltol * np.abs(a["u_final"]).max(0)
+    assert (np.abs(a["u_final"] - b["u_final"]).max(0) / scale).max() < 0.1
+
+
 def test_ds_table_is_the_generator_output():
     """csrc/ds_table.h is what csrc/gen_dstab.py writes (60-digit mpmath)."""
     pytest.importorskip("mpmath")
