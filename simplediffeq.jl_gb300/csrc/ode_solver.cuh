@@ -1,8 +1,8 @@
 /* Device side of the ensemble solver: one trajectory per thread.
  *
  * Compiled ahead of time by nvcc (kern_*.cu) and at run time by NVRTC for
- * combinations that are not prebuilt, so it includes nothing but the two
- * project headers and uses only CUDA built-ins.
+ * combinations that are not prebuilt, so it includes nothing but project
+ * headers (launch parameters, tables, bitops.h) and uses only CUDA built-ins.
  *
  * The solver loop is the reference's (SimpleDiffEq.jl):
  *   adaptive:  src/tsit5/gpuatsit5.jl:250-320, src/verner/gpuvern7.jl:353-520,
@@ -23,11 +23,16 @@
  *     are compiled with --fmad=false);
  *   - stage times t + c*dt and Horner steps of the dense-output polynomials
  *     are fused, as Julia fuses scalar muladd;
- *   - the error norm EEst and the step-size factor q (q11 = EEst^beta1,
- *     qold^beta2, the clamps and the reciprocal applied to dt) are computed in
- *     single precision, q with the deterministic ctrl_pow below (the norm in
- *     double when abstol < 1e-30); dt, t and the state keep the solver
- *     precision;
+ *   - FP64 solves (default, GBODE_CTRL_DS): the error norm EEst and the
+ *     step-size factor q (EEst^beta1 / qold^beta2 and its clamps, taken on
+ *     logarithms) are computed in double-single arithmetic, pairs of singles
+ *     split from the doubles by integer operations (ds_* below), the error
+ *     estimate's sum multiplied by dt inside the norm, and dt times the
+ *     factor as fma(dt, l, dt * h); the norm is double when abstol < 1e-30.
+ *     With GBODE_CTRL64 q is double on logarithms (log_dev, exp_dev) on a
+ *     single-precision norm; without either, norm and q are single precision
+ *     (q with the deterministic ctrl_pow below).  dt, t and the state keep
+ *     the solver precision;
  *   - the dense-output abscissa theta multiplies by recip(dt) (a float
  *     reciprocal refined by one Newton step) and the polynomials that start at
  *     theta^2 multiply by one shared theta^2;
