@@ -154,6 +154,27 @@ def test_avern9_r3bp_fp32_kahan(pkg, po):
     assert_bitexact(sol, dev)
 
 
+@pytest.mark.parametrize("schedule", ["plain", "persistent"])
+@pytest.mark.parametrize("abstol,reltol", [(1e-32, 1e-8), (0.0, 1e-8), (1e-25, 1e-10)])
+def test_norm_edge_branches_bitexact(pkg, po, schedule, abstol, reltol):
+    """The error norm's edge branches, bit for bit against the oracle: abstol
+    below 1e-30 (the norm in double), abstol 0 (scales of m * reltol only, a
+    zero component giving a zero scale), abstol near the single range's edge,
+    and trajectories whose state is NaN (accepted like the reference, retcode
+    3) among ordinary ones."""
+    u0, p = lorenz_inputs(256, seed=9)
+    u0[:, 7] = np.nan
+    u0[0, 11] = 0.0
+    u0[1, 11] = 0.0
+    sv = np.linspace(0, 1, 9)
+    sol = gpu(pkg, pkg.GPUSimpleATsit5(), "lorenz", u0, p, (0.0, 1.0), 0.1, abstol=abstol, reltol=reltol, saveat=sv,
+              schedule=schedule, throw=False)
+    ref = po.solve("ATsit5", "lorenz", u0, p, (0, 1), 0.1, rounding="device", abstol=abstol, reltol=reltol,
+                   saveat=sv, nthreads=8)
+    assert_bitexact(sol, ref)
+    assert sol.retcode[7] == 3
+
+
 def test_dtmin_raises_like_reference(pkg):
     """abstol=0, reltol=1e-30 forces dt below dtmin: the reference throws
     error("dt<dtmin"); the ensemble marks the trajectory and raises."""

@@ -179,6 +179,9 @@ def test_nan_is_accepted_like_reference(po):
     o = po.solve("ATsit5", "lorenz", u0, p, (0, 1), 0.1)
     assert o["retcode"][0] == 3 and o["t_final"][0] == 1.0
     assert np.isnan(o["u_final"]).all()
+    for ctrl in ("ds", "fp64", "fp32"):  # the device canon ends the same way with every controller
+        o = po.solve("ATsit5", "lorenz", u0, p, (0, 1), 0.1, rounding="device", controller=ctrl)
+        assert o["retcode"][0] == 3 and o["t_final"][0] == 1.0, ctrl
 
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
