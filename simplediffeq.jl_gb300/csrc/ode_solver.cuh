@@ -688,7 +688,7 @@ struct RhsR3BP {
 template <class R, class T, int DD>
 struct RhsKuramoto {
   enum { D = DD, NP = DD + 1 };
-  R p[DD + 1];
+  R p[DD + 1];  /* omega_1..omega_D, then K / D (rhs_loaded divides the loaded K once) */
   __device__ __forceinline__ void operator()(const R (&u)[DD], T t, R (&du)[DD]) const {
     R sn[DD], cs[DD], S = 0, C = 0;
 #pragma unroll 1
@@ -697,11 +697,20 @@ struct RhsKuramoto {
       S = S + sn[j];
       C = C + cs[j];
     }
-    const R kd = p[DD] / (R)DD;
+    const R kd = p[DD];
 #pragma unroll
     for (int i = 0; i < DD; ++i) du[i] = fmaR(kd, fmaR(cs[i], S, -(sn[i] * C)), p[i]);
   }
 };
+
+/* Called once after a trajectory's parameters are loaded from the caller's
+ * array: the Kuramoto coupling K / D is divided there, not in every
+ * right-hand-side evaluation (a double division is about nine FP64
+ * instructions); the same IEEE operation on the same operands. */
+template <class F> __device__ __forceinline__ void rhs_loaded(F&) {}
+template <class R, class T, int DD> __device__ __forceinline__ void rhs_loaded(RhsKuramoto<R, T, DD>& f) {
+  f.p[DD] = f.p[DD] / (R)DD;
+}
 
 template <class R, class T, int DD>
 struct RhsLinear {
@@ -1230,6 +1239,7 @@ __device__ __forceinline__ void lane_load(const KParams& P, long long idx, Lane<
   l.idx = idx;
 #pragma unroll
   for (int j = 0; j < F::NP; ++j) l.f.p[j] = (R)P.p[(long long)j * P.n + idx];
+  rhs_loaded(l.f);
 #pragma unroll
   for (int d = 0; d < D; ++d) {
     l.uh[d] = (R)P.u0[(long long)d * P.n + idx];
@@ -2187,6 +2197,7 @@ struct FixedSplitTsit5 {
     F f;
 #pragma unroll
     for (int j = 0; j < F::NP; ++j) f.p[j] = (R)P.p[(long long)j * P.n + idx];
+    rhs_loaded(f);
     R uh[1] = {(R)P.u0[(long long)C * P.n + idx]}, uc[1] = {(R)0};
     T t = (T)P.t0;
     const T dt = (T)P.dt;
