@@ -118,3 +118,35 @@ def test_abi_version_matches_header():
     text = open(JL).read()
     v = re.search(r"const ABI_VERSION = (\d+)", text).group(1)
     assert re.search(r"#define ODE_ABI_VERSION %s\b" % v, open(HDR).read())
+
+
+# the Julia module's symbol tables against the header's enums (names as the header spells them)
+ENUM_MAPS = {
+    "RHS_BUILTIN": {"lorenz": "ODE_RHS_LORENZ", "vanderpol": "ODE_RHS_VANDERPOL", "r3bp": "ODE_RHS_R3BP",
+                    "kuramoto": "ODE_RHS_KURAMOTO", "linear": "ODE_RHS_LINEAR"},
+    "PRECISION": {"fp64": "ODE_FP64", "fp32": "ODE_FP32", "fp32_kahan": "ODE_FP32_KAHAN"},
+    "SCHEDULE": {"plain": "ODE_SCHED_PLAIN", "persistent": "ODE_SCHED_PERSISTENT", "learned": "ODE_SCHED_LEARNED"},
+    "CONTROLLER": {"ds": "ODE_CTRL_DS", "fp64": "ODE_CTRL_FP64", "fp32": "ODE_CTRL_FP32"},
+    "SDE_BUILTIN": {"gbm": "ODE_SDE_GBM", "ou": "ODE_SDE_OU", "lorenz": "ODE_SDE_LORENZ", "mult": "ODE_SDE_MULT"},
+}
+
+
+def test_symbol_tables_match_header_enums(tmp_path):
+    """Every `const X = Dict(:name => id, ...)` table of the Julia module
+    names exactly the header's enumerators, with the values the C compiler
+    gives them (so a renumbered enum fails here)."""
+    text = open(JL).read()
+    names = sorted({c for m in ENUM_MAPS.values() for c in m.values()})
+    src = tmp_path / "enums.c"
+    src.write_text('#include <stdio.h>\n#include "%s"\nint main(void) {\n%s  return 0;\n}\n' % (
+        HDR, "".join('  printf("%s %%d\\n", (int)%s);\n' % (n, n) for n in names)))
+    exe = tmp_path / "enums"
+    subprocess.run(["gcc", "-std=c11", "-o", str(exe), str(src)], check=True, capture_output=True)
+    value = {k: int(v) for k, v in (line.split() for line in
+                                     subprocess.run([str(exe)], capture_output=True, text=True,
+                                                    check=True).stdout.splitlines())}
+    for table, mapping in ENUM_MAPS.items():
+        m = re.search(r"^const %s = Dict\((.*?)\)\s*$" % table, text, re.M)
+        assert m, table
+        got = {k: int(v) for k, v in re.findall(r":(\w+) => (\d+)", m.group(1))}
+        assert got == {k: value[c] for k, c in mapping.items()}, table
