@@ -137,3 +137,32 @@ def test_rhs_builtin_without_handle(pkg):
     lib = pkg._lib.load()
     rid = ctypes.c_int(-1)
     assert lib.ode_rhs_builtin(None, 0, 3, ctypes.byref(rid), None) == pkg._lib.EINVAL
+
+
+def test_python_symbol_tables_match_header_enums(pkg, tmp_path):
+    """The package's id tables (_lib.ALG, RHS, PREC, SCHED, CTRL, LAYOUT,
+    OUTPUT, KERNEL, SDE) hold the header's enum values, as the C compiler
+    gives them."""
+    L = pkg._lib
+    tables = {
+        "ALG": {k: "ODE_ALG_" + k.upper() for k in L.ALG},
+        "RHS": {k: "ODE_RHS_" + k.upper() for k in L.RHS},
+        "PREC": {"fp64": "ODE_FP64", "fp32": "ODE_FP32", "fp32_kahan": "ODE_FP32_KAHAN"},
+        "SCHED": {k: "ODE_SCHED_" + k.upper() for k in L.SCHED},
+        "CTRL": {k: "ODE_CTRL_" + k.upper() for k in L.CTRL},
+        "LAYOUT": {k: "ODE_LAYOUT_" + k.upper() for k in L.LAYOUT},
+        "OUTPUT": {"state": "ODE_OUTPUT_STATE", "kuramoto_r": "ODE_OUTPUT_KURAMOTO_R"},
+        "SDE": {k: "ODE_SDE_" + k.upper() for k in L.SDE},
+    }
+    kernels = {v: "ODE_KERNEL_" + v.upper() for v in L.KERNEL.values()}
+    names = sorted({c for t in tables.values() for c in t.values()} | set(kernels.values()))
+    src = tmp_path / "enums.c"
+    src.write_text('#include <stdio.h>\n#include "%s"\nint main(void) {\n%s  return 0;\n}\n' % (
+        HEADER, "".join('  printf("%s %%d\\n", (int)%s);\n' % (n, n) for n in names)))
+    exe = tmp_path / "enums"
+    subprocess.run(["gcc", "-std=c11", "-o", str(exe), str(src)], check=True, capture_output=True)
+    value = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                          check=True).stdout.splitlines())
+    for table, mapping in tables.items():
+        assert getattr(L, table) == {k: int(value[c]) for k, c in mapping.items()}, table
+    assert L.KERNEL == {int(value[c]): k for k, c in kernels.items()}
