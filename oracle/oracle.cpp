@@ -154,16 +154,21 @@ static inline void sincos_of(R x, R* s, R* c) {
  * precision mu * y^3, y = 1/sqrt(r) from Lomont's bit-level seed (magic
  * constant 0x5f375a86) and three Newton steps y (3/2 - (r/2) y^2) */
 static inline double r3bp_pull_dev(double mu, double r) { return mu / (r * std::sqrt(r)); }
-static inline float r3bp_pull_dev(float mu, float r) {
-  int32_t ri;
-  std::memcpy(&ri, &r, 4);
-  const int32_t yi = 0x5f375a86 - (ri >> 1);
+/* 1/sqrt(x) for a positive normal single (kernels: rsqrt_nr) */
+static inline float rsqrt_nr_f(float x) {
+  int32_t xi;
+  std::memcpy(&xi, &x, 4);
+  const int32_t yi = 0x5f375a86 - (xi >> 1);
   float y;
   std::memcpy(&y, &yi, 4);
-  const float hx = 0.5f * r;
+  const float hx = 0.5f * x;
   y = y * std::fma(-(hx * y), y, 1.5f);
   y = y * std::fma(-(hx * y), y, 1.5f);
   y = y * std::fma(-(hx * y), y, 1.5f);
+  return y;
+}
+static inline float r3bp_pull_dev(float mu, float r) {
+  const float y = rsqrt_nr_f(r);
   return mu * ((y * y) * y);
 }
 
@@ -1630,7 +1635,79 @@ double exp_dev(double x) {
 
 /* normals z_{2P}, z_{2P+1} of trajectory idx's stream: Philox counter
  * (P low, P high, idx low, idx high), key = seed, then Box-Muller */
+/* the SDE normals in double-single arithmetic (kernels: sde_solver.cuh's
+ * normal_pair): v 2^-e from an integer's top 24 and next 24 bits; sqrt by
+ * rsqrt_nr and one correction; sin and cos of |r| <= pi/4 by Taylor series */
+static DS ds_from_u64(uint64_t v, int e) {
+  const int z = __builtin_clzll(v);
+  const uint64_t m = v << z;
+  const float hi = (float)(uint32_t)(m >> 40) * bits_f((40 - z - e + 127) << 23);
+  const float lo = (float)(uint32_t)((m >> 16) & 0xffffff) * bits_f((16 - z - e + 127) << 23);
+  return {hi, lo};
+}
+static DS ds_sqrt(DS y) {
+  if (!(y.h > 0.0f)) return {0.0f, 0.0f};
+  const float r = rsqrt_nr_f(y.h);
+  const float sq = y.h * r;
+  const float p = sq * sq, pe = std::fma(sq, sq, -p);
+  return ds_fast(sq, (((y.h - p) - pe) + y.l) * (0.5f * r));
+}
+static void ds_sincos_reduced(DS r, DS* sn, DS* cs) {
+  const DS r2 = ds_sqr(r);
+  float ts = std::fma(r2.h, GBODE_DS_SIN_T7, GBODE_DS_SIN_T6);
+  ts = std::fma(r2.h, ts, GBODE_DS_SIN_T5);
+  DS ps = {ts, 0.0f};
+  ps = ds_add(ds_mul(ps, r2), DS{GBODE_DS_SIN_C4_H, GBODE_DS_SIN_C4_L});
+  ps = ds_add(ds_mul(ps, r2), DS{GBODE_DS_SIN_C3_H, GBODE_DS_SIN_C3_L});
+  ps = ds_add(ds_mul(ps, r2), DS{GBODE_DS_SIN_C2_H, GBODE_DS_SIN_C2_L});
+  ps = ds_add(ds_mul(ps, r2), DS{GBODE_DS_SIN_C1_H, GBODE_DS_SIN_C1_L});
+  ps = ds_add(ds_mul(ps, r2), DS{1.0f, 0.0f});
+  *sn = ds_mul(r, ps);
+  float tc = std::fma(r2.h, GBODE_DS_COS_T8, GBODE_DS_COS_T7);
+  tc = std::fma(r2.h, tc, GBODE_DS_COS_T6);
+  tc = std::fma(r2.h, tc, GBODE_DS_COS_T5);
+  DS pc = {tc, 0.0f};
+  pc = ds_add(ds_mul(pc, r2), DS{GBODE_DS_COS_C4_H, GBODE_DS_COS_C4_L});
+  pc = ds_add(ds_mul(pc, r2), DS{GBODE_DS_COS_C3_H, GBODE_DS_COS_C3_L});
+  pc = ds_add(ds_mul(pc, r2), DS{GBODE_DS_COS_C2_H, GBODE_DS_COS_C2_L});
+  pc = ds_add(ds_mul(pc, r2), DS{GBODE_DS_COS_C1_H, GBODE_DS_COS_C1_L});
+  *cs = ds_add(ds_mul(pc, r2), DS{1.0f, 0.0f});
+}
+static inline double ds_to_double(DS x) { return f2d_bits(x.h) + f2d_bits(x.l); }
+
+/* normals z_{2P}, z_{2P+1} of trajectory idx's stream: Philox counter
+ * (P low, P high, idx low, idx high), key = seed; u1 = (a + 1) 2^-53, u2 =
+ * c 2^-53; r = sqrt(-2 ln u1); angle 2 pi u2 = (k + f) pi/2 with k =
+ * round(4 u2) (half up) and f exact in integers; (r cos, r sin) */
 void normal_pair(uint64_t seed, int64_t P, int64_t idx, double* z0, double* z1) {
+  const uint32_t c[4] = {(uint32_t)P, (uint32_t)((uint64_t)P >> 32), (uint32_t)idx, (uint32_t)((uint64_t)idx >> 32)};
+  const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  uint32_t r[4];
+  philox(c, key, r);
+  const uint64_t a = ((uint64_t)(r[0] >> 5) << 26) | (r[1] >> 6);
+  const uint64_t cc = ((uint64_t)(r[2] >> 5) << 26) | (r[3] >> 6);
+  const DS lg = ds_log(ds_from_u64(a + 1, 53));
+  const DS rad = ds_sqrt(DS{-2.0f * lg.h, -2.0f * lg.l});
+  const uint64_t k = (cc + (1ULL << 50)) >> 51;
+  const int64_t fi = (int64_t)cc - (int64_t)(k << 51);
+  DS f = {0.0f, 0.0f};
+  if (fi != 0) {
+    f = ds_from_u64((uint64_t)(fi < 0 ? -fi : fi), 51);
+    if (fi < 0) f = ds_neg(f);
+  }
+  DS sr, cr;
+  ds_sincos_reduced(ds_mul(f, DS{GBODE_DS_PIO2_H, GBODE_DS_PIO2_L}), &sr, &cr);
+  const int q = (int)(k & 3);
+  const DS sn = q == 0 ? sr : q == 1 ? cr : q == 2 ? ds_neg(sr) : ds_neg(cr);
+  const DS cs = q == 0 ? cr : q == 1 ? ds_neg(sr) : q == 2 ? ds_neg(cr) : sr;
+  *z0 = ds_to_double(ds_mul(rad, cs));
+  *z1 = ds_to_double(ds_mul(rad, sn));
+}
+
+/* the same pair in the reference's rounding: the 53-bit uniforms as doubles
+ * and the Box-Muller transform with libm's log, sqrt, sin and cos (as a
+ * Float64 randn built from these uniforms would compute it) */
+void normal_pair_ref(uint64_t seed, int64_t P, int64_t idx, double* z0, double* z1) {
   const uint32_t c[4] = {(uint32_t)P, (uint32_t)((uint64_t)P >> 32), (uint32_t)idx, (uint32_t)((uint64_t)idx >> 32)};
   const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
   uint32_t r[4];
@@ -1639,11 +1716,10 @@ void normal_pair(uint64_t seed, int64_t P, int64_t idx, double* z0, double* z1) 
   const uint64_t cc = ((uint64_t)(r[2] >> 5) << 26) | (r[3] >> 6);
   const double u1 = (double)(a + 1) * 0x1.0p-53;
   const double u2 = (double)cc * 0x1.0p-53;
-  const double rad = std::sqrt(-2.0 * log_dev(u1));
-  double sn, cs;
-  sincos_dev(u2 * 0x1.921fb54442d18p+2, &sn, &cs);
-  *z0 = rad * cs;
-  *z1 = rad * sn;
+  const double rad = std::sqrt(-2.0 * std::log(u1));
+  const double ang = 2.0 * M_PI * u2;
+  *z0 = rad * std::cos(ang);
+  *z1 = rad * std::sin(ang);
 }
 
 constexpr int MAXM = 16;  /* noise dimensions of a non-diagonal SDE */
@@ -1680,8 +1756,10 @@ void sde_fg(const oracle_sde_args* a, bool dev, const double* u, const double* p
 }
 
 /* xi[0..N) = z_{kN} .. z_{kN+N-1} of trajectory i's normal stream; a pair
- * that straddles two steps is drawn once, its second normal kept in carry */
-void step_normals(uint64_t seed, int64_t k, int N, int64_t i, double* xi, double* carry) {
+ * that straddles two steps is drawn once, its second normal kept in carry;
+ * device rounding: the kernels' double-single normals, reference rounding:
+ * libm's */
+void step_normals(uint64_t seed, int64_t k, int N, int64_t i, double* xi, double* carry, bool dev) {
   for (int d = 0; d < N; ++d) {
     const int64_t gi = k * N + d;
     if (d == 0 && (gi & 1)) {
@@ -1690,7 +1768,8 @@ void step_normals(uint64_t seed, int64_t k, int N, int64_t i, double* xi, double
     }
     if (gi & 1) continue;  /* filled with its pair */
     double z1;
-    normal_pair(seed, gi / 2, i, &xi[d], &z1);
+    if (dev) normal_pair(seed, gi / 2, i, &xi[d], &z1);
+    else normal_pair_ref(seed, gi / 2, i, &xi[d], &z1);
     if (d + 1 < N) xi[d + 1] = z1;
     else *carry = z1;
   }
@@ -1718,7 +1797,7 @@ void solve_em(const oracle_sde_args* a, int64_t i) {
     (void)t;  /* the built-in SDEs are autonomous */
     sde_fg(a, dev, u, p, f, g);
     /* step k takes the next D (diagonal) or M normals of the stream */
-    step_normals(a->seed, k, M > 0 ? M : D, i, xi, &carry);
+    step_normals(a->seed, k, M > 0 ? M : D, i, xi, &carry, dev);
     for (int d = 0; d < D; ++d) {
       if (M > 0) {
         double s = g[d * M] * xi[0];

@@ -1,7 +1,9 @@
-"""Tables and constants of the double-single error norm and step-size
-controller (ODE_CTRL_DS): values held as unevaluated sums hi + lo of two
-IEEE single-precision numbers (about 48 significant bits), so that the
-logarithm and exponential of the controller run on the single-precision pipe.
+"""Tables and constants of the double-single arithmetic: the error norm and
+step-size controller of the FP64 solves (ODE_CTRL_DS) and the Box-Muller
+normals of the SDE solver, with values held as unevaluated sums hi + lo of two
+IEEE single-precision numbers (about 48 significant bits), so that their
+logarithm, exponential, square root, sine and cosine run on the
+single-precision pipe.
 
 Logarithm (after P. T. P. Tang, ACM TOMS 16(4), 1990, with single-precision
 parts): a = 2^E m, m in [1, 2); the top 7 bits of m's fraction pick row j;
@@ -19,6 +21,11 @@ controller's constants (src/SimpleDiffEq.jl: beta1 = 7/50, beta2 = 2/25,
 qmax = 10, qmin = 1/5, gamma = 9/10, qoldinit = 1e-4, each first rounded to
 double as the reference's Float64 cache holds it) are written as hi + lo
 singles, their logarithms as hi + lo of the logarithm of that double.
+
+Sine and cosine (the normals' angle, reduced to |r| <= pi/4 exactly): the
+Taylor series of sin r / r and cos r in r^2, the terms above 2^-24 in
+double-single, the rest in single precision (truncation below 2^-50); pi/2 as
+a double-single pair.
 
 All values in 60-digit arithmetic (mpmath).  Writes ds_table.h next to this
 script; ode_solver.cuh and the oracle include it.
@@ -86,10 +93,17 @@ def header():
         "EXP_L_A": ea, "EXP_L_B": eb, "EXP_L_C": ec,
         "EXP_INV_L": f32(NEXP / ln2),
     }
+    fact = mp.factorial
+    # sin r / r = 1 + r2 (S1 + r2 (S2 + r2 (S3 + r2 (S4 + r2 T(r2))))), T in single precision; cos alike
+    trig_ds = {"SIN_C%d" % i: (-1) ** i / fact(2 * i + 1) for i in range(1, 5)}
+    trig_ds.update({"COS_C%d" % i: (-1) ** i / fact(2 * i) for i in range(1, 5)})
+    trig_ds["PIO2"] = mp.pi / 2
+    consts.update({"SIN_T%d" % i: f32((-1) ** i / fact(2 * i + 1)) for i in range(5, 8)})
+    consts.update({"COS_T%d" % i: f32((-1) ** i / fact(2 * i)) for i in range(5, 9)})
     dbl = {"B1": 7.0 / 50.0, "B2": 2.0 / 25.0}
     logs = {"LN_QMAXI": 1.0 / 10.0, "LN_QMINI": 5.0, "LN_GAMMA": 9.0 / 10.0, "LN_QOLDINIT": 1.0e-4}
-    out = ["/* generated by gen_dstab.py: tables and constants of the double-single error norm and\n",
-           " * step-size controller (values as hi + lo single-precision pairs) */\n",
+    out = ["/* generated by gen_dstab.py: tables and constants of the double-single error norm,\n",
+           " * step-size controller and normals (values as hi + lo single-precision pairs) */\n",
            "#pragma once\n",
            "#ifndef GBODE_DSTAB_SPACE\n#define GBODE_DSTAB_SPACE static const\n#endif\n"]
     for k, v in consts.items():
@@ -99,6 +113,9 @@ def header():
         out.append("#define GBODE_DS_%s_H %s\n#define GBODE_DS_%s_L %s\n" % (k, hexf(h), k, hexf(l)))
     for k, v in logs.items():
         h, l = split2(mp.log(mp.mpf(v)))
+        out.append("#define GBODE_DS_%s_H %s\n#define GBODE_DS_%s_L %s\n" % (k, hexf(h), k, hexf(l)))
+    for k, v in trig_ds.items():
+        h, l = split2(mp.mpf(v))
         out.append("#define GBODE_DS_%s_H %s\n#define GBODE_DS_%s_L %s\n" % (k, hexf(h), k, hexf(l)))
     out.append("/* row j: c_j (a multiple of 2^-8), -ln c_j = hi + lo */\n")
     out.append("GBODE_DSTAB_SPACE float kDsLogTab[%d][3] = {\n" % NLOG)

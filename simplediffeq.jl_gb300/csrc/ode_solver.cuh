@@ -498,6 +498,8 @@ __device__ __forceinline__ double f2d_bits(float f) {
 }
 /* d * (x.h + x.l) as fma(d, x.l, d * x.h): two double operations */
 __device__ __forceinline__ double ds_scale(double d, dsf x) { return __fma_rn(d, f2d_bits(x.l), d * f2d_bits(x.h)); }
+/* h + l as a double: both parts moved into doubles by their bits, one double addition */
+__device__ __forceinline__ double ds_to_double(dsf x) { return f2d_bits(x.h) + f2d_bits(x.l); }
 
 /* With the double-single norm the FP64 kernels hand the error estimate over
  * unscaled: sum(btilde_i k_i), which the norm multiplies by dt in

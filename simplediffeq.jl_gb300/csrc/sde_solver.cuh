@@ -19,9 +19,10 @@
  *     high word), key = seed, gives z_{2P} and z_{2P+1}:
  *   - two 53-bit uniforms u1 in (0, 1], u2 in [0, 1) and the Box-Muller pair
  *     (G. E. P. Box, M. E. Muller, 1958) r = sqrt(-2 log u1),
- *     (r cos 2 pi u2, r sin 2 pi u2), with ode_solver.cuh's log_dev and
- *     ode_solver.cuh's sincos_cw, so that the oracle reproduces every normal
- *     bit for bit.
+ *     (r cos 2 pi u2, r sin 2 pi u2), evaluated in double-single arithmetic
+ *     on the single-precision pipe (normal_pair below: within about 2^-44 of
+ *     the exact values; two double operations a pair), so that the oracle
+ *     reproduces every normal bit for bit.
  * Non-diagonal noise takes M normals a step from the same stream.
  * Update rounding (device canon): diagonal u = fma(sqdt*g, xi, fma(f, dt, u));
  * non-diagonal s = G[d][0] xi_0, s = fma(G[d][m], xi_m, s) for m = 1..M-1,
@@ -65,6 +66,61 @@ __device__ __forceinline__ U4 philox4x32_10(U4 c, unsigned k0, unsigned k1) {
 }
 
 /* Normals z_{2P} and z_{2P+1} of trajectory idx's stream. */
+/* v 2^-e for 0 < v < 2^64 as a double-single pair, with integer operations:
+ * v is shifted left by its leading zeros, h = its top 24 bits and l = the next
+ * 24 (both exact singles) scaled through the exponent field; bits below those
+ * 48 are dropped (v 2^-e must leave both scales in the normal single range). */
+__device__ __forceinline__ dsf ds_from_u64(unsigned long long v, int e) {
+  const int z = __clzll((long long)v);
+  const unsigned long long m = v << z;
+  const float hi = (float)(unsigned)(m >> 40) * __int_as_float((40 - z - e + 127) << 23);
+  const float lo = (float)(unsigned)((m >> 16) & 0xffffff) * __int_as_float((16 - z - e + 127) << 23);
+  return {hi, lo};
+}
+
+/* sqrt(y) for y >= 0: s = y.h rsqrt_nr(y.h), then one correction (y - s^2) /
+ * (2 s) with s^2 an exact product pair (y.h - s^2 is exact by Sterbenz) */
+__device__ __forceinline__ dsf ds_sqrt(dsf y) {
+  if (!(y.h > 0.0f)) return {0.0f, 0.0f};
+  const float r = rsqrt_nr(y.h);
+  const float sq = y.h * r;
+  const float p = sq * sq, pe = __fmaf_rn(sq, sq, -p);
+  return ds_fast(sq, (((y.h - p) - pe) + y.l) * (0.5f * r));
+}
+
+/* sin r and cos r for |r| <= pi/4 + tiny: Taylor series of sin r / r and
+ * cos r in r^2, the terms above 2^-24 in double-single and the rest in single
+ * precision (truncation below 2^-50) */
+__device__ __forceinline__ void ds_sincos_reduced(dsf r, dsf* sn, dsf* cs) {
+  const dsf r2 = ds_sqr(r);
+  float ts = __fmaf_rn(r2.h, GBODE_DS_SIN_T7, GBODE_DS_SIN_T6);
+  ts = __fmaf_rn(r2.h, ts, GBODE_DS_SIN_T5);
+  dsf ps = {ts, 0.0f};
+  ps = ds_add(ds_mul(ps, r2), dsf{GBODE_DS_SIN_C4_H, GBODE_DS_SIN_C4_L});
+  ps = ds_add(ds_mul(ps, r2), dsf{GBODE_DS_SIN_C3_H, GBODE_DS_SIN_C3_L});
+  ps = ds_add(ds_mul(ps, r2), dsf{GBODE_DS_SIN_C2_H, GBODE_DS_SIN_C2_L});
+  ps = ds_add(ds_mul(ps, r2), dsf{GBODE_DS_SIN_C1_H, GBODE_DS_SIN_C1_L});
+  ps = ds_add(ds_mul(ps, r2), dsf{1.0f, 0.0f});
+  *sn = ds_mul(r, ps);
+  float tc = __fmaf_rn(r2.h, GBODE_DS_COS_T8, GBODE_DS_COS_T7);
+  tc = __fmaf_rn(r2.h, tc, GBODE_DS_COS_T6);
+  tc = __fmaf_rn(r2.h, tc, GBODE_DS_COS_T5);
+  dsf pc = {tc, 0.0f};
+  pc = ds_add(ds_mul(pc, r2), dsf{GBODE_DS_COS_C4_H, GBODE_DS_COS_C4_L});
+  pc = ds_add(ds_mul(pc, r2), dsf{GBODE_DS_COS_C3_H, GBODE_DS_COS_C3_L});
+  pc = ds_add(ds_mul(pc, r2), dsf{GBODE_DS_COS_C2_H, GBODE_DS_COS_C2_L});
+  pc = ds_add(ds_mul(pc, r2), dsf{GBODE_DS_COS_C1_H, GBODE_DS_COS_C1_L});
+  *cs = ds_add(ds_mul(pc, r2), dsf{1.0f, 0.0f});
+}
+
+/* The normals z_{2P}, z_{2P+1} of trajectory idx: Philox gives two 53-bit
+ * integers a, c; u1 = (a + 1) 2^-53 and u2 = c 2^-53 are taken as
+ * double-single pairs straight from the integers (ds_from_u64); r =
+ * sqrt(-2 ln u1) (ds_log, ds_sqrt); the angle 2 pi u2 = k pi/2 + f pi/2 with
+ * 4 u2 = k + f, k = round(4 u2) (half up) and f = (c - k 2^51) 2^-51 in
+ * [-1/2, 1/2], both exact in integers, then sin and cos of f pi/2 and the
+ * quadrant k mod 4; z0 = r cos, z1 = r sin, each a double from its pair (one
+ * double addition). */
 __device__ __forceinline__ void normal_pair(unsigned long long seed, long long P, long long idx, double* z0,
                                             double* z1) {
   const U4 r = philox4x32_10(U4{(unsigned)P, (unsigned)((unsigned long long)P >> 32), (unsigned)idx,
@@ -72,13 +128,22 @@ __device__ __forceinline__ void normal_pair(unsigned long long seed, long long P
                              (unsigned)seed, (unsigned)(seed >> 32));
   const unsigned long long a = ((unsigned long long)(r.x >> 5) << 26) | (r.y >> 6);
   const unsigned long long c = ((unsigned long long)(r.z >> 5) << 26) | (r.w >> 6);
-  const double u1 = (double)(a + 1) * 0x1.0p-53;  /* (0, 1] */
-  const double u2 = (double)c * 0x1.0p-53;        /* [0, 1) */
-  const double rad = __dsqrt_rn(-2.0 * log_dev(u1));
-  double sn, cs;
-  sincos_cw(u2 * 0x1.921fb54442d18p+2, &sn, &cs);  /* 2 pi */
-  *z0 = rad * cs;
-  *z1 = rad * sn;
+  const dsf lg = ds_log(ds_from_u64(a + 1, 53));
+  const dsf rad = ds_sqrt(dsf{-2.0f * lg.h, -2.0f * lg.l});
+  const unsigned long long k = (c + (1ULL << 50)) >> 51;
+  const long long fi = (long long)c - (long long)(k << 51);
+  dsf f = {0.0f, 0.0f};
+  if (fi != 0) {
+    f = ds_from_u64((unsigned long long)(fi < 0 ? -fi : fi), 51);
+    if (fi < 0) f = ds_neg(f);
+  }
+  dsf sr, cr;
+  ds_sincos_reduced(ds_mul(f, dsf{GBODE_DS_PIO2_H, GBODE_DS_PIO2_L}), &sr, &cr);
+  const int q = (int)(k & 3);
+  const dsf sn = q == 0 ? sr : q == 1 ? cr : q == 2 ? ds_neg(sr) : ds_neg(cr);
+  const dsf cs = q == 0 ? cr : q == 1 ? ds_neg(sr) : q == 2 ? ds_neg(cr) : sr;
+  *z0 = ds_to_double(ds_mul(rad, cs));
+  *z1 = ds_to_double(ds_mul(rad, sn));
 }
 
 /* ------------------------------------------------------------------ built-in SDEs (diagonal noise) */

@@ -325,6 +325,26 @@ def test_counter_based_normals(po):
     assert po.normal_pair(7, 3, 9) != po.normal_pair(7, 3 + (1 << 32), 9)  # the pair index's high word counts
 
 
+def test_normals_are_box_muller_of_the_philox_uniforms(po):
+    """The double-single normals against the exact Box-Muller transform of the
+    same 53-bit uniforms (40-digit values): within 2^-42 of max(1, r)."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 40
+    seed = 7
+    worst = 0
+    for P in range(0, 400, 3):
+        for i in (0, 1, 12345, (1 << 33) + 5):
+            r = po.philox([P & 0xffffffff, P >> 32, i & 0xffffffff, i >> 32], [seed, 0])
+            a = ((r[0] >> 5) << 26) | (r[1] >> 6)
+            c = ((r[2] >> 5) << 26) | (r[3] >> 6)
+            rad = mp.sqrt(-2 * mp.log(mp.mpf(a + 1) / 2 ** 53))
+            ang = 2 * mp.pi * mp.mpf(c) / 2 ** 53
+            g0, g1 = po.normal_pair(seed, P, i)
+            err = max(abs(mp.mpf(g0) - rad * mp.cos(ang)), abs(mp.mpf(g1) - rad * mp.sin(ang))) / max(1, rad)
+            worst = max(worst, err)
+    assert worst < mp.mpf(2) ** -42, float(worst)
+
+
 @pytest.mark.parametrize("dim", [1, 2, 3, 5])
 def test_simple_em_consumes_the_normal_stream_in_order(po, dim):
     """Step k of a dim-D SDE takes normals z_{kD} .. z_{kD+D-1} of its
