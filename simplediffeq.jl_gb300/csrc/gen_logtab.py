@@ -1,4 +1,5 @@
-"""Table of the double logarithm used by the SimpleEM normal generator.
+"""Table of the double logarithm used by the FP64 step-size controller
+(ODE_CTRL_FP64).
 
 Table-driven logarithm after P. T. P. Tang, "Table-driven implementation of
 the logarithm function in IEEE floating-point arithmetic", ACM TOMS 16(4),
@@ -45,7 +46,7 @@ def table():
 
 def header():
     out = ["/* generated by gen_logtab.py: {1/F_j, T_j hi, T_j lo} for F_j = 1 + j/128, the logarithm table of\n",
-           " * the SimpleEM normal generator (T_j = -log(1/F_j rounded), minus ln 2 for j >= %d) */\n" % SHIFT_FROM,
+           " * the FP64 step-size controller (T_j = -log(1/F_j rounded), minus ln 2 for j >= %d) */\n" % SHIFT_FROM,
            "#pragma once\n",
            "#ifndef GBODE_LOGTAB_SPACE\n#define GBODE_LOGTAB_SPACE static const\n#endif\n",
            "#define GBODE_LOGTAB_SHIFT_FROM %d\n" % SHIFT_FROM,
