@@ -302,9 +302,10 @@ int ode_output_compile(ode_handle* h, const char* body, int dim, int nparams, in
  * noise_dim normals.  The reference draws xi_k with Julia's randn; here each
  * trajectory has one stream of normals from a counter-based generator
  * (Philox4x32-10 keyed by `seed`, counter = pair index, trajectory;
- * Box-Muller with the library's own log and sin/cos) that its steps consume in
- * order, so results depend only on (seed, trajectory index) and are
- * reproducible on the CPU. */
+ * Box-Muller of the two 53-bit uniforms in double-single arithmetic, within
+ * about 2^-43 of the exact transform) that its steps consume in order, so
+ * results depend only on (seed, trajectory index) and are reproducible on
+ * the CPU. */
 enum {
   ODE_SDE_GBM = 0,     /* geometric Brownian motion: f = mu u, g = sigma u (any dim), p = (mu, sigma) */
   ODE_SDE_OU = 1,      /* Ornstein-Uhlenbeck: f = theta (mu - u), g = sigma (any dim), p = (theta, mu, sigma) */
