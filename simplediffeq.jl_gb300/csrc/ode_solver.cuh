@@ -87,7 +87,10 @@ __device__ __forceinline__ float absR(float x) { return fabsf(x); }
  * below 1e-30 instead of a relative one.  Every step is one IEEE double operation, so the oracle reproduces it
  * bit for bit.  |x| >= 2^19 and non-finite x go to CUDA's sincos. */
 __device__ __forceinline__ void sincos_cw(double x, double* s, double* c) {
-  if (!(fabs(x) < 524288.0)) {
+  /* |x| < 2^19 as an integer compare of the magnitude bits (a double compare
+   * would issue on the FP64 pipe; NaN's bits lie above 2^19's, as its IEEE
+   * compare is false) */
+  if (!(((unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL) < 0x4120000000000000ULL)) {
     sincos(x, s, c);
     return;
   }
@@ -111,8 +114,11 @@ __device__ __forceinline__ void sincos_cw(double x, double* s, double* c) {
   pc = __fma_rn(pc, z, 0x1.555555554f0a9p-5);
   pc = __fma_rn(pc, z, -0x1.fffffffffff96p-2);
   const double cr = __fma_rn(z, pc, 1.0);
-  *s = q == 0 ? sr : q == 1 ? cr : q == 2 ? -sr : -cr;
-  *c = q == 0 ? cr : q == 1 ? -sr : q == 2 ? -cr : sr;
+  /* quadrant q: (sin, cos) = (sr, cr), (cr, -sr), (-sr, -cr), (-cr, sr); the
+   * negations flip the sign bit of the high word, off the FP64 pipe */
+  const double so = (q & 1) ? cr : sr, co = (q & 1) ? sr : cr;
+  *s = __hiloint2double(__double2hiint(so) ^ (int)((unsigned)(q & 2) << 30), __double2loint(so));
+  *c = __hiloint2double(__double2hiint(co) ^ (int)((unsigned)((q + 1) & 2) << 30), __double2loint(co));
 }
 /* sine and cosine of one argument with a single argument reduction */
 __device__ __forceinline__ void sincosR(double x, double* s, double* c) { sincos_cw(x, s, c); }
