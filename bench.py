@@ -305,6 +305,27 @@ def parity_vs_ref(cfg, u0, p, sv, res, m=4096):
     return out
 
 
+def bitexact_vs_oracle(cfg, u0, p, sv, res, m=4096):
+    """Fraction of the first m trajectories whose every output (final state,
+    accepted and rejected steps, saveat values) is bit-identical to the
+    oracle's REF rounding with correctly rounded powers (controller "ref"),
+    the restatement of the reference-arithmetic mode."""
+    import __graft_entry__ as g
+    po = g.oracle()
+    m = min(m, u0.shape[1])
+    ref = po.solve(cfg["alg"], cfg["rhs"], np.ascontiguousarray(u0[:, :m]), np.ascontiguousarray(p[:, :m]),
+                   cfg["tspan"], cfg["dt"], rounding="ref", controller="ref", abstol=cfg["abstol"],
+                   reltol=cfg["reltol"], saveat=sv, nthreads=os.cpu_count(), output=cfg["output"])
+    def eq(a, b):
+        return (a == b) | (np.isnan(a) & np.isnan(b))
+    same = np.all(eq(res["u_final"][:, :m], ref["u_final"]), axis=0)
+    same &= (res["naccept"][:m] == ref["naccept"]) & (res["nreject"][:m] == ref["nreject"])
+    if sv is not None and res.get("us") is not None:
+        same &= np.all(eq(res["us"][:, :, :m], ref["us"]), axis=(0, 1))
+    return {"trajectories": m, "frac_bit_identical": float(same.mean()),
+            "oracle": "REF rounding with correctly rounded powers"}
+
+
 WORKLOAD_TIMEOUT_S = 420
 
 
@@ -671,6 +692,23 @@ def main():
         ctl32_sample = {"u_final": outs["u_final"][:, :m_par].cpu().numpy(),
                         "naccept": outs["naccept"][:m_par].cpu().numpy(),
                         "us": us_sample()}
+
+    # the reference's own arithmetic throughout (ODE_CTRL_REF: unfused vector multiply-adds, the right-hand
+    # side as written, IEEE division and square root, the PI controller with correctly rounded powers), same
+    # schedule, tuned alike: what following the reference operation for operation costs, its parity with the
+    # reference's rounding, and its bit-identity with the oracle's restatement of that arithmetic
+    refa = None
+    if not fixed and cfg["precision"] == "fp64" and not long_solve:  # every rank: timed() holds barriers
+        if tune is not None and "unavailable" not in tune:
+            h.autotune(args_for(schedule, L.MEM_DEVICE, du0.data_ptr(), dp.data_ptr(), controller="ref"),
+                       args.tune_sample)
+        rk, _, _, _ = timed(schedule, max(1, min(args.steps, 3)), 1, controller="ref")
+        refa = {"ms_per_step": sum(rk) / len(rk), "value": n / (sum(rk) / len(rk) * 1e-3),
+                "cost_vs_default": (sum(rk) / len(rk)) / step_ms}
+        refa_sample = {"u_final": outs["u_final"][:, :m_par].cpu().numpy(),
+                       "naccept": outs["naccept"][:m_par].cpu().numpy(),
+                       "nreject": outs["nreject"][:m_par].cpu().numpy(),
+                       "us": us_sample()}
     scale = cfg["abstol"] + cfg["reltol"] * np.abs(uf_plain).max(0)
     dev_err = np.abs(uf_measured - uf_plain).max(0) / scale
     dev_err = dev_err[np.isfinite(dev_err)] if np.isfinite(dev_err).any() else np.zeros(1)
@@ -775,6 +813,10 @@ def main():
         if args.config != 4:
             ctl32["parity_vs_ref"] = parity_vs_ref(cfg, u0, p, sv, ctl32_sample)
         line["fp32_controller"] = ctl32
+    if refa is not None:
+        refa["parity_vs_ref"] = parity_vs_ref(cfg, u0, p, sv, refa_sample)
+        refa["bitexact_vs_oracle"] = bitexact_vs_oracle(cfg, u0, p, sv, refa_sample)
+        line["ref_arithmetic"] = refa
     if tune is not None:
         line["autotune"] = tune
     if args.config == 4:

@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define ODE_ABI_VERSION 5
+#define ODE_ABI_VERSION 6
 
 /* status codes */
 enum {
@@ -116,7 +116,8 @@ enum {
 
 /* arithmetic of the error norm and step-size controller of adaptive FP64 solves
  * (ode_solve_args.controller); single-precision solves always use their own
- * single-precision norm and controller */
+ * single-precision norm and controller.  ODE_CTRL_REF changes the arithmetic
+ * of the whole solve, fixed-step ones included. */
 enum {
   ODE_CTRL_DS = 0,   /* default: the norm EEst and the factor q = EEst^beta1 / qold^beta2 with its
                         clamps in double-single arithmetic (pairs of floats, about 48 bits, on the
@@ -128,8 +129,15 @@ enum {
   ODE_CTRL_FP64 = 1, /* the factor q in double precision (table-driven log and exp) on a
                         single-precision norm, whose 2^-24 rounding (times beta1) bounds how closely
                         step sizes follow the reference's; FP64 precision only */
-  ODE_CTRL_FP32 = 2  /* the norm and the factor q in single precision (deterministic power
+  ODE_CTRL_FP32 = 2, /* the norm and the factor q in single precision (deterministic power
                         function): step sizes follow the reference's to about 2^-24 relative */
+  ODE_CTRL_REF = 3   /* the reference's arithmetic throughout, FP64 only: the vector expressions'
+                        products and sums rounded separately (the reference's SVector muladd does
+                        not fuse), its right-hand-side and RK4 expressions as written, the dense
+                        abscissa by division, the norm in IEEE double and the PI controller with
+                        pow (CUDA's pow and sin/cos, which can differ from another libm in the last
+                        bit); slower, for results that follow the reference operation for
+                        operation */
 };
 
 /* per-trajectory return codes */

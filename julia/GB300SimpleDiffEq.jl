@@ -26,7 +26,7 @@ using SimpleDiffEq, SciMLBase, StaticArrays
 export compile_rhs, compile_output, compile_sde, learn_fit!, everystep_solve
 
 const lib = get(ENV, "GB300ODE_LIB", "libgb300ode.so")
-const ABI_VERSION = 5
+const ABI_VERSION = 6
 
 # ----------------------------------------------------------------------------- C structs
 
@@ -176,7 +176,7 @@ const AdaptiveAlg = Union{GPUSimpleATsit5, GPUSimpleAVern7, GPUSimpleAVern9}
 const RHS_BUILTIN = Dict(:lorenz => 0, :vanderpol => 1, :r3bp => 2, :kuramoto => 3, :linear => 4)
 const PRECISION = Dict(:fp64 => 0, :fp32 => 1, :fp32_kahan => 2)
 const SCHEDULE = Dict(:plain => 0, :persistent => 1, :learned => 2)
-const CONTROLLER = Dict(:ds => 0, :fp64 => 1, :fp32 => 2)
+const CONTROLLER = Dict(:ds => 0, :fp64 => 1, :fp32 => 2, :ref => 3)
 const SDE_BUILTIN = Dict(:gbm => 0, :ou => 1, :lorenz => 2, :mult => 3)
 const ODE_OK, ODE_ETRAJ, ODE_ESMALL = 0, -6, -8
 const RET_DTMIN, RET_MAXITERS = 1, 2
@@ -319,7 +319,9 @@ for the adaptive algorithms' default every-step output).  `rhs`: `:lorenz`,
 `:vanderpol`, `:r3bp`, `:kuramoto`, `:linear`, an id from `compile_rhs`, or the
 CUDA C++ body itself.  `controller` picks the error norm and step-size
 controller arithmetic of adaptive FP64 solves: `:ds` (default, double-single,
-ODE_CTRL_DS), `:fp64` (ODE_CTRL_FP64) or `:fp32` (ODE_CTRL_FP32).  Keyword defaults are the reference's;
+ODE_CTRL_DS), `:fp64` (ODE_CTRL_FP64) or `:fp32` (ODE_CTRL_FP32); `:ref`
+(ODE_CTRL_REF, FP64 only) runs the reference's own arithmetic throughout the
+solve, fixed-step ones included.  Keyword defaults are the reference's;
 `dt < dtmin` raises the reference's `error("dt<dtmin")`.
 """
 function SciMLBase.solve(ep::EnsembleProblem, alg::GPUSimpleAlg; trajectories::Integer, rhs,

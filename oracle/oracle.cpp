@@ -20,7 +20,9 @@
  * Two rounding modes (oracle_round):
  *   REF     what the Julia code rounds: @muladd on SVector arithmetic falls back
  *           to a separate multiply and add, scalar muladd (stage times, Horner
- *           steps of @evalpoly) fuses, the controller uses libm pow.
+ *           steps of @evalpoly) fuses, the controller uses libm pow, or with
+ *           ctrl == 3 the correctly rounded cr_pow of the kernels'
+ *           reference-arithmetic mode (ODE_CTRL_REF).
  *   DEVICE  the device rounding canon the CUDA kernels implement: every
  *           multiply-add of the reference's expressions is one fused
  *           multiply-add (linear combinations accumulate left to right in
@@ -43,6 +45,7 @@
 #include "../simplediffeq.jl_gb300/csrc/log_table.h"
 #include "../simplediffeq.jl_gb300/csrc/exp_table.h"
 #include "../simplediffeq.jl_gb300/csrc/ds_table.h"
+#include "../simplediffeq.jl_gb300/csrc/crpow.h"
 
 #include <algorithm>
 #include <cmath>
@@ -1134,8 +1137,10 @@ static void solve_adaptive(const oracle_args* a, oracle_out* o, int64_t i) {
       if (EEst != EEst) saw_nan = true;
 
       if (!P::DEV) {
-        R q11 = std::pow(EEst, beta1);
-        R q = (EEst == (R)0) ? (R)1 / qmax : q11 / std::pow(qold, beta2);
+        const bool crp = a->ctrl == 3 && sizeof(R) == sizeof(double);
+        R q11 = crp ? (R)gbode::cr_pow((double)EEst, (double)beta1) : std::pow(EEst, beta1);
+        R q = (EEst == (R)0) ? (R)1 / qmax
+                             : q11 / (crp ? (R)gbode::cr_pow((double)qold, (double)beta2) : std::pow(qold, beta2));
         if (EEst > (R)1) {
           dt = dt / (T)jmin((R)1 / qmin, q11 / gamma);
           ++nrej;

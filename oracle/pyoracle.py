@@ -25,8 +25,9 @@ FIXED = {"RK4", "Tsit5", "Vern7", "Vern9", "SimpleTsit5", "Euler"}
 RHS = {"lorenz": 0, "vanderpol": 1, "r3bp": 2, "kuramoto": 3, "linear": 4}
 PREC = {"fp64": 0, "fp32": 1, "fp32_kahan": 2}
 ROUND = {"ref": 0, "device": 1}
-# error norm and step-size controller of the FP64 adaptive solves (DEVICE rounding), as ODE_CTRL_*
-CTRL = {"ds": 0, "fp64": 1, "fp32": 2}
+# error norm and step-size controller of the FP64 adaptive solves (DEVICE rounding), as ODE_CTRL_*; with
+# REF rounding "ref" takes the controller's powers correctly rounded (the kernels' ODE_CTRL_REF mode)
+CTRL = {"ds": 0, "fp64": 1, "fp32": 2, "ref": 3}
 
 
 class _Args(ctypes.Structure):

@@ -343,7 +343,11 @@ def solve(prob, alg, trajectories=None, dt=0.1, abstol=1e-6, reltol=1e-3, saveat
     norm and step-size controller arithmetic of adaptive FP64 solves: "ds"
     (default, double-single: step sizes follow the reference's to about
     2^-44), "fp64" (double factors on a single-precision norm) or "fp32"
-    (single precision throughout), ODE_CTRL_DS / _FP64 / _FP32."""
+    (single precision throughout), ODE_CTRL_DS / _FP64 / _FP32; or "ref"
+    (ODE_CTRL_REF, FP64 only), the reference's arithmetic throughout the
+    solve, fixed-step ones included: no fused vector multiply-adds, the
+    right-hand sides as written, IEEE division and square root, pow in the
+    controller (slower)."""
     single = isinstance(prob, (ODEProblem, SDEProblem))
     eprob = EnsembleProblem(prob) if single else prob
     if isinstance(eprob.prob, SDEProblem) or isinstance(alg, SimpleEM):

@@ -17,7 +17,7 @@ ALG = {"RK4": 0, "Tsit5": 1, "ATsit5": 2, "Vern7": 3, "AVern7": 4, "Vern9": 5, "
 RHS = {"lorenz": 0, "vanderpol": 1, "r3bp": 2, "kuramoto": 3, "linear": 4}
 PREC = {"fp64": 0, "fp32": 1, "fp32_kahan": 2}
 KERNEL = {0: "plain", 1: "persistent", 2: "staged", 3: "fixed", 4: "fixedsplit", 5: "onestep"}
-CTRL = {"ds": 0, "fp64": 1, "fp32": 2}
+CTRL = {"ds": 0, "fp64": 1, "fp32": 2, "ref": 3}
 LAYOUT = {"soa": 0, "traj": 1}
 SCHED = {"plain": 0, "persistent": 1, "learned": 2}
 MEM_HOST, MEM_DEVICE = 0, 1

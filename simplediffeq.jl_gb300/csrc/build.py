@@ -94,7 +94,8 @@ def gen_sources():
     for fname, var in (("ode_solver.cuh", "kSrc_ode_solver_cuh"), ("ode_kparams.h", "kSrc_ode_kparams_h"),
                        ("tableaus.h", "kSrc_tableaus_h"), ("sde_solver.cuh", "kSrc_sde_solver_cuh"),
                        ("log_table.h", "kSrc_log_table_h"), ("exp_table.h", "kSrc_exp_table_h"),
-                       ("ds_table.h", "kSrc_ds_table_h"), ("bitops.h", "kSrc_bitops_h")):
+                       ("ds_table.h", "kSrc_ds_table_h"), ("bitops.h", "kSrc_bitops_h"),
+                       ("crpow.h", "kSrc_crpow_h"), ("crpow_table.h", "kSrc_crpow_table_h")):
         text = open(os.path.join(HERE, fname)).read()
         assert ")GBSRC\"" not in text
         parts.append('static const char* %s = R"GBSRC(%s)GBSRC";\n' % (var, text))
@@ -155,7 +156,7 @@ def build(verbose=False, jobs=None):
     os.makedirs(LIB, exist_ok=True)
     headers = [os.path.join(HERE, f) for f in ("ode_solver.cuh", "ode_kparams.h", "tableaus.h", "ode_host.h",
                                                "jlrange.h", "sde_solver.cuh", "log_table.h", "exp_table.h",
-                                               "ds_table.h", "bitops.h")] + [
+                                               "ds_table.h", "bitops.h", "crpow.h", "crpow_table.h")] + [
         os.path.join(PKG, "..", "include", "gb300ode.h")]
     host_tus = [os.path.join(HERE, f) for f in ("ode_capi.cu", "learn.cu", "noalloc.cu", "sde_capi.cu")]
     gen = [os.path.join(BUILD, "aot_registry.inc"), os.path.join(BUILD, "embedded_src.inc")]

@@ -1,0 +1,157 @@
+/* Correctly rounded power function x^y of the reference-arithmetic mode
+ * (ODE_CTRL_REF): exp(y log x) with the logarithm, the product and the
+ * exponential carried in double-double arithmetic (unevaluated sums hi + lo
+ * of two doubles, about 100 significant bits; T. J. Dekker, "A
+ * floating-point technique for extending the available precision", Numer.
+ * Math. 18, 1971), so that the double nearest the double-double result is
+ * the correctly rounded x^y unless x^y lies within about 2^-97 relative of a
+ * midpoint between two doubles.  Table-driven logarithm and exponential
+ * after P. T. P. Tang (ACM TOMS 16(4), 1990 and 15(2), 1989); the tables and
+ * the method's details are in gen_crpow.py.
+ *
+ * Every step is an IEEE double operation or an explicit fused multiply-add,
+ * so the kernels (nvcc / NVRTC, --fmad=false) and the CPU oracle (host C++,
+ * -ffp-contract=off) compute the same bits.  Domain: x >= 0 or NaN, any
+ * finite y (the controller's EEst^beta1 and qold^beta2); x < 0 gives NaN.
+ * Results that overflow give +Inf; results below 2^-1022 (subnormal) are
+ * not correctly rounded, and below about 2^-1021.9 are flushed to 0. */
+#pragma once
+
+#if defined(__CUDACC__) || defined(__CUDACC_RTC__)
+#define GBODE_CR __device__ __forceinline__
+#define GBODE_CRPOW_SPACE __device__ const
+namespace gbode {
+GBODE_CR double cr_fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+GBODE_CR long long cr_bits(double x) { return __double_as_longlong(x); }
+GBODE_CR double cr_from_bits(long long b) { return __longlong_as_double(b); }
+}  // namespace gbode
+#else
+#include <cmath>
+#include <cstring>
+#define GBODE_CR static inline
+namespace gbode {
+GBODE_CR double cr_fma(double a, double b, double c) { return std::fma(a, b, c); }
+GBODE_CR long long cr_bits(double x) { long long b; std::memcpy(&b, &x, 8); return b; }
+GBODE_CR double cr_from_bits(long long b) { double x; std::memcpy(&x, &b, 8); return x; }
+}  // namespace gbode
+#endif
+#include "crpow_table.h"
+
+namespace gbode {
+
+struct ddr { double h, l; };
+
+/* a + b = s + e exactly (Knuth's two-sum) */
+GBODE_CR ddr cr_two_sum(double a, double b) {
+  const double s = a + b;
+  const double bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+/* a + b = s + e exactly when |a| >= |b| or a == 0 (Dekker's fast two-sum) */
+GBODE_CR ddr cr_fast(double a, double b) {
+  const double s = a + b;
+  return {s, b - (s - a)};
+}
+/* a * b = p + e exactly */
+GBODE_CR ddr cr_two_prod(double a, double b) {
+  const double p = a * b;
+  return {p, cr_fma(a, b, -p)};
+}
+GBODE_CR ddr cr_add(ddr x, ddr y) {
+  const ddr s = cr_two_sum(x.h, y.h);
+  return cr_fast(s.h, s.l + (x.l + y.l));
+}
+/* double-double times double */
+GBODE_CR ddr cr_mul_d(ddr x, double d) {
+  const ddr p = cr_two_prod(x.h, d);
+  return cr_fast(p.h, cr_fma(x.l, d, p.l));
+}
+GBODE_CR ddr cr_mul(ddr x, ddr y) {
+  const ddr p = cr_two_prod(x.h, y.h);
+  return cr_fast(p.h, p.l + cr_fma(x.h, y.l, x.l * y.h));
+}
+
+/* log x in double-double for a positive normal or subnormal x */
+GBODE_CR ddr cr_log(double x) {
+  long long b = cr_bits(x);
+  int e = 0;
+  if (b < 0x0010000000000000LL) {  /* subnormal: scale by 2^54 */
+    b = cr_bits(x * 0x1p54);
+    e = -54;
+  }
+  e += (int)(b >> 52) - 1023;
+  const int j = (int)((b >> 44) & 0xff);
+  const double m = cr_from_bits((b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
+  if (j >= GBODE_CR_FOLD_FROM) e += 1;
+  const double r = cr_fma(m, kCrLogTab[j][0], -1.0);  /* exact */
+  /* log1p(r): r + r^2 (c2 + r (c3 + ... + r c6)) in double-double, plus r^7 q(r) in double */
+  double q = GBODE_CR_LG13;
+  q = cr_fma(q, r, GBODE_CR_LG12);
+  q = cr_fma(q, r, GBODE_CR_LG11);
+  q = cr_fma(q, r, GBODE_CR_LG10);
+  q = cr_fma(q, r, GBODE_CR_LG9);
+  q = cr_fma(q, r, GBODE_CR_LG8);
+  q = cr_fma(q, r, GBODE_CR_LG7);
+  ddr a = cr_add({GBODE_CR_LG6_H, GBODE_CR_LG6_L}, cr_fast(0.0, q * r));
+  a = cr_add({GBODE_CR_LG5_H, GBODE_CR_LG5_L}, cr_mul_d(a, r));
+  a = cr_add({GBODE_CR_LG4_H, GBODE_CR_LG4_L}, cr_mul_d(a, r));
+  a = cr_add({GBODE_CR_LG3_H, GBODE_CR_LG3_L}, cr_mul_d(a, r));
+  a = cr_add({GBODE_CR_LG2_H, GBODE_CR_LG2_L}, cr_mul_d(a, r));
+  const ddr l1p = cr_add(cr_fast(r, 0.0), cr_mul(a, cr_two_prod(r, r)));
+  /* e ln2 + T_j: e ln2_a exact, e ln2_b exact as a product pair, e ln2_c in double */
+  const double ed = (double)e;
+  ddr s = cr_add(cr_two_prod(ed, GBODE_CR_LN2_B), cr_fast(ed * GBODE_CR_LN2_A, ed * GBODE_CR_LN2_C));
+  s = cr_add(s, {kCrLogTab[j][1], kCrLogTab[j][2]});
+  return cr_add(s, l1p);
+}
+
+/* exp z for a double-double z with |z.h| <= 709.7 (2^-1022 <= result <= DBL_MAX) */
+GBODE_CR ddr cr_exp(ddr z) {
+  const double kb = cr_fma(z.h, GBODE_CR_INV_L64, 0x1.8p52);
+  const double kd = kb - 0x1.8p52;
+  const int k = (int)(cr_bits(kb) & 0xffffffffLL);  /* kd as a two's-complement integer */
+  /* r = z - k ln2/64: k L64_a exact, z.h - k L64_a exact (Sterbenz, or k == 0) */
+  const double t1 = cr_fma(-kd, GBODE_CR_L64_A, z.h);
+  ddr r = cr_add(cr_two_sum(t1, z.l), cr_two_prod(-kd, GBODE_CR_L64_B));
+  r = cr_add(r, cr_fast(-kd * GBODE_CR_L64_C, 0.0));
+  /* exp(r.h) (1 + r.l): 1 + r + r^2 (1/2 + r (1/6 + r (1/24 + r (1/120 + r q(r))))) */
+  const double x = r.h;
+  double q = GBODE_CR_EX11;
+  q = cr_fma(q, x, GBODE_CR_EX10);
+  q = cr_fma(q, x, GBODE_CR_EX9);
+  q = cr_fma(q, x, GBODE_CR_EX8);
+  q = cr_fma(q, x, GBODE_CR_EX7);
+  q = cr_fma(q, x, GBODE_CR_EX6);
+  ddr a = cr_add({GBODE_CR_EX5_H, GBODE_CR_EX5_L}, cr_fast(0.0, q * x));
+  a = cr_add({GBODE_CR_EX4_H, GBODE_CR_EX4_L}, cr_mul_d(a, x));
+  a = cr_add({GBODE_CR_EX3_H, GBODE_CR_EX3_L}, cr_mul_d(a, x));
+  a = cr_add({GBODE_CR_EX2_H, GBODE_CR_EX2_L}, cr_mul_d(a, x));
+  ddr er = cr_add(cr_fast(1.0, x), cr_mul(a, cr_two_prod(x, x)));
+  er = cr_add(er, cr_mul_d(er, r.l));
+  const int jj = k & 63;
+  const ddr res = cr_mul({kCrExpTab[jj][0], kCrExpTab[jj][1]}, er);
+  /* times 2^(k >> 6): split in two factors so that each is a normal double */
+  const int n = k >> 6;
+  const int n1 = n / 2, n2 = n - n1;
+  const double s1 = cr_from_bits((long long)(n1 + 1023) << 52), s2 = cr_from_bits((long long)(n2 + 1023) << 52);
+  return {(res.h * s1) * s2, (res.l * s1) * s2};
+}
+
+/* x^y, correctly rounded (see the header comment) */
+GBODE_CR double cr_pow(double x, double y) {
+  if (x != x || y != y) return x + y;
+  if (y == 0.0) return 1.0;
+  if (x < 0.0) return cr_from_bits(0x7ff8000000000000LL);
+  if (x == 0.0) return y > 0.0 ? 0.0 : cr_from_bits(0x7ff0000000000000LL);
+  if (cr_bits(x) == 0x7ff0000000000000LL) return y > 0.0 ? x : 0.0;
+  if (x == 1.0) return 1.0;
+  const ddr lx = cr_log(x);
+  const ddr z = cr_mul_d(lx, y);
+  if (z.h > 709.7) return cr_from_bits(0x7ff0000000000000LL);
+  if (z.h < -708.3) return 0.0;
+  /* v is normalized (v.h is the double nearest v.h + v.l) and the scaling
+   * by 2^n in cr_exp is exact for normal results */
+  return cr_exp(z).h;
+}
+
+}  // namespace gbode

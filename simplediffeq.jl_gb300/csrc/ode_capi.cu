@@ -279,7 +279,7 @@ const char* entry_kind(int alg, int sched, int64_t nsave) {
 bool use_fixed_split(const ode_handle* h, const ode_solve_args* a) {
   const bool separable = a->rhs == ODE_RHS_LORENZ || a->rhs == ODE_RHS_VANDERPOL || a->rhs == ODE_RHS_LINEAR;
   return a->alg == ODE_ALG_TSIT5 && separable && a->nsave == 0 && a->output == ODE_OUTPUT_STATE &&
-         a->precision == ODE_FP64 && a->dim >= 2 && a->dim <= 8 &&
+         a->precision == ODE_FP64 && a->controller != ODE_CTRL_REF && a->dim >= 2 && a->dim <= 8 &&
          (a->n + 31) / 32 <= (int64_t)h->nsm * 2;
 }
 
@@ -357,17 +357,24 @@ int output_width(ode_handle* h, const ode_solve_args* a) {
 
 /* The norm/controller variant a kernel is compiled with: the controller
  * choice applies to adaptive FP64 kernels, every other kernel is the same
- * whichever is asked (and is built as the default, ODE_CTRL_DS). */
+ * whichever is asked (and is built as the default, ODE_CTRL_DS), except that
+ * ODE_CTRL_REF (FP64 only) sets the arithmetic of every kernel. */
 int ctrl_variant(const ode_solve_args* a) {
+  if (a->controller == ODE_CTRL_REF) return ODE_CTRL_REF;
   if (is_fixed(a->alg) || a->precision != ODE_FP64) return ODE_CTRL_DS;
   return a->controller;
+}
+
+/* kernel-key suffix of a controller variant */
+const char* ctrl_suffix(int v) {
+  return v == ODE_CTRL_FP64 ? "|c64" : v == ODE_CTRL_FP32 ? "|c32" : v == ODE_CTRL_REF ? "|ref" : "";
 }
 
 std::string kernel_key(ode_handle* h, const ode_solve_args* a, int sched) {
   char b[160];
   snprintf(b, sizeof b, "%s|%s|%d|%d|%s|%d%s%s", alg_name(a->alg), kernel_kind(h, a, sched), a->rhs, a->dim,
            prec_name(a->precision), a->output >= ODE_OUTPUT_USER ? a->output : 0, h->bounds_check ? "|chk" : "",
-           ctrl_variant(a) == ODE_CTRL_FP64 ? "|c64" : ctrl_variant(a) == ODE_CTRL_FP32 ? "|c32" : "");
+           ctrl_suffix(ctrl_variant(a)));
   return b;
 }
 
@@ -377,6 +384,7 @@ std::string jit_source(ode_handle* h, const ode_solve_args* a, int sched) {
   std::string src;
   if (ctrl_variant(a) == ODE_CTRL_FP64) src += "#define GBODE_CTRL64 1\n";
   if (ctrl_variant(a) == ODE_CTRL_DS) src += "#define GBODE_CTRL_DS 1\n";
+  if (ctrl_variant(a) == ODE_CTRL_REF) src += "#define GBODE_REF 1\n";
   if (a->output >= ODE_OUTPUT_USER) {
     /* the output function goes before the solver header, whose store_point calls it */
     const UserOutput& u = h->outputs[a->output - ODE_OUTPUT_USER];
@@ -421,10 +429,10 @@ int nvrtc_cubin(const std::string& src, const std::vector<std::string>& extra_op
   }
   nvrtcProgram prog;
   const char* hdrs[] = {kSrc_ode_solver_cuh, kSrc_ode_kparams_h, kSrc_tableaus_h, kSrc_sde_solver_cuh, kSrc_log_table_h,
-                        kSrc_exp_table_h, kSrc_ds_table_h, kSrc_bitops_h};
+                        kSrc_exp_table_h, kSrc_ds_table_h, kSrc_bitops_h, kSrc_crpow_h, kSrc_crpow_table_h};
   const char* names[] = {"ode_solver.cuh", "ode_kparams.h", "tableaus.h", "sde_solver.cuh", "log_table.h",
-                         "exp_table.h", "ds_table.h", "bitops.h"};
-  nvrtcResult r = g_nvrtc.create(&prog, src.c_str(), "gbode_jit.cu", 8, hdrs, names);
+                         "exp_table.h", "ds_table.h", "bitops.h", "crpow.h", "crpow_table.h"};
+  nvrtcResult r = g_nvrtc.create(&prog, src.c_str(), "gbode_jit.cu", 10, hdrs, names);
   if (r != NVRTC_SUCCESS) {
     *err = std::string("nvrtcCreateProgram: ") + g_nvrtc.errstr(r);
     return ODE_ENVRTC;
@@ -621,15 +629,15 @@ static std::string gpu_tag(ode_handle* h) {
   return name + "/" + std::to_string(prop.multiProcessorCount);
 }
 
-/* kernel keys are alg|kind|rhs|dim|prec|output[|chk][|c64 or |c32]; only built-in ids travel, and
- * no bounds-check build */
+/* kernel keys are alg|kind|rhs|dim|prec|output[|chk][|c64, |c32 or |ref]; only built-in ids travel,
+ * and no bounds-check build */
 static bool portable_key(const std::string& key) {
   std::vector<std::string> f;
   size_t a = 0;
   for (size_t b; (b = key.find('|', a)) != std::string::npos; a = b + 1) f.push_back(key.substr(a, b - a));
   f.push_back(key.substr(a));
-  const bool ctrl_suffix = f.size() == 7 && (f[6] == "c64" || f[6] == "c32");
-  return (f.size() == 6 || ctrl_suffix) && std::atoi(f[2].c_str()) < ODE_RHS_USER &&
+  const bool has_ctrl = f.size() == 7 && (f[6] == "c64" || f[6] == "c32" || f[6] == "ref");
+  return (f.size() == 6 || has_ctrl) && std::atoi(f[2].c_str()) < ODE_RHS_USER &&
          std::atoi(f[5].c_str()) < ODE_OUTPUT_USER;
 }
 
@@ -849,10 +857,11 @@ int solve_impl(ode_handle* h, const ode_solve_args* a, ode_solve_out* o, ode_sol
   if (a->schedule < ODE_SCHED_PLAIN || a->schedule > ODE_SCHED_LEARNED) return fail(h, ODE_EINVAL, "unknown schedule");
   if (a->memory != ODE_MEM_HOST && a->memory != ODE_MEM_DEVICE) return fail(h, ODE_EINVAL, "unknown memory kind");
   if (a->layout != ODE_LAYOUT_SOA && a->layout != ODE_LAYOUT_TRAJ) return fail(h, ODE_EINVAL, "unknown output layout");
-  if (a->controller != ODE_CTRL_DS && a->controller != ODE_CTRL_FP64 && a->controller != ODE_CTRL_FP32)
+  if (a->controller != ODE_CTRL_DS && a->controller != ODE_CTRL_FP64 && a->controller != ODE_CTRL_FP32 &&
+      a->controller != ODE_CTRL_REF)
     return fail(h, ODE_EINVAL, "unknown step-size controller");
-  if (a->controller == ODE_CTRL_FP64 && a->precision != ODE_FP64)
-    return fail(h, ODE_ENOTSUP, "the FP64 step-size controller applies to FP64 solves");
+  if ((a->controller == ODE_CTRL_FP64 || a->controller == ODE_CTRL_REF) && a->precision != ODE_FP64)
+    return fail(h, ODE_ENOTSUP, "the FP64 and reference-arithmetic controllers apply to FP64 solves");
   if (a->n < 0 || a->n > 0x7fffffffLL) return fail(h, ODE_EINVAL, "n must be in [0, 2^31)");
   if (a->n > 0 && (!a->u0 || (a->nparams > 0 && !a->p))) return fail(h, ODE_EINVAL, "u0/p missing");
   if (!(a->t0 == a->t0) || !(a->tf == a->tf) || !(a->dt == a->dt))
@@ -1433,10 +1442,11 @@ int ode_ensemble_solve_everystep(ode_handle* h, const ode_solve_args* a, ode_eve
     return fail(h, ODE_EINVAL, "every-step output takes no saveat and the state output");
   if (a->memory != ODE_MEM_HOST && a->memory != ODE_MEM_DEVICE) return fail(h, ODE_EINVAL, "unknown memory kind");
   if (a->layout != ODE_LAYOUT_SOA && a->layout != ODE_LAYOUT_TRAJ) return fail(h, ODE_EINVAL, "unknown output layout");
-  if (a->controller != ODE_CTRL_DS && a->controller != ODE_CTRL_FP64 && a->controller != ODE_CTRL_FP32)
+  if (a->controller != ODE_CTRL_DS && a->controller != ODE_CTRL_FP64 && a->controller != ODE_CTRL_FP32 &&
+      a->controller != ODE_CTRL_REF)
     return fail(h, ODE_EINVAL, "unknown step-size controller");
-  if (a->controller == ODE_CTRL_FP64 && a->precision != ODE_FP64)
-    return fail(h, ODE_ENOTSUP, "the FP64 step-size controller applies to FP64 solves");
+  if ((a->controller == ODE_CTRL_FP64 || a->controller == ODE_CTRL_REF) && a->precision != ODE_FP64)
+    return fail(h, ODE_ENOTSUP, "the FP64 and reference-arithmetic controllers apply to FP64 solves");
   if (a->n < 0 || a->n > 0x7fffffffLL) return fail(h, ODE_EINVAL, "n must be in [0, 2^31)");
   CK(cudaSetDevice(h->device), "cudaSetDevice");
   const int64_t n = a->n;

@@ -41,10 +41,22 @@
  *   - in the single-precision modes the error norm and the controller use
  *     rcp_nr, log2_nr and exp2_nr (no IEEE division, square root or branch;
  *     the PI factors on log2 EEst).
+ * GBODE_REF (ODE_CTRL_REF, FP64 only) compiles the reference's arithmetic
+ * instead: a*b + c of the vector expressions rounded twice (Julia's generic
+ * muladd on SVector does not fuse), the right-hand sides and the RK4 update
+ * as their plain Julia expressions, theta = (t_save - told) / dt, the
+ * polynomials from theta^2 multiplied by theta twice, the error norm in IEEE
+ * double with division and square root, and the PI controller with a
+ * correctly rounded pow (cr_pow, crpow.h; src/SimpleDiffEq.jl:67-77,
+ * src/tsit5/gpuatsit5.jl:272-299); sine and cosine are CUDA's.  Scalar muladds (stage times, Horner steps) stay fused,
+ * as Julia fuses them.
  */
 #pragma once
 #include "ode_kparams.h"
 #include "bitops.h"
+#ifdef GBODE_REF
+#include "crpow.h"
+#endif
 #include "tableaus.h"
 #define GBODE_LOGTAB_SPACE __device__ const
 #include "log_table.h"
@@ -121,7 +133,13 @@ __device__ __forceinline__ void sincos_cw(double x, double* s, double* c) {
   *c = __hiloint2double(__double2hiint(co) ^ (int)((unsigned)((q + 1) & 2) << 30), __double2loint(co));
 }
 /* sine and cosine of one argument with a single argument reduction */
-__device__ __forceinline__ void sincosR(double x, double* s, double* c) { sincos_cw(x, s, c); }
+__device__ __forceinline__ void sincosR(double x, double* s, double* c) {
+#ifdef GBODE_REF
+  sincos(x, s, c);
+#else
+  sincos_cw(x, s, c);
+#endif
+}
 __device__ __forceinline__ void sincosR(float x, float* s, float* c) { sincosf(x, s, c); }
 
 /* Julia's min/max propagate NaN; @fastmath min/max are compare-and-select. */
@@ -170,6 +188,38 @@ __device__ __forceinline__ double recip(double x) {
   return __fma_rn(r0, e, r0);
 }
 __device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
+
+/* a*b + c of a vector expression (linear combinations, state updates): one
+ * fused multiply-add, or with GBODE_REF two roundings as the reference's
+ * SVector arithmetic does it (the files are compiled with --fmad=false). */
+template <class X> __device__ __forceinline__ X vmaddR(X a, X b, X c) {
+#ifdef GBODE_REF
+  return a * b + c;
+#else
+  return fmaR(a, b, c);
+#endif
+}
+
+/* The dense-output abscissa (t_save - told) / dtold: times recip(dtold), or
+ * with GBODE_REF the IEEE division. */
+template <class T> __device__ __forceinline__ T theta_of(T ts, T told, T dtold, T inv) {
+#ifdef GBODE_REF
+  return (ts - told) / dtold;
+#else
+  return (ts - told) * inv;
+#endif
+}
+
+/* b = theta^2 * ex of a dense-output polynomial that starts at theta^2:
+ * one shared theta^2, or with GBODE_REF theta * (theta * ex) as @evalpoly
+ * with two leading zero coefficients evaluates it. */
+template <class R> __device__ __forceinline__ R th2_times(R th, R th2, R ex) {
+#ifdef GBODE_REF
+  return th * (th * ex);
+#else
+  return th2 * ex;
+#endif
+}
 
 /* Small integers as singles without a conversion instruction (integer-to-
  * float conversions issue on this GPU's FP64 pipe): the bits of 2^23 + i
@@ -566,7 +616,7 @@ __device__ __forceinline__ void lc_acc(R (&s)[D]) {}
 template <int D, class R, class K, class... Rest>
 __device__ __forceinline__ void lc_acc(R (&s)[D], R c, const K& k, const Rest&... rest) {
 #pragma unroll
-  for (int d = 0; d < D; ++d) s[d] = fmaR(c, k[d], s[d]);
+  for (int d = 0; d < D; ++d) s[d] = vmaddR(c, k[d], s[d]);
   lc_acc(s, rest...);
 }
 /* k: any row indexable by d (a register array, or a RingRow of staged stage values) */
@@ -580,7 +630,7 @@ __device__ __forceinline__ void lc(R (&s)[D], R c, const K& k, const Rest&... re
 template <int D, class R>
 __device__ __forceinline__ void axpy(R (&out)[D], const R (&base)[D], R h, const R (&s)[D]) {
 #pragma unroll
-  for (int d = 0; d < D; ++d) out[d] = fmaR(h, s[d], base[d]);
+  for (int d = 0; d < D; ++d) out[d] = vmaddR(h, s[d], base[d]);
 }
 /* stage time t + c*dt */
 template <class T>
@@ -601,7 +651,7 @@ __device__ __forceinline__ void state_update(const typename PR::R (&uh)[D], cons
       nc[d] = (sum - uh[d]) - y;
       nh[d] = sum;
     } else {
-      nh[d] = fmaR(h, s[d], uh[d]);
+      nh[d] = vmaddR(h, s[d], uh[d]);
       nc[d] = (R)0;
     }
   }
@@ -614,21 +664,27 @@ __device__ __forceinline__ void finish_dense(const typename PR::R (&uh)[D], cons
 #pragma unroll
   for (int d = 0; d < D; ++d) {
     if (PR::KAHAN) out[d] = ((double)uh[d] - (double)uc[d]) + (double)(h * s[d]);
-    else out[d] = (double)fmaR(h, s[d], uh[d]);
+    else out[d] = (double)vmaddR(h, s[d], uh[d]);
   }
 }
 
 /* ------------------------------------------------------------------ right-hand sides */
 /* Each functor holds its parameters in registers and evaluates du = f(u, p, t).
- * The forms match the oracle's DEVICE forms term for term. */
+ * The forms match the oracle's DEVICE forms term for term, and with GBODE_REF
+ * its REF forms (the plain Julia expressions). */
 template <class R, class T>
 struct RhsLorenz {
   enum { D = 3, NP = 3 };
   R p[3];
   __device__ __forceinline__ void operator()(const R (&u)[3], T t, R (&du)[3]) const {
     du[0] = p[0] * (u[1] - u[0]);
+#ifdef GBODE_REF
+    du[1] = u[0] * (p[1] - u[2]) - u[1];
+    du[2] = u[0] * u[1] - p[2] * u[2];
+#else
     du[1] = fmaR(u[0], p[1] - u[2], -u[1]);
     du[2] = fmaR(u[0], u[1], -(p[2] * u[2]));
+#endif
   }
 };
 
@@ -637,9 +693,13 @@ struct RhsVanDerPol {
   enum { D = 2, NP = 1 };
   R p[1];
   __device__ __forceinline__ void operator()(const R (&u)[2], T t, R (&du)[2]) const {
-    R w = fmaR(-u[0], u[0], (R)1);
     du[0] = u[1];
+#ifdef GBODE_REF
+    du[1] = p[0] * ((R)1 - u[0] * u[0]) * u[1] - u[0];
+#else
+    R w = fmaR(-u[0], u[0], (R)1);
     du[1] = fmaR(p[0] * w, u[1], -u[0]);
+#endif
   }
 };
 
@@ -676,12 +736,19 @@ struct RhsR3BP {
     const R mu = p[0], mu1 = (R)1 - mu;
     const R x = u[0], y = u[1], vx = u[2], vy = u[3];
     const R a = x + mu, b = x - mu1;
-    const R r1 = fmaR(a, a, y * y), r2 = fmaR(b, b, y * y);
-    const R g1 = r3bp_pull(mu1, r1), g2 = r3bp_pull(mu, r2);
     du[0] = vx;
     du[1] = vy;
+#ifdef GBODE_REF
+    const R r1 = a * a + y * y, r2 = b * b + y * y;
+    const R d1 = r1 * sqrtR(r1), d2 = r2 * sqrtR(r2);
+    du[2] = x + (R)2 * vy - mu1 * a / d1 - mu * b / d2;
+    du[3] = y - (R)2 * vx - mu1 * y / d1 - mu * y / d2;
+#else
+    const R r1 = fmaR(a, a, y * y), r2 = fmaR(b, b, y * y);
+    const R g1 = r3bp_pull(mu1, r1), g2 = r3bp_pull(mu, r2);
     du[2] = fmaR(-g2, b, fmaR(-g1, a, fmaR((R)2, vy, x)));
     du[3] = fmaR(-g2, y, fmaR(-g1, y, fmaR((R)-2, vx, y)));
+#endif
   }
 };
 
@@ -707,7 +774,13 @@ struct RhsKuramoto {
     }
     const R kd = p[DD];
 #pragma unroll
-    for (int i = 0; i < DD; ++i) du[i] = fmaR(kd, fmaR(cs[i], S, -(sn[i] * C)), p[i]);
+    for (int i = 0; i < DD; ++i) {
+#ifdef GBODE_REF
+      du[i] = p[i] + kd * (cs[i] * S - sn[i] * C);
+#else
+      du[i] = fmaR(kd, fmaR(cs[i], S, -(sn[i] * C)), p[i]);
+#endif
+    }
   }
 };
 
@@ -729,7 +802,7 @@ struct RhsLinear {
     for (int i = 0; i < DD; ++i) {
       R s = p[i * DD] * u[0];
 #pragma unroll
-      for (int j = 1; j < DD; ++j) s = fmaR(p[i * DD + j], u[j], s);
+      for (int j = 1; j < DD; ++j) s = vmaddR(p[i * DD + j], u[j], s);
       du[i] = s;
     }
   }
@@ -750,9 +823,14 @@ struct MTsit5 {
 #define C5T(x) CB<T>::t5(tsit5_##x)
     R tmp[D], s[D];
     const R h = (R)dt;
+#ifdef GBODE_REF
+#pragma unroll
+    for (int d = 0; d < D; ++d) tmp[d] = h * (C5(a21) * k[0][d]) + uh[d];
+#else
     const R a = (R)(dt * C5T(a21));
 #pragma unroll
     for (int d = 0; d < D; ++d) tmp[d] = fmaR(a, k[0][d], uh[d]);
+#endif
     f(tmp, stime(t, C5T(c1), dt), k[1]);
     lc(s, C5(a31), k[0], C5(a32), k[1]);
     axpy(tmp, uh, h, s);
@@ -786,7 +864,7 @@ struct MTsit5 {
     ex = C5(r14); ex = fmaR(th, ex, C5(r13)); ex = fmaR(th, ex, C5(r12)); ex = fmaR(th, ex, C5(r11)); b1 = th * ex;
 #define TSIT5_B(i, out_)                                                        \
   ex = C5(r##i##4); ex = fmaR(th, ex, C5(r##i##3)); ex = fmaR(th, ex, C5(r##i##2)); \
-  out_ = th2 * ex;
+  out_ = th2_times(th, th2, ex);
     TSIT5_B(2, b2) TSIT5_B(3, b3) TSIT5_B(4, b4) TSIT5_B(5, b5) TSIT5_B(6, b6) TSIT5_B(7, b7)
 #undef TSIT5_B
     R s[D];
@@ -816,7 +894,7 @@ struct MVern7 {
     f(uh, t, k[0]);
     const R a = (R)(dt * C7T(a021));
 #pragma unroll
-    for (int d = 0; d < D; ++d) tmp[d] = fmaR(a, k[0][d], uh[d]);
+    for (int d = 0; d < D; ++d) tmp[d] = vmaddR(a, k[0][d], uh[d]);
     f(tmp, stime(t, C7T(c2), dt), k[1]);
     lc(s, C7(a031), k[0], C7(a032), k[1]);
     axpy(tmp, uh, h, s); f(tmp, stime(t, C7T(c3), dt), k[2]);
@@ -899,7 +977,7 @@ struct MVern7 {
 #define V7B(i, j)                                                                      \
   ex = R7(r##i##7); ex = fmaR(th, ex, R7(r##i##6)); ex = fmaR(th, ex, R7(r##i##5));        \
   ex = fmaR(th, ex, R7(r##i##4)); ex = fmaR(th, ex, R7(r##i##3)); ex = fmaR(th, ex, R7(r##i##2)); \
-  b[j] = th2 * ex;
+  b[j] = th2_times(th, th2, ex);
     V7B(04, 1) V7B(05, 2) V7B(06, 3) V7B(07, 4) V7B(08, 5) V7B(09, 6)
     V7B(11, 7) V7B(12, 8) V7B(13, 9) V7B(14, 10) V7B(15, 11) V7B(16, 12)
 #undef V7B
@@ -938,7 +1016,7 @@ struct MVern9Impl {
     f(uh, t, k[0]);
     const R a = (R)(dt * C9T(a0201));
 #pragma unroll
-    for (int d = 0; d < D; ++d) tmp[d] = fmaR(a, k[0][d], uh[d]);
+    for (int d = 0; d < D; ++d) tmp[d] = vmaddR(a, k[0][d], uh[d]);
     f(tmp, stime(t, C9T(c1), dt), k[1]);
     lc(s, C9(a0301), k[0], C9(a0302), k[1]);
     axpy(tmp, uh, h, s); f(tmp, stime(t, C9T(c2), dt), k[2]);
@@ -1079,7 +1157,7 @@ struct MVern9Impl {
 #define V9B(i, j)                                                                             \
   ex = R9(r##i##9); ex = fmaR(th, ex, R9(r##i##8)); ex = fmaR(th, ex, R9(r##i##7));               \
   ex = fmaR(th, ex, R9(r##i##6)); ex = fmaR(th, ex, R9(r##i##5)); ex = fmaR(th, ex, R9(r##i##4)); \
-  ex = fmaR(th, ex, R9(r##i##3)); ex = fmaR(th, ex, R9(r##i##2)); b[j] = th2 * ex;
+  ex = fmaR(th, ex, R9(r##i##3)); ex = fmaR(th, ex, R9(r##i##2)); b[j] = th2_times(th, th2, ex);
     V9B(08, 1) V9B(09, 2) V9B(10, 3) V9B(11, 4) V9B(12, 5) V9B(13, 6) V9B(14, 7) V9B(15, 8)
     V9B(17, 9) V9B(18, 10) V9B(19, 11) V9B(20, 12) V9B(21, 13) V9B(22, 14) V9B(23, 15) V9B(24, 16)
     V9B(25, 17) V9B(26, 18)
@@ -1103,6 +1181,15 @@ template <class PR, int D, class F> struct MAVern9 : MVern9Impl<PR, D, F, true> 
 template <class PR, int D, class F> struct MVern9 : MVern9Impl<PR, D, F, false> {};
 
 /* ------------------------------------------------------------------ classic RK4 (fixed step) */
+/* uprev + (dt/2) k of RK4's middle stages: one fused multiply-add with the
+ * halved step, or with GBODE_REF the reference's dt * (1/2 * k) + uprev */
+template <class R> __device__ __forceinline__ R half_step(R h, R hh, R k, R u) {
+#ifdef GBODE_REF
+  return h * ((R)0.5 * k) + u;
+#else
+  return fmaR(hh, k, u);
+#endif
+}
 /* src/rk4/gpurk4.jl:73-84; the stage time t is the END of the step (ts[i]). */
 template <class PR, int D, class F>
 struct MRK4 {
@@ -1115,21 +1202,28 @@ struct MRK4 {
     const R hh = h * (R)0.5;
     f(uh, t, k1);
 #pragma unroll
-    for (int d = 0; d < D; ++d) tmp[d] = fmaR(hh, k1[d], uh[d]);
+    for (int d = 0; d < D; ++d) tmp[d] = half_step(h, hh, k1[d], uh[d]);
     f(tmp, fmaR((T)0.5, dt, t), k2);
 #pragma unroll
-    for (int d = 0; d < D; ++d) tmp[d] = fmaR(hh, k2[d], uh[d]);
+    for (int d = 0; d < D; ++d) tmp[d] = half_step(h, hh, k2[d], uh[d]);
     f(tmp, fmaR((T)0.5, dt, t), k3);
 #pragma unroll
-    for (int d = 0; d < D; ++d) tmp[d] = fmaR(h, k3[d], uh[d]);
+    for (int d = 0; d < D; ++d) tmp[d] = vmaddR(h, k3[d], uh[d]);
     f(tmp, t + dt, k4);
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       R sum = k1[d] + k4[d];
-      sum = fmaR((R)2, k2[d], sum);
-      s[d] = fmaR((R)2, k3[d], sum);
+      sum = vmaddR((R)2, k2[d], sum);
+      s[d] = vmaddR((R)2, k3[d], sum);
     }
+#ifdef GBODE_REF
+    /* u = uprev + dt * (1/6 * (k1 + 2k2 + 2k3 + k4)) */
+#pragma unroll
+    for (int d = 0; d < D; ++d) s[d] = (R)(1.0 / 6.0) * s[d];
+    state_update<PR, D>(uh, uc, h, s, nh, nc);
+#else
     state_update<PR, D>(uh, uc, h * (R)(1.0 / 6.0), s, nh, nc);
+#endif
   }
 };
 
@@ -1163,6 +1257,9 @@ struct Lane {
 #endif
 #ifdef GBODE_CTRL_DS
   dsf lqds; /* beta2 * log(qold) of the double-single controller */
+#endif
+#ifdef GBODE_REF
+  double qold; /* the reference controller's qold */
 #endif
   long long idx, att, cur, ninterp;
   int nacc, nrej;
@@ -1203,11 +1300,15 @@ __device__ __forceinline__ void store_point(const KParams& P, long long idx, lon
 #pragma unroll 1
     for (int d = 0; d < D; ++d) {
       double sn, cs;
-      sincos_cw(v[d], &sn, &cs);
+      sincosR(v[d], &sn, &cs);
       C = C + cs;
       S = S + sn;
     }
+#ifdef GBODE_REF
+    *us_at(P, j, 0, idx) = __dsqrt_rn(C * C + S * S) / (double)D;
+#else
     *us_at(P, j, 0, idx) = __dsqrt_rn(__fma_rn(C, C, S * S)) / (double)D;
+#endif
     return;
   }
 #pragma unroll
@@ -1263,6 +1364,9 @@ __device__ __forceinline__ void lane_load(const KParams& P, long long idx, Lane<
 #endif
 #ifdef GBODE_CTRL_DS
   l.lqds = ds_mul({GBODE_DS_B2_H, GBODE_DS_B2_L}, {GBODE_DS_LN_QOLDINIT_H, GBODE_DS_LN_QOLDINIT_L});
+#endif
+#ifdef GBODE_REF
+  l.qold = 1.0e-4;
 #endif
   l.att = 0;
   l.cur = 0;
@@ -1365,6 +1469,48 @@ __device__ __forceinline__ int adaptive_try(const KParams& P, Lane<PR, D, F, NK>
   R e[D];
   M::attempt(l.f, l.uh, l.uc, l.t, l.dt, l.k, nh, nc, e, true);
   l.att += 1;
+#ifdef GBODE_REF
+  if (sizeof(R) == sizeof(double)) {
+    /* The reference's norm and PI controller in IEEE double (ODE_CTRL_REF):
+     * EEst = sqrt(sum((e ./ (abstol .+ max.(|uprev|, |u|) .* reltol)).^2) / D),
+     * q11 = EEst^beta1; reject: dt /= min(1/qmin, q11/gamma); accept:
+     * q = q11 / qold^beta2 (1/qmax when EEst == 0), dt /= max(1/qmax,
+     * min(1/qmin, q/gamma)), qold = max(EEst, qoldinit) -- with
+     * (beta1, beta2, qmax, qmin, gamma, qoldinit) = (7/50, 2/25, 10, 1/5,
+     * 9/10, 1e-4), src/SimpleDiffEq.jl:67-77, src/tsit5/gpuatsit5.jl:276-299;
+     * 1/qmax and 1/qmin are 0.1 and 5.0 in double; the powers correctly
+     * rounded (cr_pow, crpow.h). */
+    const R abstol = (R)P.abstol, reltol = (R)P.reltol;
+    R acc = (R)0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const R m = jmax(absR(l.uh[d]), absR(nh[d]));
+      const R r = e[d] / (abstol + m * reltol);
+      acc = (d == 0) ? r * r : acc + r * r;
+    }
+    const R EEst = sqrtR(acc / (R)D);
+    if (EEst != EEst) l.nan_seen = true;
+    const R q11 = cr_pow(EEst, (R)(7.0 / 50.0));
+    if (EEst > (R)1) {
+      l.dt = l.dt / (T)jmin((R)5.0, q11 / (R)(9.0 / 10.0));
+      l.nrej += 1;
+      return TRY_REJECTED;
+    }
+    R q = (EEst == (R)0) ? (R)0.1 : q11 / cr_pow((R)l.qold, (R)(2.0 / 25.0));
+    q = fm_max((R)0.1, fm_min((R)5.0, q / (R)(9.0 / 10.0)));
+    l.qold = jmax(EEst, (R)1.0e-4);
+    const T dtold = l.dt;
+    const T dtn = l.dt / (T)q;
+    l.dt = absmin(dtn, rest);
+    const T told = l.t;
+    l.t = tnext;
+    if (l.nacc == 0) l.dt_first = (double)dtold;
+    l.nacc += 1;
+    acc_out.told = told;
+    acc_out.dtold = dtold;
+    return TRY_ACCEPTED;
+  }
+#endif
 #ifdef GBODE_CTRL_DS
   if (sizeof(R) == sizeof(double)) {
     /* Double-single norm and controller: a = EEst^2 = mean((e ./ (abstol .+
@@ -1628,7 +1774,7 @@ __device__ __forceinline__ bool adaptive_iter(const KParams& P, Lane<PR, D, F, N
   T inv_dt = (T)0;
   if (l.cur < P.nsave && t_le<PR>(P.saveat[l.cur], l.t)) inv_dt = recip(dtold);
   while (l.cur < P.nsave && t_le<PR>(P.saveat[l.cur], l.t)) {
-    const T theta = ((T)P.saveat[l.cur] - told) * inv_dt;
+    const T theta = theta_of((T)P.saveat[l.cur], told, dtold, inv_dt);
     double v[D];
     M::dense(l.f, l.uh, l.uc, told, l.t, dtold, theta, l.k, v);
     store_point<PR, D>(P, l.idx, l.cur, v);
@@ -1799,7 +1945,7 @@ __device__ __forceinline__ void run_adaptive_staged(const KParams& P) {
       /* the abscissa is computed here, by all lanes of the round at once, rather
        * than by the few lanes that crossed a save point in their step */
       const T told = tv[slot], dtold = tv[2 * CAP + slot];
-      const T theta = ((T)P.saveat[jv[slot]] - told) * recip(dtold);
+      const T theta = theta_of((T)P.saveat[jv[slot]], told, dtold, recip(dtold));
       M::dense(f2, uh, uc, told, tv[CAP + slot], dtold, theta, kk, v);
       store_point<PR, D>(P, iv[slot], jv[slot], v);
     }
@@ -1882,7 +2028,7 @@ __device__ __forceinline__ void run_adaptive_staged(const KParams& P) {
           }
         } else {
           /* the ring is full: interpolate here */
-          const T theta = ((T)P.saveat[j] - st.told) * recip(st.dtold);
+          const T theta = theta_of((T)P.saveat[j], st.told, st.dtold, recip(st.dtold));
           double v[D];
           M::dense(l.f, l.uh, l.uc, st.told, l.t, st.dtold, theta, l.k, v);
           store_point<PR, D>(P, l.idx, j, v);
@@ -1996,7 +2142,7 @@ __device__ __forceinline__ void run_adaptive_staged2(const KParams& P) {
         uc[d] = PR::KAHAN ? rv[(D + d) * CR + slot] : (R)0;
       }
       const T told = tv[slot], dtold = tv[2 * CR + slot];
-      const T theta = ((T)P.saveat[j] - told) * recip(dtold);
+      const T theta = theta_of((T)P.saveat[j], told, dtold, recip(dtold));
       const RingStages<R, D, CR> kk{rv + KOFF * CR + slot};
       const RingStages<R, D, CR> xx{rv + XOFF * CR + slot};
       double v[D];
@@ -2101,7 +2247,7 @@ __device__ __forceinline__ void run_adaptive_staged2(const KParams& P) {
         /* more save points in one iteration than the point queue holds: interpolate here */
         for (int q = 0; q < njobs; ++q) {
           const long long j = l.cur + q;
-          const T theta = ((T)P.saveat[j] - st.told) * recip(st.dtold);
+          const T theta = theta_of((T)P.saveat[j], st.told, st.dtold, recip(st.dtold));
           double v[D];
           M::dense(l.f, l.uh, l.uc, st.told, l.t, st.dtold, theta, l.k, v);
           store_point<PR, D>(P, l.idx, j, v);

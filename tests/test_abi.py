@@ -32,7 +32,7 @@ def test_library_exports_every_declared_symbol(pkg):
     for name in declared_functions():
         assert name in exported, name
         assert getattr(lib, name) is not None
-    assert lib.ode_abi_version() == 5
+    assert lib.ode_abi_version() == 6
 
 
 def test_library_needs_no_driver_at_load_time(pkg):

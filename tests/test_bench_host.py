@@ -1,11 +1,14 @@
 """Host logic of bench.py that needs no GPU: the child processes that measure
 the other workloads after the headline line (their command lines, and how a
-failed, silent or timed-out child is recorded)."""
+failed, silent or timed-out child is recorded), and the bit-identity count of
+the reference-arithmetic leg."""
 import json
 import os
 import subprocess
 import sys
 import types
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
@@ -51,3 +54,21 @@ def test_workload_list_is_parsed(monkeypatch):
                         or types.SimpleNamespace(returncode=0, stdout='{"value": 1}', stderr=""))
     out = bench.run_workloads(types.SimpleNamespace(workloads="5, 3", steps=2, warmup=3))
     assert seen == ["5", "3"] and sorted(out) == ["3", "5"]
+
+
+def test_bitexact_vs_oracle_counts_identical_trajectories():
+    """bench.bitexact_vs_oracle on the oracle's own REF results with correctly
+    rounded powers is 1.0, and a one-ulp change in one trajectory's saveat
+    value, or one extra rejected step, takes exactly that trajectory out."""
+    import bench
+    import __graft_entry__ as g
+    cfg = dict(bench.CONFIGS[2], n=64)
+    u0, p = cfg["inputs"](64, 3)
+    sv = np.linspace(cfg["tspan"][0], cfg["tspan"][1], cfg["nsave"])
+    ref = g.oracle().solve(cfg["alg"], cfg["rhs"], u0, p, cfg["tspan"], cfg["dt"], rounding="ref", controller="ref",
+                           abstol=cfg["abstol"], reltol=cfg["reltol"], saveat=sv, nthreads=4)
+    res = {k: ref[k].copy() for k in ("u_final", "naccept", "nreject", "us")}
+    assert bench.bitexact_vs_oracle(cfg, u0, p, sv, res)["frac_bit_identical"] == 1.0
+    res["us"][50, 1, 7] = np.nextafter(res["us"][50, 1, 7], np.inf)
+    res["nreject"][9] += 1
+    assert bench.bitexact_vs_oracle(cfg, u0, p, sv, res)["frac_bit_identical"] == 62 / 64

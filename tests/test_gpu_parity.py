@@ -308,3 +308,94 @@ def test_fp64_controller_needs_fp64(pkg):
     with pytest.raises(pkg.GB300ODEError) as e:
         gpu(pkg, pkg.GPUSimpleATsit5(), "lorenz", u0, p, (0.0, 1.0), 0.1, precision="fp32", controller="fp64")
     assert e.value.code == pkg._lib.ENOTSUP
+
+
+def ref_mode_inputs(rhs, n, seed):
+    """Inputs of the reference-arithmetic tests: the workloads' distributions."""
+    rng = np.random.default_rng(seed)
+    if rhs == "lorenz":
+        u0, p = lorenz_inputs(n, seed=seed)
+        return u0, p, (0.0, 10.0), dict(abstol=1e-8, reltol=1e-6)
+    if rhs == "vanderpol":
+        u0 = rng.uniform(-2, 2, (2, n))
+        p = np.exp(rng.uniform(np.log(0.1), np.log(10.0), n))[None, :]
+        return u0, p, (0.0, 20.0), dict(abstol=1e-10, reltol=1e-8)
+    if rhs == "r3bp":
+        u0 = np.array([0.994, 0.0, 0.0, -2.00158510637908])[:, None] + rng.normal(0, 1e-4, (4, n))
+        return u0, np.full((1, n), 0.012277471), (0.0, 17.0652165601579625588917206249), dict(abstol=1e-10,
+                                                                                             reltol=1e-10)
+    if rhs == "linear":
+        u0 = rng.normal(0, 1, (4, n))
+        p = rng.normal(0, 0.5, (16, n)) - 0.5 * np.eye(4).reshape(16, 1)
+        return u0, p, (0.0, 5.0), dict(abstol=1e-9, reltol=1e-7)
+    th = rng.uniform(0, 2 * np.pi, (12, n))
+    p = np.vstack([rng.normal(0, 1, (12, n)), rng.uniform(0, 4, (1, n))])
+    return th, p, (0.0, 20.0), dict(abstol=1e-8, reltol=1e-6)
+
+
+@pytest.mark.parametrize("alg,rhs", [("Tsit5", "lorenz"), ("Vern7", "lorenz"), ("Vern9", "lorenz"), ("RK4", "lorenz"),
+                                     ("Euler", "lorenz"), ("Tsit5", "vanderpol"), ("Vern9", "r3bp"),
+                                     ("Vern7", "linear")])
+def test_reference_arithmetic_fixed_step_bitexact(pkg, po, alg, rhs):
+    """ODE_CTRL_REF on the fixed-step algorithms: the reference's own
+    arithmetic (unfused SVector multiply-adds, the right-hand sides and RK4's
+    update as written, theta by division, the polynomials from theta^2 by two
+    multiplications), bit-identical to the oracle's REF rounding over a chaotic
+    Lorenz run and the other right-hand sides, saveat included."""
+    u0, p, _, _ = ref_mode_inputs(rhs, 2048, 21)
+    tspan = (0.0, 2.0)
+    kw = dict(save_everystep=True) if alg in ("RK4", "Euler") else dict(saveat=np.linspace(0.0, 2.0, 21))
+    sol = gpu(pkg, getattr(pkg, "GPUSimple" + alg)(), rhs, u0, p, tspan, 0.01, controller="ref", **kw)
+    ref = po.solve(alg, rhs, u0, p, tspan, 0.01, rounding="ref", nthreads=8, **kw)
+    assert sol.stats.jit == 1
+    assert_bitexact(sol, ref)
+
+
+@pytest.mark.parametrize("alg,rhs,schedule", [("ATsit5", "lorenz", "plain"), ("ATsit5", "lorenz", "persistent"),
+                                              ("AVern7", "vanderpol", "persistent"), ("AVern9", "r3bp", "plain"),
+                                              ("ATsit5", "linear", "persistent")])
+def test_reference_arithmetic_adaptive_bitexact(pkg, po, alg, rhs, schedule):
+    """ODE_CTRL_REF on the adaptive algorithms: the reference's norm in IEEE
+    double and its PI controller with correctly rounded powers (crpow.h),
+    bit-identical to the oracle's REF rounding with the same powers
+    (controller "ref"), every output, step counts and saveat values included,
+    staged saveat rings too."""
+    u0, p, tspan, kw = ref_mode_inputs(rhs, 3000, 22)
+    sv = np.linspace(tspan[0], tspan[1], 37)
+    sol = gpu(pkg, getattr(pkg, "GPUSimple" + alg)(), rhs, u0, p, tspan, 0.1, saveat=sv, schedule=schedule,
+              controller="ref", throw=False, **kw)
+    ref = po.solve(alg, rhs, u0, p, tspan, 0.1, rounding="ref", controller="ref", saveat=sv, nthreads=8, **kw)
+    assert sol.stats.jit == 1
+    assert_bitexact(sol, ref)
+
+
+def test_reference_arithmetic_against_libm_pow_and_kuramoto(pkg, po):
+    """Where the reference's platform functions enter (libm pow in the oracle's
+    plain REF rounding; sine and cosine, which the kernels take from CUDA and
+    the oracle from libm), the reference-arithmetic mode meets the parity
+    tolerance: final states within 10x the error scale and accepted steps
+    within +/-1.  (glibc's pow misrounds about 0.09% of its results on x86,
+    so a Lorenz trajectory of a few hundred attempts meets one now and then
+    and then differs from the kernels' in the last bits.)"""
+    u0, p, tspan, kw = ref_mode_inputs("lorenz", 4000, 23)
+    sol = gpu(pkg, pkg.GPUSimpleATsit5(), "lorenz", u0, p, tspan, 0.1, controller="ref", **kw)
+    ref = po.solve("ATsit5", "lorenz", u0, p, tspan, 0.1, rounding="ref", nthreads=8, **kw)
+    scale = kw["abstol"] + kw["reltol"] * np.abs(ref["u_final"]).max(0)
+    assert (np.abs(sol.u_final - ref["u_final"]).max(0) <= 10 * scale).all()
+    assert np.abs(sol.naccept - ref["naccept"]).max() <= 1
+    th, pk, tspan, kw = ref_mode_inputs("kuramoto", 2000, 24)
+    sv = np.linspace(tspan[0], tspan[1], 11)
+    sol = gpu(pkg, pkg.GPUSimpleATsit5(), "kuramoto", th, pk, tspan, 0.1, controller="ref", saveat=sv, **kw)
+    ref = po.solve("ATsit5", "kuramoto", th, pk, tspan, 0.1, rounding="ref", controller="ref", saveat=sv, nthreads=8,
+                   **kw)
+    scale = kw["abstol"] + kw["reltol"] * np.abs(ref["u_final"]).max(0)
+    assert (np.abs(sol.u_final - ref["u_final"]).max(0) <= 10 * scale).all()
+    assert np.abs(sol.naccept - ref["naccept"]).max() <= 1
+
+
+def test_reference_arithmetic_needs_fp64(pkg):
+    u0, p = lorenz_inputs(16, seed=1)
+    for precision in ("fp32", "fp32_kahan"):
+        with pytest.raises(pkg.GB300ODEError) as e:
+            gpu(pkg, pkg.GPUSimpleATsit5(), "lorenz", u0, p, (0.0, 1.0), 0.1, precision=precision, controller="ref")
+        assert e.value.code == pkg._lib.ENOTSUP

@@ -126,7 +126,7 @@ ENUM_MAPS = {
                     "kuramoto": "ODE_RHS_KURAMOTO", "linear": "ODE_RHS_LINEAR"},
     "PRECISION": {"fp64": "ODE_FP64", "fp32": "ODE_FP32", "fp32_kahan": "ODE_FP32_KAHAN"},
     "SCHEDULE": {"plain": "ODE_SCHED_PLAIN", "persistent": "ODE_SCHED_PERSISTENT", "learned": "ODE_SCHED_LEARNED"},
-    "CONTROLLER": {"ds": "ODE_CTRL_DS", "fp64": "ODE_CTRL_FP64", "fp32": "ODE_CTRL_FP32"},
+    "CONTROLLER": {"ds": "ODE_CTRL_DS", "fp64": "ODE_CTRL_FP64", "fp32": "ODE_CTRL_FP32", "ref": "ODE_CTRL_REF"},
     "SDE_BUILTIN": {"gbm": "ODE_SDE_GBM", "ou": "ODE_SDE_OU", "lorenz": "ODE_SDE_LORENZ", "mult": "ODE_SDE_MULT"},
 }
 
