@@ -137,6 +137,72 @@ GBODE_CR ddr cr_exp(ddr z) {
   return {(res.h * s1) * s2, (res.l * s1) * s2};
 }
 
+/* First phase (A. Ziv, "Fast evaluation of elementary mathematical functions
+ * with correctly rounded last bit", ACM TOMS 17(3), 1991): the same
+ * reductions with the polynomials in double, x^y as hi + lo within 2^-65.5
+ * relative for |y| <= 1 (log x to 2^-68 absolute, exp's polynomial and sums
+ * to 2^-67); returns true with *out = the double nearest x^y when every value
+ * within 2^-63 |hi| of hi + lo rounds to the same double, false otherwise (in
+ * about one call in 500), and then cr_pow takes the double-double path. */
+GBODE_CR bool cr_pow_fast(double x, double y, double* out) {
+  long long b = cr_bits(x);
+  int e = 0;
+  if (b < 0x0010000000000000LL) {
+    b = cr_bits(x * 0x1p54);
+    e = -54;
+  }
+  e += (int)(b >> 52) - 1023;
+  const int j = (int)((b >> 44) & 0xff);
+  const double m = cr_from_bits((b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
+  if (j >= GBODE_CR_FOLD_FROM) e += 1;
+  const double r = cr_fma(m, kCrLogTab[j][0], -1.0);  /* exact */
+  /* log1p(r) - r = r^2 (-1/2 + r/3 - ... + r^7/9), in double */
+  double q = GBODE_CR_LG9;
+  q = cr_fma(q, r, GBODE_CR_LG8);
+  q = cr_fma(q, r, GBODE_CR_LG7);
+  q = cr_fma(q, r, GBODE_CR_LG6_H);
+  q = cr_fma(q, r, GBODE_CR_LG5_H);
+  q = cr_fma(q, r, GBODE_CR_LG4_H);
+  q = cr_fma(q, r, GBODE_CR_LG3_H);
+  q = cr_fma(q, r, GBODE_CR_LG2_H);
+  const double pl = (r * r) * q;
+  const double ed = (double)e;
+  const ddr a = cr_two_sum(ed * GBODE_CR_LN2_A, kCrLogTab[j][1]);
+  const ddr s = cr_two_sum(a.h, r);
+  const double lo = ((a.l + s.l) + (pl + kCrLogTab[j][2])) + cr_fma(ed, GBODE_CR_LN2_B, ed * GBODE_CR_LN2_C);
+  const ddr z = cr_mul_d(cr_fast(s.h, lo), y);
+  if (!(z.h <= 709.0 && z.h >= -708.0)) return false;
+  /* exp(z) = 2^(k>>6) 2^((k&63)/64) exp(r), r = rh + rl */
+  const double kb = cr_fma(z.h, GBODE_CR_INV_L64, 0x1.8p52);
+  const double kd = kb - 0x1.8p52;
+  const int k = (int)(cr_bits(kb) & 0xffffffffLL);
+  const double t1 = cr_fma(-kd, GBODE_CR_L64_A, z.h);  /* exact */
+  const ddr rr = cr_two_sum(t1, cr_fma(-kd, GBODE_CR_L64_B, z.l));
+  const double rh = rr.h, rl = cr_fma(-kd, GBODE_CR_L64_C, rr.l);
+  /* exp(r) - 1 = rh + (rl + rh^2 (1/2 + rh/6 + ... + rh^5/5040)) */
+  double p = GBODE_CR_EX7;
+  p = cr_fma(p, rh, GBODE_CR_EX6);
+  p = cr_fma(p, rh, GBODE_CR_EX5_H);
+  p = cr_fma(p, rh, GBODE_CR_EX4_H);
+  p = cr_fma(p, rh, GBODE_CR_EX3_H);
+  p = cr_fma(p, rh, GBODE_CR_EX2_H);
+  const double pl2 = cr_fma(rh * rh, p, rl);
+  const int jj = k & 63;
+  const double th = kCrExpTab[jj][0], tl = kCrExpTab[jj][1];
+  /* T (1 + rh + pl2), T = th + tl */
+  const ddr tp = cr_two_prod(th, rh);
+  const double lo2 = cr_fma(th, pl2, tp.l) + cr_fma(tl, rh, tl);
+  const ddr u = cr_two_sum(th, tp.h);
+  const ddr v = cr_fast(u.h, u.l + lo2);
+  const double d = 0x1p-63 * (v.h < 0.0 ? -v.h : v.h);
+  const double up = v.h + (v.l + d), dn = v.h + (v.l - d);
+  if (up != dn) return false;
+  const int n = k >> 6;
+  const int n1 = n / 2, n2 = n - n1;
+  *out = (up * cr_from_bits((long long)(n1 + 1023) << 52)) * cr_from_bits((long long)(n2 + 1023) << 52);
+  return true;
+}
+
 /* x^y, correctly rounded (see the header comment) */
 GBODE_CR double cr_pow(double x, double y) {
   if (x != x || y != y) return x + y;
@@ -145,6 +211,8 @@ GBODE_CR double cr_pow(double x, double y) {
   if (x == 0.0) return y > 0.0 ? 0.0 : cr_from_bits(0x7ff0000000000000LL);
   if (cr_bits(x) == 0x7ff0000000000000LL) return y > 0.0 ? x : 0.0;
   if (x == 1.0) return 1.0;
+  double f;
+  if ((y <= 1.0 && y >= -1.0) && cr_pow_fast(x, y, &f)) return f;
   const ddr lx = cr_log(x);
   const ddr z = cr_mul_d(lx, y);
   if (z.h > 709.7) return cr_from_bits(0x7ff0000000000000LL);

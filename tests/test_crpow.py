@@ -21,6 +21,17 @@ SHIM = r'''
 extern "C" void vpow(const double* x, const double* y, double* o, long n) {
   for (long i = 0; i < n; ++i) o[i] = gbode::cr_pow(x[i], y[i]);
 }
+/* first phase against the double-double path: returns how many differ, *fell = how many fell through */
+extern "C" long vphases(const double* x, const double* y, long n, long* fell) {
+  long bad = 0;
+  *fell = 0;
+  for (long i = 0; i < n; ++i) {
+    double f;
+    if (!gbode::cr_pow_fast(x[i], y[i], &f)) { ++*fell; continue; }
+    if (f != gbode::cr_exp(gbode::cr_mul_d(gbode::cr_log(x[i]), y[i])).h) ++bad;
+  }
+  return bad;
+}
 '''
 
 
@@ -36,6 +47,8 @@ def lib(tmp_path_factory):
                     str(so)], check=True)
     L = ctypes.CDLL(str(so))
     L.vpow.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_long]
+    L.vphases.argtypes = [ctypes.c_void_p] * 2 + [ctypes.c_long, ctypes.POINTER(ctypes.c_long)]
+    L.vphases.restype = ctypes.c_long
     return L
 
 
@@ -66,6 +79,19 @@ def test_correctly_rounded(lib):
             assert g == float(ex), (xi.hex(), yi, g.hex(), float(ex).hex())
             checked += 1
     assert checked > 20000
+
+
+def test_first_phase_agrees_with_double_double_path(lib):
+    """Ziv's first phase (double polynomials, a rounding test with a 2^-63
+    margin; its error measured below 2^-68) returns what the double-double
+    path returns, and falls through in about 0.15% of calls."""
+    rng = np.random.default_rng(6)
+    x = np.concatenate([10.0 ** rng.uniform(-12, 3, 300000), 10.0 ** rng.uniform(-300, 300, 100000),
+                        1 + rng.uniform(-1e-3, 1e-3, 100000)])
+    for y in (np.full(x.size, 7.0 / 50.0), np.full(x.size, 2.0 / 25.0), rng.uniform(-1, 1, x.size)):
+        fell = ctypes.c_long(0)
+        assert lib.vphases(x.ctypes.data, np.ascontiguousarray(y).ctypes.data, x.size, ctypes.byref(fell)) == 0
+        assert fell.value < 0.005 * x.size
 
 
 def test_special_values(lib):
