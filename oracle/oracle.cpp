@@ -20,9 +20,10 @@
  * Two rounding modes (oracle_round):
  *   REF     what the Julia code rounds: @muladd on SVector arithmetic falls back
  *           to a separate multiply and add, scalar muladd (stage times, Horner
- *           steps of @evalpoly) fuses, the controller uses libm pow, or with
- *           ctrl == 3 the correctly rounded cr_pow of the kernels'
- *           reference-arithmetic mode (ODE_CTRL_REF).
+ *           steps of @evalpoly) fuses, the controller uses libm pow and the
+ *           Kuramoto functions libm sin/cos, or with ctrl == 3 the correctly
+ *           rounded cr_pow and cr_sincos of the kernels' reference-arithmetic
+ *           mode (ODE_CTRL_REF).
  *   DEVICE  the device rounding canon the CUDA kernels implement: every
  *           multiply-add of the reference's expressions is one fused
  *           multiply-add (linear combinations accumulate left to right in
@@ -140,8 +141,21 @@ static void sincos_dev(double x, double* s, double* c) {
   }
 }
 
+/* REF rounding with ctrl == 3 (the kernels' reference-arithmetic mode): the
+ * correctly rounded sine and cosine of crpow.h below 2^19; set per worker
+ * thread by oracle_solve */
+static thread_local bool g_cr_trig = false;
+
 template <class R, bool DEV>
 static inline void sincos_of(R x, R* s, R* c) {
+  if (!DEV && g_cr_trig && sizeof(R) == sizeof(double)) {
+    double sd, cd;
+    if (gbode::cr_sincos((double)x, &sd, &cd)) {
+      *s = (R)sd;
+      *c = (R)cd;
+      return;
+    }
+  }
   if (DEV && sizeof(R) == sizeof(double)) {
     double sd, cd;
     sincos_dev((double)x, &sd, &cd);
@@ -750,7 +764,7 @@ static inline void put_us(const oracle_args* a, oracle_out* o, int64_t i, int64_
       double sn, cs;
       if (dev) {
         sincos_dev(v[d], &sn, &cs);
-      } else {
+      } else if (!(g_cr_trig && gbode::cr_sincos(v[d], &sn, &cs))) {
         sn = std::sin(v[d]);
         cs = std::cos(v[d]);
       }
@@ -1557,6 +1571,7 @@ extern "C" int oracle_solve(const oracle_args* a, oracle_out* o) {
   int nt = a->nthreads > 0 ? a->nthreads : 1;
   if ((int64_t)nt > a->n) nt = (int)std::max<int64_t>(1, a->n);
   auto run = [&](int64_t i0, int64_t i1) {
+    g_cr_trig = a->rounding != ORACLE_ROUND_DEVICE && a->ctrl == 3;
     if (a->rounding == ORACLE_ROUND_DEVICE) solve_range_prec<true>(a, o, i0, i1);
     else solve_range_prec<false>(a, o, i0, i1);
   };

@@ -51,9 +51,9 @@ typedef struct {
   int output;            /* 0: state at saveat points; 1: Kuramoto order parameter r(t) of it */
   int ctrl;              /* DEVICE rounding, FP64 adaptive solves: error norm and step-size controller, as
                             ODE_CTRL_*: 0 double-single, 1 FP64 factors (single norm), 2 single precision.
-                            REF rounding: 3 (ODE_CTRL_REF) takes the controller's powers correctly
-                            rounded (crpow.h, the kernels' reference-arithmetic mode), any other value
-                            libm pow */
+                            REF rounding: 3 (ODE_CTRL_REF) takes the controller's powers and the sines
+                            and cosines correctly rounded (crpow.h, the kernels' reference-arithmetic
+                            mode), any other value libm's */
 } oracle_args;
 
 typedef struct {

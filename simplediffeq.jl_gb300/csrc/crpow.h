@@ -1,5 +1,6 @@
-/* Correctly rounded power function x^y of the reference-arithmetic mode
- * (ODE_CTRL_REF): exp(y log x) with the logarithm, the product and the
+/* Correctly rounded power function x^y, sine and cosine (cr_sincos, at the
+ * end of this file) of the reference-arithmetic mode (ODE_CTRL_REF).
+ * x^y = exp(y log x) with the logarithm, the product and the
  * exponential carried in double-double arithmetic (unevaluated sums hi + lo
  * of two doubles, about 100 significant bits; T. J. Dekker, "A
  * floating-point technique for extending the available precision", Numer.
@@ -220,6 +221,94 @@ GBODE_CR double cr_pow(double x, double y) {
   /* v is normalized (v.h is the double nearest v.h + v.l) and the scaling
    * by 2^n in cr_exp is exact for normal results */
   return cr_exp(z).h;
+}
+
+/* Sine and cosine of x, correctly rounded (the two phases of cr_pow): x =
+ * k pi/2 + r, |r| <= pi/4, with pi/2 in four parts (the reduction's error is
+ * below 2^-105 |r| for |x| < 2^19), r = a_j + s with a_j = j/64, and
+ * sin r = sin a_j (1 + C(s)) + cos a_j (s + S(s)), cos r = cos a_j (1 + C(s))
+ * - sin a_j (s + S(s)), C(s) = cos s - 1, S(s) = sin s - s.  The first phase
+ * takes C and S in double (within 2^-66 relative), the second in
+ * double-double.  Returns false for |x| >= 2^19 and non-finite x, which the
+ * caller hands to its math library. */
+GBODE_CR bool cr_sincos(double x, double* sn, double* cs) {
+  const long long ax = cr_bits(x) & 0x7fffffffffffffffLL;
+  if (!(ax < 0x4120000000000000LL)) return false;  /* |x| < 2^19, not NaN */
+  if (ax < 0x3e40000000000000LL) {                 /* |x| < 2^-27: sin x = x, cos x = 1 rounded */
+    *sn = x;
+    *cs = 1.0;
+    return true;
+  }
+  const double kb = cr_fma(x, GBODE_CR_TWO_OVER_PI, 0x1.8p52);
+  const double kd = kb - 0x1.8p52;
+  const int q = (int)(cr_bits(kb) & 3);
+  const double t = cr_fma(-kd, GBODE_CR_PIO2_A, x);  /* exact */
+  const ddr p2 = cr_two_prod(kd, GBODE_CR_PIO2_B), p3 = cr_two_prod(kd, GBODE_CR_PIO2_C);
+  const ddr r0 = cr_two_sum(t, -p2.h);
+  const ddr r = cr_two_sum(r0.h, ((r0.l - p2.l) - p3.h) - (p3.l + kd * GBODE_CR_PIO2_D));
+  const double rh = r.h;
+  const double rabs = rh < 0.0 ? -rh : rh;
+  const int j = (int)(rabs * 64.0 + 0.5);
+  const double aj = rh < 0.0 ? -(double)j * 0x1p-6 : (double)j * 0x1p-6;
+  const ddr sd = cr_two_sum(rh - aj, r.l);  /* rh - aj exact */
+  const double sa_h = rh < 0.0 ? -kCrTrigTab[j][0] : kCrTrigTab[j][0];
+  const double sa_l = rh < 0.0 ? -kCrTrigTab[j][1] : kCrTrigTab[j][1];
+  const double ca_h = kCrTrigTab[j][2], ca_l = kCrTrigTab[j][3];
+  double sr, cr;
+  {
+    /* first phase */
+    const double z = sd.h * sd.h;
+    double c = GBODE_CR_COS4_H;
+    c = cr_fma(c, z, GBODE_CR_COS3_H);
+    c = cr_fma(c, z, GBODE_CR_COS2_H);
+    c = cr_fma(c, z, GBODE_CR_COS1_H);
+    const double cm = z * c;                                   /* cos s - 1 */
+    double sv = GBODE_CR_SIN3_H;
+    sv = cr_fma(sv, z, GBODE_CR_SIN2_H);
+    sv = cr_fma(sv, z, GBODE_CR_SIN1_H);
+    const double sm = (z * sd.h) * sv;                          /* sin s - s */
+    const double tail = sd.l + sm;
+    /* sin r = sa + ca sh + (sa cm + ca tail + ca_l sh + sa_l) */
+    const ddr m1 = cr_two_prod(ca_h, sd.h);
+    const ddr u1 = cr_two_sum(sa_h, m1.h);
+    const double lo1 = u1.l + (m1.l + (cr_fma(sa_h, cm, sa_l) + cr_fma(ca_h, tail, ca_l * sd.h)));
+    const ddr vs = cr_fast(u1.h, lo1);
+    /* cos r = ca - sa sh + (ca cm - sa tail - sa_l sh + ca_l) */
+    const ddr m2 = cr_two_prod(-sa_h, sd.h);
+    const ddr u2 = cr_two_sum(ca_h, m2.h);
+    const double lo2 = u2.l + (m2.l + (cr_fma(ca_h, cm, ca_l) - cr_fma(sa_h, tail, sa_l * sd.h)));
+    const ddr vc = cr_fast(u2.h, lo2);
+    const double ds = 0x1p-62 * (vs.h < 0.0 ? -vs.h : vs.h), dc = 0x1p-62 * vc.h;
+    const bool oks = vs.h + (vs.l + ds) == vs.h + (vs.l - ds), okc = vc.h + (vc.l + dc) == vc.h + (vc.l - dc);
+    sr = vs.h + vs.l;
+    cr = vc.h + vc.l;
+    if (!(oks && okc)) {
+      /* second phase: C and S in double-double */
+      const ddr zz = cr_add(cr_two_prod(sd.h, sd.h), cr_fast(0.0, 2.0 * sd.h * sd.l));
+      ddr ac = {GBODE_CR_COS6_H, GBODE_CR_COS6_L};
+      ac = cr_add({GBODE_CR_COS5_H, GBODE_CR_COS5_L}, cr_mul(ac, zz));
+      ac = cr_add({GBODE_CR_COS4_H, GBODE_CR_COS4_L}, cr_mul(ac, zz));
+      ac = cr_add({GBODE_CR_COS3_H, GBODE_CR_COS3_L}, cr_mul(ac, zz));
+      ac = cr_add({GBODE_CR_COS2_H, GBODE_CR_COS2_L}, cr_mul(ac, zz));
+      ac = cr_add({GBODE_CR_COS1_H, GBODE_CR_COS1_L}, cr_mul(ac, zz));
+      const ddr cmd = cr_mul(ac, zz);                          /* cos s - 1 */
+      ddr as = {GBODE_CR_SIN6_H, GBODE_CR_SIN6_L};
+      as = cr_add({GBODE_CR_SIN5_H, GBODE_CR_SIN5_L}, cr_mul(as, zz));
+      as = cr_add({GBODE_CR_SIN4_H, GBODE_CR_SIN4_L}, cr_mul(as, zz));
+      as = cr_add({GBODE_CR_SIN3_H, GBODE_CR_SIN3_L}, cr_mul(as, zz));
+      as = cr_add({GBODE_CR_SIN2_H, GBODE_CR_SIN2_L}, cr_mul(as, zz));
+      as = cr_add({GBODE_CR_SIN1_H, GBODE_CR_SIN1_L}, cr_mul(as, zz));
+      const ddr ssd = cr_add(sd, cr_mul(cr_mul(as, zz), sd));  /* sin s */
+      const ddr sa = {sa_h, sa_l}, ca = {ca_h, ca_l};
+      const ddr one_c = cr_add(cr_fast(1.0, 0.0), cmd);       /* cos s */
+      sr = cr_add(cr_mul(sa, one_c), cr_mul(ca, ssd)).h;
+      const ddr nsa = {-sa_h, -sa_l};
+      cr = cr_add(cr_mul(ca, one_c), cr_mul(nsa, ssd)).h;
+    }
+  }
+  *sn = q == 0 ? sr : q == 1 ? cr : q == 2 ? -sr : -cr;
+  *cs = q == 0 ? cr : q == 1 ? -sr : q == 2 ? -cr : sr;
+  return true;
 }
 
 }  // namespace gbode

@@ -1,5 +1,5 @@
-"""Tables and constants of the correctly rounded power function of the
-reference-arithmetic mode (crpow.h): x^y = exp(y log x) for x > 0 with log x
+"""Tables and constants of the correctly rounded power function, sine and
+cosine of the reference-arithmetic mode (crpow.h): x^y = exp(y log x) for x > 0 with log x
 and the exponential carried in double-double arithmetic (unevaluated sums
 hi + lo of two doubles), about 100 significant bits, so that rounding the
 result to double gives the correctly rounded x^y except when x^y lies within
@@ -25,6 +25,18 @@ double-double, the rest in double.  ln 2 and ln2/64 are split in three
 doubles, the first with 40 and 36 significant bits, so that e ln2_a
 (|e| < 2^11) and k (ln2/64)_a (|k| < 2^17) are exact.
 
+Sine and cosine (cr_sincos, the same two-phase method): x = k pi/2 + r with
+pi/2 split in four doubles (the first with 33 significant bits, so that
+k (pi/2)_a is exact for |k| < 2^20), r in double-double; r = a_j + s with
+a_j = j/64 (|s| <= 1/128) and
+
+    sin r = sin a_j (1 + C(s)) + cos a_j (s + S(s)),
+    cos r = cos a_j (1 + C(s)) - sin a_j (s + S(s)),
+
+C(s) = cos s - 1, S(s) = sin s - s, with sin a_j and cos a_j (j = 0..50)
+from this table in double-double and the series coefficients 1/n! in
+double-double.
+
 All values in 60-digit arithmetic (mpmath).  Writes crpow_table.h next to
 this script; crpow.h includes it.
 
@@ -37,6 +49,7 @@ import mpmath as mp
 mp.mp.dps = 60
 NLOG = 256
 NEXP = 64
+NTRIG = 51  # a_j = j/64 covers |r| <= pi/4 + 1/128
 
 
 def dbl(x):
@@ -76,6 +89,10 @@ def log_rows():
     return rows
 
 
+def sincos_rows():
+    return [split2(mp.sin(mp.mpf(j) / 64)) + split2(mp.cos(mp.mpf(j) / 64)) for j in range(NTRIG)]
+
+
 def exp_rows():
     return [split2(mp.mpf(2) ** (mp.mpf(j) / NEXP)) for j in range(NEXP)]
 
@@ -90,7 +107,14 @@ def header():
     consts["LN2_A"], consts["LN2_B"], consts["LN2_C"] = split3(ln2, 40)
     consts["L64_A"], consts["L64_B"], consts["L64_C"] = split3(ln2 / NEXP, 36)
     consts["INV_L64"] = dbl(NEXP / ln2)
-    out = ["/* generated by gen_crpow.py: tables and constants of the correctly rounded power function */\n",
+    pio2 = mp.pi / 2
+    a = split3(pio2, 33)[0]
+    b = dbl(pio2 - mp.mpf(a))
+    c = dbl(pio2 - mp.mpf(a) - mp.mpf(b))
+    d = dbl(pio2 - mp.mpf(a) - mp.mpf(b) - mp.mpf(c))
+    consts["PIO2_A"], consts["PIO2_B"], consts["PIO2_C"], consts["PIO2_D"] = a, b, c, d
+    consts["TWO_OVER_PI"] = dbl(2 / mp.pi)
+    out = ["/* generated by gen_crpow.py: tables and constants of the correctly rounded power, sine and cosine */\n",
            "#pragma once\n",
            "#ifndef GBODE_CRPOW_SPACE\n#define GBODE_CRPOW_SPACE static const\n#endif\n"]
     for k, v in consts.items():
@@ -107,6 +131,17 @@ def header():
         out.append("#define GBODE_CR_EX%d_H %s\n#define GBODE_CR_EX%d_L %s\n" % (n, hexd(h), n, hexd(l)))
     for n in range(6, 12):
         out.append("#define GBODE_CR_EX%d %s\n" % (n, hexd(dbl(1 / mp.factorial(n)))))
+    # (-1)^n / (2n)! for cos s - 1 and (-1)^n / (2n+1)! for sin s - s, n = 1..6, double-double
+    for n in range(1, 7):
+        h, l = split2(mp.mpf(-1) ** n / mp.factorial(2 * n))
+        out.append("#define GBODE_CR_COS%d_H %s\n#define GBODE_CR_COS%d_L %s\n" % (n, hexd(h), n, hexd(l)))
+        h, l = split2(mp.mpf(-1) ** n / mp.factorial(2 * n + 1))
+        out.append("#define GBODE_CR_SIN%d_H %s\n#define GBODE_CR_SIN%d_L %s\n" % (n, hexd(h), n, hexd(l)))
+    out.append("/* row j: sin(j/64) = hi + lo, cos(j/64) = hi + lo */\n")
+    out.append("GBODE_CRPOW_SPACE double kCrTrigTab[%d][4] = {\n" % NTRIG)
+    for sh, sl, ch, cl in sincos_rows():
+        out.append("    {%s, %s, %s, %s},\n" % (hexd(sh), hexd(sl), hexd(ch), hexd(cl)))
+    out.append("};\n")
     out.append("/* row j: c_j (a multiple of 2^-9), T_j = hi + lo, and 1 where T_j holds -ln 2 */\n")
     out.append("GBODE_CRPOW_SPACE double kCrLogTab[%d][3] = {\n" % NLOG)
     rows = log_rows()

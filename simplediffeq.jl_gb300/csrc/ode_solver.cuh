@@ -48,8 +48,9 @@
  * polynomials from theta^2 multiplied by theta twice, the error norm in IEEE
  * double with division and square root, and the PI controller with a
  * correctly rounded pow (cr_pow, crpow.h; src/SimpleDiffEq.jl:67-77,
- * src/tsit5/gpuatsit5.jl:272-299); sine and cosine are CUDA's.  Scalar muladds (stage times, Horner steps) stay fused,
- * as Julia fuses them.
+ * src/tsit5/gpuatsit5.jl:272-299); sine and cosine are correctly rounded
+ * too (cr_sincos) below 2^19, CUDA's beyond.  Scalar muladds (stage times,
+ * Horner steps) stay fused, as Julia fuses them.
  */
 #pragma once
 #include "ode_kparams.h"
@@ -135,7 +136,7 @@ __device__ __forceinline__ void sincos_cw(double x, double* s, double* c) {
 /* sine and cosine of one argument with a single argument reduction */
 __device__ __forceinline__ void sincosR(double x, double* s, double* c) {
 #ifdef GBODE_REF
-  sincos(x, s, c);
+  if (!cr_sincos(x, s, c)) sincos(x, s, c);  /* correctly rounded below 2^19 */
 #else
   sincos_cw(x, s, c);
 #endif

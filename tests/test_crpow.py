@@ -18,6 +18,11 @@ CSRC = os.path.join(ROOT, "simplediffeq.jl_gb300", "csrc")
 
 SHIM = r'''
 #include "crpow.h"
+extern "C" long vsincos(const double* x, double* s, double* c, long n) {
+  long handled = 0;
+  for (long i = 0; i < n; ++i) handled += gbode::cr_sincos(x[i], s + i, c + i);
+  return handled;
+}
 extern "C" void vpow(const double* x, const double* y, double* o, long n) {
   for (long i = 0; i < n; ++i) o[i] = gbode::cr_pow(x[i], y[i]);
 }
@@ -49,6 +54,8 @@ def lib(tmp_path_factory):
     L.vpow.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_long]
     L.vphases.argtypes = [ctypes.c_void_p] * 2 + [ctypes.c_long, ctypes.POINTER(ctypes.c_long)]
     L.vphases.restype = ctypes.c_long
+    L.vsincos.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_long]
+    L.vsincos.restype = ctypes.c_long
     return L
 
 
@@ -92,6 +99,28 @@ def test_first_phase_agrees_with_double_double_path(lib):
         fell = ctypes.c_long(0)
         assert lib.vphases(x.ctypes.data, np.ascontiguousarray(y).ctypes.data, x.size, ctypes.byref(fell)) == 0
         assert fell.value < 0.005 * x.size
+
+
+def test_sincos_correctly_rounded(lib):
+    """cr_sincos: both results the doubles nearest sin x and cos x (mpmath at
+    300 bits) for |x| < 2^19, near multiples of pi/2 (the reduction's
+    cancellation) and for tiny x; beyond 2^19 and for non-finite x it
+    declines (the caller's math library takes over)."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.prec = 300
+    rng = np.random.default_rng(7)
+    k = np.arange(-400, 400) * (np.pi / 2)
+    x = np.concatenate([rng.uniform(-7, 7, 4000), rng.uniform(-1000, 1000, 4000),
+                        10.0 ** rng.uniform(-30, 5.7, 2000) * rng.choice([-1.0, 1.0], 2000), k,
+                        np.nextafter(k, np.inf), np.nextafter(k, -np.inf), np.array([0.0, -0.0, 5e-324, 2.0 ** -27])])
+    s, c = np.empty_like(x), np.empty_like(x)
+    assert lib.vsincos(x.ctypes.data, s.ctypes.data, c.ctypes.data, x.size) == x.size
+    for xi, si, ci in zip(x, s, c):
+        assert si == float(mp.sin(mp.mpf(xi))) and ci == float(mp.cos(mp.mpf(xi))), xi.hex()
+    assert np.signbit(s[-3]) and not np.signbit(s[-4])
+    big = np.array([2.0 ** 19, -1e6, np.inf, np.nan])
+    sb, cb = np.empty_like(big), np.empty_like(big)
+    assert lib.vsincos(big.ctypes.data, sb.ctypes.data, cb.ctypes.data, big.size) == 0
 
 
 def test_special_values(lib):

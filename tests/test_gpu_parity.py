@@ -335,31 +335,33 @@ def ref_mode_inputs(rhs, n, seed):
 
 @pytest.mark.parametrize("alg,rhs", [("Tsit5", "lorenz"), ("Vern7", "lorenz"), ("Vern9", "lorenz"), ("RK4", "lorenz"),
                                      ("Euler", "lorenz"), ("Tsit5", "vanderpol"), ("Vern9", "r3bp"),
-                                     ("Vern7", "linear")])
+                                     ("Vern7", "linear"), ("Tsit5", "kuramoto")])
 def test_reference_arithmetic_fixed_step_bitexact(pkg, po, alg, rhs):
     """ODE_CTRL_REF on the fixed-step algorithms: the reference's own
     arithmetic (unfused SVector multiply-adds, the right-hand sides and RK4's
     update as written, theta by division, the polynomials from theta^2 by two
-    multiplications), bit-identical to the oracle's REF rounding over a chaotic
-    Lorenz run and the other right-hand sides, saveat included."""
+    multiplications, correctly rounded sines and cosines), bit-identical to the
+    oracle's REF rounding with the same functions over a chaotic Lorenz run
+    and the other right-hand sides, saveat included."""
     u0, p, _, _ = ref_mode_inputs(rhs, 2048, 21)
     tspan = (0.0, 2.0)
     kw = dict(save_everystep=True) if alg in ("RK4", "Euler") else dict(saveat=np.linspace(0.0, 2.0, 21))
     sol = gpu(pkg, getattr(pkg, "GPUSimple" + alg)(), rhs, u0, p, tspan, 0.01, controller="ref", **kw)
-    ref = po.solve(alg, rhs, u0, p, tspan, 0.01, rounding="ref", nthreads=8, **kw)
+    ref = po.solve(alg, rhs, u0, p, tspan, 0.01, rounding="ref", controller="ref", nthreads=8, **kw)
     assert sol.stats.jit == 1
     assert_bitexact(sol, ref)
 
 
 @pytest.mark.parametrize("alg,rhs,schedule", [("ATsit5", "lorenz", "plain"), ("ATsit5", "lorenz", "persistent"),
                                               ("AVern7", "vanderpol", "persistent"), ("AVern9", "r3bp", "plain"),
-                                              ("ATsit5", "linear", "persistent")])
+                                              ("ATsit5", "linear", "persistent"), ("ATsit5", "kuramoto", "persistent")])
 def test_reference_arithmetic_adaptive_bitexact(pkg, po, alg, rhs, schedule):
     """ODE_CTRL_REF on the adaptive algorithms: the reference's norm in IEEE
-    double and its PI controller with correctly rounded powers (crpow.h),
-    bit-identical to the oracle's REF rounding with the same powers
-    (controller "ref"), every output, step counts and saveat values included,
-    staged saveat rings too."""
+    double and its PI controller with correctly rounded powers (crpow.h; the
+    Kuramoto phases' sines and cosines correctly rounded too), bit-identical
+    to the oracle's REF rounding with the same functions (controller "ref"),
+    every output, step counts and saveat values included, staged saveat
+    rings too."""
     u0, p, tspan, kw = ref_mode_inputs(rhs, 3000, 22)
     sv = np.linspace(tspan[0], tspan[1], 37)
     sol = gpu(pkg, getattr(pkg, "GPUSimple" + alg)(), rhs, u0, p, tspan, 0.1, saveat=sv, schedule=schedule,
@@ -369,12 +371,11 @@ def test_reference_arithmetic_adaptive_bitexact(pkg, po, alg, rhs, schedule):
     assert_bitexact(sol, ref)
 
 
-def test_reference_arithmetic_against_libm_pow_and_kuramoto(pkg, po):
-    """Where the reference's platform functions enter (libm pow in the oracle's
-    plain REF rounding; sine and cosine, which the kernels take from CUDA and
-    the oracle from libm), the reference-arithmetic mode meets the parity
-    tolerance: final states within 10x the error scale and accepted steps
-    within +/-1.  (glibc's pow misrounds about 0.09% of its results on x86,
+def test_reference_arithmetic_against_libm(pkg, po):
+    """Against the oracle's plain REF rounding, with the platform's libm pow,
+    sin and cos in place of the correctly rounded ones, the
+    reference-arithmetic mode meets the parity tolerance: final states within
+    10x the error scale and accepted steps within +/-1.  (glibc's pow misrounds about 0.09% of its results on x86,
     so a Lorenz trajectory of a few hundred attempts meets one now and then
     and then differs from the kernels' in the last bits.)"""
     u0, p, tspan, kw = ref_mode_inputs("lorenz", 4000, 23)
@@ -386,8 +387,7 @@ def test_reference_arithmetic_against_libm_pow_and_kuramoto(pkg, po):
     th, pk, tspan, kw = ref_mode_inputs("kuramoto", 2000, 24)
     sv = np.linspace(tspan[0], tspan[1], 11)
     sol = gpu(pkg, pkg.GPUSimpleATsit5(), "kuramoto", th, pk, tspan, 0.1, controller="ref", saveat=sv, **kw)
-    ref = po.solve("ATsit5", "kuramoto", th, pk, tspan, 0.1, rounding="ref", controller="ref", saveat=sv, nthreads=8,
-                   **kw)
+    ref = po.solve("ATsit5", "kuramoto", th, pk, tspan, 0.1, rounding="ref", saveat=sv, nthreads=8, **kw)
     scale = kw["abstol"] + kw["reltol"] * np.abs(ref["u_final"]).max(0)
     assert (np.abs(sol.u_final - ref["u_final"]).max(0) <= 10 * scale).all()
     assert np.abs(sol.naccept - ref["naccept"]).max() <= 1
