@@ -134,9 +134,10 @@ enum {
   ODE_CTRL_REF = 3   /* the reference's arithmetic throughout, FP64 only: the vector expressions'
                         products and sums rounded separately (the reference's SVector muladd does
                         not fuse), its right-hand-side and RK4 expressions as written, the dense
-                        abscissa by division, the norm in IEEE double and the PI controller with
-                        pow (CUDA's pow and sin/cos, which can differ from another libm in the last
-                        bit); slower, for results that follow the reference operation for
+                        abscissa by division, the norm in IEEE double, the PI controller with pow,
+                        and pow, sin and cos correctly rounded (the double nearest the exact value,
+                        where libm implementations can differ in the last bit; sin and cos for
+                        |x| < 2^19); slower, for results that follow the reference operation for
                         operation */
 };
 
