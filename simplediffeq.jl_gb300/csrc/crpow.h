@@ -20,6 +20,9 @@
 
 #if defined(__CUDACC__) || defined(__CUDACC_RTC__)
 #define GBODE_CR __device__ __forceinline__
+/* the second phases, taken in about one call in 500: out of line on the
+ * device, so that each inlined call site stays small */
+#define GBODE_CR_COLD __device__ __noinline__
 #define GBODE_CRPOW_SPACE __device__ const
 namespace gbode {
 GBODE_CR double cr_fma(double a, double b, double c) { return __fma_rn(a, b, c); }
@@ -30,6 +33,7 @@ GBODE_CR double cr_from_bits(long long b) { return __longlong_as_double(b); }
 #include <cmath>
 #include <cstring>
 #define GBODE_CR static inline
+#define GBODE_CR_COLD static inline
 namespace gbode {
 GBODE_CR double cr_fma(double a, double b, double c) { return std::fma(a, b, c); }
 GBODE_CR long long cr_bits(double x) { long long b; std::memcpy(&b, &x, 8); return b; }
@@ -204,6 +208,17 @@ GBODE_CR bool cr_pow_fast(double x, double y, double* out) {
   return true;
 }
 
+/* x^y in double-double, rounded: the second phase */
+GBODE_CR_COLD double cr_pow_dd(double x, double y) {
+  const ddr lx = cr_log(x);
+  const ddr z = cr_mul_d(lx, y);
+  if (z.h > 709.7) return cr_from_bits(0x7ff0000000000000LL);
+  if (z.h < -708.3) return 0.0;
+  /* v is normalized (v.h is the double nearest v.h + v.l) and the scaling
+   * by 2^n in cr_exp is exact for normal results */
+  return cr_exp(z).h;
+}
+
 /* x^y, correctly rounded (see the header comment) */
 GBODE_CR double cr_pow(double x, double y) {
   if (x != x || y != y) return x + y;
@@ -214,13 +229,33 @@ GBODE_CR double cr_pow(double x, double y) {
   if (x == 1.0) return 1.0;
   double f;
   if ((y <= 1.0 && y >= -1.0) && cr_pow_fast(x, y, &f)) return f;
-  const ddr lx = cr_log(x);
-  const ddr z = cr_mul_d(lx, y);
-  if (z.h > 709.7) return cr_from_bits(0x7ff0000000000000LL);
-  if (z.h < -708.3) return 0.0;
-  /* v is normalized (v.h is the double nearest v.h + v.l) and the scaling
-   * by 2^n in cr_exp is exact for normal results */
-  return cr_exp(z).h;
+  return cr_pow_dd(x, y);
+}
+
+/* The second phase of cr_sincos: sin r and cos r from s = r - a_j (sd) and
+ * the table's sin a_j, cos a_j, with C(s) and S(s) in double-double */
+GBODE_CR_COLD void cr_sincos_dd(ddr sd, double sa_h, double sa_l, double ca_h, double ca_l, double* sr,
+                                double* cr) {
+  const ddr zz = cr_add(cr_two_prod(sd.h, sd.h), cr_fast(0.0, 2.0 * sd.h * sd.l));
+  ddr ac = {GBODE_CR_COS6_H, GBODE_CR_COS6_L};
+  ac = cr_add({GBODE_CR_COS5_H, GBODE_CR_COS5_L}, cr_mul(ac, zz));
+  ac = cr_add({GBODE_CR_COS4_H, GBODE_CR_COS4_L}, cr_mul(ac, zz));
+  ac = cr_add({GBODE_CR_COS3_H, GBODE_CR_COS3_L}, cr_mul(ac, zz));
+  ac = cr_add({GBODE_CR_COS2_H, GBODE_CR_COS2_L}, cr_mul(ac, zz));
+  ac = cr_add({GBODE_CR_COS1_H, GBODE_CR_COS1_L}, cr_mul(ac, zz));
+  const ddr cmd = cr_mul(ac, zz);                          /* cos s - 1 */
+  ddr as = {GBODE_CR_SIN6_H, GBODE_CR_SIN6_L};
+  as = cr_add({GBODE_CR_SIN5_H, GBODE_CR_SIN5_L}, cr_mul(as, zz));
+  as = cr_add({GBODE_CR_SIN4_H, GBODE_CR_SIN4_L}, cr_mul(as, zz));
+  as = cr_add({GBODE_CR_SIN3_H, GBODE_CR_SIN3_L}, cr_mul(as, zz));
+  as = cr_add({GBODE_CR_SIN2_H, GBODE_CR_SIN2_L}, cr_mul(as, zz));
+  as = cr_add({GBODE_CR_SIN1_H, GBODE_CR_SIN1_L}, cr_mul(as, zz));
+  const ddr ssd = cr_add(sd, cr_mul(cr_mul(as, zz), sd));  /* sin s */
+  const ddr sa = {sa_h, sa_l}, ca = {ca_h, ca_l};
+  const ddr one_c = cr_add(cr_fast(1.0, 0.0), cmd);       /* cos s */
+  *sr = cr_add(cr_mul(sa, one_c), cr_mul(ca, ssd)).h;
+  const ddr nsa = {-sa_h, -sa_l};
+  *cr = cr_add(cr_mul(ca, one_c), cr_mul(nsa, ssd)).h;
 }
 
 /* Sine and cosine of x, correctly rounded (the two phases of cr_pow): x =
@@ -282,29 +317,7 @@ GBODE_CR bool cr_sincos(double x, double* sn, double* cs) {
     const bool oks = vs.h + (vs.l + ds) == vs.h + (vs.l - ds), okc = vc.h + (vc.l + dc) == vc.h + (vc.l - dc);
     sr = vs.h + vs.l;
     cr = vc.h + vc.l;
-    if (!(oks && okc)) {
-      /* second phase: C and S in double-double */
-      const ddr zz = cr_add(cr_two_prod(sd.h, sd.h), cr_fast(0.0, 2.0 * sd.h * sd.l));
-      ddr ac = {GBODE_CR_COS6_H, GBODE_CR_COS6_L};
-      ac = cr_add({GBODE_CR_COS5_H, GBODE_CR_COS5_L}, cr_mul(ac, zz));
-      ac = cr_add({GBODE_CR_COS4_H, GBODE_CR_COS4_L}, cr_mul(ac, zz));
-      ac = cr_add({GBODE_CR_COS3_H, GBODE_CR_COS3_L}, cr_mul(ac, zz));
-      ac = cr_add({GBODE_CR_COS2_H, GBODE_CR_COS2_L}, cr_mul(ac, zz));
-      ac = cr_add({GBODE_CR_COS1_H, GBODE_CR_COS1_L}, cr_mul(ac, zz));
-      const ddr cmd = cr_mul(ac, zz);                          /* cos s - 1 */
-      ddr as = {GBODE_CR_SIN6_H, GBODE_CR_SIN6_L};
-      as = cr_add({GBODE_CR_SIN5_H, GBODE_CR_SIN5_L}, cr_mul(as, zz));
-      as = cr_add({GBODE_CR_SIN4_H, GBODE_CR_SIN4_L}, cr_mul(as, zz));
-      as = cr_add({GBODE_CR_SIN3_H, GBODE_CR_SIN3_L}, cr_mul(as, zz));
-      as = cr_add({GBODE_CR_SIN2_H, GBODE_CR_SIN2_L}, cr_mul(as, zz));
-      as = cr_add({GBODE_CR_SIN1_H, GBODE_CR_SIN1_L}, cr_mul(as, zz));
-      const ddr ssd = cr_add(sd, cr_mul(cr_mul(as, zz), sd));  /* sin s */
-      const ddr sa = {sa_h, sa_l}, ca = {ca_h, ca_l};
-      const ddr one_c = cr_add(cr_fast(1.0, 0.0), cmd);       /* cos s */
-      sr = cr_add(cr_mul(sa, one_c), cr_mul(ca, ssd)).h;
-      const ddr nsa = {-sa_h, -sa_l};
-      cr = cr_add(cr_mul(ca, one_c), cr_mul(nsa, ssd)).h;
-    }
+    if (!(oks && okc)) cr_sincos_dd(sd, sa_h, sa_l, ca_h, ca_l, &sr, &cr);
   }
   *sn = q == 0 ? sr : q == 1 ? cr : q == 2 ? -sr : -cr;
   *cs = q == 0 ? cr : q == 1 ? -sr : q == 2 ? -cr : sr;
