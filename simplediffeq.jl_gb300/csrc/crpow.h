@@ -281,13 +281,18 @@ GBODE_CR bool cr_sincos(double x, double* sn, double* cs) {
   const ddr p2 = cr_two_prod(kd, GBODE_CR_PIO2_B), p3 = cr_two_prod(kd, GBODE_CR_PIO2_C);
   const ddr r0 = cr_two_sum(t, -p2.h);
   const ddr r = cr_two_sum(r0.h, ((r0.l - p2.l) - p3.h) - (p3.l + kd * GBODE_CR_PIO2_D));
+  /* signs, magnitudes and the row index by integer operations (a double
+   * compare, negation or conversion would take an FP64-pipe slot): j =
+   * |rh| * 64 rounded to nearest by the 1.5 * 2^52 shifter, a_j = +-j/64 */
   const double rh = r.h;
-  const double rabs = rh < 0.0 ? -rh : rh;
-  const int j = (int)(rabs * 64.0 + 0.5);
-  const double aj = rh < 0.0 ? -(double)j * 0x1p-6 : (double)j * 0x1p-6;
+  const long long sgn = cr_bits(rh) & (long long)0x8000000000000000ULL;
+  const double rabs = cr_from_bits(cr_bits(rh) ^ sgn);
+  const double jb = cr_fma(rabs, 64.0, 0x1.8p52);
+  const int j = (int)(cr_bits(jb) & 0xff);
+  const double aj = cr_from_bits(cr_bits((jb - 0x1.8p52) * 0x1p-6) | sgn);
   const ddr sd = cr_two_sum(rh - aj, r.l);  /* rh - aj exact */
-  const double sa_h = rh < 0.0 ? -kCrTrigTab[j][0] : kCrTrigTab[j][0];
-  const double sa_l = rh < 0.0 ? -kCrTrigTab[j][1] : kCrTrigTab[j][1];
+  const double sa_h = cr_from_bits(cr_bits(kCrTrigTab[j][0]) ^ sgn);
+  const double sa_l = cr_from_bits(cr_bits(kCrTrigTab[j][1]) ^ sgn);
   const double ca_h = kCrTrigTab[j][2], ca_l = kCrTrigTab[j][3];
   double sr, cr;
   {
@@ -313,14 +318,20 @@ GBODE_CR bool cr_sincos(double x, double* sn, double* cs) {
     const ddr u2 = cr_two_sum(ca_h, m2.h);
     const double lo2 = u2.l + (m2.l + (cr_fma(ca_h, cm, ca_l) - cr_fma(sa_h, tail, sa_l * sd.h)));
     const ddr vc = cr_fast(u2.h, lo2);
-    const double ds = 0x1p-62 * (vs.h < 0.0 ? -vs.h : vs.h), dc = 0x1p-62 * vc.h;
-    const bool oks = vs.h + (vs.l + ds) == vs.h + (vs.l - ds), okc = vc.h + (vc.l + dc) == vc.h + (vc.l - dc);
+    const double ds = 0x1p-62 * cr_from_bits(cr_bits(vs.h) & 0x7fffffffffffffffLL), dc = 0x1p-62 * vc.h;
+    /* the rounding tests compare bits (neither side is zero or NaN here) */
+    const bool oks = cr_bits(vs.h + (vs.l + ds)) == cr_bits(vs.h + (vs.l - ds));
+    const bool okc = cr_bits(vc.h + (vc.l + dc)) == cr_bits(vc.h + (vc.l - dc));
     sr = vs.h + vs.l;
     cr = vc.h + vc.l;
     if (!(oks && okc)) cr_sincos_dd(sd, sa_h, sa_l, ca_h, ca_l, &sr, &cr);
   }
-  *sn = q == 0 ? sr : q == 1 ? cr : q == 2 ? -sr : -cr;
-  *cs = q == 0 ? cr : q == 1 ? -sr : q == 2 ? -cr : sr;
+  /* quadrant q: (sin, cos) = (sr, cr), (cr, -sr), (-sr, -cr), (-cr, sr), the
+   * negations as sign-bit flips */
+  const long long fs = (long long)((unsigned long long)(q & 2) << 62);
+  const long long fc = (long long)((unsigned long long)((q + 1) & 2) << 62);
+  *sn = cr_from_bits(cr_bits((q & 1) ? cr : sr) ^ fs);
+  *cs = cr_from_bits(cr_bits((q & 1) ? sr : cr) ^ fc);
   return true;
 }
 
