@@ -41,6 +41,7 @@ GBODE_CR double cr_from_bits(long long b) { double x; std::memcpy(&x, &b, 8); re
 }  // namespace gbode
 #endif
 #include "crpow_table.h"
+#include "bitops.h"
 
 namespace gbode {
 
@@ -176,7 +177,7 @@ GBODE_CR bool cr_pow_fast(double x, double y, double* out) {
   const ddr s = cr_two_sum(a.h, r);
   const double lo = ((a.l + s.l) + (pl + kCrLogTab[j][2])) + cr_fma(ed, GBODE_CR_LN2_B, ed * GBODE_CR_LN2_C);
   const ddr z = cr_mul_d(cr_fast(s.h, lo), y);
-  if (!(z.h <= 709.0 && z.h >= -708.0)) return false;
+  if (!(bo_le(z.h, 709.0) && bo_le(-708.0, z.h))) return false;
   /* exp(z) = 2^(k>>6) 2^((k&63)/64) exp(r), r = rh + rl */
   const double kb = cr_fma(z.h, GBODE_CR_INV_L64, 0x1.8p52);
   const double kd = kb - 0x1.8p52;
@@ -199,9 +200,9 @@ GBODE_CR bool cr_pow_fast(double x, double y, double* out) {
   const double lo2 = cr_fma(th, pl2, tp.l) + cr_fma(tl, rh, tl);
   const ddr u = cr_two_sum(th, tp.h);
   const ddr v = cr_fast(u.h, u.l + lo2);
-  const double d = 0x1p-63 * (v.h < 0.0 ? -v.h : v.h);
+  const double d = 0x1p-63 * v.h;  /* v.h > 0 */
   const double up = v.h + (v.l + d), dn = v.h + (v.l - d);
-  if (up != dn) return false;
+  if (cr_bits(up) != cr_bits(dn)) return false;  /* both positive */
   const int n = k >> 6;
   const int n1 = n / 2, n2 = n - n1;
   *out = (up * cr_from_bits((long long)(n1 + 1023) << 52)) * cr_from_bits((long long)(n2 + 1023) << 52);
@@ -221,14 +222,19 @@ GBODE_CR_COLD double cr_pow_dd(double x, double y) {
 
 /* x^y, correctly rounded (see the header comment) */
 GBODE_CR double cr_pow(double x, double y) {
-  if (x != x || y != y) return x + y;
-  if (y == 0.0) return 1.0;
-  if (x < 0.0) return cr_from_bits(0x7ff8000000000000LL);
-  if (x == 0.0) return y > 0.0 ? 0.0 : cr_from_bits(0x7ff0000000000000LL);
-  if (cr_bits(x) == 0x7ff0000000000000LL) return y > 0.0 ? x : 0.0;
-  if (x == 1.0) return 1.0;
+  /* the special cases by integer tests of the bits (a double compare would
+   * take an FP64-pipe slot) */
+  const long long bx = cr_bits(x), by = cr_bits(y);
+  const long long ax = bx & 0x7fffffffffffffffLL, ay = by & 0x7fffffffffffffffLL;
+  if (ax > 0x7ff0000000000000LL || ay > 0x7ff0000000000000LL) return x + y;  /* NaN */
+  if (ay == 0) return 1.0;
+  const bool ypos = by > 0;                                                     /* y > 0 */
+  if (ax == 0) return ypos ? 0.0 : cr_from_bits(0x7ff0000000000000LL);          /* x = +-0 */
+  if (bx < 0) return cr_from_bits(0x7ff8000000000000LL);                        /* x < 0 */
+  if (bx == 0x7ff0000000000000LL) return ypos ? x : 0.0;                        /* x = +Inf */
+  if (bx == 0x3ff0000000000000LL) return 1.0;                                   /* x = 1 */
   double f;
-  if ((y <= 1.0 && y >= -1.0) && cr_pow_fast(x, y, &f)) return f;
+  if (ay <= 0x3ff0000000000000LL && cr_pow_fast(x, y, &f)) return f;            /* |y| <= 1 */
   return cr_pow_dd(x, y);
 }
 

@@ -1481,25 +1481,34 @@ __device__ __forceinline__ int adaptive_try(const KParams& P, Lane<PR, D, F, NK>
      * 9/10, 1e-4), src/SimpleDiffEq.jl:67-77, src/tsit5/gpuatsit5.jl:276-299;
      * 1/qmax and 1/qmin are 0.1 and 5.0 in double; the powers correctly
      * rounded (cr_pow, crpow.h). */
-    const R abstol = (R)P.abstol, reltol = (R)P.reltol;
-    R acc = (R)0;
+    /* The comparisons, maxima and minima are the integer forms of bitops.h
+     * and ds_absmax (the same results; a double compare would take an
+     * FP64-pipe slot), with Julia's NaN propagation for min and max and the
+     * @fastmath clamps' compare-and-select. */
+    const double abstol = P.abstol, reltol = P.reltol;
+    double acc = 0.0;
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-      const R m = jmax(absR(l.uh[d]), absR(nh[d]));
-      const R r = e[d] / (abstol + m * reltol);
+      const double m = ds_absmax((double)l.uh[d], (double)nh[d]);
+      const double r = (double)e[d] / (abstol + m * reltol);
       acc = (d == 0) ? r * r : acc + r * r;
     }
-    const R EEst = sqrtR(acc / (R)D);
-    if (EEst != EEst) l.nan_seen = true;
-    const R q11 = cr_pow(EEst, (R)(7.0 / 50.0));
-    if (EEst > (R)1) {
-      l.dt = l.dt / (T)jmin((R)5.0, q11 / (R)(9.0 / 10.0));
+    const double EEst = sqrtR(acc / (double)D);
+    const bool enan = bo_isnan(EEst);
+    if (enan) l.nan_seen = true;
+    const double q11 = cr_pow(EEst, 7.0 / 50.0);
+    if (bo_lt(1.0, EEst)) {
+      const double f = q11 / (9.0 / 10.0);  /* min(1/qmin, q11/gamma), q11 >= 0 */
+      l.dt = l.dt / (T)(bo_isnan(f) || bo_lt(f, 5.0) ? f : 5.0);
       l.nrej += 1;
       return TRY_REJECTED;
     }
-    R q = (EEst == (R)0) ? (R)0.1 : q11 / cr_pow((R)l.qold, (R)(2.0 / 25.0));
-    q = fm_max((R)0.1, fm_min((R)5.0, q / (R)(9.0 / 10.0)));
-    l.qold = jmax(EEst, (R)1.0e-4);
+    const bool ezero = (__double_as_longlong(EEst) & 0x7fffffffffffffffLL) == 0;
+    double q = ezero ? 0.1 : q11 / cr_pow(l.qold, 2.0 / 25.0);
+    const double g = q / (9.0 / 10.0);
+    const double gm = bo_lt(5.0, g) ? 5.0 : g;  /* fm_min(1/qmin, q/gamma) */
+    q = bo_lt(0.1, gm) ? gm : 0.1;              /* fm_max(1/qmax, .) */
+    l.qold = enan ? EEst : (bo_lt(EEst, 1.0e-4) ? 1.0e-4 : EEst);  /* max(EEst, qoldinit), EEst >= 0 */
     const T dtold = l.dt;
     const T dtn = l.dt / (T)q;
     l.dt = absmin(dtn, rest);
