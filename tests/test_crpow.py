@@ -160,3 +160,19 @@ def test_oracle_ref_with_correctly_rounded_powers(po):
     f1 = po.solve("Tsit5", "lorenz", u0, p, (0.0, 1.0), 0.01, rounding="ref", controller="ref")
     f2 = po.solve("Tsit5", "lorenz", u0, p, (0.0, 1.0), 0.01, rounding="ref")
     assert np.array_equal(f1["u_final"], f2["u_final"])
+
+
+def test_oracle_ref_with_correctly_rounded_sines(po):
+    """Kuramoto-12 in the oracle's REF rounding with correctly rounded sines
+    and cosines (controller "ref") against libm's: the same accepted steps
+    and final phases within a small fraction of the error scale."""
+    rng = np.random.default_rng(4)
+    n = 200
+    th = rng.uniform(0, 2 * np.pi, (12, n))
+    p = np.vstack([rng.normal(0, 1, (12, n)), rng.uniform(0, 4, (1, n))])
+    kw = dict(rounding="ref", abstol=1e-8, reltol=1e-6, nthreads=4)
+    a = po.solve("ATsit5", "kuramoto", th, p, (0.0, 10.0), 0.1, controller="ref", **kw)
+    b = po.solve("ATsit5", "kuramoto", th, p, (0.0, 10.0), 0.1, **kw)
+    assert np.abs(a["naccept"].astype(int) - b["naccept"]).max() <= 1
+    scale = 1e-8 + 1e-6 * np.abs(b["u_final"]).max(0)
+    assert (np.abs(a["u_final"] - b["u_final"]).max(0) / scale).max() < 1.0
