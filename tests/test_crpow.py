@@ -90,7 +90,7 @@ def test_correctly_rounded(lib):
 
 def test_first_phase_agrees_with_double_double_path(lib):
     """Ziv's first phase (double polynomials, a rounding test with a 2^-63
-    margin; its error measured below 2^-68) returns what the double-double
+    margin; its largest error measured about 2^-68) returns what the double-double
     path returns, and falls through in about 0.15% of calls."""
     rng = np.random.default_rng(6)
     x = np.concatenate([10.0 ** rng.uniform(-12, 3, 300000), 10.0 ** rng.uniform(-300, 300, 100000),
